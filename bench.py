@@ -1,0 +1,395 @@
+#!/usr/bin/env python
+"""Benchmark: RK4 particle-steps/s of flowVC's FTLE workload on a tet mesh.
+
+Workload (one bench step = one complete FTLE window, the unit ompVC's FTLE
+output is produced in): a unit cube of 64^3 cells split into 6 Kuhn
+tetrahedra (1,572,864 tets, 274,625 nodes, interior nodes jittered +-0.2h
+with seed 0), ABC velocity scaled by (1 + 0.1 sin 2 pi t) at 51 frames
+dt = 0.02, an FTLE seed grid of 128^3 points over [0,1]^3 integrated forward
+over T = 1 with RK4 h = 0.005, neighbour-walk point location with the global
+search fallback (LocalSearchChecking = 1).  Inputs are synthetic, generated
+here with fixed seeds (no dataset is involved).
+
+value      accepted RK4 steps / s with mesh and frames resident in HBM; each
+           step seeds and locates the grid, advects every interval
+           (including the early-FTLE advections of points that leave) and
+           reduces the FTLE field.
+e2e        the same through the C ABI from pinned host buffers: mesh and all
+           frames copied host->device inside each step, FTLE fields copied back.
+roofline   the main advection kernel (k_ftle_pass1) against the measured HBM
+           copy bandwidth, 1,384 algorithmic bytes per unstructured FP64 RK4
+           step (4 stages x (connectivity 16 + node coordinates 96 + 4 nodes x
+           2 frames x 3 x 8) + final containment 112 + state 56).
+cpu_baseline  the CPU oracle (the reference's algorithm restated in C,
+           OpenMP over all host cores) on a bounded sample: the same grid and
+           mesh over the first 5 frame intervals (T = 0.1).
+
+--impl reference runs that CPU implementation alone, every step one bounded
+sample, on the same metric.  Multi-GPU (torchrun, N > 1): every rank runs the
+whole workload on its own GPU (replicas; the window has no exchange step),
+value = all ranks' steps / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "flowvc-1_gb300")
+for _p in (PKG, os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+BYTES_PER_STEP = 1384        # unstructured FP64 RK4 step, algorithmic
+CUBE_N = 64
+NFRAMES, DT = 51, 0.02
+H = 0.005
+T_WINDOW = 1.0
+SAMPLE_T = 0.1               # CPU sample: first 5 frame intervals
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--grid", type=int, default=128, help="FTLE seed grid edge")
+    ap.add_argument("--cube", type=int, default=CUBE_N, help="mesh cells per edge")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    return ap.parse_args()
+
+
+def make_inputs(n):
+    import synth
+    xyz, conn, adj = synth.kuhn_cube_mesh(n, jitter=0.2, seed=0)
+    frames = [synth.abc_flow(xyz, f * DT) for f in range(NFRAMES)]
+    return xyz, conn, adj, frames
+
+
+def grid_tuple(g):
+    return (0.0, 1.0, 0.0, 1.0, 0.0, 1.0, g, g, g)
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks and throttle reasons)."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax = float(f[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        finally:
+            try:
+                os.remove(self.path)
+            except OSError:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ peaks
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per k_ftle_pass1 launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "ftle_pass1_traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_step"), d
+    except (OSError, ValueError):
+        return None, None
+
+
+# ------------------------------------------------------------------ CPU side
+
+def cpu_sample(inputs, grid, threads, tmpdir):
+    """The oracle on the bounded sample; returns (steps/s, steps, seconds, threads)."""
+    import oracle_lib
+    import synth
+    xyz, conn, adj, frames = inputs
+    d = os.path.join(tmpdir, "c2")
+    if not os.path.exists(os.path.join(d, "cube_coordinates.bin")):
+        os.makedirs(d, exist_ok=True)
+        synth.write_unstructured_mesh(os.path.join(d, "cube"), xyz, conn, adj)
+        nfr = int(round(SAMPLE_T / DT)) + 2
+        for f in range(min(nfr, NFRAMES)):
+            synth.write_frame(os.path.join(d, f"cube_vel.{f}.bin"), f * DT, frames[f])
+    out = os.path.join(tmpdir, "c2out")
+    os.makedirs(out, exist_ok=True)
+    inp = os.path.join(tmpdir, "c2.in")
+    g = grid
+    synth.write_in_file(
+        inp, Path_Data=d + "/", Path_Output=out + "/", Dimensions=3, Data_MeshType=1, Data_InFilePrefix="cube",
+        Data_TRes=NFRAMES, Data_TDelta=DT, FTLE_Compute=1, FTLE_IntTLength=SAMPLE_T, Int_TimeStep=H,
+        LocalSearchChecking=1, **{"Data_MeshBounds.XMin": 0.0, "Data_MeshBounds.XMax": 1.0,
+                                  "Data_MeshBounds.YMin": 0.0, "Data_MeshBounds.YMax": 1.0,
+                                  "Data_MeshBounds.ZMin": 0.0, "Data_MeshBounds.ZMax": 1.0,
+                                  "FTLE_MeshBounds.ZMax": 1.0, "FTLE_MeshBounds.XRes": g,
+                                  "FTLE_MeshBounds.YRes": g, "FTLE_MeshBounds.ZRes": g})
+    nthr = threads if threads > 0 else (os.cpu_count() or 1)
+    rc, secs, steps, err = oracle_lib.run(inp, nthr)
+    if rc:
+        raise RuntimeError(f"oracle failed: {err}")
+    return steps / secs, steps, secs, nthr
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    inputs = make_inputs(args.cube)
+    with tempfile.TemporaryDirectory() as td:
+        for _ in range(args.warmup):
+            cpu_sample(inputs, args.grid, args.cpu_threads, td)
+        vals, steps_tot, secs_tot = [], 0, 0.0
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            v, st, secs, nthr = cpu_sample(inputs, args.grid, args.cpu_threads, td)
+            vals.append(v)
+            steps_tot += st
+            secs_tot += secs
+        wall = time.perf_counter() - t0
+    value = steps_tot / secs_tot
+    line = {
+        "impl": "reference", "metric": "RK4 particle-steps/s", "value": value, "unit": "steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"FTLE {args.grid}^3 seeds, {args.cube}^3x6 jittered Kuhn tets, ABC flow, "
+                               f"RK4 h={H}; sample: first {int(round(SAMPLE_T / DT))} frame intervals (T={SAMPLE_T})",
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": nthr, "kind": "port",
+                         "sample": f"FTLE {args.grid}^3 over T={SAMPLE_T} (5 of 50 intervals), advection phase timed"},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ ranks
+
+def reduce_over_ranks(secs, units, world):
+    """(max seconds over ranks, sum of units over ranks).  Every rank calls it;
+    uses the process group's device (CUDA for NCCL, CPU for gloo)."""
+    if world <= 1:
+        return float(secs), float(units)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(secs)], dtype=torch.float64, device=dev)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
+# ------------------------------------------------------------------ GPU side
+
+def run_engine(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    import flow
+    import fvc
+    import build as fvc_build
+
+    fvc_build.build()
+    torch.cuda.set_device(local_rank)
+    inputs = make_inputs(args.cube)
+    xyz, conn, adj, frames = inputs
+    ax = flow.TimeAxis(0.0, DT, NFRAMES, 0)
+    grid = grid_tuple(args.grid)
+    npts = args.grid ** 3
+
+    try:
+        fma_s, div_s = fvc.probe_fp64(local_rank)
+        fp64 = {"fma_per_s": fma_s, "div_per_s": div_s}
+    except fvc.FvcError:
+        fp64 = None
+    ctx = fvc.Context(3, 1, device=local_rank)
+    ctx.set_unstruct_mesh(xyz, conn, adj)
+    ctx.set_bounds([0, 1, 0, 1, 0, 1])
+    ctx.set_integrator(1, H, 0)
+    flow.upload_frames(ctx, ax, frames)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+
+    for _ in range(args.warmup):
+        flow.run_ftle(ctx, ax, grid, T_WINDOW)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    stats = []
+    steps_total = 0
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            wT, wN, st, js = flow.run_ftle(ctx, ax, grid, T_WINDOW)
+            steps_total += st
+            stats.append(js)
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1)
+    clocks = clk.summary()
+    secs = ms / 1000.0
+    secs_max, steps_all = reduce_over_ranks(secs, steps_total, world)
+
+    # roofline of the main advection kernel from its CUDA-event times
+    ms_main = sum(s["ms_main"] for s in stats)
+    steps_main = sum(s["steps_main"] for s in stats)
+    launches_main = sum(s["intervals"] for s in stats)
+    peak, peak_kind = measured_peak()
+    achieved = (steps_main * BYTES_PER_STEP) / (ms_main / 1000.0) / 1e9 if ms_main > 0 else 0.0
+    traffic_per_step, _ = profiled_traffic()
+    traffic = traffic_per_step * steps_main / launches_main if traffic_per_step else None
+    gpu_launches = int(sum(s["launches"] for s in stats))
+
+    # end to end through the C ABI from pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+        pxyz, pconn, padj = pin(xyz), pin(conn), pin(adj)
+        pframes = [pin(f) for f in frames]
+        h2d = pxyz.nbytes + pconn.nbytes + padj.nbytes + sum(f.nbytes for f in pframes)
+        d2h = 2 * 8 * npts
+        ctx.close()
+        barrier()
+        t0 = time.perf_counter()
+        e2e_steps = 0
+        for _ in range(args.steps):
+            c2 = fvc.Context(3, 1, device=local_rank)
+            c2.set_unstruct_mesh(pxyz, pconn, padj)
+            c2.set_bounds([0, 1, 0, 1, 0, 1])
+            c2.set_integrator(1, H, 0)
+            flow.upload_frames(c2, ax, pframes)
+            wT, wN, st, _ = flow.run_ftle(c2, ax, grid, T_WINDOW)
+            e2e_steps += st
+            c2.close()
+        barrier()
+        e2e_secs, e2e_all = reduce_over_ranks(time.perf_counter() - t0, e2e_steps, world)
+        e2e = {"value": e2e_all / e2e_secs, "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+    else:
+        ctx.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        with tempfile.TemporaryDirectory() as td:
+            v, st, s2, nthr = cpu_sample(inputs, args.grid, args.cpu_threads, td)
+        cpu = {"value": v, "unit": "steps/s", "cores": nthr, "kind": "port",
+               "sample": f"FTLE {args.grid}^3 over T={SAMPLE_T} (5 of 50 intervals), {st} steps in {s2:.2f} s "
+                         f"of advection"}
+
+    if rank == 0:
+        value = steps_all / secs_max
+        line = {
+            "metric": "RK4 particle-steps/s", "value": value, "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"FTLE {args.grid}^3 seeds over T={T_WINDOW}, {args.cube}^3x6 jittered Kuhn tets "
+                                   f"({6 * args.cube ** 3} tets), ABC flow {NFRAMES} frames, RK4 h={H}",
+                       "l2": "inputs larger than L2 (frames 51 x 8.8 MB + 420 MB of grid state)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "ftle_points_per_s": npts * args.steps * world / secs_max,
+            "steps_main": int(steps_main), "steps_early": int(sum(s["steps_early"] for s in stats)),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "k_ftle_pass1", "bytes_per_step": BYTES_PER_STEP},
+            "gpu_launches": gpu_launches,
+            "phases_ms_per_step": {k: sum(s[k] for s in stats) / args.steps
+                                   for k in ("ms_setup", "ms_main", "ms_early", "ms_reduce")},
+            "fp64_probe": fp64,
+            "clocks": clocks,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    run_engine(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

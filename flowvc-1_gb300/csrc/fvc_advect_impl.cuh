@@ -1,0 +1,368 @@
+// fvc_advect_impl.cuh -- kernels that run the integrators, templated on the
+// dimension D and mesh type M (0 Cartesian, 1 unstructured).  Each variant is
+// instantiated in its own translation unit (fvc_variant_*.cu) so the four
+// compile in parallel.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fvc_device.cuh"
+#include "fvc_ftle_math.cuh"
+#include "fvc_kernels.h"
+
+namespace fvc {
+
+#ifndef FVC_MINBLOCKS
+#define FVC_MINBLOCKS 4
+#endif
+
+static inline unsigned vblk(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+__device__ __forceinline__ void load_pt(Pt& p, long i, const double* X, const double* V,
+                                        const int* eid, const int* left, const double* ldt) {
+  p.X[0] = X[3 * i];
+  p.X[1] = X[3 * i + 1];
+  p.X[2] = X[3 * i + 2];
+  if (V) {
+    p.V[0] = V[3 * i];
+    p.V[1] = V[3 * i + 1];
+    p.V[2] = V[3 * i + 2];
+  } else {
+    p.V[0] = p.V[1] = p.V[2] = 0.0;
+  }
+  p.eid = eid ? eid[i] : -1;
+  p.left = left[i];
+  p.ldt = ldt[i];
+}
+
+template <int D, int M>
+__global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_advect(DevMesh m, DevWindow w, DevInteg in, int n, double* X, double* V, int* eid,
+                         int* left, double* ldt, double t0, double t1, DevCounters* ctr) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned steps = 0;
+  int err = 0;
+  if (i < n) {
+    Pt p;
+    load_pt(p, i, X, V, eid, left, ldt);
+    if (!(p.left && !in.extrapolate)) {
+      err = advect<D, M>(m, w, in, p, t0, t1, steps);
+      X[3 * i] = p.X[0];
+      X[3 * i + 1] = p.X[1];
+      X[3 * i + 2] = p.X[2];
+      if (V) {
+        V[3 * i] = p.V[0];
+        V[3 * i + 1] = p.V[1];
+        V[3 * i + 2] = p.V[2];
+      }
+      if (eid) eid[i] = p.eid;
+      left[i] = p.left;
+      ldt[i] = p.ldt;
+    }
+  }
+  flush_counters(&ctr->steps, &ctr->status, steps, err);
+}
+
+
+template <int D, int M>
+__global__ void k_velocity(DevMesh m, DevWindow w, int n, const double* X, int* eid, int* left,
+                           double tq, double* out, DevCounters* ctr) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  int err = 0;
+  if (i < n) {
+    double x[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]}, v[3] = {0, 0, 0};
+    int e = eid ? eid[i] : -1, l = left[i];
+    err = velocity<D, M>(m, w, tq, -1, x, e, l, v);
+    out[3 * i] = v[0];
+    out[3 * i + 1] = v[1];
+    out[3 * i + 2] = v[2];
+    if (eid) eid[i] = e;
+    left[i] = l;
+  }
+  flush_counters(&ctr->steps, &ctr->status, 0, err);
+}
+
+
+
+// Launch velocity of a slide (ompVC/ftle.c:84-96): on a Cartesian grid it
+// flags points outside the velocity grid.
+template <int D, int M>
+__global__ void k_ftle_launch(DevMesh m, DevWindow w, FtleDev f, double t, DevCounters* ctr) {
+  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  int err = 0;
+  if (p < f.n && !f.left[p]) {
+    double x[3] = {f.X[3 * p], f.X[3 * p + 1], f.X[3 * p + 2]}, v[3];
+    int e = f.eid[p], l = 0;
+    err = velocity<D, M>(m, w, t, -1, x, e, l, v);
+    f.V[3 * p] = v[0];
+    f.V[3 * p + 1] = v[1];
+    f.V[3 * p + 2] = v[2];
+    f.eid[p] = e;
+    if (l) f.left[p] = 1;
+  }
+  flush_counters(&ctr->steps, &ctr->status, 0, err);
+}
+
+
+// Pass 1: every live point from its frame-start state (ompVC/ftle.c:109-130).
+template <int D, int M>
+__global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_pass1(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
+                                                    double t1, double t2, DevCounters* ctr) {
+  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned steps = 0;
+  int err = 0;
+  if (p < f.n) {
+    unsigned char fl = 0;
+    if (f.ldt[p] > -FVC_TINY && (!f.left[p] || in.extrapolate)) {
+      Pt t;
+      load_pt(t, p, f.X, f.V, f.eid, f.left, f.ldt);
+      err = advect<D, M>(m, w, in, t, t1, t2, steps);
+      fl = 1 | ((t.left && !in.extrapolate) ? 2 : 0) | (t.left ? 4 : 0);
+      f.Xn[3 * p] = t.X[0];
+      f.Xn[3 * p + 1] = t.X[1];
+      f.Xn[3 * p + 2] = t.X[2];
+      f.Vn[3 * p] = t.V[0];
+      f.Vn[3 * p + 1] = t.V[1];
+      f.Vn[3 * p + 2] = t.V[2];
+      f.en[p] = t.eid;
+      f.te[p] = t.ldt;
+    }
+    f.flag[p] = fl;
+  }
+  flush_counters(&ctr->steps, &ctr->status, steps, err);
+}
+
+
+
+
+template <int D, int M>
+__device__ __forceinline__ int adv_from_start(const DevMesh& m, const DevWindow& w, const DevInteg& in,
+                                              const FtleDev& f, long p, int eid, double t1, double t2,
+                                              Pt& out, unsigned& steps) {
+  out.X[0] = f.X[3 * p];
+  out.X[1] = f.X[3 * p + 1];
+  out.X[2] = f.X[3 * p + 2];
+  out.V[0] = f.V[3 * p];
+  out.V[1] = f.V[3 * p + 1];
+  out.V[2] = f.V[3 * p + 2];
+  out.left = f.left[p];
+  out.eid = eid;
+  out.ldt = 0.0;
+  return advect<D, M>(m, w, in, out, t1, t2, steps);
+}
+
+// Pass 2b: GetFTLEForPointEarly (ompVC/ftle.c:788-1048) for every served point
+// q with its trigger's exit time te, spread over four launches so the up to
+// thirteen advections of one point run in parallel:
+//   A  each of q's six neighbours from its frame-start state to te
+//   B  MinExitTime = min(te, the neighbours' exit times)   (ftle.c:878)
+//   C  q itself to MinExitTime, and the neighbours again when MinExitTime
+//      differs from te (Advect is deterministic: when it equals te, the
+//      positions from A are the ones the reference recomputes)
+//   D  the stencil, Cauchy-Green tensor and FTLE          (ftle.c:882-1046)
+// Points the serial loop has passed before the trigger carry their
+// end-of-interval element into these advections (ftle.c:167-168).
+__device__ __forceinline__ void served_geometry(const FtleDev& f, long q, long nb[6], int& i, int& j, int& k) {
+  int YZ = f.yr * f.zr, zr = f.zr;
+  k = (int)(q % zr);
+  j = (int)((q / zr) % f.yr);
+  i = (int)(q / YZ);
+  nb[0] = i > 0 ? q - YZ : -1;
+  nb[1] = i < f.xr - 1 ? q + YZ : -1;
+  nb[2] = j > 0 ? q - zr : -1;
+  nb[3] = j < f.yr - 1 ? q + zr : -1;
+  nb[4] = k > 0 ? q - 1 : -1;
+  nb[5] = k < zr - 1 ? q + 1 : -1;
+}
+
+__device__ __forceinline__ int eid_at_trigger(const FtleDev& f, long pp, long trig) {
+  return (pp < trig && (f.flag[pp] & 1) && !(f.flag[pp] & 2)) ? f.en[pp] : f.eid[pp];
+}
+
+template <int D, int M>
+__global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_early_nb(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
+                                                       double t1, DevCounters* ctr) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nserved = *(volatile int*)&ctr->count;
+  unsigned steps = 0;
+  int err = 0;
+  long s = idx / 6;
+  int c = (int)(idx % 6);
+  if (s < nserved) {
+    long q = f.served[s], trig = f.trig[s];
+    double te = f.te[trig];
+    long nb[6];
+    int i, j, k;
+    served_geometry(f, q, nb, i, j, k);
+    double lt = te;
+    double* pos = f.epos + (s * 7 + c) * 3;
+    if (nb[c] >= 0) {
+      Pt t;
+      err = adv_from_start<D, M>(m, w, in, f, nb[c], eid_at_trigger(f, nb[c], trig), t1, te, t, steps);
+      if (t.left) lt = t.ldt;
+      pos[0] = t.X[0];
+      pos[1] = t.X[1];
+      pos[2] = t.X[2];
+    }
+    f.elt[s * 6 + c] = lt;
+  }
+  flush_counters(&ctr->steps_early, &ctr->status, steps, err);
+}
+
+template <int D>
+__global__ void k_ftle_early_mid(FtleDev f, DevCounters* ctr) {
+  long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nserved = *(volatile int*)&ctr->count;
+  if (s >= nserved) return;
+  double te = f.te[f.trig[s]];
+  const double* lt = f.elt + s * 6;
+  f.emt[s] = dmin(te, dmin(lt[5], dmin(lt[4], dmin(lt[3], dmin(lt[2], dmin(lt[1], lt[0]))))));
+}
+
+template <int D, int M>
+__global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_early_self(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
+                                                         double t1, DevCounters* ctr) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nserved = *(volatile int*)&ctr->count;
+  unsigned steps = 0;
+  int err = 0;
+  long s = idx / 7;
+  int c = (int)(idx % 7);
+  if (s < nserved) {
+    long q = f.served[s], trig = f.trig[s];
+    double te = f.te[trig], mt = f.emt[s];
+    long nb[6];
+    int i, j, k;
+    served_geometry(f, q, nb, i, j, k);
+    long p = c == 6 ? q : nb[c];
+    if (p >= 0 && (c == 6 || mt != te)) {
+      Pt t;
+      err = adv_from_start<D, M>(m, w, in, f, p, eid_at_trigger(f, p, trig), t1, mt, t, steps);
+      double* pos = f.epos + (s * 7 + c) * 3;
+      pos[0] = t.X[0];
+      pos[1] = t.X[1];
+      pos[2] = t.X[2];
+    }
+  }
+  flush_counters(&ctr->steps_early, &ctr->status, steps, err);
+}
+
+template <int D>
+__global__ void k_ftle_early_final(FtleDev f, DevCounters* ctr) {
+  long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nserved = *(volatile int*)&ctr->count;
+  if (s >= nserved) return;
+  long q = f.served[s];
+  double mt = f.emt[s];
+  long nb[6];
+  int i, j, k;
+  served_geometry(f, q, nb, i, j, k);
+  const double* pos = f.epos + s * 21;
+  const double* self = pos + 18;
+  const double *L, *R, *B, *T, *Bk, *F;
+  double fx, fy, fz;
+  if (i == 0) { L = self; R = pos + 3; fx = 1.0; }
+  else if (i == f.xr - 1) { L = pos; R = self; fx = 1.0; }
+  else { L = pos; R = pos + 3; fx = 2.0; }
+  if (j == 0) { B = self; T = pos + 9; fy = 1.0; }
+  else if (j == f.yr - 1) { B = pos + 6; T = self; fy = 1.0; }
+  else { B = pos + 6; T = pos + 9; fy = 2.0; }
+  if (D == 3) {
+    if (k == 0) { Bk = self; F = pos + 15; fz = 1.0; }
+    else if (k == f.zr - 1) { Bk = pos + 12; F = self; fz = 1.0; }
+    else { Bk = pos + 12; F = pos + 15; fz = 2.0; }
+  } else { Bk = F = self; fz = 1.0; }
+  double lam = stencil_lambda(D, L, R, B, T, Bk, F, fx, fy, fz, f.dx, f.dy, f.dz);
+  double wT = 0.0, wN = 0.0;
+  if (lam > 1.0 - FVC_TINY && !(fabs(mt - f.start) < FVC_TINY)) {
+    wT = (0.5 * log(lam)) / fabs(mt - f.start);
+    wN = 0.5 * log(lam);
+  }
+  f.ftT[q] = wT;
+  f.ftN[q] = wN;
+  f.have[q] = 1;
+}
+
+template <int D, int M>
+__global__ void k_tracer_launch(DevMesh m, DevWindow w, TracerDev t, double tq, DevCounters* ctr) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  int err = 0;
+  if (i < t.n && !t.left[i]) {
+    double x[3] = {t.X[3 * i], t.X[3 * i + 1], t.X[3 * i + 2]}, v[3];
+    int e = t.eid[i], l = 0;
+    err = velocity<D, M>(m, w, tq, -1, x, e, l, v);
+    t.V[3 * i] = v[0];
+    t.V[3 * i + 1] = v[1];
+    t.V[3 * i + 2] = v[2];
+    t.eid[i] = e;
+    if (l) t.left[i] = 1;
+  }
+  flush_counters(&ctr->steps, &ctr->status, 0, err);
+}
+
+
+template <int D, int M>
+__global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_tracer_advance(DevMesh m, DevWindow w, DevInteg in, TracerDev t,
+                                                        double t1, double t2, DevCounters* ctr) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned steps = 0;
+  int err = 0;
+  if (i < t.n && t.ldt[i] > -FVC_TINY && (!t.left[i] || in.extrapolate)) {
+    Pt p;
+    load_pt(p, i, t.X, t.V, t.eid, t.left, t.ldt);
+    err = advect<D, M>(m, w, in, p, t1, t2, steps);
+    t.X[3 * i] = p.X[0];
+    t.X[3 * i + 1] = p.X[1];
+    t.X[3 * i + 2] = p.X[2];
+    t.V[3 * i] = p.V[0];
+    t.V[3 * i + 1] = p.V[1];
+    t.V[3 * i + 2] = p.V[2];
+    t.eid[i] = p.eid;
+    t.left[i] = p.left;
+    t.ldt[i] = p.ldt;
+  }
+  flush_counters(&ctr->steps, &ctr->status, steps, err);
+}
+
+
+
+template <int D, int M>
+struct Variant {
+  static void advect(const DevMesh& m, const DevWindow& w, const DevInteg& in, int n, double* X,
+                     double* V, int* eid, int* left, double* ldt, double t0, double t1,
+                     DevCounters* ctr, cudaStream_t s) {
+    k_advect<D, M><<<vblk(n, 128), 128, 0, s>>>(m, w, in, n, X, V, eid, left, ldt, t0, t1, ctr);
+  }
+  static void velocity(const DevMesh& m, const DevWindow& w, int n, const double* X, int* eid,
+                       int* left, double tq, double* out, DevCounters* ctr, cudaStream_t s) {
+    k_velocity<D, M><<<vblk(n, 128), 128, 0, s>>>(m, w, n, X, eid, left, tq, out, ctr);
+  }
+  static void ftle_launch(const DevMesh& m, const DevWindow& w, const FtleDev& f, double t,
+                          DevCounters* ctr, cudaStream_t s) {
+    k_ftle_launch<D, M><<<vblk(f.n, 128), 128, 0, s>>>(m, w, f, t, ctr);
+  }
+  static void ftle_pass1(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
+                         double t1, double t2, DevCounters* ctr, cudaStream_t s) {
+    k_ftle_pass1<D, M><<<vblk(f.n, 128), 128, 0, s>>>(m, w, in, f, t1, t2, ctr);
+  }
+  static void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
+                         double t1, DevCounters* ctr, cudaStream_t s) {
+    k_ftle_early_nb<D, M><<<vblk(6L * f.n, 128), 128, 0, s>>>(m, w, in, f, t1, ctr);
+    k_ftle_early_mid<D><<<vblk(f.n, 256), 256, 0, s>>>(f, ctr);
+    k_ftle_early_self<D, M><<<vblk(7L * f.n, 128), 128, 0, s>>>(m, w, in, f, t1, ctr);
+    k_ftle_early_final<D><<<vblk(f.n, 128), 128, 0, s>>>(f, ctr);
+  }
+  static void tracer_launch(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq,
+                            DevCounters* ctr, cudaStream_t s) {
+    k_tracer_launch<D, M><<<vblk(t.n, 128), 128, 0, s>>>(m, w, t, tq, ctr);
+  }
+  static void tracer_advance(const DevMesh& m, const DevWindow& w, const DevInteg& in,
+                             const TracerDev& t, double t1, double t2, DevCounters* ctr, cudaStream_t s) {
+    k_tracer_advance<D, M><<<vblk(t.n, 128), 128, 0, s>>>(m, w, in, t, t1, t2, ctr);
+  }
+};
+
+extern template struct Variant<2, 0>;
+extern template struct Variant<3, 0>;
+extern template struct Variant<2, 1>;
+extern template struct Variant<3, 1>;
+
+}  // namespace fvc

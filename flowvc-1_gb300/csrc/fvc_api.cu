@@ -1,0 +1,890 @@
+// fvc_api.cu -- the C ABI of include/fvc.h: contexts, device-resident mesh
+// and frames, step-level calls and the FTLE / tracer jobs.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "fvc.h"
+#include "fvc_kernels.h"
+
+using namespace fvc;
+
+struct fvc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DevMesh mesh{};
+  bool mesh_set = false;
+  DevInteg integ{1, 0.01, 0};
+  bool integ_set = false;
+  DevWindow window{};
+  bool window_set = false;
+  long frame_nodes = 0;  // nodes per frame
+  // device buffers
+  int4* d_elem = nullptr;
+  double* d_geom = nullptr;
+  double4_32a* d_nodes = nullptr;
+  int* d_cell_start = nullptr;
+  int* d_cell_ids = nullptr;
+  BucketGrid grid{};
+  std::unordered_map<int, double4_32a*> frames;
+  double* d_stage = nullptr;  // frame upload staging, 3 doubles a node
+  DevCounters* d_ctr = nullptr;
+  double4_32a* d_vt = nullptr;  // stage-time node velocities
+  int vt_slots = 0;
+  // scratch for array calls
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  std::string err;
+};
+
+struct fvc_job {
+  fvc_ctx* ctx = nullptr;
+  int kind = 0;  // 0 FTLE, 1 tracers
+  FtleDev f{};
+  TracerDev t{};
+  void* mem = nullptr;  // one allocation for all per-job arrays
+  fvc_job_stats stats{};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+static void job_events(fvc_job* j) {
+  for (int k = 0; k < 4; k++)
+    if (!j->ev[k]) cudaEventCreate(&j->ev[k]);
+}
+
+static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) ms = 0.f;
+  return ms;
+}
+
+// ------------------------------------------------------------------ helpers
+
+static fvc_status fail(fvc_ctx* c, fvc_status code, const char* fmt, ...) {
+  if (c) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    c->err = buf;
+  }
+  return code;
+}
+
+#define FVC_CUDA(c, x)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (x);                                                                \
+    if (e_ != cudaSuccess) return fail((c), FVC_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
+  } while (0)
+
+static fvc_status use_device(fvc_ctx* c) {
+  FVC_CUDA(c, cudaSetDevice(c->device));
+  return FVC_OK;
+}
+
+static fvc_status check_launch(fvc_ctx* c, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(c, FVC_ERR_CUDA, "%s launch: %s", what, cudaGetErrorString(e));
+  return FVC_OK;
+}
+
+// Reads and clears the counters; maps device fault bits to a status.
+static fvc_status finish(fvc_ctx* c, const char* what, long long* steps, DevCounters* out = nullptr) {
+  DevCounters h{};
+  FVC_CUDA(c, cudaMemcpyAsync(&h, c->d_ctr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (steps) *steps = (long long)(h.steps + h.steps_early);
+  if (out) *out = h;
+  FVC_CUDA(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), c->stream));
+  if (h.status & PT_ERR_STATE)
+    return fail(c, FVC_ERR_STATE, "%s: a point that had left the domain was advected", what);
+  if (h.status & PT_ERR_TLOC)
+    return fail(c, FVC_ERR_TLOC, "%s: query time outside the loaded frame interval", what);
+  if (h.status & PT_ERR_WALK)
+    return fail(c, FVC_ERR_WALK, "%s: neighbour walk failed (indeterminate neighbour or hop cap)", what);
+  return FVC_OK;
+}
+
+static fvc_status ensure_scratch(fvc_ctx* c, size_t bytes) {
+  if (bytes <= c->scratch_bytes) return FVC_OK;
+  if (c->d_scratch) cudaFree(c->d_scratch);
+  c->d_scratch = nullptr;
+  c->scratch_bytes = 0;
+  if (cudaMalloc(&c->d_scratch, bytes) != cudaSuccess)
+    return fail(c, FVC_ERR_OOM, "could not allocate %zu bytes of device scratch", bytes);
+  c->scratch_bytes = bytes;
+  return FVC_OK;
+}
+
+static inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// ------------------------------------------------------------------ context
+
+extern "C" int fvc_abi_version(void) { return FVC_ABI_VERSION; }
+
+extern "C" fvc_status fvc_create(fvc_ctx** out, const fvc_opts* o) {
+  if (!out || !o) return FVC_ERR_ARG;
+  *out = nullptr;
+  if ((o->dims != 2 && o->dims != 3) || (o->mesh_type != 0 && o->mesh_type != 1)) return FVC_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return FVC_ERR_CUDA;
+  if (o->device < 0 || o->device >= ndev) return FVC_ERR_ARG;
+  fvc_ctx* c = new fvc_ctx();
+  c->device = o->device;
+  c->mesh.dims = o->dims;
+  c->mesh.mesh_type = o->mesh_type;
+  c->mesh.max_hops = o->max_hops > 0 ? o->max_hops : 65536;
+  for (int a = 0; a < 3; a++) {
+    c->mesh.bounds[2 * a] = -1e300;
+    c->mesh.bounds[2 * a + 1] = 1e300;
+  }
+  if (cudaSetDevice(c->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->d_ctr, sizeof(DevCounters)) != cudaSuccess ||
+      cudaMemset(c->d_ctr, 0, sizeof(DevCounters)) != cudaSuccess) {
+    fvc_destroy(c);
+    return FVC_ERR_CUDA;
+  }
+  *out = c;
+  return FVC_OK;
+}
+
+extern "C" void fvc_destroy(fvc_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->frames) cudaFree(kv.second);
+  cudaFree(c->d_elem);
+  cudaFree(c->d_geom);
+  cudaFree(c->d_nodes);
+  cudaFree(c->d_cell_start);
+  cudaFree(c->d_cell_ids);
+  cudaFree(c->d_stage);
+  cudaFree(c->d_ctr);
+  cudaFree(c->d_scratch);
+  cudaFree(c->d_vt);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" const char* fvc_last_error(const fvc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+// ---------------------------------------------------------------- mesh
+
+extern "C" fvc_status fvc_set_cart_mesh(fvc_ctx* c, double xmin, double xmax, int xres, double ymin,
+                                        double ymax, int yres, double zmin, double zmax, int zres) {
+  if (!c) return FVC_ERR_ARG;
+  if (c->mesh.mesh_type != 0) return fail(c, FVC_ERR_STATE, "context is not Cartesian");
+  // derived parameters as ompVC/mesh.c:101-121
+  if (xres < 2 || xmin >= xmax) return fail(c, FVC_ERR_ARG, "Insufficient resolution of velocity data in x-direction");
+  if (yres < 2 || ymin >= ymax) return fail(c, FVC_ERR_ARG, "Insufficient resolution of velocity data in y-direction");
+  DevMesh& m = c->mesh;
+  m.xmin = xmin; m.xres = xres; m.dx = (xmax - xmin) / (xres - 1);
+  m.ymin = ymin; m.yres = yres; m.dy = (ymax - ymin) / (yres - 1);
+  if (m.dims == 3) {
+    if (zres < 2 || zmin >= zmax) return fail(c, FVC_ERR_ARG, "Insufficient resolution of velocity data in z-direction");
+    m.zmin = zmin; m.zres = zres; m.dz = (zmax - zmin) / (zres - 1);
+  } else {
+    m.zmin = 0; m.zres = 1; m.dz = 0;
+  }
+  long nn = (long)m.xres * m.yres * m.zres;
+  if (c->frame_nodes && c->frame_nodes != nn) {
+    for (auto& kv : c->frames) cudaFree(kv.second);
+    c->frames.clear();
+  }
+  c->frame_nodes = nn;
+  c->mesh_set = true;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double* xyz, int nelem,
+                                            const int* conn, const int* adj) {
+  if (!c) return FVC_ERR_ARG;
+  if (c->mesh.mesh_type != 1) return fail(c, FVC_ERR_STATE, "context is not unstructured");
+  if (nnodes <= 0 || nelem <= 0 || !xyz || !conn || !adj) return fail(c, FVC_ERR_ARG, "empty mesh");
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  const int nv = c->mesh.dims == 3 ? 4 : 3;
+  // host-side validation keeps every device gather in bounds
+  for (long e = 0; e < nelem; e++) {
+    for (int k = 0; k < nv; k++) {
+      int nd = conn[4 * e + k], nb = adj[4 * e + k];
+      if (nd < 0 || nd >= nnodes) return fail(c, FVC_ERR_ARG, "element %ld: node %d out of range", e, nd);
+      if (nb < -1 || nb >= nelem) return fail(c, FVC_ERR_ARG, "element %ld: neighbour %d out of range", e, nb);
+    }
+  }
+  std::vector<int4> he(2 * (size_t)nelem);
+  for (long e = 0; e < nelem; e++) {
+    const int* n = conn + 4 * e;
+    const int* a = adj + 4 * e;
+    he[2 * e] = make_int4(n[0], n[1], n[2], nv == 4 ? n[3] : n[2]);
+    he[2 * e + 1] = make_int4(a[0], a[1], a[2], nv == 4 ? a[3] : -1);
+  }
+  std::vector<double4_32a> hn((size_t)nnodes);
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (long i = 0; i < nnodes; i++) {
+    hn[i] = make_double4_32a(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0);
+    for (int a = 0; a < 3; a++) {
+      lo[a] = fmin(lo[a], xyz[3 * i + a]);
+      hi[a] = fmax(hi[a], xyz[3 * i + a]);
+    }
+  }
+  cudaFree(c->d_elem); c->d_elem = nullptr;
+  cudaFree(c->d_geom); c->d_geom = nullptr;
+  cudaFree(c->d_nodes); c->d_nodes = nullptr;
+  cudaFree(c->d_cell_start); c->d_cell_start = nullptr;
+  cudaFree(c->d_cell_ids); c->d_cell_ids = nullptr;
+  const int gstride = c->mesh.dims == 3 ? 16 : 12;
+  if (cudaMalloc(&c->d_elem, sizeof(int4) * he.size()) != cudaSuccess ||
+      cudaMalloc(&c->d_geom, sizeof(double) * gstride * (size_t)nelem) != cudaSuccess ||
+      cudaMalloc(&c->d_nodes, sizeof(double4_32a) * hn.size()) != cudaSuccess)
+    return fail(c, FVC_ERR_OOM, "mesh allocation failed");
+  FVC_CUDA(c, cudaMemcpyAsync(c->d_elem, he.data(), sizeof(int4) * he.size(), cudaMemcpyHostToDevice, c->stream));
+  FVC_CUDA(c, cudaMemcpyAsync(c->d_nodes, hn.data(), sizeof(double4_32a) * hn.size(), cudaMemcpyHostToDevice, c->stream));
+  DevMesh& m = c->mesh;
+  m.elem = c->d_elem;
+  m.geom = c->d_geom;
+  m.nodes = c->d_nodes;
+  m.nelem = nelem;
+  m.nnodes = nnodes;
+  launch_geometry(m, c->d_geom, c->stream);
+  if ((st = check_launch(c, "geometry"))) return st;
+
+  // Uniform bucket grid over the mesh's bounding box, about two elements per
+  // cell, for the lowest-id global search.
+  BucketGrid& g = c->grid;
+  int dims = m.dims;
+  double ext[3], vol = 1.0;
+  for (int a = 0; a < 3; a++) {
+    double pad = 1e-6 * fmax(hi[a] - lo[a], 1e-300) + 1e-300;
+    g.lo[a] = lo[a] - pad;
+    ext[a] = (hi[a] + pad) - g.lo[a];
+    if (a < dims) vol *= ext[a];
+  }
+  double cell = pow(vol / fmax(1.0, nelem / 2.0), 1.0 / dims);
+  long ncells = 1;
+  for (int a = 0; a < 3; a++) {
+    if (a >= dims) {
+      g.n[a] = 1;
+      g.inv[a] = 0.0;
+      continue;
+    }
+    long na = (long)ceil(ext[a] / cell);
+    na = na < 1 ? 1 : (na > 4096 ? 4096 : na);
+    g.n[a] = (int)na;
+    g.inv[a] = (double)na / ext[a];
+    ncells *= na;
+  }
+  if (ncells > (1L << 26)) return fail(c, FVC_ERR_ARG, "bucket grid too large");
+  int* d_count = nullptr;
+  long long* d_tmp = nullptr;
+  if (cudaMalloc(&c->d_cell_start, sizeof(int) * (ncells + 1)) != cudaSuccess ||
+      cudaMalloc(&d_count, sizeof(int) * ncells) != cudaSuccess ||
+      cudaMalloc(&d_tmp, sizeof(long long) * (ncells / 1024 + 8)) != cudaSuccess) {
+    cudaFree(d_count);
+    cudaFree(d_tmp);
+    return fail(c, FVC_ERR_OOM, "bucket grid allocation failed");
+  }
+  bucket_count(m, g, d_count, (int)ncells, nullptr, c->stream);
+  scan_counts(d_count, c->d_cell_start, (int)ncells, d_tmp, c->stream);
+  int total = 0;
+  FVC_CUDA(c, cudaMemcpyAsync(&total, c->d_cell_start + ncells, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (total < 0 || cudaMalloc(&c->d_cell_ids, sizeof(int) * ((size_t)total + 1)) != cudaSuccess) {
+    cudaFree(d_count);
+    cudaFree(d_tmp);
+    return fail(c, FVC_ERR_OOM, "bucket list allocation failed (%d entries)", total);
+  }
+  g.start = c->d_cell_start;
+  g.ids = c->d_cell_ids;
+  bucket_fill(m, g, c->d_cell_start, d_count, c->d_cell_ids, (int)ncells, nullptr, c->stream);
+  if ((st = check_launch(c, "bucket grid"))) return st;
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  cudaFree(d_count);
+  cudaFree(d_tmp);
+  if (c->frame_nodes && c->frame_nodes != nnodes) {
+    for (auto& kv : c->frames) cudaFree(kv.second);
+    c->frames.clear();
+  }
+  c->frame_nodes = nnodes;
+  c->mesh_set = true;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_set_bounds(fvc_ctx* c, const double b[6]) {
+  if (!c || !b) return FVC_ERR_ARG;
+  for (int i = 0; i < 6; i++) c->mesh.bounds[i] = b[i];
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_set_integrator(fvc_ctx* c, int int_type, double h, int extrapolate) {
+  if (!c) return FVC_ERR_ARG;
+  if (int_type != 0 && int_type != 1 && int_type != 3)
+    return fail(c, FVC_ERR_ARG, "Int_Type %d not supported (0 Euler, 1 RK4, 3 AB2)", int_type);
+  if (!(h > 0)) return fail(c, FVC_ERR_ARG, "Int_TimeStep must be positive");
+  c->integ.type = int_type;
+  c->integ.h = h;
+  c->integ.extrapolate = extrapolate ? 1 : 0;
+  c->integ_set = true;
+  return FVC_OK;
+}
+
+// ---------------------------------------------------------------- frames
+
+extern "C" fvc_status fvc_upload_frame(fvc_ctx* c, int frame_id, const double* uvw) {
+  if (!c || !uvw) return FVC_ERR_ARG;
+  if (!c->mesh_set) return fail(c, FVC_ERR_STATE, "set the mesh before uploading frames");
+  if (frame_id < 0 || frame_id >= 65536) return fail(c, FVC_ERR_ARG, "frame id %d out of range", frame_id);
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  long n = c->frame_nodes;
+  if (!c->d_stage && cudaMalloc(&c->d_stage, sizeof(double) * 3 * (size_t)n) != cudaSuccess)
+    return fail(c, FVC_ERR_OOM, "frame staging allocation failed");
+  double4_32a*& dst = c->frames[frame_id];
+  if (!dst && cudaMalloc(&dst, sizeof(double4_32a) * (size_t)n) != cudaSuccess) {
+    c->frames.erase(frame_id);
+    return fail(c, FVC_ERR_OOM, "frame allocation failed");
+  }
+  FVC_CUDA(c, cudaMemcpyAsync(c->d_stage, uvw, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  pack_frame(c->d_stage, dst, n, c->stream);
+  if ((st = check_launch(c, "pack_frame"))) return st;
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_set_window(fvc_ctx* c, int lo, int hi, double tmin, double tmax) {
+  if (!c) return FVC_ERR_ARG;
+  auto a = c->frames.find(lo), b = c->frames.find(hi);
+  if (a == c->frames.end() || b == c->frames.end())
+    return fail(c, FVC_ERR_STATE, "frames %d / %d are not resident", lo, hi);
+  c->window.f0 = a->second;
+  c->window.f1 = b->second;
+  c->window.tmin = tmin;
+  c->window.tmax = tmax;
+  c->window.nslots = 0;
+  c->window_set = true;
+  return FVC_OK;
+}
+
+// The stage times of an advection call from t1 to t2, computed with the
+// integrators' own arithmetic (ompVC/integration.c:345-352, 402), and, on an
+// unstructured mesh, the node velocities at each of them.  A slot is only a
+// hint: the kernels compare its time with the time they compute before using
+// it, so the table can end early (slot cap, tloc out of range) without
+// changing any result.
+static fvc_status prepare_slots(fvc_ctx* c, double t1, double t2) {
+  DevWindow& w = c->window;
+  w.nslots = 0;
+  int n = 0;
+  auto add = [&](double tq) {
+    if (n >= FVC_MAX_SLOTS) return false;
+    double tloc = (tq - w.tmin) / (w.tmax - w.tmin);
+    if ((tloc > 1 + 1.0e-10) || (tloc < 0 - 1.0e-10)) return false;
+    w.tq[n] = tq;
+    w.tl[n] = tloc;
+    n++;
+    return true;
+  };
+  double tc = t1, h = (t2 - t1) >= 0.0 ? fabs(c->integ.h) : -fabs(c->integ.h);
+  bool ok = true;
+  while ((tc - t2) * (t2 - t1) < 0.0) {
+    if ((tc + h - t2) * (tc + h - t1) > 0.0) h = (t2 - t1) >= 0.0 ? fabs(t2 - tc) : -fabs(t2 - tc);
+    if (!add(tc) || !add(tc + h / 2)) {
+      ok = false;
+      break;
+    }
+    tc = tc + h;
+  }
+  if (ok) add(tc);
+  w.nslots = n;
+  if (c->mesh.mesh_type != 1 || n == 0) return FVC_OK;
+  if (n > c->vt_slots) {
+    cudaFree(c->d_vt);
+    c->d_vt = nullptr;
+    c->vt_slots = 0;
+    if (cudaMalloc(&c->d_vt, sizeof(double4_32a) * (size_t)n * (size_t)c->mesh.nnodes) != cudaSuccess) {
+      w.nslots = 0;  // run without the table
+      return FVC_OK;
+    }
+    c->vt_slots = n;
+  }
+  w.vt = c->d_vt;
+  w.vt_stride = c->mesh.nnodes;
+  time_fields(c->mesh, w, c->d_vt, c->stream);
+  return check_launch(c, "time fields");
+}
+
+static fvc_status ready(fvc_ctx* c, bool need_window) {
+  if (!c) return FVC_ERR_ARG;
+  if (!c->mesh_set) return fail(c, FVC_ERR_STATE, "mesh not set");
+  if (need_window && !c->window_set) return fail(c, FVC_ERR_STATE, "frame window not set");
+  return use_device(c);
+}
+
+// ---------------------------------------------------------------- step level
+
+extern "C" fvc_status fvc_advect_device(fvc_ctx* c, int n, double* dX, double* dV, int* deid,
+                                        int* dleft, double* dldt, double t0, double t1, long long* steps) {
+  fvc_status st;
+  if ((st = ready(c, true))) return st;
+  if (n < 0 || (n > 0 && (!dX || !dleft || !dldt))) return fail(c, FVC_ERR_ARG, "bad arrays");
+  if (c->mesh.mesh_type == 1 && n > 0 && !deid) return fail(c, FVC_ERR_ARG, "unstructured advection needs element ids");
+  if (c->integ.extrapolate && n > 0 && !dV) return fail(c, FVC_ERR_ARG, "extrapolation needs V");
+  if ((st = prepare_slots(c, t0, t1))) return st;
+  launch_advect(c->mesh, c->window, c->integ, n, dX, dV, deid, dleft, dldt, t0, t1, c->d_ctr, c->stream);
+  if ((st = check_launch(c, "advect"))) return st;
+  return finish(c, "advect", steps);
+}
+
+extern "C" fvc_status fvc_advect(fvc_ctx* c, int n, double* X, double* V, int* eid, int* left,
+                                 double* ldt, double t0, double t1, long long* steps) {
+  fvc_status st;
+  if ((st = ready(c, true))) return st;
+  if (n < 0 || (n > 0 && (!X || !left || !ldt))) return fail(c, FVC_ERR_ARG, "bad arrays");
+  if (steps) *steps = 0;
+  if (n == 0) return FVC_OK;
+  size_t bx = al256(sizeof(double) * 3 * (size_t)n), bi = al256(sizeof(int) * (size_t)n),
+         bd = al256(sizeof(double) * (size_t)n);
+  if ((st = ensure_scratch(c, 2 * bx + 2 * bi + bd))) return st;
+  char* p = (char*)c->d_scratch;
+  double* dX = (double*)p; p += bx;
+  double* dV = (double*)p; p += bx;
+  int* de = (int*)p; p += bi;
+  int* dl = (int*)p; p += bi;
+  double* dt = (double*)p;
+  cudaStream_t s = c->stream;
+  FVC_CUDA(c, cudaMemcpyAsync(dX, X, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  if (V) FVC_CUDA(c, cudaMemcpyAsync(dV, V, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  if (eid) FVC_CUDA(c, cudaMemcpyAsync(de, eid, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  FVC_CUDA(c, cudaMemcpyAsync(dl, left, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  FVC_CUDA(c, cudaMemcpyAsync(dt, ldt, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  if (c->mesh.mesh_type == 1 && !eid) return fail(c, FVC_ERR_ARG, "unstructured advection needs element ids");
+  if (c->integ.extrapolate && !V) return fail(c, FVC_ERR_ARG, "extrapolation needs V");
+  if ((st = prepare_slots(c, t0, t1))) return st;
+  launch_advect(c->mesh, c->window, c->integ, n, dX, V ? dV : nullptr, eid ? de : nullptr, dl, dt, t0,
+                t1, c->d_ctr, s);
+  if ((st = check_launch(c, "advect"))) return st;
+  FVC_CUDA(c, cudaMemcpyAsync(X, dX, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+  if (V) FVC_CUDA(c, cudaMemcpyAsync(V, dV, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+  if (eid) FVC_CUDA(c, cudaMemcpyAsync(eid, de, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  FVC_CUDA(c, cudaMemcpyAsync(left, dl, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  FVC_CUDA(c, cudaMemcpyAsync(ldt, dt, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  return finish(c, "advect", steps);
+}
+
+extern "C" fvc_status fvc_velocity(fvc_ctx* c, int n, const double* X, int* eid, int* left, double tq,
+                                   double* out) {
+  fvc_status st;
+  if ((st = ready(c, true))) return st;
+  if (n < 0 || (n > 0 && (!X || !left || !out))) return fail(c, FVC_ERR_ARG, "bad arrays");
+  if (c->mesh.mesh_type == 1 && n > 0 && !eid) return fail(c, FVC_ERR_ARG, "unstructured velocity needs element ids");
+  if (n == 0) return FVC_OK;
+  size_t bx = al256(sizeof(double) * 3 * (size_t)n), bi = al256(sizeof(int) * (size_t)n);
+  if ((st = ensure_scratch(c, 2 * bx + 2 * bi))) return st;
+  char* p = (char*)c->d_scratch;
+  double* dX = (double*)p; p += bx;
+  double* dO = (double*)p; p += bx;
+  int* de = (int*)p; p += bi;
+  int* dl = (int*)p;
+  cudaStream_t s = c->stream;
+  FVC_CUDA(c, cudaMemcpyAsync(dX, X, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  if (eid) FVC_CUDA(c, cudaMemcpyAsync(de, eid, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  FVC_CUDA(c, cudaMemcpyAsync(dl, left, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  launch_velocity(c->mesh, c->window, n, dX, eid ? de : nullptr, dl, tq, dO, c->d_ctr, s);
+  if ((st = check_launch(c, "velocity"))) return st;
+  FVC_CUDA(c, cudaMemcpyAsync(out, dO, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+  if (eid) FVC_CUDA(c, cudaMemcpyAsync(eid, de, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  FVC_CUDA(c, cudaMemcpyAsync(left, dl, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  return finish(c, "velocity", nullptr);
+}
+
+extern "C" fvc_status fvc_local_search(fvc_ctx* c, int n, const double* X, const int* guess, int* out) {
+  fvc_status st;
+  if ((st = ready(c, false))) return st;
+  if (c->mesh.mesh_type != 1) return fail(c, FVC_ERR_STATE, "local search needs an unstructured mesh");
+  if (n < 0 || (n > 0 && (!X || !guess || !out))) return fail(c, FVC_ERR_ARG, "bad arrays");
+  if (n == 0) return FVC_OK;
+  size_t bx = al256(sizeof(double) * 3 * (size_t)n), bi = al256(sizeof(int) * (size_t)n);
+  if ((st = ensure_scratch(c, bx + 2 * bi))) return st;
+  char* p = (char*)c->d_scratch;
+  double* dX = (double*)p; p += bx;
+  int* dg = (int*)p; p += bi;
+  int* dO = (int*)p;
+  cudaStream_t s = c->stream;
+  FVC_CUDA(c, cudaMemcpyAsync(dX, X, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  FVC_CUDA(c, cudaMemcpyAsync(dg, guess, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  launch_local_search(c->mesh, n, dX, dg, dO, c->d_ctr, s);
+  if ((st = check_launch(c, "local search"))) return st;
+  FVC_CUDA(c, cudaMemcpyAsync(out, dO, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  return finish(c, "local search", nullptr);
+}
+
+extern "C" fvc_status fvc_global_search(fvc_ctx* c, int n, const double* X, int* out) {
+  fvc_status st;
+  if ((st = ready(c, false))) return st;
+  if (c->mesh.mesh_type != 1) return fail(c, FVC_ERR_STATE, "global search needs an unstructured mesh");
+  if (n < 0 || (n > 0 && (!X || !out))) return fail(c, FVC_ERR_ARG, "bad arrays");
+  if (n == 0) return FVC_OK;
+  size_t bx = al256(sizeof(double) * 3 * (size_t)n), bi = al256(sizeof(int) * (size_t)n);
+  if ((st = ensure_scratch(c, bx + bi))) return st;
+  char* p = (char*)c->d_scratch;
+  double* dX = (double*)p; p += bx;
+  int* dO = (int*)p;
+  cudaStream_t s = c->stream;
+  FVC_CUDA(c, cudaMemcpyAsync(dX, X, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  launch_global_search(c->mesh, c->grid, n, dX, nullptr, dO, s);
+  if ((st = check_launch(c, "global search"))) return st;
+  FVC_CUDA(c, cudaMemcpyAsync(out, dO, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  return finish(c, "global search", nullptr);
+}
+
+// ---------------------------------------------------------------- jobs
+
+extern "C" void fvc_job_destroy(fvc_job* j) {
+  if (!j) return;
+  if (j->ctx) {
+    cudaSetDevice(j->ctx->device);
+    cudaStreamSynchronize(j->ctx->stream);
+  }
+  cudaFree(j->mem);
+  for (int k = 0; k < 4; k++)
+    if (j->ev[k]) cudaEventDestroy(j->ev[k]);
+  delete j;
+}
+
+extern "C" fvc_status fvc_job_get_stats(fvc_job* j, fvc_job_stats* out) {
+  if (!j || !out) return FVC_ERR_ARG;
+  *out = j->stats;
+  return FVC_OK;
+}
+
+extern "C" void* fvc_stream(fvc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+// Carves one allocation into the arrays listed in sizes (bytes each).
+static fvc_status carve(fvc_ctx* c, void** mem, std::vector<std::pair<void**, size_t>> parts) {
+  size_t total = 0;
+  for (auto& p : parts) total += al256(p.second);
+  if (cudaMalloc(mem, total ? total : 256) != cudaSuccess)
+    return fail(c, FVC_ERR_OOM, "could not allocate %zu bytes for the job", total);
+  char* q = (char*)*mem;
+  for (auto& p : parts) {
+    *p.first = q;
+    q += al256(p.second);
+  }
+  return FVC_OK;
+}
+
+static fvc_status run_chain(fvc_ctx* c, const ChainArgs& a, const double* dX, const int* dleft0, int* deid,
+                            long long* launches) {
+  size_t words = 4 * (size_t)a.n + 2 * ((size_t)a.res[0] * a.res[1] + 1) + 2 * ((size_t)a.res[0] + 1) +
+                 2 * ((size_t)a.n / 1024 + 2) + 16;
+  int* work = nullptr;
+  if (cudaMalloc(&work, sizeof(int) * words) != cudaSuccess) return fail(c, FVC_ERR_OOM, "seed-chain scratch");
+  int rounds = locate_chain(c->mesh, c->grid, a, dX, dleft0, deid, work, c->d_ctr, c->stream);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(work);
+  if (rounds < 0) {
+    fvc_status st = finish(c, "seed location", nullptr);
+    return st ? st : fail(c, FVC_ERR_CUDA, "seed location failed");
+  }
+  // global search + first-found, then per round the guess kernels and the walk
+  *launches += 2 + (long long)rounds * (a.kind == 0 ? 6 : 4);
+  return FVC_OK;
+}
+
+static int center_element(fvc_ctx* c, const double X[3]) {
+  double* dX = nullptr;
+  int* dO = nullptr;
+  int r = -1;
+  if (cudaMalloc(&dX, 3 * sizeof(double)) != cudaSuccess || cudaMalloc(&dO, sizeof(int)) != cudaSuccess) {
+    cudaFree(dX);
+    return -2;
+  }
+  cudaMemcpyAsync(dX, X, 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  launch_global_search(c->mesh, c->grid, 1, dX, nullptr, dO, c->stream);
+  cudaMemcpyAsync(&r, dO, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) r = -2;
+  cudaFree(dX);
+  cudaFree(dO);
+  return r;
+}
+
+extern "C" fvc_status fvc_ftle_create(fvc_ctx* c, const fvc_ftle_spec* sp, fvc_job** out) {
+  fvc_status st;
+  if (!out || !sp) return fail(c, FVC_ERR_ARG, "null argument");
+  *out = nullptr;
+  if ((st = ready(c, false))) return st;
+  int dims = c->mesh.dims;
+  int xr = sp->xres, yr = sp->yres, zr = dims == 3 ? sp->zres : 1;
+  if (xr < 2 || yr < 2 || (dims == 3 && zr < 2) || zr < 1) return fail(c, FVC_ERR_ARG, "FTLE grid resolution too small");
+  long n = (long)xr * yr * zr;
+  if (n > (1L << 30)) return fail(c, FVC_ERR_ARG, "FTLE grid too large");
+  fvc_job* j = new fvc_job();
+  j->ctx = c;
+  j->kind = 0;
+  FtleDev& f = j->f;
+  f.n = (int)n;
+  f.xr = xr;
+  f.yr = yr;
+  f.zr = zr;
+  // FTLE_CartMesh deltas, ompVC/parameters.c:311-320
+  f.dx = (sp->xmax - sp->xmin) / (xr - 1);
+  f.dy = (sp->ymax - sp->ymin) / (yr - 1);
+  f.dz = dims == 3 ? (sp->zmax - sp->zmin) / (zr - 1) : 0.0;
+  f.start = sp->start_time;
+  int* left0 = nullptr;
+  st = carve(c, &j->mem,
+             {{(void**)&f.X, 24 * n}, {(void**)&f.V, 24 * n}, {(void**)&f.ldt, 8 * n}, {(void**)&f.ftT, 8 * n},
+              {(void**)&f.ftN, 8 * n}, {(void**)&f.eid, 4 * n}, {(void**)&f.left, 4 * n}, {(void**)&f.have, 4 * n},
+              {(void**)&f.Xn, 24 * n}, {(void**)&f.Vn, 24 * n}, {(void**)&f.te, 8 * n}, {(void**)&f.en, 4 * n},
+              {(void**)&f.flag, n}, {(void**)&f.served, 4 * n}, {(void**)&f.trig, 4 * n}, {(void**)&f.out, 16 * n},
+              {(void**)&f.epos, 168 * n}, {(void**)&f.elt, 48 * n}, {(void**)&f.emt, 8 * n},
+              {(void**)&left0, 4 * n}});
+  if (st) {
+    delete j;
+    return st;
+  }
+  job_events(j);
+  cudaEventRecord(j->ev[3], c->stream);
+  if (sp->generate) {
+    double zmin = dims == 3 ? sp->zmin : 0.0;
+    ftle_seed_grid(c->mesh, f, sp->xmin, sp->ymin, zmin, left0, c->stream);
+    if ((st = check_launch(c, "ftle seed"))) { fvc_job_destroy(j); return st; }
+    if (c->mesh.mesh_type == 1) {
+      // centre seed, ompVC/ftle.c:457-465
+      double Xs[3] = {sp->xmin + ((int)(xr / 2)) * f.dx, sp->ymin + ((int)(yr / 2)) * f.dy,
+                      zmin + ((int)(zr / 2)) * f.dz};
+      int center = center_element(c, Xs);
+      if (center < -1) { fvc_job_destroy(j); return fail(c, FVC_ERR_CUDA, "centre search failed"); }
+      ChainArgs a{0, (int)n, {xr, yr, zr}, sp->local_search_checking, center};
+      j->stats.launches += 1;
+      if ((st = run_chain(c, a, f.X, left0, f.eid, &j->stats.launches))) { fvc_job_destroy(j); return st; }
+    }
+    ftle_init_marks(c->mesh, f, left0, c->stream);
+    ftle_mark_outside(f, c->stream);
+    j->stats.launches += 3;
+    if ((st = check_launch(c, "ftle marks"))) { fvc_job_destroy(j); return st; }
+  }
+  cudaEventRecord(j->ev[0], c->stream);
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  j->stats.ms_setup += ev_ms(j->ev[3], j->ev[0]);
+  *out = j;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_ftle_set_state(fvc_job* j, const double* X, const int* eid, const int* left,
+                                         const double* ldt, const int* have, const double* wT, const double* wN) {
+  if (!j || j->kind != 0) return FVC_ERR_ARG;
+  fvc_ctx* c = j->ctx;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  FtleDev& f = j->f;
+  size_t n = (size_t)f.n;
+  cudaStream_t s = c->stream;
+  if (X) FVC_CUDA(c, cudaMemcpyAsync(f.X, X, 24 * n, cudaMemcpyHostToDevice, s));
+  if (eid) {
+    std::vector<int> chk(eid, eid + n);
+    for (size_t i = 0; i < n; i++)
+      if (chk[i] >= c->mesh.nelem && c->mesh.mesh_type == 1) return fail(c, FVC_ERR_ARG, "element id out of range");
+    FVC_CUDA(c, cudaMemcpyAsync(f.eid, eid, 4 * n, cudaMemcpyHostToDevice, s));
+  }
+  if (left) FVC_CUDA(c, cudaMemcpyAsync(f.left, left, 4 * n, cudaMemcpyHostToDevice, s));
+  if (ldt) FVC_CUDA(c, cudaMemcpyAsync(f.ldt, ldt, 8 * n, cudaMemcpyHostToDevice, s));
+  if (have) FVC_CUDA(c, cudaMemcpyAsync(f.have, have, 4 * n, cudaMemcpyHostToDevice, s));
+  if (wT) FVC_CUDA(c, cudaMemcpyAsync(f.ftT, wT, 8 * n, cudaMemcpyHostToDevice, s));
+  if (wN) FVC_CUDA(c, cudaMemcpyAsync(f.ftN, wN, 8 * n, cudaMemcpyHostToDevice, s));
+  FVC_CUDA(c, cudaMemsetAsync(f.V, 0, 24 * n, s));
+  FVC_CUDA(c, cudaStreamSynchronize(s));
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_ftle_get_state(fvc_job* j, double* X, int* eid, int* left, double* ldt, int* have,
+                                         double* wT, double* wN) {
+  if (!j || j->kind != 0) return FVC_ERR_ARG;
+  fvc_ctx* c = j->ctx;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  FtleDev& f = j->f;
+  size_t n = (size_t)f.n;
+  cudaStream_t s = c->stream;
+  if (X) FVC_CUDA(c, cudaMemcpyAsync(X, f.X, 24 * n, cudaMemcpyDeviceToHost, s));
+  if (eid) FVC_CUDA(c, cudaMemcpyAsync(eid, f.eid, 4 * n, cudaMemcpyDeviceToHost, s));
+  if (left) FVC_CUDA(c, cudaMemcpyAsync(left, f.left, 4 * n, cudaMemcpyDeviceToHost, s));
+  if (ldt) FVC_CUDA(c, cudaMemcpyAsync(ldt, f.ldt, 8 * n, cudaMemcpyDeviceToHost, s));
+  if (have) FVC_CUDA(c, cudaMemcpyAsync(have, f.have, 4 * n, cudaMemcpyDeviceToHost, s));
+  if (wT) FVC_CUDA(c, cudaMemcpyAsync(wT, f.ftT, 8 * n, cudaMemcpyDeviceToHost, s));
+  if (wN) FVC_CUDA(c, cudaMemcpyAsync(wN, f.ftN, 8 * n, cudaMemcpyDeviceToHost, s));
+  FVC_CUDA(c, cudaStreamSynchronize(s));
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, double t2, long long* steps) {
+  if (!j || j->kind != 0) return FVC_ERR_ARG;
+  fvc_ctx* c = j->ctx;
+  fvc_status st;
+  if ((st = ready(c, true))) return st;
+  cudaStream_t s = c->stream;
+  job_events(j);
+  if ((st = prepare_slots(c, t1, t2))) return st;
+  if (launch) ftle_launch(c->mesh, c->window, j->f, j->f.start, c->d_ctr, s);
+  cudaEventRecord(j->ev[0], s);
+  ftle_pass1(c->mesh, c->window, c->integ, j->f, t1, t2, c->d_ctr, s);
+  cudaEventRecord(j->ev[1], s);
+  if (!c->integ.extrapolate) {
+    ftle_triggers(j->f, c->d_ctr, s);
+    ftle_early(c->mesh, c->window, c->integ, j->f, t1, c->d_ctr, s);
+  }
+  cudaEventRecord(j->ev[2], s);
+  ftle_update(c->mesh, c->integ, j->f, s);
+  if ((st = check_launch(c, "ftle interval"))) return st;
+  DevCounters h{};
+  st = finish(c, "ftle interval", steps, &h);
+  j->stats.intervals++;
+  j->stats.launches += (launch ? 1 : 0) + 1 + (c->integ.extrapolate ? 0 : 5) + 1 + (c->mesh.mesh_type == 1 ? 1 : 0);
+  j->stats.steps_main += (long long)h.steps;
+  j->stats.steps_early += (long long)h.steps_early;
+  j->stats.ms_main += ev_ms(j->ev[0], j->ev[1]);
+  j->stats.ms_early += ev_ms(j->ev[1], j->ev[2]);
+  return st;
+}
+
+extern "C" fvc_status fvc_ftle_reduce(fvc_job* j, double int_t, double* wT, double* wN) {
+  if (!j || j->kind != 0) return FVC_ERR_ARG;
+  fvc_ctx* c = j->ctx;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  job_events(j);
+  cudaEventRecord(j->ev[0], c->stream);
+  ftle_final(j->f, c->mesh.dims, int_t, c->stream);
+  cudaEventRecord(j->ev[1], c->stream);
+  if ((st = check_launch(c, "ftle reduce"))) return st;
+  size_t n = (size_t)j->f.n;
+  if (wT) FVC_CUDA(c, cudaMemcpyAsync(wT, j->f.out, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  if (wN) FVC_CUDA(c, cudaMemcpyAsync(wN, j->f.out + n, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  j->stats.ms_reduce += ev_ms(j->ev[0], j->ev[1]);
+  j->stats.launches += 1;
+  return FVC_OK;
+}
+
+// ---------------------------------------------------------------- tracers
+
+extern "C" fvc_status fvc_tracer_create(fvc_ctx* c, const fvc_tracer_spec* sp, int n, const double* seeds,
+                                        fvc_job** out) {
+  fvc_status st;
+  if (!out || !sp) return fail(c, FVC_ERR_ARG, "null argument");
+  *out = nullptr;
+  if ((st = ready(c, false))) return st;
+  if (n < 0 || (n > 0 && !seeds)) return fail(c, FVC_ERR_ARG, "bad seed array");
+  fvc_job* j = new fvc_job();
+  j->ctx = c;
+  j->kind = 1;
+  TracerDev& t = j->t;
+  t.n = n;
+  long nn = n > 0 ? n : 1;
+  long nb = (nn + 1023) / 1024;
+  int* left0 = nullptr;
+  st = carve(c, &j->mem,
+             {{(void**)&t.X, 24 * nn}, {(void**)&t.V, 24 * nn}, {(void**)&t.ldt, 8 * nn}, {(void**)&t.eid, 4 * nn},
+              {(void**)&t.left, 4 * nn}, {(void**)&t.outX, 24 * nn},
+              {(void**)&t.block_cnt, sizeof(int) * (2 * nb + 16) + sizeof(long long) * (nb / 1024 + 8)},
+              {(void**)&left0, 4 * nn}});
+  if (st) {
+    delete j;
+    return st;
+  }
+  cudaStream_t s = c->stream;
+  if (n > 0) {
+    FVC_CUDA(c, cudaMemcpyAsync(t.X, seeds, 24 * (size_t)n, cudaMemcpyHostToDevice, s));
+    outside_domain_flags(c->mesh, n, t.X, left0, s);
+    FVC_CUDA(c, cudaMemsetAsync(t.eid, 0xff, 4 * (size_t)n, s));
+    if (c->mesh.mesh_type == 1) {
+      int center = -1;
+      if (sp->seed_chain == 1) {
+        center = center_element(c, sp->center);
+        if (center < -1) { fvc_job_destroy(j); return fail(c, FVC_ERR_CUDA, "centre search failed"); }
+      }
+      ChainArgs a{sp->seed_chain == 1 ? 2 : 1, n, {n, 1, 1}, sp->local_search_checking, center};
+      if (sp->seed_chain == 1) j->stats.launches += 1;
+      if ((st = run_chain(c, a, t.X, left0, t.eid, &j->stats.launches))) { fvc_job_destroy(j); return st; }
+    }
+    tracer_init_marks(c->mesh, t, left0, sp->seed_chain, s);
+    j->stats.launches += 2;
+    if ((st = check_launch(c, "tracer init"))) { fvc_job_destroy(j); return st; }
+    FVC_CUDA(c, cudaStreamSynchronize(s));
+  }
+  *out = j;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_tracer_launch(fvc_job* j, double t_start) {
+  if (!j || j->kind != 1) return FVC_ERR_ARG;
+  fvc_ctx* c = j->ctx;
+  fvc_status st;
+  if ((st = ready(c, true))) return st;
+  tracer_launch_vel(c->mesh, c->window, j->t, t_start, c->d_ctr, c->stream);
+  if ((st = check_launch(c, "tracer launch"))) return st;
+  j->stats.launches += 1;
+  return finish(c, "tracer launch", nullptr);
+}
+
+extern "C" fvc_status fvc_tracer_advance(fvc_job* j, double t1, double t2, long long* steps) {
+  if (!j || j->kind != 1) return FVC_ERR_ARG;
+  fvc_ctx* c = j->ctx;
+  fvc_status st;
+  if ((st = ready(c, true))) return st;
+  job_events(j);
+  if ((st = prepare_slots(c, t1, t2))) return st;
+  cudaEventRecord(j->ev[0], c->stream);
+  tracer_advance(c->mesh, c->window, c->integ, j->t, t1, t2, c->d_ctr, c->stream);
+  cudaEventRecord(j->ev[1], c->stream);
+  if ((st = check_launch(c, "tracer advance"))) return st;
+  DevCounters h{};
+  st = finish(c, "tracer advance", steps, &h);
+  j->stats.intervals++;
+  j->stats.launches += 1;
+  j->stats.steps_main += (long long)h.steps;
+  j->stats.ms_main += ev_ms(j->ev[0], j->ev[1]);
+  return st;
+}
+
+extern "C" fvc_status fvc_tracer_snapshot(fvc_job* j, int always, double* X_out, long long* count) {
+  if (!j || j->kind != 1 || !count) return FVC_ERR_ARG;
+  fvc_ctx* c = j->ctx;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  tracer_compact(j->t, always, c->d_ctr, c->stream);
+  if ((st = check_launch(c, "tracer snapshot"))) return st;
+  j->stats.launches += 5;
+  int cnt = 0;
+  FVC_CUDA(c, cudaMemcpyAsync(&cnt, &c->d_ctr->count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  *count = cnt;
+  if (X_out && cnt > 0)
+    FVC_CUDA(c, cudaMemcpyAsync(X_out, j->t.outX, 24 * (size_t)cnt, cudaMemcpyDeviceToHost, c->stream));
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_tracer_get_state(fvc_job* j, double* X, int* eid, int* left, double* ldt) {
+  if (!j || j->kind != 1) return FVC_ERR_ARG;
+  fvc_ctx* c = j->ctx;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  size_t n = (size_t)j->t.n;
+  cudaStream_t s = c->stream;
+  if (n == 0) return FVC_OK;
+  if (X) FVC_CUDA(c, cudaMemcpyAsync(X, j->t.X, 24 * n, cudaMemcpyDeviceToHost, s));
+  if (eid) FVC_CUDA(c, cudaMemcpyAsync(eid, j->t.eid, 4 * n, cudaMemcpyDeviceToHost, s));
+  if (left) FVC_CUDA(c, cudaMemcpyAsync(left, j->t.left, 4 * n, cudaMemcpyDeviceToHost, s));
+  if (ldt) FVC_CUDA(c, cudaMemcpyAsync(ldt, j->t.ldt, 8 * n, cudaMemcpyDeviceToHost, s));
+  FVC_CUDA(c, cudaStreamSynchronize(s));
+  return FVC_OK;
+}

@@ -1,0 +1,613 @@
+// fvc_device.cuh -- device-side FP64 interpolation, point location and
+// integrators of the flowVC advection path.
+//
+// Every expression keeps the operation order of the ompVC routine cited
+// beside it, and this file is compiled with --fmad=false, so each multiply
+// and add is rounded on its own exactly as gcc -O3 does on x86-64: element
+// ids, exit flags and positions come out bit-identical to ompVC.
+//
+// Layout in HBM (see fvc_state.h):
+//   elements  int4 pairs {nodes, neighbours}   32 B per element, one sector
+//   geometry  per element the natural-coordinate map (a11..a33, V, x0, y0,
+//             z0) precomputed once from the node coordinates; recomputing
+//             it gives the same doubles, so precomputing changes no bit
+//   frames    double4_32a (u, v, w, 0) per node, one 32 B sector per gather
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fvc_state.h"
+
+namespace fvc {
+
+#define FVC_TINY 1.0e-10
+
+struct Pt {
+  double X[3];
+  double V[3];
+  int eid;
+  int left;
+  double ldt;
+};
+
+__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
+__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double dsign(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
+
+// TestOutsideDomain, ompVC/velocity.c:654-669
+__device__ __forceinline__ int outside_domain(const DevMesh& m, const double X[3]) {
+  if (X[0] < (m.bounds[0] - FVC_TINY) || X[0] > (m.bounds[1] + FVC_TINY)) return 1;
+  if (X[1] < (m.bounds[2] - FVC_TINY) || X[1] > (m.bounds[3] + FVC_TINY)) return 1;
+  if (X[2] < (m.bounds[4] - FVC_TINY) || X[2] > (m.bounds[5] + FVC_TINY)) return 1;
+  return 0;
+}
+
+// ------------------------------------------------------------------ Cartesian
+
+// TestOutsideCartVelDomain, ompVC/velocity.c:624-651
+template <int DIMS>
+__device__ __forceinline__ int outside_cart_grid(const DevMesh& m, const double X[3]) {
+  int imin = (int)floor((X[0] - m.xmin) / m.dx);
+  int jmin = (int)floor((X[1] - m.ymin) / m.dy);
+  int kmin = DIMS == 3 ? (int)floor((X[2] - m.zmin) / m.dz) : 0;
+  int imax = (int)ceil((X[0] - m.xmin) / m.dx);
+  int jmax = (int)ceil((X[1] - m.ymin) / m.dy);
+  int kmax = DIMS == 3 ? (int)ceil((X[2] - m.zmin) / m.dz) : 0;
+  return imin < 0 || imax > (m.xres - 1) || jmin < 0 || jmax > (m.yres - 1) || kmin < 0 ||
+         kmax > (m.zres - 1);
+}
+
+// one 32-byte node record as two read-only 16-byte loads
+__device__ __forceinline__ double4_32a ldf(const double4_32a* p) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+  double2 a = __ldg(q), b = __ldg(q + 1);
+  return make_double4_32a(a.x, a.y, b.x, b.y);
+}
+
+// GetVelocity_Cartesian, ompVC/velocity.c:257-457.  The 16 space-time
+// weights and the summation order f0000*V16 + ... + f1111*V1 are the
+// reference's.  In 2D the reference's zloc is 0, so the eight weights with a
+// zloc factor are exactly zero and adding their zero products leaves every
+// partial sum unchanged; the 2D branch skips them.
+// tloc of a query time (ompVC/velocity.c:275-277): from the slot table when
+// the query is a tabulated stage time, else computed and range-checked.
+__device__ __forceinline__ bool slot_hit(const DevWindow& w, int slot, double tq) {
+  return slot >= 0 && slot < w.nslots && w.tq[slot] == tq;
+}
+__device__ __forceinline__ int get_tloc(const DevWindow& w, int slot, double tq, double& tloc) {
+  if (slot_hit(w, slot, tq)) {
+    tloc = w.tl[slot];
+    return 0;
+  }
+  tloc = (tq - w.tmin) / (w.tmax - w.tmin);
+  if ((tloc > 1 + FVC_TINY) || (tloc < 0 - FVC_TINY)) return PT_ERR_TLOC;
+  return 0;
+}
+
+template <int DIMS>
+__device__ __forceinline__ int vel_cart(const DevMesh& m, const DevWindow& w, double tq, int tslot,
+                                        const double X[3], int& left, double out[3]) {
+  if (outside_cart_grid<DIMS>(m, X)) {
+    out[0] = out[1] = out[2] = 0.0;
+    left = 1;
+    return 0;
+  }
+  double tloc;
+  if (get_tloc(w, tslot, tq, tloc)) return PT_ERR_TLOC;
+  double xloc, yloc;
+  int i = (int)floor((X[0] - m.xmin) / m.dx);
+  if (i == (m.xres - 1)) {
+    i = m.xres - 2;
+    xloc = 1.0;
+  } else
+    xloc = (X[0] - m.xmin - i * m.dx) / m.dx;
+  int j = (int)floor((X[1] - m.ymin) / m.dy);
+  if (j == (m.yres - 1)) {
+    j = m.yres - 2;
+    yloc = 1.0;
+  } else
+    yloc = (X[1] - m.ymin - j * m.dy) / m.dy;
+  const long nx = m.xres, ny = m.yres;
+  const double4_32a* A = w.f0;
+  const double4_32a* B = w.f1;
+  if (DIMS == 3) {
+    double zloc;
+    int k = (int)floor((X[2] - m.zmin) / m.dz);
+    if (k == (m.zres - 1)) {
+      k = m.zres - 2;
+      zloc = 1.0;
+    } else
+      zloc = (X[2] - m.zmin - k * m.dz) / m.dz;
+    double V1 = (tloc) * (xloc) * (yloc) * (zloc);
+    double V2 = (tloc) * (xloc) * (yloc) * (1 - zloc);
+    double V3 = (tloc) * (xloc) * (1 - yloc) * (zloc);
+    double V4 = (tloc) * (xloc) * (1 - yloc) * (1 - zloc);
+    double V5 = (tloc) * (1 - xloc) * (yloc) * (zloc);
+    double V6 = (tloc) * (1 - xloc) * (yloc) * (1 - zloc);
+    double V7 = (tloc) * (1 - xloc) * (1 - yloc) * (zloc);
+    double V8 = (tloc) * (1 - xloc) * (1 - yloc) * (1 - zloc);
+    double V9 = (1 - tloc) * (xloc) * (yloc) * (zloc);
+    double V10 = (1 - tloc) * (xloc) * (yloc) * (1 - zloc);
+    double V11 = (1 - tloc) * (xloc) * (1 - yloc) * (zloc);
+    double V12 = (1 - tloc) * (xloc) * (1 - yloc) * (1 - zloc);
+    double V13 = (1 - tloc) * (1 - xloc) * (yloc) * (zloc);
+    double V14 = (1 - tloc) * (1 - xloc) * (yloc) * (1 - zloc);
+    double V15 = (1 - tloc) * (1 - xloc) * (1 - yloc) * (zloc);
+    double V16 = (1 - tloc) * (1 - xloc) * (1 - yloc) * (1 - zloc);
+    long o000 = ((long)k * ny + j) * nx + i;
+    long o100 = o000 + 1, o010 = o000 + nx, o110 = o000 + nx + 1;
+    long sk = nx * ny;
+    double4_32a a000 = ldf(A + o000), a001 = ldf(A + o000 + sk), a010 = ldf(A + o010), a011 = ldf(A + o010 + sk);
+    double4_32a a100 = ldf(A + o100), a101 = ldf(A + o100 + sk), a110 = ldf(A + o110), a111 = ldf(A + o110 + sk);
+    double4_32a b000 = ldf(B + o000), b001 = ldf(B + o000 + sk), b010 = ldf(B + o010), b011 = ldf(B + o010 + sk);
+    double4_32a b100 = ldf(B + o100), b101 = ldf(B + o100 + sk), b110 = ldf(B + o110), b111 = ldf(B + o110 + sk);
+#define FVC_CSUM(c)                                                                                \
+  (a000.c * V16 + a001.c * V15 + a010.c * V14 + a011.c * V13 + a100.c * V12 + a101.c * V11 +       \
+   a110.c * V10 + a111.c * V9 + b000.c * V8 + b001.c * V7 + b010.c * V6 + b011.c * V5 +            \
+   b100.c * V4 + b101.c * V3 + b110.c * V2 + b111.c * V1)
+    out[0] = FVC_CSUM(x);
+    out[1] = FVC_CSUM(y);
+    out[2] = FVC_CSUM(z);
+#undef FVC_CSUM
+  } else {
+    // zloc = 0: (1 - zloc) == 1 exactly, so V2 == tloc*xloc*yloc etc.
+    double V2 = (tloc) * (xloc) * (yloc);
+    double V4 = (tloc) * (xloc) * (1 - yloc);
+    double V6 = (tloc) * (1 - xloc) * (yloc);
+    double V8 = (tloc) * (1 - xloc) * (1 - yloc);
+    double V10 = (1 - tloc) * (xloc) * (yloc);
+    double V12 = (1 - tloc) * (xloc) * (1 - yloc);
+    double V14 = (1 - tloc) * (1 - xloc) * (yloc);
+    double V16 = (1 - tloc) * (1 - xloc) * (1 - yloc);
+    long o000 = (long)j * nx + i;
+    double4_32a a000 = ldf(A + o000), a010 = ldf(A + o000 + nx), a100 = ldf(A + o000 + 1), a110 = ldf(A + o000 + nx + 1);
+    double4_32a b000 = ldf(B + o000), b010 = ldf(B + o000 + nx), b100 = ldf(B + o000 + 1), b110 = ldf(B + o000 + nx + 1);
+#define FVC_CSUM2(c)                                                                               \
+  (a000.c * V16 + a010.c * V14 + a100.c * V12 + a110.c * V10 + b000.c * V8 + b010.c * V6 +         \
+   b100.c * V4 + b110.c * V2)
+    out[0] = FVC_CSUM2(x);
+    out[1] = FVC_CSUM2(y);
+    out[2] = FVC_CSUM2(z);
+#undef FVC_CSUM2
+  }
+  return 0;
+}
+
+// --------------------------------------------------------------- unstructured
+
+// One element's record: the natural-coordinate map precomputed from its node
+// coordinates (ompVC/velocity.c:497-510 and 529-535; recomputing it gives the
+// same doubles) and its node ids.
+//   3D, 16 doubles: a11 a12 a13 a21 a22 a23 a31 a32 a33 V x0 y0 z0 - | nodes
+//   2D, 12 doubles: a11 a12 a21 a22 V x0 y0 - | nodes | -
+template <int DIMS>
+struct Geo {
+  double a[DIMS == 3 ? 9 : 4];
+  double V, x0, y0, z0;
+  int4 nd;
+};
+
+template <int DIMS>
+__device__ __forceinline__ void load_geo(const DevMesh& m, int e, Geo<DIMS>& g) {
+  if (DIMS == 3) {
+    const double2* p = reinterpret_cast<const double2*>(m.geom + (long)e * 16);
+    double2 g0 = __ldg(p + 0), g1 = __ldg(p + 1), g2 = __ldg(p + 2), g3 = __ldg(p + 3);
+    double2 g4 = __ldg(p + 4), g5 = __ldg(p + 5), g6 = __ldg(p + 6);
+    g.nd = __ldg(reinterpret_cast<const int4*>(p + 7));
+    g.a[0] = g0.x; g.a[1] = g0.y; g.a[2] = g1.x; g.a[3] = g1.y; g.a[4] = g2.x;
+    g.a[5] = g2.y; g.a[6] = g3.x; g.a[7] = g3.y; g.a[8] = g4.x;
+    g.V = g4.y; g.x0 = g5.x; g.y0 = g5.y; g.z0 = g6.x;
+  } else {
+    const double2* p = reinterpret_cast<const double2*>(m.geom + (long)e * 12);
+    double2 g0 = __ldg(p + 0), g1 = __ldg(p + 1), g2 = __ldg(p + 2), g3 = __ldg(p + 3);
+    g.nd = __ldg(reinterpret_cast<const int4*>(p + 4));
+    g.a[0] = g0.x; g.a[1] = g0.y; g.a[2] = g1.x; g.a[3] = g1.y;
+    g.V = g2.x; g.x0 = g2.y; g.y0 = g3.x; g.z0 = 0.0;
+  }
+}
+
+// Natural coordinates of X (ompVC/velocity.c:512-517 and 537-542, the same in
+// ompVC/mesh.c:542-547 and 587-591); returns d, their minimum.
+template <int DIMS>
+__device__ __forceinline__ double natural_from(const Geo<DIMS>& g, const double X[3], double& r,
+                                               double& s, double& t, double& wv) {
+  if (DIMS == 3) {
+    double dx = X[0] - g.x0, dy = X[1] - g.y0, dz = X[2] - g.z0;
+    r = (g.a[0] * dx + g.a[1] * dy + g.a[2] * dz) / g.V;
+    s = (g.a[3] * dx + g.a[4] * dy + g.a[5] * dz) / g.V;
+    t = (g.a[6] * dx + g.a[7] * dy + g.a[8] * dz) / g.V;
+    wv = 1 - r - s - t;
+    return dmin(r, dmin(s, dmin(t, wv)));
+  } else {
+    double dx = X[0] - g.x0, dy = X[1] - g.y0;
+    r = (g.a[0] * dx + g.a[1] * dy) / g.V;
+    s = (g.a[2] * dx + g.a[3] * dy) / g.V;
+    t = 0;
+    wv = 1 - r - s;
+    return dmin(r, dmin(s, wv));
+  }
+}
+
+template <int DIMS>
+__device__ __forceinline__ double natural(const DevMesh& m, int e, const double X[3], double& r,
+                                          double& s, double& t, double& wv) {
+  Geo<DIMS> g;
+  load_geo<DIMS>(m, e, g);
+  return natural_from<DIMS>(g, X, r, s, t, wv);
+}
+
+// Natural coordinates computed by the last point location at the current
+// position: a walk that tests the same element at the same position gets the
+// same doubles, so the first velocity evaluation after a locate reuses them.
+struct NatCache {
+  int e;
+  int4 nd;
+  double r, s, t, w, d;
+};
+
+// The node velocities a tabulated stage evaluation interpolates, gathered
+// right after the element record so the loads overlap the containment test.
+template <int DIMS>
+struct NodeVel {
+  double u[DIMS == 3 ? 4 : 3], v[DIMS == 3 ? 4 : 3], w[DIMS == 3 ? 4 : 3];
+};
+
+template <int DIMS>
+__device__ __forceinline__ void load_slot_nodes(const DevWindow& w, int tslot, int4 nd, NodeVel<DIMS>& nv) {
+  const int ids[4] = {nd.x, nd.y, nd.z, nd.w};
+  const double* F = reinterpret_cast<const double*>(w.vt + (long)tslot * w.vt_stride);
+#pragma unroll
+  for (int c = 0; c < (DIMS == 3 ? 4 : 3); c++) {
+    const double* q = F + 4L * ids[c];
+    double2 uv = __ldg(reinterpret_cast<const double2*>(q));
+    nv.u[c] = uv.x;
+    nv.v[c] = uv.y;
+    nv.w[c] = DIMS == 3 ? __ldg(q + 2) : 0.0;
+  }
+}
+
+// GetVelocity_Unstructured, ompVC/velocity.c:459-621: walk from eid until the
+// element passes (d + TINY) >= 0, then P1 in space and linear in time.
+template <int DIMS>
+__device__ __forceinline__ int vel_unstruct(const DevMesh& m, const DevWindow& w, double tq, int tslot,
+                                            const double X[3], int& eid, int& left, double out[3],
+                                            const NatCache* nc) {
+  if (eid < 0 || eid >= m.nelem) return PT_ERR_WALK;
+  const bool tab = slot_hit(w, tslot, tq);
+  double tloc = 0.0;
+  if (!tab) {
+    tloc = (tq - w.tmin) / (w.tmax - w.tmin);
+    if ((tloc > 1 + FVC_TINY) || (tloc < 0 - FVC_TINY)) return PT_ERR_TLOC;
+  }
+  for (int hop = 0; hop < m.max_hops; hop++) {
+    double r, s, t, wv, d;
+    int4 nd;
+    NodeVel<DIMS> nv;
+    if (nc && nc->e == eid) {
+      nd = nc->nd;
+      if (tab) load_slot_nodes<DIMS>(w, tslot, nd, nv);
+      r = nc->r;
+      s = nc->s;
+      t = nc->t;
+      wv = nc->w;
+      d = nc->d;
+    } else {
+      Geo<DIMS> g;
+      load_geo<DIMS>(m, eid, g);
+      nd = g.nd;
+      if (tab) load_slot_nodes<DIMS>(w, tslot, nd, nv);
+      d = natural_from<DIMS>(g, X, r, s, t, wv);
+    }
+    if ((d + FVC_TINY) >= 0) {
+      if (!tab) {
+        // query time off the table: interpolate the two frames in time
+        const int ids[4] = {nd.x, nd.y, nd.z, nd.w};
+#pragma unroll
+        for (int c = 0; c < (DIMS == 3 ? 4 : 3); c++) {
+          double4_32a a = ldf(w.f0 + ids[c]), b = ldf(w.f1 + ids[c]);
+          nv.u[c] = (1 - tloc) * a.x + tloc * b.x;
+          nv.v[c] = (1 - tloc) * a.y + tloc * b.y;
+          nv.w[c] = (1 - tloc) * a.z + tloc * b.z;
+        }
+      }
+      if (DIMS == 3) {
+        out[0] = nv.u[0] + (nv.u[1] - nv.u[0]) * fabs(r) + (nv.u[2] - nv.u[0]) * fabs(s) + (nv.u[3] - nv.u[0]) * fabs(t);
+        out[1] = nv.v[0] + (nv.v[1] - nv.v[0]) * fabs(r) + (nv.v[2] - nv.v[0]) * fabs(s) + (nv.v[3] - nv.v[0]) * fabs(t);
+        out[2] = nv.w[0] + (nv.w[1] - nv.w[0]) * fabs(r) + (nv.w[2] - nv.w[0]) * fabs(s) + (nv.w[3] - nv.w[0]) * fabs(t);
+      } else {
+        out[0] = nv.u[0] + (nv.u[1] - nv.u[0]) * fabs(r) + (nv.u[2] - nv.u[0]) * fabs(s);
+        out[1] = nv.v[0] + (nv.v[1] - nv.v[0]) * fabs(r) + (nv.v[2] - nv.v[0]) * fabs(s);
+        out[2] = 0.0;
+      }
+      return 0;
+    }
+    // neighbour across the face of the minimal coordinate, first match in the
+    // order r, s, t, 1-r-s-t (ompVC/velocity.c:588-609)
+    int slot;
+    if (fabs(r - d) < FVC_TINY) slot = 0;
+    else if (fabs(s - d) < FVC_TINY) slot = 1;
+    else if (DIMS == 3 && fabs(t - d) < FVC_TINY) slot = 2;
+    else if (fabs(wv - d) < FVC_TINY) slot = DIMS == 3 ? 3 : 2;
+    else return PT_ERR_WALK;
+    int4 nb = __ldg(m.elem + 2 * (long)eid + 1);
+    eid = slot == 0 ? nb.x : slot == 1 ? nb.y : slot == 2 ? nb.z : nb.w;
+    if (eid == -1) {
+      left = 1;
+      out[0] = out[1] = out[2] = 0.0;
+      return 0;
+    }
+  }
+  return PT_ERR_WALK;
+}
+
+// Get_Element_Local_Search, ompVC/mesh.c:496-611: containment d > -TINY;
+// returns -1 when the walk leaves through a boundary face.  On success nc
+// (if given) receives the natural coordinates of the element found.
+template <int DIMS>
+__device__ __forceinline__ int locate_walk(const DevMesh& m, const double X[3], int guess, int& err,
+                                           NatCache* nc = nullptr) {
+  if (nc) nc->e = -1;
+  if (guess < 0) return -1;
+  if (guess >= m.nelem) {
+    err |= PT_ERR_WALK;
+    return -1;
+  }
+  for (int hop = 0; hop < m.max_hops; hop++) {
+    double r, s, t, wv;
+    Geo<DIMS> g;
+    load_geo<DIMS>(m, guess, g);
+    double d = natural_from<DIMS>(g, X, r, s, t, wv);
+    if (d > -FVC_TINY) {
+      if (nc) {
+        nc->e = guess;
+        nc->nd = g.nd;
+        nc->r = r;
+        nc->s = s;
+        nc->t = t;
+        nc->w = wv;
+        nc->d = d;
+      }
+      return guess;
+    }
+    int slot;
+    if (fabs(r - d) < FVC_TINY) slot = 0;
+    else if (fabs(s - d) < FVC_TINY) slot = 1;
+    else if (DIMS == 3 && fabs(t - d) < FVC_TINY) slot = 2;
+    else if (fabs(d - wv) < FVC_TINY) slot = DIMS == 3 ? 3 : 2;
+    else {
+      err |= PT_ERR_WALK;
+      return -1;
+    }
+    int4 nb = __ldg(m.elem + 2 * (long)guess + 1);
+    guess = slot == 0 ? nb.x : slot == 1 ? nb.y : slot == 2 ? nb.z : nb.w;
+    if (guess == -1) return -1;
+  }
+  err |= PT_ERR_WALK;
+  return -1;
+}
+
+// Containment test of one element (the predicate of
+// Get_Element_Global_Search, ompVC/mesh.c:360 and 389).
+template <int DIMS>
+__device__ __forceinline__ bool contains(const DevMesh& m, int e, const double X[3]) {
+  double r, s, t, wv;
+  return natural<DIMS>(m, e, X, r, s, t, wv) > -FVC_TINY;
+}
+
+// GetVelocity dispatch, ompVC/velocity.c:236-247.  tslot names the stage
+// time in the call's table (-1: none); nc the last locate's coordinates.
+template <int DIMS, int MESH>
+__device__ __forceinline__ int velocity(const DevMesh& m, const DevWindow& w, double tq, int tslot,
+                                        const double X[3], int& eid, int& left, double out[3],
+                                        const NatCache* nc = nullptr) {
+  if (MESH == 0) return vel_cart<DIMS>(m, w, tq, tslot, X, left, out);
+  return vel_unstruct<DIMS>(m, w, tq, tslot, X, eid, left, out, nc);
+}
+
+// ---------------------------------------------------------------- integrators
+//
+// Step k of a call evaluates at the stage times of slots 2k (tc), 2k+1
+// (tc + h/2) and 2k+2 (tc + h); the slot is only a hint, checked against the
+// time it names before its table entry is used.
+
+// velocity at the accepted position for extrapolation (Int_Extrapolate),
+// kept out of line: it is off the common path
+template <int DIMS, int MESH>
+__device__ __noinline__ int velocity_cold(const DevMesh& m, const DevWindow& w, double tq, int tslot,
+                                          const double* X, int* eid, int* left, double* out) {
+  return velocity<DIMS, MESH>(m, w, tq, tslot, X, *eid, *left, out);
+}
+
+// Euler, ompVC/integration.c:222-311
+template <int DIMS, int MESH>
+__device__ __noinline__ double euler(const DevMesh& m, const DevWindow& w, const DevInteg& in,
+                                     Pt& p, double tstart, double tend, unsigned& steps, int& err) {
+  double tc = tstart, h = dsign(in.h, tend - tstart), ve[3];
+  NatCache nc;
+  nc.e = -1;
+  int k = 0;
+  while ((tc - tend) * (tend - tstart) < 0.0) {
+    if ((tc + h - tend) * (tc + h - tstart) > 0.0) h = dsign(tend - tc, tend - tstart);
+    if ((err |= velocity<DIMS, MESH>(m, w, tc, 2 * k, p.X, p.eid, p.left, ve, &nc))) return tend;
+    p.X[0] = p.X[0] + h * ve[0];
+    p.X[1] = p.X[1] + h * ve[1];
+    p.X[2] = p.X[2] + h * ve[2];
+    tc = tc + h;
+    k++;
+    if (MESH == 1) p.eid = locate_walk<DIMS>(m, p.X, p.eid, err, &nc);
+    if (err) return tend;
+    if ((MESH == 0 && outside_domain(m, p.X)) || (MESH == 1 && p.eid < 0)) {
+      p.left = 1;
+      p.ldt = tc - h;
+      p.X[0] = p.X[0] - h * ve[0];
+      p.X[1] = p.X[1] - h * ve[1];
+      p.X[2] = p.X[2] - h * ve[2];
+      return p.ldt;
+    }
+    steps++;
+    if (in.extrapolate && (err |= velocity_cold<DIMS, MESH>(m, w, tc, 2 * k, p.X, &p.eid, &p.left, p.V)))
+      return tend;
+  }
+  return tend;
+}
+
+// The four stage evaluations of one RK4 step (ompVC/integration.c:362-396);
+// e[]/l[] are the stage points' persistent element hints and exit flags.
+template <int DIMS, int MESH>
+__device__ __forceinline__ int rk4_stages(const DevMesh& m, const DevWindow& w, const Pt& p,
+                                          double tc, double h, int k, int e[4], int l[4],
+                                          double kk[4][3], const NatCache* nc) {
+  double M[3];
+  int err;
+  M[0] = p.X[0];
+  M[1] = p.X[1];
+  M[2] = p.X[2];
+  if ((err = velocity<DIMS, MESH>(m, w, tc, 2 * k, M, e[0], l[0], kk[0], nc))) return err;
+  M[0] = p.X[0] + 0.5 * kk[0][0] * h;
+  M[1] = p.X[1] + 0.5 * kk[0][1] * h;
+  M[2] = p.X[2] + 0.5 * kk[0][2] * h;
+  if ((err = velocity<DIMS, MESH>(m, w, tc + h / 2, 2 * k + 1, M, e[1], l[1], kk[1]))) return err;
+  M[0] = p.X[0] + 0.5 * kk[1][0] * h;
+  M[1] = p.X[1] + 0.5 * kk[1][1] * h;
+  M[2] = p.X[2] + 0.5 * kk[1][2] * h;
+  if ((err = velocity<DIMS, MESH>(m, w, tc + h / 2, 2 * k + 1, M, e[2], l[2], kk[2]))) return err;
+  M[0] = p.X[0] + kk[2][0] * h;
+  M[1] = p.X[1] + kk[2][1] * h;
+  M[2] = p.X[2] + kk[2][2] * h;
+  return velocity<DIMS, MESH>(m, w, tc + h, 2 * k + 2, M, e[3], l[3], kk[3]);
+}
+
+// RK4, ompVC/integration.c:317-462
+template <int DIMS, int MESH>
+__device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, const DevInteg& in,
+                                      Pt& p, double tstart, double tend, unsigned& steps, int& err) {
+  int e[4] = {p.eid, p.eid, p.eid, p.eid};
+  int l[4] = {p.left, p.left, p.left, p.left};
+  double kk[4][3];
+  NatCache nc;
+  nc.e = -1;
+  double tc = tstart, h = dsign(in.h, tend - tstart);
+  int k = 0;
+  while ((tc - tend) * (tend - tstart) < 0.0) {
+    if ((tc + h - tend) * (tc + h - tstart) > 0.0) h = dsign(tend - tc, tend - tstart);
+    if ((err |= rk4_stages<DIMS, MESH>(m, w, p, tc, h, k, e, l, kk, &nc))) return tend;
+#pragma unroll
+    for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]) / 6;
+    tc = tc + h;
+    k++;
+    if (MESH == 1) p.eid = locate_walk<DIMS>(m, p.X, p.eid, err, &nc);
+    if (err) return tend;
+    if ((MESH == 0 && outside_domain(m, p.X)) || (MESH == 1 && p.eid < 0) || l[0] || l[1] || l[2] ||
+        l[3]) {
+      p.left = 1;
+      p.ldt = tc - h;
+#pragma unroll
+      for (int q = 0; q < 3; q++) p.X[q] = p.X[q] - h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]) / 6;
+      return p.ldt;
+    }
+    steps++;
+    if (in.extrapolate && (err |= velocity_cold<DIMS, MESH>(m, w, tc, 2 * k, p.X, &p.eid, &p.left, p.V)))
+      return tend;
+  }
+  return tend;
+}
+
+// Two-step Adams-Bashforth (Int_Type 3, cudaVC's numbering,
+// cudaVC/src/main.cu:225).  ompVC has no multistep integrator; this is the
+// textbook variable-step AB2 X_{n+1} = X_n + h (c1 f_n - c0 f_{n-1}) with
+// c0 = h / (2 h_prev), c1 = 1 + c0, bootstrapped by one RK4 step at the start
+// of every call and using RK4's clip, relocation and exit rules.
+template <int DIMS, int MESH>
+__device__ __noinline__ double ab2(const DevMesh& m, const DevWindow& w, const DevInteg& in,
+                                   Pt& p, double tstart, double tend, unsigned& steps, int& err) {
+  int e[4] = {p.eid, p.eid, p.eid, p.eid};
+  int l[4] = {p.left, p.left, p.left, p.left};
+  double kk[4][3], fprev[3] = {0, 0, 0}, hprev = 0.0;
+  NatCache nc;
+  nc.e = -1;
+  double tc = tstart, h = dsign(in.h, tend - tstart);
+  bool first = true;
+  int k = 0;
+  while ((tc - tend) * (tend - tstart) < 0.0) {
+    if ((tc + h - tend) * (tc + h - tstart) > 0.0) h = dsign(tend - tc, tend - tstart);
+    double inc[3], f[3];
+    int lf = 0;
+    if (first) {
+      if ((err |= rk4_stages<DIMS, MESH>(m, w, p, tc, h, k, e, l, kk, &nc))) return tend;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        inc[q] = h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]) / 6;
+        f[q] = kk[0][q];
+      }
+      lf = l[0] || l[1] || l[2] || l[3];
+    } else {
+      int ef = p.eid;
+      if ((err |= velocity<DIMS, MESH>(m, w, tc, 2 * k, p.X, ef, lf, f, &nc))) return tend;
+      double c0 = h / (2.0 * hprev), c1 = 1.0 + c0;
+#pragma unroll
+      for (int q = 0; q < 3; q++) inc[q] = h * (c1 * f[q] - c0 * fprev[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + inc[q];
+    tc = tc + h;
+    k++;
+    if (MESH == 1) p.eid = locate_walk<DIMS>(m, p.X, p.eid, err, &nc);
+    if (err) return tend;
+    if ((MESH == 0 && outside_domain(m, p.X)) || (MESH == 1 && p.eid < 0) || lf) {
+      p.left = 1;
+      p.ldt = tc - h;
+#pragma unroll
+      for (int q = 0; q < 3; q++) p.X[q] = p.X[q] - inc[q];
+      return p.ldt;
+    }
+    steps++;
+#pragma unroll
+    for (int q = 0; q < 3; q++) fprev[q] = f[q];
+    hprev = h;
+    first = false;
+    if (in.extrapolate && (err |= velocity_cold<DIMS, MESH>(m, w, tc, 2 * k, p.X, &p.eid, &p.left, p.V)))
+      return tend;
+  }
+  return tend;
+}
+
+// Advect, ompVC/integration.c:22-45 (Int_Type 0 Euler, 1 RK4, 3 AB2).
+// Euler and AB2 are called out of line so that kernels inline only RK4.
+template <int DIMS, int MESH>
+__device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, const DevInteg& in,
+                                      Pt& p, double tstart, double tend, unsigned& steps) {
+  int err = 0;
+  if (p.left && in.extrapolate) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + p.V[q] * (tend - tstart);
+    return 0;
+  }
+  if (p.left) return PT_ERR_STATE;  // "integrate point that already left domain"
+  if (MESH == 1 && p.eid < 0) return PT_ERR_STATE;
+  double stop;
+  if (in.type == 1) stop = rk4<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
+  else if (in.type == 3) stop = ab2<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
+  else stop = euler<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
+  if (!err && (fabs(stop - tend) > FVC_TINY) && in.extrapolate) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + p.V[q] * (tend - stop);
+  }
+  return err;
+}
+
+// ------------------------------------------------------------- reductions
+
+// Warp-aggregated accumulation of accepted steps and fault bits.
+__device__ __forceinline__ void flush_counters(unsigned long long* step_ctr, int* status,
+                                               unsigned steps, int err) {
+  unsigned long long s = steps;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  int e = __reduce_or_sync(0xffffffffu, err);
+  if ((threadIdx.x & 31) == 0) {
+    if (s) atomicAdd(step_ctr, s);
+    if (e) atomicOr(status, e);
+  }
+}
+
+}  // namespace fvc

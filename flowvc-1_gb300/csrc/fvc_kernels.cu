@@ -1,0 +1,876 @@
+// fvc_kernels.cu -- sm_103a kernels of the flowVC advection engine: mesh
+// preprocessing, bucket grid, seed-location chain, FTLE bookkeeping and the
+// tracer output compaction; the integrator kernels live in fvc_variant_*.cu.
+//
+// Built with --fmad=false: the FP64 paths must round every multiply and add
+// separately to reproduce ompVC's results bit for bit (see fvc_device.cuh).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "fvc_device.cuh"
+#include "fvc_advect_impl.cuh"
+#include "fvc_ftle_math.cuh"
+#include "fvc_kernels.h"
+
+namespace fvc {
+
+
+static inline unsigned nblk(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// ============================================================ mesh geometry
+
+// Natural-coordinate map of every element, from the expressions of
+// ompVC/velocity.c:497-510 (3D) and 529-535 (2D), with the element's node ids
+// in the same record so one gather serves the containment test and the
+// interpolation (layout in fvc_device.cuh, struct Geo).
+template <int DIMS>
+__global__ void k_geometry(DevMesh m, double* geom) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.nelem) return;
+  int4 nd = m.elem[2 * (long)e];
+  double4_32a p0 = m.nodes[nd.x], p1 = m.nodes[nd.y], p2 = m.nodes[nd.z];
+  double x0 = p0.x, y0 = p0.y, x1 = p1.x, y1 = p1.y, x2 = p2.x, y2 = p2.y;
+  if (DIMS == 3) {
+    double4_32a p3 = m.nodes[nd.w];
+    double z0 = p0.z, z1 = p1.z, z2 = p2.z, x3 = p3.x, y3 = p3.y, z3 = p3.z;
+    double* g = geom + (long)e * 16;
+    g[0] = (z3 - z0) * (y2 - y3) - (z2 - z3) * (y3 - y0);   // a11
+    g[3] = (z3 - z0) * (y0 - y1) - (z0 - z1) * (y3 - y0);   // a21
+    g[6] = (z1 - z2) * (y0 - y1) - (z0 - z1) * (y1 - y2);   // a31
+    g[1] = (x3 - x0) * (z2 - z3) - (x2 - x3) * (z3 - z0);   // a12
+    g[4] = (x3 - x0) * (z0 - z1) - (x0 - x1) * (z3 - z0);   // a22
+    g[7] = (x1 - x2) * (z0 - z1) - (x0 - x1) * (z1 - z2);   // a32
+    g[2] = (y3 - y0) * (x2 - x3) - (y2 - y3) * (x3 - x0);   // a13
+    g[5] = (y3 - y0) * (x0 - x1) - (y0 - y1) * (x3 - x0);   // a23
+    g[8] = (y1 - y2) * (x0 - x1) - (y0 - y1) * (x1 - x2);   // a33
+    g[9] = (x1 - x0) * ((y2 - y0) * (z3 - z0) - (z2 - z0) * (y3 - y0)) +
+           (x2 - x0) * ((y0 - y1) * (z3 - z0) - (z0 - z1) * (y3 - y0)) +
+           (x3 - x0) * ((y1 - y0) * (z2 - z0) - (z1 - z0) * (y2 - y0));  // V
+    g[10] = x0;
+    g[11] = y0;
+    g[12] = z0;
+    g[13] = 0.0;
+    reinterpret_cast<int4*>(g + 14)[0] = nd;
+  } else {
+    double* g = geom + (long)e * 12;
+    g[0] = y2 - y0;  // a11
+    g[1] = x0 - x2;  // a12
+    g[2] = y0 - y1;  // a21
+    g[3] = x1 - x0;  // a22
+    g[4] = (x1 - x0) * (y2 - y0) - (x2 - x0) * (y1 - y0);  // V
+    g[5] = x0;
+    g[6] = y0;
+    g[7] = 0.0;
+    reinterpret_cast<int4*>(g + 8)[0] = nd;
+    g[10] = g[11] = 0.0;
+  }
+}
+
+void launch_geometry(const DevMesh& m, double* geom, cudaStream_t s) {
+  if (m.dims == 3) k_geometry<3><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom);
+  else k_geometry<2><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom);
+}
+
+// =============================================================== scans
+
+// Exclusive prefix sum of a block's values (blockDim.x a multiple of 32,
+// at most 1024); returns the block total in *total.
+__device__ __forceinline__ long long block_exclusive_sum(long long v, long long* total) {
+  __shared__ long long warp_sums[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    long long ws = lane < nw ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      long long y = __shfl_up_sync(0xffffffffu, ws, o);
+      if (lane >= o) ws += y;
+    }
+    if (lane < nw) warp_sums[lane] = ws;
+  }
+  __syncthreads();
+  long long off = wid > 0 ? warp_sums[wid - 1] : 0;
+  *total = warp_sums[nw - 1];
+  __syncthreads();
+  return off + x - v;
+}
+
+// Block-wise exclusive scan of int counts into int offsets (two levels).
+__global__ void k_scan_blocks(const int* in, int* out, int n, long long* block_tot) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long v = i < n ? in[i] : 0, tot;
+  long long ex = block_exclusive_sum(v, &tot);
+  if (i < n) out[i] = (int)ex;
+  if (threadIdx.x == 0) block_tot[blockIdx.x] = tot;
+}
+__global__ void k_scan_tops(long long* block_tot, int nb, int* grand) {
+  // single thread: nb is small (n / 1024)
+  if (threadIdx.x || blockIdx.x) return;
+  long long run = 0;
+  for (int b = 0; b < nb; b++) {
+    long long t = block_tot[b];
+    block_tot[b] = run;
+    run += t;
+  }
+  *grand = (int)run;
+}
+__global__ void k_scan_add(int* out, int n, const long long* block_off) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += (int)block_off[blockIdx.x];
+}
+// out[0..n-1] = exclusive scan of in, out[n] = total.  tmp holds n/1024+1 longs.
+static void exclusive_scan(const int* in, int* out, int n, long long* tmp, cudaStream_t s) {
+  unsigned nb = nblk(n, 1024);
+  k_scan_blocks<<<nb, 1024, 0, s>>>(in, out, n, tmp);
+  k_scan_tops<<<1, 32, 0, s>>>(tmp, (int)nb, out + n);
+  k_scan_add<<<nb, 1024, 0, s>>>(out, n, tmp);
+}
+
+// ========================================================== bucket grid
+
+template <int DIMS>
+__device__ __forceinline__ void elem_cells(const DevMesh& m, const BucketGrid& g, int e, int lo[3],
+                                           int hi[3]) {
+  int4 nd = m.elem[2 * (long)e];
+  double4_32a p[4];
+  p[0] = m.nodes[nd.x];
+  p[1] = m.nodes[nd.y];
+  p[2] = m.nodes[nd.z];
+  p[3] = DIMS == 3 ? m.nodes[nd.w] : p[2];
+  double bmin[3] = {p[0].x, p[0].y, p[0].z}, bmax[3] = {p[0].x, p[0].y, p[0].z};
+  for (int c = 1; c < 4; c++) {
+    bmin[0] = fmin(bmin[0], p[c].x); bmax[0] = fmax(bmax[0], p[c].x);
+    bmin[1] = fmin(bmin[1], p[c].y); bmax[1] = fmax(bmax[1], p[c].y);
+    bmin[2] = fmin(bmin[2], p[c].z); bmax[2] = fmax(bmax[2], p[c].z);
+  }
+  // A point passes the containment test d > -TINY only within ~1e-10 of the
+  // element (in units of its size); pad the box by 1e-7 of its extent.
+  double ext = fmax(bmax[0] - bmin[0], fmax(bmax[1] - bmin[1], DIMS == 3 ? bmax[2] - bmin[2] : 0.0));
+  double pad = 1e-7 * ext + 1e-300;
+  for (int a = 0; a < 3; a++) {
+    if (a == 2 && DIMS == 2) { lo[a] = hi[a] = 0; continue; }
+    int l = (int)floor((bmin[a] - pad - g.lo[a]) * g.inv[a]);
+    int h = (int)floor((bmax[a] + pad - g.lo[a]) * g.inv[a]);
+    lo[a] = max(0, min(g.n[a] - 1, l));
+    hi[a] = max(0, min(g.n[a] - 1, h));
+  }
+}
+
+template <int DIMS>
+__global__ void k_bucket_count(DevMesh m, BucketGrid g, int* cnt) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.nelem) return;
+  int lo[3], hi[3];
+  elem_cells<DIMS>(m, g, e, lo, hi);
+  for (int k = lo[2]; k <= hi[2]; k++)
+    for (int j = lo[1]; j <= hi[1]; j++)
+      for (int i = lo[0]; i <= hi[0]; i++) atomicAdd(&cnt[((long)k * g.n[1] + j) * g.n[0] + i], 1);
+}
+
+template <int DIMS>
+__global__ void k_bucket_fill(DevMesh m, BucketGrid g, const int* start, int* cursor, int* ids) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.nelem) return;
+  int lo[3], hi[3];
+  elem_cells<DIMS>(m, g, e, lo, hi);
+  for (int k = lo[2]; k <= hi[2]; k++)
+    for (int j = lo[1]; j <= hi[1]; j++)
+      for (int i = lo[0]; i <= hi[0]; i++) {
+        long c = ((long)k * g.n[1] + j) * g.n[0] + i;
+        ids[start[c] + atomicAdd(&cursor[c], 1)] = e;
+      }
+}
+
+// ascending element ids within each cell, so the first hit is the lowest id
+__global__ void k_bucket_sort(const int* start, int* ids, int ncells) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  int b = start[c], e = start[c + 1];
+  for (int i = b + 1; i < e; i++) {
+    int v = ids[i], j = i - 1;
+    while (j >= b && ids[j] > v) {
+      ids[j + 1] = ids[j];
+      j--;
+    }
+    ids[j + 1] = v;
+  }
+}
+
+long long bucket_count(const DevMesh& m, BucketGrid& g, int* cell_count, int ncells, int* d_total,
+                       cudaStream_t s) {
+  (void)d_total;
+  cudaMemsetAsync(cell_count, 0, sizeof(int) * (size_t)ncells, s);
+  if (m.dims == 3) k_bucket_count<3><<<nblk(m.nelem, 256), 256, 0, s>>>(m, g, cell_count);
+  else k_bucket_count<2><<<nblk(m.nelem, 256), 256, 0, s>>>(m, g, cell_count);
+  return 0;
+}
+
+void bucket_fill(const DevMesh& m, const BucketGrid& g, int* cell_start, int* cursor, int* ids,
+                 int ncells, int* scan_tmp, cudaStream_t s) {
+  (void)scan_tmp;
+  cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)ncells, s);
+  if (m.dims == 3) k_bucket_fill<3><<<nblk(m.nelem, 256), 256, 0, s>>>(m, g, cell_start, cursor, ids);
+  else k_bucket_fill<2><<<nblk(m.nelem, 256), 256, 0, s>>>(m, g, cell_start, cursor, ids);
+  k_bucket_sort<<<nblk(ncells, 256), 256, 0, s>>>(cell_start, ids, ncells);
+}
+
+// exported scan for the API layer (cell offsets)
+void scan_counts(const int* in, int* out, int n, long long* tmp, cudaStream_t s) {
+  exclusive_scan(in, out, n, tmp, s);
+}
+
+// Get_Element_Global_Search (ompVC/mesh.c:304-398): lowest element id whose
+// containment test d > -TINY passes, from the point's bucket.
+template <int DIMS>
+__device__ __forceinline__ int global_find(const DevMesh& m, const BucketGrid& g, const double X[3]) {
+  int c[3];
+  for (int a = 0; a < 3; a++) {
+    if (a == 2 && DIMS == 2) { c[a] = 0; continue; }
+    double f = (X[a] - g.lo[a]) * g.inv[a];
+    if (!(f >= 0.0) || f >= (double)g.n[a]) return -1;
+    c[a] = min(g.n[a] - 1, (int)f);
+  }
+  long cell = ((long)c[2] * g.n[1] + c[1]) * g.n[0] + c[0];
+  int b = __ldg(g.start + cell), e = __ldg(g.start + cell + 1);
+  for (int i = b; i < e; i++) {
+    int el = __ldg(g.ids + i);
+    if (contains<DIMS>(m, el, X)) return el;
+  }
+  return -1;
+}
+
+template <int DIMS>
+__global__ void k_global(DevMesh m, BucketGrid g, int n, const double* X, const int* skip, int* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (skip && skip[i]) {
+    out[i] = -1;
+    return;
+  }
+  double x[3] = {X[3 * (long)i], X[3 * (long)i + 1], X[3 * (long)i + 2]};
+  out[i] = global_find<DIMS>(m, g, x);
+}
+
+void launch_global_search(const DevMesh& m, const BucketGrid& g, int n, const double* X,
+                          const int* skip, int* out, cudaStream_t s) {
+  if (n <= 0) return;
+  if (m.dims == 3) k_global<3><<<nblk(n, 128), 128, 0, s>>>(m, g, n, X, skip, out);
+  else k_global<2><<<nblk(n, 128), 128, 0, s>>>(m, g, n, X, skip, out);
+}
+
+// ============================================================ step level
+
+template <int D>
+__global__ void k_local(DevMesh m, int n, const double* X, const int* guess, int* out, DevCounters* ctr) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  int err = 0;
+  if (i < n) {
+    double x[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
+    out[i] = locate_walk<D>(m, x, guess[i], err);
+  }
+  flush_counters(&ctr->steps, &ctr->status, 0, err);
+}
+
+void launch_local_search(const DevMesh& m, int n, const double* X, const int* guess, int* out,
+                         DevCounters* ctr, cudaStream_t s) {
+  if (n <= 0) return;
+  if (m.dims == 3) k_local<3><<<nblk(n, 128), 128, 0, s>>>(m, n, X, guess, out, ctr);
+  else k_local<2><<<nblk(n, 128), 128, 0, s>>>(m, n, X, guess, out, ctr);
+}
+
+__global__ void k_outside(DevMesh m, int n, const double* X, int* left0) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
+  left0[i] = outside_domain(m, x);
+}
+
+void outside_domain_flags(const DevMesh& m, int n, const double* X, int* left0, cudaStream_t s) {
+  if (n <= 0) return;
+  k_outside<<<nblk(n, 256), 256, 0, s>>>(m, n, X, left0);
+}
+
+// (1 - tloc) * U0 + tloc * U1 at every node for every stage time of the call
+// (the expression of ompVC/velocity.c:547-571), so stage evaluations read it.
+__global__ void k_time_fields(DevWindow w, long nnodes, double4_32a* vt) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  int sl = blockIdx.y;
+  if (i >= nnodes || sl >= w.nslots) return;
+  double tloc = w.tl[sl];
+  double4_32a a = w.f0[i], b = w.f1[i];
+  vt[(long)sl * nnodes + i] = make_double4_32a((1 - tloc) * a.x + tloc * b.x, (1 - tloc) * a.y + tloc * b.y,
+                                               (1 - tloc) * a.z + tloc * b.z, 0.0);
+}
+
+void time_fields(const DevMesh& m, const DevWindow& w, double4_32a* vt, cudaStream_t s) {
+  if (w.nslots <= 0 || m.nnodes <= 0) return;
+  dim3 grid(nblk(m.nnodes, 256), w.nslots);
+  k_time_fields<<<grid, 256, 0, s>>>(w, m.nnodes, vt);
+}
+
+__global__ void k_pack_frame(const double* uvw, double4_32a* out, long n) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = make_double4_32a(uvw[3 * i], uvw[3 * i + 1], uvw[3 * i + 2], 0.0);
+}
+
+void pack_frame(const double* uvw, double4_32a* out, long n, cudaStream_t s) {
+  k_pack_frame<<<nblk(n, 256), 256, 0, s>>>(uvw, out, n);
+}
+
+// ====================================================== seed location chain
+//
+// ompVC locates seeds one after another, each neighbour walk starting from
+// the element found for an earlier seed (its "guess").  The walk's answer
+// depends on the guess only for seeds within TINY of a shared face, so the
+// chain is solved as a fixed point: start from the lowest-id containing
+// element of every seed (bucketed global search), derive every seed's guess
+// from the current answers with the reference's rules, redo every seed's
+// walk from that guess in parallel, and repeat until nothing changes.  If
+// the answers for seeds 0..m-1 equal the serial ones, the guess and hence the
+// answer for seed m do too, so each round fixes at least the first
+// difference and the fixed point is the serial result.
+
+struct ChainDev {
+  const double* X;
+  const int* left0;
+  const int* R0;   // global-search answer of every seed
+  int* R;          // current answers
+  int* Rn;         // next answers
+  int* g;          // guess of every seed
+  int* rowfirst;   // kind 0: first answer in each (i, j) row
+  int* rowstart;   // kind 0: guess at the start of each row
+  int* planefirst; // kind 0
+  int* planestart; // kind 0
+  int* chunk_last; // kinds 1, 2
+  int* chunk_carry;
+  int n, nrows, nplanes, nchunks;
+  int res[3];
+  int kind, lsc, seed, pstar, init_guess;
+};
+
+// kind 0 (ompVC/ftle.c:467-601): a row restarts from the first element found
+// in the previous row (jguess), a plane from the first found in the previous
+// plane (iguess); within a row the guess is the last element found.
+__global__ void k_chain_rowfirst(ChainDev c) {
+  int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= c.nrows) return;
+  int zr = c.res[2], first = -1;
+  for (int k = 0; k < zr; k++) {
+    int r = c.R[(long)row * zr + k];
+    if (r >= 0) { first = r; break; }
+  }
+  c.rowfirst[row] = first;
+}
+__global__ void k_chain_planefirst(ChainDev c) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.nplanes) return;
+  int first = -1;
+  for (int j = 0; j < c.res[1]; j++) {
+    int r = c.rowfirst[(long)i * c.res[1] + j];
+    if (r >= 0) { first = r; break; }
+  }
+  c.planefirst[i] = first;
+}
+__global__ void k_chain_planes(ChainDev c) {
+  if (threadIdx.x || blockIdx.x) return;
+  int G = c.init_guess;
+  for (int i = 0; i < c.nplanes; i++) {
+    c.planestart[i] = G;
+    if (c.planefirst[i] >= 0) G = c.planefirst[i];
+  }
+}
+__global__ void k_chain_rows(ChainDev c) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.nplanes) return;
+  int G = c.planestart[i];
+  for (int j = 0; j < c.res[1]; j++) {
+    long row = (long)i * c.res[1] + j;
+    c.rowstart[row] = G;
+    if (c.rowfirst[row] >= 0) G = c.rowfirst[row];
+  }
+}
+__global__ void k_chain_row_guess(ChainDev c) {
+  int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= c.nrows) return;
+  int zr = c.res[2], cur = c.rowstart[row];
+  for (int k = 0; k < zr; k++) {
+    long p = (long)row * zr + k;
+    c.g[p] = cur;
+    if (c.R[p] >= 0) cur = c.R[p];
+  }
+}
+
+// kinds 1 and 2 (ompVC/tracers.c:1156-1243, 1379-1524): the guess is the
+// last element found before the seed in list order.
+__global__ void k_chain_chunk_last(ChainDev c) {
+  __shared__ int best;
+  if (threadIdx.x == 0) best = -1;
+  __syncthreads();
+  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < c.n && c.R[p] >= 0) atomicMax(&best, (int)p);
+  __syncthreads();
+  if (threadIdx.x == 0) c.chunk_last[blockIdx.x] = best;
+}
+__global__ void k_chain_carry(ChainDev c) {
+  if (threadIdx.x || blockIdx.x) return;
+  int run = -1;
+  for (int b = 0; b < c.nchunks; b++) {
+    c.chunk_carry[b] = run;
+    if (c.chunk_last[b] >= 0) run = c.chunk_last[b];
+  }
+}
+__global__ void k_chain_linear_guess(ChainDev c) {
+  // exclusive max-scan of "index of a found seed" within the block
+  __shared__ int warp_max[32];
+  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int v = (p < c.n && c.R[p] >= 0) ? (int)p : -1;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x = max(x, y);
+  }
+  if (lane == 31) warp_max[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int ws = lane < nw ? warp_max[lane] : -1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, ws, o);
+      if (lane >= o) ws = max(ws, y);
+    }
+    if (lane < nw) warp_max[lane] = ws;
+  }
+  __syncthreads();
+  int before_warp = wid > 0 ? warp_max[wid - 1] : -1;
+  int incl = max(x, before_warp);
+  int excl_in_block = __shfl_up_sync(0xffffffffu, incl, 1);
+  if (lane == 0) excl_in_block = before_warp;
+  int last = max(excl_in_block, c.chunk_carry[blockIdx.x]);
+  if (p < c.n) c.g[p] = last >= 0 ? c.R[last] : c.init_guess;
+}
+
+template <int DIMS>
+__global__ void k_chain_eval(DevMesh m, ChainDev c, DevCounters* ctr) {
+  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  int err = 0, changed = 0;
+  if (p < c.n) {
+    int r;
+    if (c.left0[p]) r = -1;
+    else if (p <= c.pstar) r = c.R0[p];
+    else {
+      double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
+      r = locate_walk<DIMS>(m, x, c.g[p], err);
+      if (r < 0 && c.kind != 1) r = locate_walk<DIMS>(m, x, c.seed, err);
+      if (r < 0 && c.lsc) r = c.R0[p];
+    }
+    c.Rn[p] = r;
+    changed = r != c.R[p];
+  }
+  int any = __reduce_or_sync(0xffffffffu, changed);
+  int e = __reduce_or_sync(0xffffffffu, err);
+  if ((threadIdx.x & 31) == 0) {
+    if (any) atomicOr(&ctr->changed, 1);
+    if (e) atomicOr(&ctr->status, e);
+  }
+}
+
+__global__ void k_first_found(int n, const int* left0, const int* R0, int* out) {
+  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n && !left0[p] && R0[p] >= 0) atomicMin(out, (int)p);
+}
+
+int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, const double* X,
+                 const int* left0, int* eid, int* work, DevCounters* ctr, cudaStream_t s) {
+  ChainDev c;
+  int n = a.n;
+  c.X = X;
+  c.left0 = left0;
+  c.n = n;
+  c.kind = a.kind;
+  c.lsc = a.lsc;
+  c.res[0] = a.res[0];
+  c.res[1] = a.res[1];
+  c.res[2] = a.res[2];
+  c.nplanes = a.kind == 0 ? a.res[0] : 0;
+  c.nrows = a.kind == 0 ? a.res[0] * a.res[1] : 0;
+  c.nchunks = nblk(n, 1024);
+  int* w = work;
+  int* R0 = w; w += n;
+  c.R = w; w += n;
+  c.Rn = w; w += n;
+  c.g = w; w += n;
+  c.rowfirst = w; w += c.nrows + 1;
+  c.rowstart = w; w += c.nrows + 1;
+  c.planefirst = w; w += c.nplanes + 1;
+  c.planestart = w; w += c.nplanes + 1;
+  c.chunk_last = w; w += c.nchunks + 1;
+  c.chunk_carry = w; w += c.nchunks + 1;
+  int* d_first = w; w += 1;
+  c.R0 = R0;
+  launch_global_search(m, g, n, X, left0, R0, s);
+  // first seed found by the global search: the chain's start when no centre
+  // element is known (and always for a tracer list)
+  int big = 0x7fffffff, first = big;
+  cudaMemcpyAsync(d_first, &big, sizeof(int), cudaMemcpyHostToDevice, s);
+  k_first_found<<<nblk(n, 256), 256, 0, s>>>(n, left0, R0, d_first);
+  cudaMemcpyAsync(&first, d_first, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  if (a.kind != 1 && a.center_eid >= 0) {
+    c.seed = a.center_eid;
+    c.pstar = -1;
+    c.init_guess = a.center_eid;
+  } else if (first == big) {  // nothing inside the mesh
+    cudaMemcpyAsync(eid, R0, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    return 0;
+  } else {
+    int sv = 0;
+    cudaMemcpyAsync(&sv, R0 + first, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    c.seed = sv;
+    c.pstar = first;
+    c.init_guess = -1;
+  }
+  cudaMemcpyAsync(c.R, R0, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+  int rounds = 0;
+  for (;;) {
+    rounds++;
+    if (a.kind == 0) {
+      k_chain_rowfirst<<<nblk(c.nrows, 128), 128, 0, s>>>(c);
+      k_chain_planefirst<<<nblk(c.nplanes, 128), 128, 0, s>>>(c);
+      k_chain_planes<<<1, 32, 0, s>>>(c);
+      k_chain_rows<<<nblk(c.nplanes, 128), 128, 0, s>>>(c);
+      k_chain_row_guess<<<nblk(c.nrows, 128), 128, 0, s>>>(c);
+    } else {
+      k_chain_chunk_last<<<c.nchunks, 1024, 0, s>>>(c);
+      k_chain_carry<<<1, 32, 0, s>>>(c);
+      k_chain_linear_guess<<<c.nchunks, 1024, 0, s>>>(c);
+    }
+    cudaMemsetAsync(&ctr->changed, 0, sizeof(int), s);
+    if (m.dims == 3) k_chain_eval<3><<<nblk(n, 128), 128, 0, s>>>(m, c, ctr);
+    else k_chain_eval<2><<<nblk(n, 128), 128, 0, s>>>(m, c, ctr);
+    int changed = 0, status = 0;
+    cudaMemcpyAsync(&changed, &ctr->changed, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&status, &ctr->status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess || status) return -1;
+    int* t = c.R;
+    c.R = c.Rn;
+    c.Rn = t;
+    if (!changed || rounds > n + 1) break;
+  }
+  cudaMemcpyAsync(eid, c.R, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+  return rounds;
+}
+
+// ================================================================ FTLE
+
+__global__ void k_ftle_seed(DevMesh m, FtleDev f, double xmin, double ymin, double zmin, int* left0) {
+  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= f.n) return;
+  int k = (int)(p % f.zr), j = (int)((p / f.zr) % f.yr), i = (int)(p / ((long)f.zr * f.yr));
+  // InitializeFTLEArray, ompVC/ftle.c:410-423
+  double x[3] = {xmin + i * f.dx, ymin + j * f.dy, zmin + k * f.dz};
+  f.X[3 * p] = x[0];
+  f.X[3 * p + 1] = x[1];
+  f.X[3 * p + 2] = x[2];
+  f.V[3 * p] = f.V[3 * p + 1] = f.V[3 * p + 2] = 0.0;
+  f.ftT[p] = 0.0;
+  f.ftN[p] = 0.0;
+  f.have[p] = 0;
+  f.left[p] = 0;
+  f.ldt[p] = 0.0;
+  f.eid[p] = -1;
+  left0[p] = outside_domain(m, x);
+}
+
+void ftle_seed_grid(const DevMesh& m, const FtleDev& f, double xmin, double ymin, double zmin,
+                    int* left0, cudaStream_t s) {
+  k_ftle_seed<<<nblk(f.n, 256), 256, 0, s>>>(m, f, xmin, ymin, zmin, left0);
+}
+
+// Points outside the domain or the mesh: FTLE -1, and no FTLE is computed
+// for them or their six neighbours (ompVC/ftle.c:429-449, 476-496).  The
+// left flag marks them on entry.
+__global__ void k_ftle_outside(FtleDev f) {
+  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= f.n || !f.left[p]) return;
+  int YZ = f.yr * f.zr;
+  int k = (int)(p % f.zr), j = (int)((p / f.zr) % f.yr), i = (int)(p / YZ);
+  f.ldt[p] = -1.0;
+  f.ftT[p] = -1.0;
+  f.ftN[p] = -1.0;
+  f.have[p] = 1;
+  if (i > 0) f.have[p - YZ] = 1;
+  if (i < f.xr - 1) f.have[p + YZ] = 1;
+  if (j > 0) f.have[p - f.zr] = 1;
+  if (j < f.yr - 1) f.have[p + f.zr] = 1;
+  if (k > 0) f.have[p - 1] = 1;
+  if (k < f.zr - 1) f.have[p + 1] = 1;
+}
+
+void ftle_mark_outside(const FtleDev& f, cudaStream_t s) {
+  k_ftle_outside<<<nblk(f.n, 256), 256, 0, s>>>(f);
+}
+
+__global__ void k_ftle_init_marks(FtleDev f, const int* left0, int unstructured) {
+  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= f.n) return;
+  f.left[p] = left0[p] || (unstructured && f.eid[p] < 0);
+}
+
+void ftle_init_marks(const DevMesh& m, const FtleDev& f, const int* left0, cudaStream_t s) {
+  k_ftle_init_marks<<<nblk(f.n, 256), 256, 0, s>>>(f, left0, m.mesh_type == 1);
+}
+
+// Pass 2a: the trigger of every point without an FTLE value is the exiting
+// member of {q} + 6 neighbours with the lowest linear index -- the exit whose
+// GetFTLEForPointEarly calls (ompVC/ftle.c:130-152) reach q first.
+__global__ void k_ftle_triggers(FtleDev f, DevCounters* ctr) {
+  long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= f.n || f.have[q]) return;
+  int YZ = f.yr * f.zr, zr = f.zr;
+  int k = (int)(q % zr), j = (int)((q / zr) % f.yr), i = (int)(q / YZ);
+  long cand[7] = {i > 0 ? q - YZ : -1, j > 0 ? q - zr : -1, k > 0 ? q - 1 : -1, q,
+                  k < zr - 1 ? q + 1 : -1, j < f.yr - 1 ? q + zr : -1, i < f.xr - 1 ? q + YZ : -1};
+  long trig = -1;
+#pragma unroll
+  for (int c = 0; c < 7; c++)
+    if (cand[c] >= 0 && (f.flag[cand[c]] & 2)) {
+      trig = cand[c];
+      break;
+    }
+  if (trig < 0) return;
+  int slot = atomicAdd(&ctr->count, 1);
+  f.served[slot] = (int)q;
+  f.trig[slot] = (int)trig;
+}
+
+void ftle_triggers(const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
+  cudaMemsetAsync(&ctr->count, 0, sizeof(int), s);
+  k_ftle_triggers<<<nblk(f.n, 256), 256, 0, s>>>(f, ctr);
+}
+
+// UpdateFTLELocations and the per-point writes of ompVC/ftle.c:155-169, 175
+__global__ void k_ftle_update(FtleDev f, int extrapolate, int unstructured) {
+  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= f.n) return;
+  unsigned char fl = f.flag[p];
+  if (!(fl & 1)) return;
+  if (fl & 2) {
+    f.left[p] = 1;
+    return;
+  }
+  f.X[3 * p] = f.Xn[3 * p];
+  f.X[3 * p + 1] = f.Xn[3 * p + 1];
+  f.X[3 * p + 2] = f.Xn[3 * p + 2];
+  f.V[3 * p] = f.Vn[3 * p];
+  f.V[3 * p + 1] = f.Vn[3 * p + 1];
+  f.V[3 * p + 2] = f.Vn[3 * p + 2];
+  if (extrapolate) f.left[p] = (fl & 4) ? 1 : 0;
+  if (unstructured) f.eid[p] = f.en[p];
+}
+
+void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, cudaStream_t s) {
+  k_ftle_update<<<nblk(f.n, 256), 256, 0, s>>>(f, in.extrapolate, m.mesh_type == 1);
+}
+
+// GetFTLEForPoint (ompVC/ftle.c:1050-1203) for points without a value, and
+// the output transpose to k, j, i order (ompVC/ftle.c:1304-1315).
+__global__ void k_ftle_final(FtleDev f, int dims, double int_t) {
+  long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= f.n) return;
+  int YZ = f.yr * f.zr, zr = f.zr;
+  int k = (int)(q % zr), j = (int)((q / zr) % f.yr), i = (int)(q / YZ);
+  double wT = f.ftT[q], wN = f.ftN[q];
+  if (!f.have[q]) {
+    if (int_t < FVC_TINY) {
+      wT = 0.0;
+      wN = 0.0;
+    } else {
+      const double* X = f.X;
+      const double *L, *R, *B, *T, *Bk, *F;
+      double fx, fy, fz;
+      if (i == 0) { L = X + 3 * q; R = X + 3 * (q + YZ); fx = 1.0; }
+      else if (i == f.xr - 1) { L = X + 3 * (q - YZ); R = X + 3 * q; fx = 1.0; }
+      else { L = X + 3 * (q - YZ); R = X + 3 * (q + YZ); fx = 2.0; }
+      if (j == 0) { B = X + 3 * q; T = X + 3 * (q + zr); fy = 1.0; }
+      else if (j == f.yr - 1) { B = X + 3 * (q - zr); T = X + 3 * q; fy = 1.0; }
+      else { B = X + 3 * (q - zr); T = X + 3 * (q + zr); fy = 2.0; }
+      if (dims == 3) {
+        if (k == 0) { Bk = X + 3 * q; F = X + 3 * (q + 1); fz = 1.0; }
+        else if (k == zr - 1) { Bk = X + 3 * (q - 1); F = X + 3 * q; fz = 1.0; }
+        else { Bk = X + 3 * (q - 1); F = X + 3 * (q + 1); fz = 2.0; }
+      } else { Bk = F = X + 3 * q; fz = 1.0; }
+      double lam = stencil_lambda(dims, L, R, B, T, Bk, F, fx, fy, fz, f.dx, f.dy, f.dz);
+      if (lam > 1.0 - FVC_TINY) {
+        wT = (0.5 * log(lam)) / int_t;
+        wN = 0.5 * log(lam);
+      } else {
+        wT = 0.0;
+        wN = 0.0;
+      }
+    }
+    f.ftT[q] = wT;
+    f.ftN[q] = wN;
+  }
+  long o = ((long)k * f.yr + j) * f.xr + i;
+  f.out[o] = wT;
+  f.out[f.n + o] = wN;
+}
+
+void ftle_final(const FtleDev& f, int dims, double int_t, cudaStream_t s) {
+  k_ftle_final<<<nblk(f.n, 128), 128, 0, s>>>(f, dims, int_t);
+}
+
+// ============================================================== tracers
+
+// LeftDomainTime of freshly located seeds: -1 outside, 0 inside
+// (ompVC/tracers.c:1246-1249).
+__global__ void k_tracer_ldt(TracerDev t) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.n) return;
+  t.ldt[i] = t.left[i] ? -1.0 : 0.0;
+  t.V[3 * i] = t.V[3 * i + 1] = t.V[3 * i + 2] = 0.0;
+}
+
+void tracer_init_ldt(const TracerDev& t, cudaStream_t s) {
+  if (t.n > 0) k_tracer_ldt<<<nblk(t.n, 256), 256, 0, s>>>(t);
+}
+
+// ReadInTraceMesh (chain 0, ompVC/tracers.c:1246-1249): LeftDomainTime -1 for
+// every point left out.  GenerateTracerMesh (chain 1, tracers.c:1353-1466)
+// sets -1 only for points inside the bounding box that no element holds and
+// leaves the rest at 0.
+__global__ void k_tracer_init_marks(TracerDev t, const int* left0, int unstructured, int chain) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.n) return;
+  int unplaced = unstructured && !left0[i] && t.eid[i] < 0;
+  int left = left0[i] || unplaced;
+  t.left[i] = left;
+  t.ldt[i] = chain == 0 ? (left ? -1.0 : 0.0) : (unplaced ? -1.0 : 0.0);
+  if (!unstructured || left) t.eid[i] = -1;
+  t.V[3 * i] = t.V[3 * i + 1] = t.V[3 * i + 2] = 0.0;
+}
+
+void tracer_init_marks(const DevMesh& m, const TracerDev& t, const int* left0, int chain_kind,
+                       cudaStream_t s) {
+  if (t.n > 0) k_tracer_init_marks<<<nblk(t.n, 256), 256, 0, s>>>(t, left0, m.mesh_type == 1, chain_kind);
+}
+
+// Output selection of ompVC/tracers.c:247: compaction in seed order with
+// warp ballots; block counts, a scan of them, then the scatter.
+__device__ __forceinline__ bool tracer_selected(const TracerDev& t, long i, int always) {
+  return i < t.n && t.ldt[i] > -FVC_TINY && (!t.left[i] || always);
+}
+
+__global__ void k_compact_count(TracerDev t, int always) {
+  __shared__ int warp_cnt[32];
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned b = __ballot_sync(0xffffffffu, tracer_selected(t, i, always));
+  if ((threadIdx.x & 31) == 0) warp_cnt[threadIdx.x >> 5] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += warp_cnt[k];
+    t.block_cnt[blockIdx.x] = s;
+  }
+}
+
+__global__ void k_compact_scatter(TracerDev t, int always, const int* block_off) {
+  __shared__ int warp_off[32];
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool sel = tracer_selected(t, i, always);
+  unsigned b = __ballot_sync(0xffffffffu, sel);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_off[wid] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+      int c = warp_off[k];
+      warp_off[k] = s;
+      s += c;
+    }
+  }
+  __syncthreads();
+  if (sel) {
+    long o = (long)block_off[blockIdx.x] + warp_off[wid] + __popc(b & ((1u << lane) - 1u));
+    t.outX[3 * o] = t.X[3 * i];
+    t.outX[3 * o + 1] = t.X[3 * i + 1];
+    t.outX[3 * o + 2] = t.X[3 * i + 2];
+  }
+}
+
+__global__ void k_copy_count(const int* src, int* dst) { *dst = *src; }
+
+void tracer_compact(const TracerDev& t, int always, DevCounters* ctr, cudaStream_t s) {
+  if (t.n <= 0) {
+    cudaMemsetAsync(&ctr->count, 0, sizeof(int), s);
+    return;
+  }
+  unsigned nb = nblk(t.n, 1024);
+  k_compact_count<<<nb, 1024, 0, s>>>(t, always);
+  // block_cnt has room for nb + 1 offsets followed by the scan's block totals
+  int* off = t.block_cnt + nb + 1;
+  long long* tmp = reinterpret_cast<long long*>(t.block_cnt + ((2 * nb + 4) & ~1u));
+  exclusive_scan(t.block_cnt, off, (int)nb, tmp, s);
+  k_compact_scatter<<<nb, 1024, 0, s>>>(t, always, off);
+  k_copy_count<<<1, 1, 0, s>>>(off + nb, &ctr->count);
+}
+
+
+// ---------------------------------------------------- per-variant dispatch
+
+#define FVC_VARIANT(m, CALL)                                          \
+  do {                                                                \
+    if ((m).mesh_type == 0) {                                         \
+      if ((m).dims == 2) Variant<2, 0>::CALL; else Variant<3, 0>::CALL; \
+    } else {                                                          \
+      if ((m).dims == 2) Variant<2, 1>::CALL; else Variant<3, 1>::CALL; \
+    }                                                                 \
+  } while (0)
+
+void launch_advect(const DevMesh& m, const DevWindow& w, const DevInteg& in, int n, double* X,
+                   double* V, int* eid, int* left, double* ldt, double t0, double t1,
+                   DevCounters* ctr, cudaStream_t s) {
+  if (n > 0) FVC_VARIANT(m, advect(m, w, in, n, X, V, eid, left, ldt, t0, t1, ctr, s));
+}
+void launch_velocity(const DevMesh& m, const DevWindow& w, int n, const double* X, int* eid,
+                     int* left, double tq, double* out, DevCounters* ctr, cudaStream_t s) {
+  if (n > 0) FVC_VARIANT(m, velocity(m, w, n, X, eid, left, tq, out, ctr, s));
+}
+void ftle_launch(const DevMesh& m, const DevWindow& w, const FtleDev& f, double t, DevCounters* ctr,
+                 cudaStream_t s) {
+  FVC_VARIANT(m, ftle_launch(m, w, f, t, ctr, s));
+}
+void ftle_pass1(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
+                double t1, double t2, DevCounters* ctr, cudaStream_t s) {
+  FVC_VARIANT(m, ftle_pass1(m, w, in, f, t1, t2, ctr, s));
+}
+void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
+                double t1, DevCounters* ctr, cudaStream_t s) {
+  FVC_VARIANT(m, ftle_early(m, w, in, f, t1, ctr, s));
+}
+void tracer_launch_vel(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq,
+                       DevCounters* ctr, cudaStream_t s) {
+  if (t.n > 0) FVC_VARIANT(m, tracer_launch(m, w, t, tq, ctr, s));
+}
+void tracer_advance(const DevMesh& m, const DevWindow& w, const DevInteg& in, const TracerDev& t,
+                    double t1, double t2, DevCounters* ctr, cudaStream_t s) {
+  if (t.n > 0) FVC_VARIANT(m, tracer_advance(m, w, in, t, t1, t2, ctr, s));
+}
+
+}  // namespace fvc

@@ -1,0 +1,139 @@
+// fvc_kernels.h -- host-side launch wrappers for the engine's kernels.
+// Each wrapper launches on the given stream and returns immediately; all
+// pointers are device pointers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fvc_state.h"
+
+namespace fvc {
+
+// Scratch counters shared by the launches of one call.
+struct DevCounters {
+  unsigned long long steps;
+  unsigned long long steps_early;  // accepted steps of the early-FTLE advections
+  int status;
+  int changed;
+  int count;
+  int pad;
+};
+
+// ---- mesh preprocessing
+void launch_geometry(const DevMesh& m, double* geom, cudaStream_t s);
+
+struct BucketGrid {
+  double lo[3], inv[3];   // origin and 1 / cell size
+  int n[3];               // cells per axis
+  const int* start;       // ncells + 1 offsets
+  const int* ids;         // element ids per cell, ascending
+};
+// Builds the grid into caller-owned buffers; returns the number of entries
+// written to ids (the caller sizes ids with bucket_count first).
+long long bucket_count(const DevMesh& m, BucketGrid& g, int* cell_count, int ncells, int* d_total,
+                       cudaStream_t s);
+void bucket_fill(const DevMesh& m, const BucketGrid& g, int* cell_start, int* cursor, int* ids,
+                 int ncells, int* scan_tmp, cudaStream_t s);
+
+void scan_counts(const int* in, int* out, int n, long long* tmp, cudaStream_t s);
+
+// ---- step level
+void launch_advect(const DevMesh& m, const DevWindow& w, const DevInteg& in, int n, double* X,
+                   double* V, int* eid, int* left, double* ldt, double t0, double t1,
+                   DevCounters* ctr, cudaStream_t s);
+void launch_velocity(const DevMesh& m, const DevWindow& w, int n, const double* X, int* eid,
+                     int* left, double tq, double* out, DevCounters* ctr, cudaStream_t s);
+void launch_local_search(const DevMesh& m, int n, const double* X, const int* guess, int* out,
+                         DevCounters* ctr, cudaStream_t s);
+void launch_global_search(const DevMesh& m, const BucketGrid& g, int n, const double* X,
+                          const int* skip, int* out, cudaStream_t s);
+
+// ---- seed location chains (element ids of seeds with ompVC's guess chain)
+struct ChainArgs {
+  int kind;        // 0 FTLE grid (ftle.c:455-602), 1 tracer list (tracers.c:1107-1251),
+                   // 2 generated tracer grid (tracers.c:1340-1530)
+  int n;
+  int res[3];      // FTLE: XRes, YRes, ZRes (i outer, k fastest)
+  int lsc;         // LocalSearchChecking
+  int center_eid;  // global search of the grid centre (kinds 0 and 2), else -1
+};
+// left0: 1 for points outside Data_MeshBounds.  On return eid holds the
+// element or -1 for points the chain could not place.  Returns the number of
+// fixed-point rounds, or -1 on a device fault.
+int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, const double* X,
+                 const int* left0, int* eid, int* work, DevCounters* ctr, cudaStream_t s);
+
+// ---- FTLE slide
+struct FtleDev {
+  int n, xr, yr, zr;
+  double dx, dy, dz;     // FTLE_CartMesh deltas
+  double start;          // StartTime
+  double* X;             // n x 3
+  double* V;             // n x 3
+  double* ldt;
+  double* ftT;
+  double* ftN;
+  int* eid;
+  int* left;
+  int* have;
+  // per-interval scratch
+  double* Xn;
+  double* Vn;
+  double* te;
+  int* en;
+  unsigned char* flag;   // bit0 integrated, bit1 exited, bit2 left after step
+  int* served;           // compacted list of points given an early FTLE
+  int* trig;
+  double* epos;          // early FTLE: 7 positions (6 neighbours, self) per served point
+  double* elt;           // early FTLE: the neighbours' exit times
+  double* emt;           // early FTLE: MinExitTime
+  double* out;           // 2 x n, output order
+};
+void ftle_seed_grid(const DevMesh& m, const FtleDev& f, double xmin, double ymin, double zmin,
+                    int* left0, cudaStream_t s);
+void ftle_mark_outside(const FtleDev& f, cudaStream_t s);
+void ftle_launch(const DevMesh& m, const DevWindow& w, const FtleDev& f, double t, DevCounters* ctr,
+                 cudaStream_t s);
+void ftle_pass1(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
+                double t1, double t2, DevCounters* ctr, cudaStream_t s);
+void ftle_triggers(const FtleDev& f, DevCounters* ctr, cudaStream_t s);
+// the number of served points is read on the device from ctr->count
+void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
+                double t1, DevCounters* ctr, cudaStream_t s);
+void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, cudaStream_t s);
+void ftle_final(const FtleDev& f, int dims, double int_t, cudaStream_t s);
+
+// ---- tracers
+struct TracerDev {
+  int n;
+  double* X;
+  double* V;
+  double* ldt;
+  int* eid;
+  int* left;
+  double* outX;
+  int* block_cnt;
+};
+void tracer_launch_vel(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq,
+                       DevCounters* ctr, cudaStream_t s);
+void tracer_advance(const DevMesh& m, const DevWindow& w, const DevInteg& in, const TracerDev& t,
+                    double t1, double t2, DevCounters* ctr, cudaStream_t s);
+void tracer_init_ldt(const TracerDev& t, cudaStream_t s);
+// Compacts the selected tracers' positions (in seed order) into t.outX;
+// the count lands in ctr->count.
+void tracer_compact(const TracerDev& t, int always, DevCounters* ctr, cudaStream_t s);
+
+// left = outside the domain or not placed by the seed chain; LeftDomainTime
+// as ompVC initialises it for each seeding routine
+void ftle_init_marks(const DevMesh& m, const FtleDev& f, const int* left0, cudaStream_t s);
+void tracer_init_marks(const DevMesh& m, const TracerDev& t, const int* left0, int chain_kind,
+                       cudaStream_t s);
+
+// Time-interpolated node velocities of every slot of w (unstructured meshes).
+void time_fields(const DevMesh& m, const DevWindow& w, double4_32a* vt, cudaStream_t s);
+
+// ---- utilities
+void outside_domain_flags(const DevMesh& m, int n, const double* X, int* left0, cudaStream_t s);
+void pack_frame(const double* uvw, double4_32a* out, long n, cudaStream_t s);
+
+}  // namespace fvc

@@ -1,0 +1,54 @@
+// fvc_state.h -- plain-old-data views of the device-resident mesh, velocity
+// window and integrator settings, passed by value to every kernel.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace fvc {
+
+// per-point fault bits, OR-ed into a launch's status word
+enum : int { PT_ERR_WALK = 1, PT_ERR_TLOC = 2, PT_ERR_STATE = 4 };
+
+struct DevMesh {
+  int dims, mesh_type;  // 2/3; 0 Cartesian, 1 unstructured
+  // Cartesian velocity grid (Vel_CartMesh, ompVC/mesh.c:67-122)
+  double xmin, ymin, zmin, dx, dy, dz;
+  int xres, yres, zres;
+  // unstructured mesh
+  const int4* elem;     // 2 x nelem: {Nodes[4]}, {NeighborIndex[4]}
+  const double* geom;   // natural-coordinate map + node ids, 16 (3D) or 12 (2D) doubles per element
+  const double4_32a* nodes; // x, y, z, 0 per node
+  int nelem, nnodes;
+  // Data_MeshBounds
+  double bounds[6];
+  int max_hops;
+};
+
+// Stage times of one advection call.  Every particle of a call starts at the
+// same t1 with the same step h, so the reference's stage times
+// tc_k, tc_k + h_k/2 and tc_k + h_k (= tc_{k+1}) form one table; slot 2k is
+// tc_k, slot 2k+1 is tc_k + h_k/2.
+#define FVC_MAX_SLOTS 40
+
+// Two resident frames bracketing [tmin, tmax] (Data_LoadedTMin/TMax), and
+// the stage-time table of the current call.  For unstructured meshes vt holds
+// the frames interpolated to every slot's time at every node, computed once
+// per call with the reference's expression (1 - tloc)*U0 + tloc*U1, so a
+// stage evaluation reads the same doubles it would compute.
+struct DevWindow {
+  const double4_32a* f0;  // frame at tmin, (u, v, w, 0) per node
+  const double4_32a* f1;  // frame at tmax
+  double tmin, tmax;
+  const double4_32a* vt;  // nslots x vt_stride time-interpolated node velocities
+  long vt_stride;
+  int nslots;
+  double tq[FVC_MAX_SLOTS];  // slot times
+  double tl[FVC_MAX_SLOTS];  // tloc of each slot, range-checked when the table is built
+};
+
+struct DevInteg {
+  int type;  // 0 Euler, 1 RK4, 3 AB2
+  double h;  // Int_TimeStep
+  int extrapolate;
+};
+
+}  // namespace fvc

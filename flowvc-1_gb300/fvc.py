@@ -1,0 +1,312 @@
+"""ctypes binding of libfvc.so (include/fvc.h) for Python callers and tests.
+
+The engine's public interface is the C ABI; this module is a thin wrapper
+that passes numpy arrays as plain pointers.  It never computes anything on
+the CPU: if the shared library cannot be loaded, or no GPU is present, every
+call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "build", "libfvc.so")
+
+FVC_OK, FVC_ERR_IO, FVC_ERR_ARG, FVC_ERR_OOM, FVC_ERR_WALK, FVC_ERR_TIMEOUT, FVC_ERR_CUDA, FVC_ERR_STATE, FVC_ERR_TLOC = range(9)
+STATUS_NAMES = {0: "FVC_OK", 1: "FVC_ERR_IO", 2: "FVC_ERR_ARG", 3: "FVC_ERR_OOM", 4: "FVC_ERR_WALK",
+                5: "FVC_ERR_TIMEOUT", 6: "FVC_ERR_CUDA", 7: "FVC_ERR_STATE", 8: "FVC_ERR_TLOC"}
+
+# every entry point include/fvc.h declares, with its C signature
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_llp = C.POINTER(C.c_longlong)
+_vp = C.c_void_p
+
+
+class Opts(C.Structure):
+    _fields_ = [("device", C.c_int), ("dims", C.c_int), ("mesh_type", C.c_int), ("max_hops", C.c_int)]
+
+
+class FtleSpec(C.Structure):
+    _fields_ = [("xmin", C.c_double), ("xmax", C.c_double), ("ymin", C.c_double), ("ymax", C.c_double),
+                ("zmin", C.c_double), ("zmax", C.c_double), ("xres", C.c_int), ("yres", C.c_int),
+                ("zres", C.c_int), ("local_search_checking", C.c_int), ("start_time", C.c_double),
+                ("stop_time", C.c_double), ("generate", C.c_int)]
+
+
+class TracerSpec(C.Structure):
+    _fields_ = [("local_search_checking", C.c_int), ("seed_chain", C.c_int), ("center", C.c_double * 3)]
+
+
+class JobStats(C.Structure):
+    _fields_ = [("intervals", C.c_longlong), ("steps_main", C.c_longlong), ("steps_early", C.c_longlong),
+                ("ms_main", C.c_double), ("ms_early", C.c_double), ("ms_reduce", C.c_double),
+                ("ms_setup", C.c_double), ("launches", C.c_longlong)]
+
+
+SIGNATURES = {
+    "fvc_abi_version": (C.c_int, []),
+    "fvc_create": (C.c_int, [C.POINTER(_vp), C.POINTER(Opts)]),
+    "fvc_destroy": (None, [_vp]),
+    "fvc_last_error": (C.c_char_p, [_vp]),
+    "fvc_set_cart_mesh": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
+                                    C.c_double, C.c_double, C.c_int]),
+    "fvc_set_unstruct_mesh": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _ip, _ip]),
+    "fvc_set_bounds": (C.c_int, [_vp, _dp]),
+    "fvc_set_integrator": (C.c_int, [_vp, C.c_int, C.c_double, C.c_int]),
+    "fvc_upload_frame": (C.c_int, [_vp, C.c_int, _dp]),
+    "fvc_set_window": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_double]),
+    "fvc_advect": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_double, _llp]),
+    "fvc_advect_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double, _llp]),
+    "fvc_velocity": (C.c_int, [_vp, C.c_int, _dp, _ip, _ip, C.c_double, _dp]),
+    "fvc_local_search": (C.c_int, [_vp, C.c_int, _dp, _ip, _ip]),
+    "fvc_global_search": (C.c_int, [_vp, C.c_int, _dp, _ip]),
+    "fvc_ftle_create": (C.c_int, [_vp, C.POINTER(FtleSpec), C.POINTER(_vp)]),
+    "fvc_ftle_set_state": (C.c_int, [_vp, _dp, _ip, _ip, _dp, _ip, _dp, _dp]),
+    "fvc_ftle_get_state": (C.c_int, [_vp, _dp, _ip, _ip, _dp, _ip, _dp, _dp]),
+    "fvc_ftle_interval": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double, _llp]),
+    "fvc_ftle_reduce": (C.c_int, [_vp, C.c_double, _dp, _dp]),
+    "fvc_tracer_create": (C.c_int, [_vp, C.POINTER(TracerSpec), C.c_int, _dp, C.POINTER(_vp)]),
+    "fvc_tracer_launch": (C.c_int, [_vp, C.c_double]),
+    "fvc_tracer_advance": (C.c_int, [_vp, C.c_double, C.c_double, _llp]),
+    "fvc_tracer_snapshot": (C.c_int, [_vp, C.c_int, _dp, _llp]),
+    "fvc_tracer_get_state": (C.c_int, [_vp, _dp, _ip, _ip, _dp]),
+    "fvc_job_get_stats": (C.c_int, [_vp, C.POINTER(JobStats)]),
+    "fvc_stream": (_vp, [_vp]),
+    "fvc_job_destroy": (None, [_vp]),
+    "fvc_probe_fp64": (C.c_int, [C.c_int, _dp]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libfvc.so and declare every entry point; raises if it is missing."""
+    global _lib
+    if _lib is not None and path == LIB_PATH:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libfvc.so not built ({path}); run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path == LIB_PATH:
+        _lib = lib
+    return lib
+
+
+def probe_fp64(device=0):
+    """(FP64 fused multiply-adds / s, IEEE divisions / s) measured on the device."""
+    lib = load()
+    r = np.zeros(2)
+    st = lib.fvc_probe_fp64(device, _d(r))
+    if st:
+        raise FvcError(st, "fvc_probe_fp64 failed")
+    return float(r[0]), float(r[1])
+
+
+class FvcError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a.reshape(shape) if shape is not None else a
+
+
+def i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Context:
+    """One fvc_ctx: a mesh, resident frames, a window and integrator settings."""
+
+    def __init__(self, dims, mesh_type, device=0, max_hops=0):
+        self.lib = load()
+        self.h = _vp()
+        o = Opts(device, dims, mesh_type, max_hops)
+        st = self.lib.fvc_create(C.byref(self.h), C.byref(o))
+        if st:
+            raise FvcError(st, "fvc_create failed (no usable GPU?)")
+        self.dims, self.mesh_type = dims, mesh_type
+
+    def _chk(self, st):
+        if st:
+            raise FvcError(st, self.lib.fvc_last_error(self.h).decode())
+
+    def stream(self):
+        """The context's cudaStream_t as an integer handle."""
+        return self.lib.fvc_stream(self.h) or 0
+
+    def close(self):
+        if self.h:
+            self.lib.fvc_destroy(self.h)
+            self.h = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- mesh and settings
+    def set_cart_mesh(self, xmin, xmax, xres, ymin, ymax, yres, zmin, zmax, zres):
+        self._chk(self.lib.fvc_set_cart_mesh(self.h, xmin, xmax, xres, ymin, ymax, yres, zmin, zmax, zres))
+
+    def set_unstruct_mesh(self, xyz, conn, adj):
+        xyz, conn, adj = f64(xyz), i32(conn), i32(adj)
+        self._chk(self.lib.fvc_set_unstruct_mesh(self.h, xyz.shape[0], _d(xyz), conn.shape[0], _i(conn), _i(adj)))
+
+    def set_bounds(self, b):
+        b = f64(b)
+        self._chk(self.lib.fvc_set_bounds(self.h, _d(b)))
+
+    def set_integrator(self, int_type, h, extrapolate=0):
+        self._chk(self.lib.fvc_set_integrator(self.h, int_type, h, extrapolate))
+
+    def upload_frame(self, frame_id, uvw):
+        uvw = f64(uvw)
+        self._chk(self.lib.fvc_upload_frame(self.h, frame_id, _d(uvw)))
+
+    def set_window(self, lo, hi, tmin, tmax):
+        self._chk(self.lib.fvc_set_window(self.h, lo, hi, tmin, tmax))
+
+    # ---- step level
+    def advect(self, X, V, eid, left, ldt, t0, t1):
+        """In-place Advect over arrays; returns the accepted step count."""
+        steps = C.c_longlong(0)
+        self._chk(self.lib.fvc_advect(self.h, X.shape[0], _d(X), _d(V), _i(eid), _i(left), _d(ldt), t0, t1,
+                                      C.byref(steps)))
+        return steps.value
+
+    def velocity(self, X, eid, left, tq):
+        out = np.zeros_like(X)
+        self._chk(self.lib.fvc_velocity(self.h, X.shape[0], _d(X), _i(eid), _i(left), tq, _d(out)))
+        return out
+
+    def local_search(self, X, guess):
+        out = np.empty(X.shape[0], np.int32)
+        self._chk(self.lib.fvc_local_search(self.h, X.shape[0], _d(f64(X)), _i(i32(guess)), _i(out)))
+        return out
+
+    def global_search(self, X):
+        out = np.empty(X.shape[0], np.int32)
+        self._chk(self.lib.fvc_global_search(self.h, X.shape[0], _d(f64(X)), _i(out)))
+        return out
+
+
+class FtleJob:
+    def __init__(self, ctx: Context, spec: FtleSpec):
+        self.ctx, self.lib = ctx, ctx.lib
+        self.h = _vp()
+        ctx._chk(self.lib.fvc_ftle_create(ctx.h, C.byref(spec), C.byref(self.h)))
+        d = ctx.dims
+        self.shape = (spec.xres, spec.yres, spec.zres if d == 3 else 1)
+        self.n = int(np.prod(self.shape))
+
+    def interval(self, launch, t1, t2):
+        steps = C.c_longlong(0)
+        self.ctx._chk(self.lib.fvc_ftle_interval(self.h, int(launch), t1, t2, C.byref(steps)))
+        return steps.value
+
+    def reduce(self, int_t):
+        wT = np.empty(self.n)
+        wN = np.empty(self.n)
+        self.ctx._chk(self.lib.fvc_ftle_reduce(self.h, int_t, _d(wT), _d(wN)))
+        return wT, wN
+
+    def stats(self):
+        st = JobStats()
+        self.ctx._chk(self.lib.fvc_job_get_stats(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in JobStats._fields_}
+
+    def get_state(self):
+        n = self.n
+        X, ldt, wT, wN = np.empty((n, 3)), np.empty(n), np.empty(n), np.empty(n)
+        eid, left, have = np.empty(n, np.int32), np.empty(n, np.int32), np.empty(n, np.int32)
+        self.ctx._chk(self.lib.fvc_ftle_get_state(self.h, _d(X), _i(eid), _i(left), _d(ldt), _i(have), _d(wT), _d(wN)))
+        return dict(X=X, eid=eid, left=left, ldt=ldt, have=have, ftT=wT, ftN=wN)
+
+    def set_state(self, s):
+        self.ctx._chk(self.lib.fvc_ftle_set_state(
+            self.h, _d(f64(s["X"])), _i(i32(s["eid"])), _i(i32(s["left"])), _d(f64(s["ldt"])),
+            _i(i32(s["have"])), _d(f64(s["ftT"])), _d(f64(s["ftN"]))))
+
+    def close(self):
+        if self.h:
+            self.lib.fvc_job_destroy(self.h)
+            self.h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TracerJob:
+    def __init__(self, ctx: Context, seeds, lsc=1, chain=0, center=(0.0, 0.0, 0.0)):
+        self.ctx, self.lib = ctx, ctx.lib
+        self.h = _vp()
+        seeds = f64(seeds)
+        self.n = seeds.shape[0]
+        sp = TracerSpec(lsc, chain, (C.c_double * 3)(*center))
+        ctx._chk(self.lib.fvc_tracer_create(ctx.h, C.byref(sp), self.n, _d(seeds), C.byref(self.h)))
+
+    def launch(self, t):
+        self.ctx._chk(self.lib.fvc_tracer_launch(self.h, t))
+
+    def advance(self, t1, t2):
+        steps = C.c_longlong(0)
+        self.ctx._chk(self.lib.fvc_tracer_advance(self.h, t1, t2, C.byref(steps)))
+        return steps.value
+
+    def snapshot(self, always=0):
+        out = np.empty((max(self.n, 1), 3))
+        cnt = C.c_longlong(0)
+        self.ctx._chk(self.lib.fvc_tracer_snapshot(self.h, always, _d(out), C.byref(cnt)))
+        return out[: cnt.value].copy()
+
+    def stats(self):
+        st = JobStats()
+        self.ctx._chk(self.lib.fvc_job_get_stats(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in JobStats._fields_}
+
+    def get_state(self):
+        n = self.n
+        X, ldt = np.empty((n, 3)), np.empty(n)
+        eid, left = np.empty(n, np.int32), np.empty(n, np.int32)
+        self.ctx._chk(self.lib.fvc_tracer_get_state(self.h, _d(X), _i(eid), _i(left), _d(ldt)))
+        return dict(X=X, eid=eid, left=left, ldt=ldt)
+
+    def close(self):
+        if self.h:
+            self.lib.fvc_job_destroy(self.h)
+            self.h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

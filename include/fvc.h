@@ -1,0 +1,210 @@
+/*
+ * fvc.h -- C ABI of the GB300 flowVC advection engine (libfvc.so).
+ *
+ * The engine replaces the hot path of ompVC (flowVC's OpenMP program):
+ * tracer and FTLE-grid advection through a time-interpolated velocity field
+ * on Cartesian grids or unstructured triangle / tetrahedral meshes, point
+ * location, and the FTLE reduction.  ompVC has no plugin layer; the entry
+ * points below replace the internal calls its driver makes once per frame
+ * interval, and each cites the ompVC routine it stands in for.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  Host arrays are read or written during
+ *     the call and never retained; the library keeps its own device copies.
+ *   - Every call returns an fvc_status; fvc_last_error() gives the text of
+ *     the last failure on a context.  Nothing calls exit().
+ *   - A context owns one CUDA stream on one device.  Calls on one context
+ *     must not overlap; separate contexts may be used from separate threads.
+ *   - Arithmetic is IEEE FP64 in ompVC's operation order: element ids, exit
+ *     flags and positions are bit-identical to ompVC built for x86-64.
+ *   - Point arrays are n x 3 doubles (x, y, z interleaved), as in ompVC's
+ *     LagrangianPoint.X.
+ */
+#ifndef FVC_H
+#define FVC_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FVC_ABI_VERSION 1
+
+typedef int fvc_status;
+enum {
+  FVC_OK = 0,
+  FVC_ERR_IO = 1,      /* file or host I/O failure */
+  FVC_ERR_ARG = 2,     /* invalid argument or unsupported option */
+  FVC_ERR_OOM = 3,     /* device or host allocation failed */
+  FVC_ERR_WALK = 4,    /* neighbour walk hit its hop cap or an indeterminate
+                          neighbour (ompVC: FatalError "Indeterminate neighbor") */
+  FVC_ERR_TIMEOUT = 5, /* a bounded device wait gave up */
+  FVC_ERR_CUDA = 6,    /* CUDA runtime error */
+  FVC_ERR_STATE = 7,   /* call out of order, or a point that left was advected */
+  FVC_ERR_TLOC = 8     /* query time outside the loaded frame interval
+                          (ompVC: FatalError "tloc must be between 0 and 1") */
+};
+
+typedef struct fvc_ctx fvc_ctx;
+typedef struct fvc_job fvc_job;
+
+typedef struct {
+  int device;    /* CUDA device ordinal */
+  int dims;      /* Dimensions: 2 or 3 */
+  int mesh_type; /* Data_MeshType: 0 Cartesian, 1 unstructured */
+  int max_hops;  /* neighbour-walk cap per point location, 0 = 65536 */
+} fvc_opts;
+
+int fvc_abi_version(void);
+
+/* Context lifetime.  Replaces ompVC's process globals (ompVC/globals.h:17-168). */
+fvc_status fvc_create(fvc_ctx **ctx, const fvc_opts *opts);
+void fvc_destroy(fvc_ctx *ctx);
+const char *fvc_last_error(const fvc_ctx *ctx);
+
+/* Cartesian velocity grid; replaces LoadCartMeshData (ompVC/mesh.c:67-122).
+ * The deltas are derived exactly as ompVC derives them. */
+fvc_status fvc_set_cart_mesh(fvc_ctx *ctx, double xmin, double xmax, int xres, double ymin,
+                             double ymax, int yres, double zmin, double zmax, int zres);
+
+/* Unstructured mesh; replaces LoadUnstructMeshData (ompVC/mesh.c:124-213).
+ * xyz: nnodes x 3; conn, adj: nelem x 4 in ompVC's layout (triangles: 4th
+ * connectivity slot -1).  Also builds the bucket grid used by global search. */
+fvc_status fvc_set_unstruct_mesh(fvc_ctx *ctx, int nnodes, const double *xyz, int nelem,
+                                 const int *conn, const int *adj);
+
+/* Data_MeshBounds: xmin xmax ymin ymax zmin zmax (TestOutsideDomain,
+ * ompVC/velocity.c:654-669). */
+fvc_status fvc_set_bounds(fvc_ctx *ctx, const double bounds[6]);
+
+/* Int_Type (0 Euler, 1 RK4, 3 two-step Adams-Bashforth), Int_TimeStep and
+ * Int_Extrapolate; replaces the globals Advect reads
+ * (ompVC/integration.c:22-45). */
+fvc_status fvc_set_integrator(fvc_ctx *ctx, int int_type, double h, int extrapolate);
+
+/* Velocity frames.  uvw is one frame as stored in a <prefix>_vel.<n>.bin file
+ * after its time stamp: (u, v, w) per node, Cartesian nodes in k, j, i order
+ * with i fastest.  Frames stay resident on the device under the caller's
+ * frame_id (0 <= frame_id < 65536) until replaced; replaces
+ * Load{Cart,Unstruct}VelDataFrame (ompVC/velocity.c:61-234). */
+fvc_status fvc_upload_frame(fvc_ctx *ctx, int frame_id, const double *uvw);
+
+/* Select the two resident frames bracketing [tmin, tmax] (Data_LoadedTMin /
+ * Data_LoadedTMax, ompVC/main.c:188-195); frame_lo is the frame at tmin. */
+fvc_status fvc_set_window(fvc_ctx *ctx, int frame_lo, int frame_hi, double tmin, double tmax);
+
+/* ---- step level ------------------------------------------------------- */
+
+/* Advect n points from t0 to t1: ompVC's Advect (ompVC/integration.c:22-45)
+ * over arrays.  X (n x 3), V (n x 3, may be NULL unless extrapolating), eid
+ * (may be NULL on Cartesian meshes), left and ldt (LeftDomainTime) are
+ * updated in place; points with left set are skipped unless extrapolating.
+ * steps (may be NULL) receives the number of accepted integration steps. */
+fvc_status fvc_advect(fvc_ctx *ctx, int n, double *X, double *V, int *eid, int *left, double *ldt,
+                      double t0, double t1, long long *steps);
+
+/* The same on arrays already in device memory (d-prefixed pointers), on the
+ * context's stream; returns after the work completes. */
+fvc_status fvc_advect_device(fvc_ctx *ctx, int n, double *dX, double *dV, int *deid, int *dleft,
+                             double *dldt, double t0, double t1, long long *steps);
+
+/* GetVelocity (ompVC/velocity.c:236-247) at time tq for n points; eid walks
+ * and left is set as the reference does.  out: n x 3. */
+fvc_status fvc_velocity(fvc_ctx *ctx, int n, const double *X, int *eid, int *left, double tq,
+                        double *out);
+
+/* Get_Element_Local_Search (ompVC/mesh.c:496-611) from guess[i]. */
+fvc_status fvc_local_search(fvc_ctx *ctx, int n, const double *X, const int *guess, int *out);
+
+/* Get_Element_Global_Search (ompVC/mesh.c:304-398): the lowest element id
+ * containing each point, -1 if none; answered from a uniform bucket grid. */
+fvc_status fvc_global_search(fvc_ctx *ctx, int n, const double *X, int *out);
+
+/* ---- FTLE job: one output slide of ompVC's FTLE computation ------------ */
+
+typedef struct {
+  /* FTLE_CartMesh: seed grid bounds and resolution (ZRes = 1 in 2D) */
+  double xmin, xmax, ymin, ymax, zmin, zmax;
+  int xres, yres, zres;
+  int local_search_checking; /* LocalSearchChecking */
+  double start_time;         /* FTLE_Launches[ss].StartTime */
+  double stop_time;          /* FTLE_Launches[ss].StopTime */
+  int generate;              /* 1: seed the grid and locate it on the device
+                                (InitializeFTLEArray, ompVC/ftle.c:383-628);
+                                0: state comes from fvc_ftle_set_state */
+} fvc_ftle_spec;
+
+fvc_status fvc_ftle_create(fvc_ctx *ctx, const fvc_ftle_spec *spec, fvc_job **job);
+
+/* FTLEPoint state in the seed grid's (i, j, k) order, k fastest
+ * (ompVC/ftle.c:616-624); any pointer may be NULL to skip that field. */
+fvc_status fvc_ftle_set_state(fvc_job *job, const double *X, const int *eid, const int *left,
+                              const double *ldt, const int *have, const double *ftle_wT,
+                              const double *ftle_woT);
+fvc_status fvc_ftle_get_state(fvc_job *job, double *X, int *eid, int *left, double *ldt, int *have,
+                              double *ftle_wT, double *ftle_woT);
+
+/* One frame interval of the slide: ComputeFTLE's body for one slide
+ * (ompVC/ftle.c:72-176) on the context's current window.  launch = 1 on the
+ * slide's first interval (evaluates the launch velocity, ftle.c:80-99).
+ * Points that leave get their FTLE early (GetFTLEForPointEarly,
+ * ftle.c:788-1048) with the result of ompVC's serial loop order. */
+fvc_status fvc_ftle_interval(fvc_job *job, int launch, double t1, double t2, long long *steps);
+
+/* FTLE of every point still without one (GetFTLEForPoint, ftle.c:1050-1203)
+ * and the two output fields in output order (k, j, i with i fastest,
+ * OutputFTLE, ftle.c:1304-1315). */
+fvc_status fvc_ftle_reduce(fvc_job *job, double int_t, double *ftle_wT, double *ftle_woT);
+
+/* ---- tracer job: one release of ompVC's tracer computation ------------- */
+
+typedef struct {
+  int local_search_checking; /* LocalSearchChecking */
+  int seed_chain;            /* element-location chain for the seeds:
+                                0 list order (ReadInTraceMesh, ompVC/tracers.c:1107-1251)
+                                1 generated grid (GenerateTracerMesh, ompVC/tracers.c:1314-1533) */
+  double center[3];          /* grid centre used by chain 1 */
+} fvc_tracer_spec;
+
+/* Seeds n x 3; points outside Data_MeshBounds or the mesh are marked as
+ * left, as ompVC marks them. */
+fvc_status fvc_tracer_create(fvc_ctx *ctx, const fvc_tracer_spec *spec, int n, const double *seeds,
+                             fvc_job **job);
+/* Release velocity at t_start (ompVC/tracers.c:190-207). */
+fvc_status fvc_tracer_launch(fvc_job *job, double t_start);
+/* Advect live tracers over [t1, t2] (ompVC/tracers.c:217-240). */
+fvc_status fvc_tracer_advance(fvc_job *job, double t1, double t2, long long *steps);
+/* Positions of the tracers ompVC writes at an output time, in seed order
+ * (ompVC/tracers.c:243-256): LeftDomainTime > -TINY and (not left or
+ * always_output).  X_out must hold n x 3; *count receives the number. */
+fvc_status fvc_tracer_snapshot(fvc_job *job, int always_output, double *X_out, long long *count);
+fvc_status fvc_tracer_get_state(fvc_job *job, double *X, int *eid, int *left, double *ldt);
+
+/* Counters of a job since its creation, from CUDA events recorded on the
+ * context's stream around each launch. */
+typedef struct {
+  long long intervals;     /* frame intervals (or advance calls) run */
+  long long steps_main;    /* accepted steps of the main advection pass */
+  long long steps_early;   /* accepted steps of the early-FTLE advections */
+  double ms_main;          /* device time of the main advection kernel */
+  double ms_early;         /* device time of trigger search + early FTLE */
+  double ms_reduce;        /* device time of the FTLE reduction */
+  double ms_setup;         /* device time of seeding and seed location */
+  long long launches;      /* kernels launched on the job's behalf */
+} fvc_job_stats;
+fvc_status fvc_job_get_stats(fvc_job *job, fvc_job_stats *out);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that record their
+ * own events on it or order their work after the engine's. */
+void *fvc_stream(fvc_ctx *ctx);
+
+void fvc_job_destroy(fvc_job *job);
+
+/* Measured FP64 rates of a device, the denominators of the exact path's
+ * FP64 roofline: rates[0] fused multiply-adds / s (one operation each),
+ * rates[1] IEEE divisions / s.  No reference counterpart (measurement aid). */
+fvc_status fvc_probe_fp64(int device, double rates[2]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -480,6 +480,19 @@ static int output_ftle(orc_run_state *S, ftle_slide *s, int ss, double IntT, cha
     int id = P->ftle_var ? s->nout : (P->int_dir > 0 ? ss : (P->out_tres - 1 - ss));
     for (int q = 0; q < s->n; q++)
         if (!s->have[q]) final_ftle(S, s, q, IntT);
+    const char *dump = getenv("ORC_DUMP_STATE");
+    if (dump && *dump) {
+        snprintf(path, sizeof(path), "%s/state.%d.bin", dump, id);
+        FILE *f = fopen(path, "wb");
+        if (f) {
+            fwrite(&s->n, 4, 1, f);
+            fwrite(s->X, 8, 3 * (size_t)s->n, f);
+            fwrite(s->eid, 4, (size_t)s->n, f);
+            fwrite(s->left, 4, (size_t)s->n, f);
+            fwrite(s->have, 4, (size_t)s->n, f);
+            fclose(f);
+        }
+    }
     double *buf = (double *)malloc(sizeof(double) * (size_t)s->n * 2);
     if (!buf) return set_err(err, errlen, ORC_ERR_OOM, "out of memory");
     long m = 0;

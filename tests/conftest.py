@@ -1,0 +1,91 @@
+"""Shared fixtures: build the oracle (CPU, test infrastructure) and the engine,
+and run golden cases through either program."""
+from __future__ import annotations
+
+import json
+import os
+import shutil
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "flowvc-1_gb300")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+for p in (PKG, os.path.join(ROOT, "tests")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a GB300 (runs the CUDA engine)")
+
+
+@pytest.fixture(scope="session")
+def oracle_bin():
+    r = subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-s"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return os.path.join(ROOT, "oracle", "build", "orcflow")
+
+
+@pytest.fixture(scope="session")
+def engine():
+    import build as fvc_build
+    fvc_build.build()
+    return fvc_build
+
+
+def golden_cases():
+    out = []
+    for name in sorted(os.listdir(GOLDEN)):
+        pj = os.path.join(GOLDEN, name, "params.json")
+        if os.path.exists(pj):
+            with open(pj) as f:
+                P = json.load(f)
+            for run in sorted(P["runs"]):
+                out.append((name, run))
+    return out
+
+
+def run_golden(exe, case, run, tmp_path, extra_args=()):
+    """Run `exe` on golden case/run with inputs copied under tmp_path; returns the output dir."""
+    import synth
+    with open(os.path.join(GOLDEN, case, "params.json")) as f:
+        P = json.load(f)
+    data = os.path.join(str(tmp_path), case + "_in")
+    if not os.path.exists(data):
+        shutil.copytree(os.path.join(GOLDEN, case, "inputs"), data)
+    out = os.path.join(str(tmp_path), case + "_" + run + "_" + os.path.basename(exe))
+    os.makedirs(out, exist_ok=True)
+    inp = os.path.join(str(tmp_path), f"{case}_{run}.in")
+    synth.write_in_file(inp, **dict(P["base"], **P["runs"][run], Path_Data=data + "/", Path_Output=out + "/"))
+    r = subprocess.run([exe, inp, *extra_args], capture_output=True, text=True)
+    assert r.returncode == 0, f"{exe} failed:\n{r.stdout[-3000:]}\n{r.stderr[-3000:]}"
+    return out, r.stdout
+
+
+# FTLE fields: the engine computes the Cauchy-Green eigenvalue with its own
+# Jacobi solver (the reference uses Householder + QL), so FTLE values agree to
+# a few ulps of lambda; log(lambda) amplifies that near lambda = 1.  Positions
+# and tracer outputs are compared bit for bit.
+FTLE_RTOL = 1e-12
+FTLE_ATOL = 1e-13
+
+
+def compare_outputs(expected_dir, got_dir, ftle_rtol=FTLE_RTOL, ftle_atol=FTLE_ATOL):
+    exp = sorted(os.listdir(expected_dir))
+    got = sorted(f for f in os.listdir(got_dir))
+    assert exp == got, f"output files differ: expected {exp}, got {got}"
+    for f in exp:
+        a = open(os.path.join(expected_dir, f), "rb").read()
+        b = open(os.path.join(got_dir, f), "rb").read()
+        if f.endswith(".info") or f.endswith("_Cartesian.bin") or f.startswith("tracer"):
+            assert a == b, f"{f}: bytes differ"
+            continue
+        assert len(a) == len(b), f"{f}: length {len(a)} != {len(b)}"
+        A = np.frombuffer(a, "<f8")
+        B = np.frombuffer(b, "<f8")
+        assert A[0] == B[0], f"{f}: time stamp"
+        np.testing.assert_allclose(B[1:], A[1:], rtol=ftle_rtol, atol=ftle_atol, err_msg=f)

@@ -1,0 +1,142 @@
+"""Array-level parity of the CUDA integrators with the CPU oracle.
+
+fvc_advect / fvc_velocity / fvc_local_search / fvc_global_search against the
+oracle's restatement of ompVC on the same inputs: positions, element ids,
+exit flags, exit times and step counts must be bit-identical."""
+import zlib
+
+import numpy as np
+import pytest
+
+import fvc
+import oracle_lib
+import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def make_field(kind, seed=0):
+    rng = np.random.default_rng(seed)
+    if kind == "cart2":
+        nx, ny = 41, 21
+        xs, ys = np.linspace(0, 2, nx), np.linspace(0, 1, ny)
+        Y, X = np.meshgrid(ys, xs, indexing="ij")
+        f = []
+        for t in (0.3, 0.4):
+            u, v = synth.double_gyre(X, Y, t)
+            f.append(np.stack([u, v, 0.01 * np.ones_like(u)], -1).reshape(-1, 3))
+        # w != 0 exercises the reference's W update in 2D; the z bounds keep
+        # points from leaving through it
+        return dict(dims=2, mesh=0, cart=(0.0, 2.0, nx, 0.0, 1.0, ny, 0.0, 0.0, 1), bounds=[0, 2, 0, 1, -1, 1],
+                    frames=f, lo=[0, 0, 0], hi=[2, 1, 0])
+    if kind == "cart3":
+        n = 13
+        g = np.linspace(0, 1, n)
+        Z, Y, X = np.meshgrid(g, g, g, indexing="ij")
+        P = np.stack([X, Y, Z], -1).reshape(-1, 3)
+        f = [synth.abc_flow(P, t) * 0.3 for t in (0.3, 0.4)]
+        return dict(dims=3, mesh=0, cart=(0.0, 1.0, n, 0.0, 1.0, n, 0.0, 1.0, n), bounds=[0, 1, 0, 1, 0, 1],
+                    frames=f, lo=[0, 0, 0], hi=[1, 1, 1])
+    if kind == "tri":
+        xyz, conn, adj = synth.tri_square_mesh(24, jitter=0.2, seed=seed, lo=0.0, hi=2.0, ny=12, yhi=1.0)
+        f = []
+        for t in (0.3, 0.4):
+            u, v = synth.double_gyre(xyz[:, 0], xyz[:, 1], t)
+            f.append(np.stack([u, v, np.zeros_like(u)], -1))
+        return dict(dims=2, mesh=1, xyz=xyz, conn=conn, adj=adj, bounds=[0, 2, 0, 1, 0, 0], frames=f,
+                    lo=[0, 0, 0], hi=[2, 1, 0])
+    xyz, conn, adj = synth.kuhn_cube_mesh(8, jitter=0.2, seed=seed)
+    f = [synth.abc_flow(xyz, t) * 0.3 for t in (0.3, 0.4)]
+    return dict(dims=3, mesh=1, xyz=xyz, conn=conn, adj=adj, bounds=[0, 1, 0, 1, 0, 1], frames=f,
+                lo=[0, 0, 0], hi=[1, 1, 1])
+
+
+def setup_pair(F, int_type, h, extrap):
+    o = oracle_lib.Oracle(F["dims"], F["mesh"])
+    g = fvc.Context(F["dims"], F["mesh"])
+    if F["mesh"] == 0:
+        o.set_cart(*F["cart"])
+        g.set_cart_mesh(*F["cart"])
+    else:
+        o.set_unstruct(F["xyz"], F["conn"], F["adj"])
+        g.set_unstruct_mesh(F["xyz"], F["conn"], F["adj"])
+    o.set_bounds(F["bounds"])
+    g.set_bounds(F["bounds"])
+    o.set_frames(F["frames"][0], F["frames"][1], 0.3, 0.4)
+    g.upload_frame(7, F["frames"][0])
+    g.upload_frame(8, F["frames"][1])
+    g.set_window(7, 8, 0.3, 0.4)
+    o.set_integrator(int_type, h, extrap)
+    g.set_integrator(int_type, h, extrap)
+    return o, g
+
+
+def seeds(F, n, rng):
+    lo, hi = np.array(F["lo"], float), np.array(F["hi"], float)
+    pad = 0.02 * (hi - lo)
+    P = rng.uniform(lo - pad, hi + pad, size=(n, 3))
+    if F["dims"] == 2:
+        P[:, 2] = 0.0
+    return P
+
+
+@pytest.mark.parametrize("kind", ["cart2", "cart3", "tri", "tet"])
+@pytest.mark.parametrize("int_type", [0, 1, 3])
+@pytest.mark.parametrize("direction", [1, -1])
+@pytest.mark.parametrize("extrap", [0, 1])
+def test_advect_bit_exact(engine, kind, int_type, direction, extrap):
+    F = make_field(kind)
+    rng = np.random.default_rng(zlib.crc32(f"{kind}{int_type}{direction}{extrap}".encode()))
+    o, g = setup_pair(F, int_type, 0.0071, extrap)
+    P = seeds(F, 3000, rng)
+    n = len(P)
+    left = np.zeros(n, np.int32)
+    if F["mesh"] == 1:
+        eid = o.global_search(P)
+        left[eid < 0] = 1
+    else:
+        eid = np.full(n, -1, np.int32)
+        left[(P[:, :F["dims"]] < np.array(F["lo"][:F["dims"]])).any(1) | (P[:, :F["dims"]] > np.array(F["hi"][:F["dims"]])).any(1)] = 1
+    V = rng.normal(size=(n, 3)) * 0.1
+    ldt = np.zeros(n)
+    t0, t1 = (0.3, 0.4) if direction > 0 else (0.4, 0.3)
+    t1 = t0 + direction * 0.0877  # a clipped last step
+    a = [P.copy(), V.copy(), eid.copy(), left.copy(), ldt.copy()]
+    b = [P.copy(), V.copy(), eid.copy(), left.copy(), ldt.copy()]
+    sa = o.advect(*a, t0, t1)
+    sb = g.advect(*b, t0, t1)
+    names = ["X", "V", "eid", "left", "ldt"]
+    for nm, x, y in zip(names, a, b):
+        assert np.array_equal(x, y), f"{nm} differs ({kind}, type {int_type})"
+    assert sa == sb > 0
+
+
+@pytest.mark.parametrize("kind", ["cart2", "cart3", "tri", "tet"])
+def test_velocity_bit_exact(engine, kind):
+    F = make_field(kind, seed=1)
+    rng = np.random.default_rng(11)
+    o, g = setup_pair(F, 1, 0.01, 0)
+    P = seeds(F, 2000, rng)
+    n = len(P)
+    if F["mesh"] == 1:
+        guess = rng.integers(0, F["conn"].shape[0], n).astype(np.int32)
+    else:
+        guess = np.full(n, -1, np.int32)
+    ea, eb = guess.copy(), guess.copy()
+    la, lb = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    va = o.velocity(P, ea, la, 0.3377)
+    vb = g.velocity(P, eb, lb, 0.3377)
+    assert np.array_equal(va, vb) and np.array_equal(ea, eb) and np.array_equal(la, lb)
+
+
+@pytest.mark.parametrize("kind", ["tri", "tet"])
+def test_searches_bit_exact(engine, kind):
+    F = make_field(kind, seed=2)
+    rng = np.random.default_rng(5)
+    o, g = setup_pair(F, 1, 0.01, 0)
+    P = seeds(F, 5000, rng)
+    # points exactly on shared faces and vertices: ties resolved identically
+    P[:200] = F["xyz"][rng.integers(0, F["xyz"].shape[0], 200)]
+    assert np.array_equal(o.global_search(P), g.global_search(P))
+    guess = rng.integers(0, F["conn"].shape[0], len(P)).astype(np.int32)
+    assert np.array_equal(o.local_search(P, guess), g.local_search(P, guess))
