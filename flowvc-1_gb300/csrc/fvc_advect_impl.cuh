@@ -102,36 +102,34 @@ __global__ void k_ftle_launch(DevMesh m, DevWindow w, FtleDev f, double t, DevCo
 }
 
 
-// Pass 1: every live point from its frame-start state (ompVC/ftle.c:109-130).
+// Pass 1: every live point from its frame-start state (ompVC/ftle.c:109-130),
+// one thread per entry of the interval's compacted live list.
 template <int D, int M>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_pass1(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
                                                     double t1, double t2, DevCounters* ctr) {
-  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nlive = *(volatile int*)&ctr->nlive;
   unsigned steps = 0;
   int err = 0;
-  if (p < f.n) {
-    unsigned char fl = 0;
-    if (f.ldt[p] > -FVC_TINY && (!f.left[p] || in.extrapolate)) {
-      Pt t;
-      load_pt(t, p, f.X, f.V, f.eid, f.left, f.ldt);
-      err = advect<D, M>(m, w, in, t, t1, t2, steps);
-      fl = 1 | ((t.left && !in.extrapolate) ? 2 : 0) | (t.left ? 4 : 0);
-      f.Xn[3 * p] = t.X[0];
-      f.Xn[3 * p + 1] = t.X[1];
-      f.Xn[3 * p + 2] = t.X[2];
+  if (idx < nlive) {
+    long p = f.live[idx];
+    Pt t;
+    load_pt(t, p, f.X, in.extrapolate ? f.V : nullptr, f.eid, f.left, f.ldt);
+    err = advect<D, M>(m, w, in, t, t1, t2, steps);
+    f.flag[p] = 1 | ((t.left && !in.extrapolate) ? 2 : 0) | (t.left ? 4 : 0);
+    f.Xn[3 * p] = t.X[0];
+    f.Xn[3 * p + 1] = t.X[1];
+    f.Xn[3 * p + 2] = t.X[2];
+    if (in.extrapolate) {
       f.Vn[3 * p] = t.V[0];
       f.Vn[3 * p + 1] = t.V[1];
       f.Vn[3 * p + 2] = t.V[2];
-      f.en[p] = t.eid;
-      f.te[p] = t.ldt;
     }
-    f.flag[p] = fl;
+    f.en[p] = t.eid;
+    f.te[p] = t.ldt;
   }
   flush_counters(&ctr->steps, &ctr->status, steps, err);
 }
-
-
-
 
 template <int D, int M>
 __device__ __forceinline__ int adv_from_start(const DevMesh& m, const DevWindow& w, const DevInteg& in,
@@ -150,8 +148,8 @@ __device__ __forceinline__ int adv_from_start(const DevMesh& m, const DevWindow&
 }
 
 // Pass 2b: GetFTLEForPointEarly (ompVC/ftle.c:788-1048) for every served point
-// q with its trigger's exit time te, spread over four launches so the up to
-// thirteen advections of one point run in parallel:
+// q with its trigger's exit time te.  Its up to thirteen advections are queued
+// as tasks so full warps run them:
 //   A  each of q's six neighbours from its frame-start state to te
 //   B  MinExitTime = min(te, the neighbours' exit times)   (ftle.c:878)
 //   C  q itself to MinExitTime, and the neighbours again when MinExitTime
@@ -177,70 +175,92 @@ __device__ __forceinline__ int eid_at_trigger(const FtleDev& f, long pp, long tr
   return (pp < trig && (f.flag[pp] & 1) && !(f.flag[pp] & 2)) ? f.en[pp] : f.eid[pp];
 }
 
-template <int D, int M>
-__global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_early_nb(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
-                                                       double t1, DevCounters* ctr) {
+// Appends (s, c) to the task list; the lanes of a warp land next to each other.
+__device__ __forceinline__ void append_task(const FtleDev& f, DevCounters* ctr, bool want, int s, int c) {
+  unsigned b = __ballot_sync(0xffffffffu, want);
+  if (!b) return;
+  int lane = threadIdx.x & 31, base = 0;
+  if (lane == 0) base = atomicAdd(&ctr->ntask, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (want) f.tasks[base + __popc(b & ((1u << lane) - 1u))] = make_int2(s, c);
+}
+
+// A: queue the neighbours that exist; boundary slots keep te as exit time.
+template <int D>
+__global__ void k_ftle_queue_nb(FtleDev f, DevCounters* ctr) {
   long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nserved = *(volatile int*)&ctr->count;
-  unsigned steps = 0;
-  int err = 0;
   long s = idx / 6;
   int c = (int)(idx % 6);
+  bool want = false;
   if (s < nserved) {
-    long q = f.served[s], trig = f.trig[s];
-    double te = f.te[trig];
     long nb[6];
     int i, j, k;
-    served_geometry(f, q, nb, i, j, k);
-    double lt = te;
-    double* pos = f.epos + (s * 7 + c) * 3;
-    if (nb[c] >= 0) {
-      Pt t;
-      err = adv_from_start<D, M>(m, w, in, f, nb[c], eid_at_trigger(f, nb[c], trig), t1, te, t, steps);
-      if (t.left) lt = t.ldt;
-      pos[0] = t.X[0];
-      pos[1] = t.X[1];
-      pos[2] = t.X[2];
-    }
-    f.elt[s * 6 + c] = lt;
+    served_geometry(f, f.served[s], nb, i, j, k);
+    want = nb[c] >= 0;
+    if (!want) f.elt[s * 6 + c] = f.te[f.trig[s]];
   }
-  flush_counters(&ctr->steps_early, &ctr->status, steps, err);
+  append_task(f, ctr, want, (int)s, c);
 }
 
+// B + C queue: MinExitTime, then q itself and (if it moved) the neighbours.
 template <int D>
-__global__ void k_ftle_early_mid(FtleDev f, DevCounters* ctr) {
-  long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long nserved = *(volatile int*)&ctr->count;
-  if (s >= nserved) return;
-  double te = f.te[f.trig[s]];
-  const double* lt = f.elt + s * 6;
-  f.emt[s] = dmin(te, dmin(lt[5], dmin(lt[4], dmin(lt[3], dmin(lt[2], dmin(lt[1], lt[0]))))));
-}
-
-template <int D, int M>
-__global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_early_self(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
-                                                         double t1, DevCounters* ctr) {
+__global__ void k_ftle_queue_self(FtleDev f, DevCounters* ctr) {
   long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nserved = *(volatile int*)&ctr->count;
-  unsigned steps = 0;
-  int err = 0;
   long s = idx / 7;
   int c = (int)(idx % 7);
+  bool want = false;
   if (s < nserved) {
+    double te = f.te[f.trig[s]];
+    const double* lt = f.elt + s * 6;
+    double mt = dmin(te, dmin(lt[5], dmin(lt[4], dmin(lt[3], dmin(lt[2], dmin(lt[1], lt[0]))))));
+    if (c == 6) {
+      f.emt[s] = mt;
+      want = true;
+    } else if (mt != te) {
+      long nb[6];
+      int i, j, k;
+      served_geometry(f, f.served[s], nb, i, j, k);
+      want = nb[c] >= 0;
+    }
+  }
+  append_task(f, ctr, want, (int)s, c);
+}
+
+// The advections of A (phase 0: to te, recording exit times) and C (phase 1:
+// to MinExitTime).
+template <int D, int M>
+__global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_tasks(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
+                                                                   double t1, int phase, DevCounters* ctr) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long ntask = *(volatile int*)&ctr->ntask;
+  unsigned steps = 0;
+  int err = 0;
+  if (idx < ntask) {
+    int2 tk = f.tasks[idx];
+    long s = tk.x;
+    int c = tk.y;
     long q = f.served[s], trig = f.trig[s];
-    double te = f.te[trig], mt = f.emt[s];
     long nb[6];
     int i, j, k;
     served_geometry(f, q, nb, i, j, k);
     long p = c == 6 ? q : nb[c];
-    if (p >= 0 && (c == 6 || mt != te)) {
-      Pt t;
-      err = adv_from_start<D, M>(m, w, in, f, p, eid_at_trigger(f, p, trig), t1, mt, t, steps);
-      double* pos = f.epos + (s * 7 + c) * 3;
-      pos[0] = t.X[0];
-      pos[1] = t.X[1];
-      pos[2] = t.X[2];
-    }
+    double tend = phase == 0 ? f.te[trig] : f.emt[s];
+    Pt t;
+    t.X[0] = f.X[3 * p];
+    t.X[1] = f.X[3 * p + 1];
+    t.X[2] = f.X[3 * p + 2];
+    t.V[0] = t.V[1] = t.V[2] = 0.0;
+    t.left = f.left[p];
+    t.eid = eid_at_trigger(f, p, trig);
+    t.ldt = 0.0;
+    err = advect<D, M>(m, w, in, t, t1, tend, steps);
+    double* pos = f.epos + (s * 7 + c) * 3;
+    pos[0] = t.X[0];
+    pos[1] = t.X[1];
+    pos[2] = t.X[2];
+    if (phase == 0) f.elt[s * 6 + c] = t.left ? t.ldt : tend;
   }
   flush_counters(&ctr->steps_early, &ctr->status, steps, err);
 }
@@ -302,10 +322,12 @@ __global__ void k_tracer_launch(DevMesh m, DevWindow w, TracerDev t, double tq, 
 template <int D, int M>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_tracer_advance(DevMesh m, DevWindow w, DevInteg in, TracerDev t,
                                                         double t1, double t2, DevCounters* ctr) {
-  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nlive = *(volatile int*)&ctr->nlive;
   unsigned steps = 0;
   int err = 0;
-  if (i < t.n && t.ldt[i] > -FVC_TINY && (!t.left[i] || in.extrapolate)) {
+  if (idx < nlive) {
+    long i = t.live[idx];
     Pt p;
     load_pt(p, i, t.X, t.V, t.eid, t.left, t.ldt);
     err = advect<D, M>(m, w, in, p, t1, t2, steps);
@@ -345,9 +367,12 @@ struct Variant {
   }
   static void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
                          double t1, DevCounters* ctr, cudaStream_t s) {
-    k_ftle_early_nb<D, M><<<vblk(6L * f.n, 128), 128, 0, s>>>(m, w, in, f, t1, ctr);
-    k_ftle_early_mid<D><<<vblk(f.n, 256), 256, 0, s>>>(f, ctr);
-    k_ftle_early_self<D, M><<<vblk(7L * f.n, 128), 128, 0, s>>>(m, w, in, f, t1, ctr);
+    cudaMemsetAsync(&ctr->ntask, 0, sizeof(int), s);
+    k_ftle_queue_nb<D><<<vblk(6L * f.n, 256), 256, 0, s>>>(f, ctr);
+    k_ftle_tasks<D, M><<<vblk(6L * f.n, 128), 128, 0, s>>>(m, w, in, f, t1, 0, ctr);
+    cudaMemsetAsync(&ctr->ntask, 0, sizeof(int), s);
+    k_ftle_queue_self<D><<<vblk(7L * f.n, 256), 256, 0, s>>>(f, ctr);
+    k_ftle_tasks<D, M><<<vblk(7L * f.n, 128), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
     k_ftle_early_final<D><<<vblk(f.n, 128), 128, 0, s>>>(f, ctr);
   }
   static void tracer_launch(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq,

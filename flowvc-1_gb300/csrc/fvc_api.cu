@@ -28,6 +28,7 @@ struct fvc_ctx {
   // device buffers
   int4* d_elem = nullptr;
   double* d_geom = nullptr;
+  float* d_geo32 = nullptr;
   double4_32a* d_nodes = nullptr;
   int* d_cell_start = nullptr;
   int* d_cell_ids = nullptr;
@@ -163,6 +164,7 @@ extern "C" void fvc_destroy(fvc_ctx* c) {
   for (auto& kv : c->frames) cudaFree(kv.second);
   cudaFree(c->d_elem);
   cudaFree(c->d_geom);
+  cudaFree(c->d_geo32);
   cudaFree(c->d_nodes);
   cudaFree(c->d_cell_start);
   cudaFree(c->d_cell_ids);
@@ -238,12 +240,14 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
   }
   cudaFree(c->d_elem); c->d_elem = nullptr;
   cudaFree(c->d_geom); c->d_geom = nullptr;
+  cudaFree(c->d_geo32); c->d_geo32 = nullptr;
   cudaFree(c->d_nodes); c->d_nodes = nullptr;
   cudaFree(c->d_cell_start); c->d_cell_start = nullptr;
   cudaFree(c->d_cell_ids); c->d_cell_ids = nullptr;
   const int gstride = c->mesh.dims == 3 ? 16 : 12;
   if (cudaMalloc(&c->d_elem, sizeof(int4) * he.size()) != cudaSuccess ||
       cudaMalloc(&c->d_geom, sizeof(double) * gstride * (size_t)nelem) != cudaSuccess ||
+      cudaMalloc(&c->d_geo32, sizeof(float) * 16 * (size_t)nelem) != cudaSuccess ||
       cudaMalloc(&c->d_nodes, sizeof(double4_32a) * hn.size()) != cudaSuccess)
     return fail(c, FVC_ERR_OOM, "mesh allocation failed");
   FVC_CUDA(c, cudaMemcpyAsync(c->d_elem, he.data(), sizeof(int4) * he.size(), cudaMemcpyHostToDevice, c->stream));
@@ -251,10 +255,11 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
   DevMesh& m = c->mesh;
   m.elem = c->d_elem;
   m.geom = c->d_geom;
+  m.geo32 = c->d_geo32;
   m.nodes = c->d_nodes;
   m.nelem = nelem;
   m.nnodes = nnodes;
-  launch_geometry(m, c->d_geom, c->stream);
+  launch_geometry(m, c->d_geom, c->d_geo32, c->stream);
   if ((st = check_launch(c, "geometry"))) return st;
 
   // Uniform bucket grid over the mesh's bounding box, about two elements per
@@ -583,7 +588,7 @@ static fvc_status carve(fvc_ctx* c, void** mem, std::vector<std::pair<void**, si
 
 static fvc_status run_chain(fvc_ctx* c, const ChainArgs& a, const double* dX, const int* dleft0, int* deid,
                             long long* launches) {
-  size_t words = 4 * (size_t)a.n + 2 * ((size_t)a.res[0] * a.res[1] + 1) + 2 * ((size_t)a.res[0] + 1) +
+  size_t words = 5 * (size_t)a.n + 2 * ((size_t)a.res[0] * a.res[1] + 1) + 2 * ((size_t)a.res[0] + 1) +
                  2 * ((size_t)a.n / 1024 + 2) + 16;
   int* work = nullptr;
   if (cudaMalloc(&work, sizeof(int) * words) != cudaSuccess) return fail(c, FVC_ERR_OOM, "seed-chain scratch");
@@ -646,6 +651,8 @@ extern "C" fvc_status fvc_ftle_create(fvc_ctx* c, const fvc_ftle_spec* sp, fvc_j
               {(void**)&f.Xn, 24 * n}, {(void**)&f.Vn, 24 * n}, {(void**)&f.te, 8 * n}, {(void**)&f.en, 4 * n},
               {(void**)&f.flag, n}, {(void**)&f.served, 4 * n}, {(void**)&f.trig, 4 * n}, {(void**)&f.out, 16 * n},
               {(void**)&f.epos, 168 * n}, {(void**)&f.elt, 48 * n}, {(void**)&f.emt, 8 * n},
+              {(void**)&f.tasks, 56 * n}, {(void**)&f.live, 4 * n},
+              {(void**)&f.block_cnt, sizeof(int) * (2 * (n / 1024 + 1) + 16) + sizeof(long long) * (n / 1048576 + 8)},
               {(void**)&left0, 4 * n}});
   if (st) {
     delete j;
@@ -734,6 +741,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   job_events(j);
   if ((st = prepare_slots(c, t1, t2))) return st;
   if (launch) ftle_launch(c->mesh, c->window, j->f, j->f.start, c->d_ctr, s);
+  compact_live(j->f.n, j->f.ldt, j->f.left, c->integ.extrapolate, j->f.live, j->f.flag, j->f.block_cnt, c->d_ctr, s);
   cudaEventRecord(j->ev[0], s);
   ftle_pass1(c->mesh, c->window, c->integ, j->f, t1, t2, c->d_ctr, s);
   cudaEventRecord(j->ev[1], s);
@@ -747,7 +755,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   DevCounters h{};
   st = finish(c, "ftle interval", steps, &h);
   j->stats.intervals++;
-  j->stats.launches += (launch ? 1 : 0) + 1 + (c->integ.extrapolate ? 0 : 5) + 1 + (c->mesh.mesh_type == 1 ? 1 : 0);
+  j->stats.launches += (launch ? 1 : 0) + 4 + 1 + (c->integ.extrapolate ? 0 : 6) + 1 + (c->mesh.mesh_type == 1 ? 1 : 0);
   j->stats.steps_main += (long long)h.steps;
   j->stats.steps_early += (long long)h.steps_early;
   j->stats.ms_main += ev_ms(j->ev[0], j->ev[1]);
@@ -795,6 +803,7 @@ extern "C" fvc_status fvc_tracer_create(fvc_ctx* c, const fvc_tracer_spec* sp, i
              {{(void**)&t.X, 24 * nn}, {(void**)&t.V, 24 * nn}, {(void**)&t.ldt, 8 * nn}, {(void**)&t.eid, 4 * nn},
               {(void**)&t.left, 4 * nn}, {(void**)&t.outX, 24 * nn},
               {(void**)&t.block_cnt, sizeof(int) * (2 * nb + 16) + sizeof(long long) * (nb / 1024 + 8)},
+              {(void**)&t.live, 4 * nn},
               {(void**)&left0, 4 * nn}});
   if (st) {
     delete j;
@@ -842,6 +851,8 @@ extern "C" fvc_status fvc_tracer_advance(fvc_job* j, double t1, double t2, long 
   if ((st = ready(c, true))) return st;
   job_events(j);
   if ((st = prepare_slots(c, t1, t2))) return st;
+  compact_live(j->t.n, j->t.ldt, j->t.left, c->integ.extrapolate, j->t.live, nullptr, j->t.block_cnt, c->d_ctr,
+               c->stream);
   cudaEventRecord(j->ev[0], c->stream);
   tracer_advance(c->mesh, c->window, c->integ, j->t, t1, t2, c->d_ctr, c->stream);
   cudaEventRecord(j->ev[1], c->stream);
@@ -849,7 +860,7 @@ extern "C" fvc_status fvc_tracer_advance(fvc_job* j, double t1, double t2, long 
   DevCounters h{};
   st = finish(c, "tracer advance", steps, &h);
   j->stats.intervals++;
-  j->stats.launches += 1;
+  j->stats.launches += 5;
   j->stats.steps_main += (long long)h.steps;
   j->stats.ms_main += ev_ms(j->ev[0], j->ev[1]);
   return st;

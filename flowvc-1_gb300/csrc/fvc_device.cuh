@@ -266,6 +266,112 @@ __device__ __forceinline__ void load_slot_nodes(const DevWindow& w, int tslot, i
   }
 }
 
+// FP32 pre-check of one walk hop.  The reference tests element e with
+// natural coordinates computed in FP64 and, when the point is outside by more
+// than TINY, steps through the face of the first coordinate within TINY of
+// the minimum (ompVC/velocity.c:545-609, mesh.c:549-560).  When the FP32
+// coordinates put the point outside by more than their error bound, with one
+// coordinate below all others by more than that bound, the FP64 test fails
+// and selects that face too, so the hop is taken without the FP64 solve.
+// Returns the face slot, or -1 when the FP64 test must decide.  The bound
+// tol = 1e-6 (1 + sum |a_ij dx_j / V|) covers the FP32 roundings of the map,
+// the offsets and the products and sums (each under 2^-24 relative).
+template <int DIMS>
+__device__ __forceinline__ int quick_hop(const DevMesh& m, int e, const double X[3]) {
+  const float* q = m.geo32 + (long)e * 16;
+  if (DIMS == 3) {
+    float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
+    float2 q2 = __ldg(reinterpret_cast<const float2*>(q + 8));
+    const double* qd = reinterpret_cast<const double*>(q + 10);
+    double x0 = __ldg(qd), y0 = __ldg(qd + 1), z0 = __ldg(qd + 2);
+    float dx = (float)(X[0] - x0), dy = (float)(X[1] - y0), dz = (float)(X[2] - z0);
+    float iv = q2.y;
+    float r0 = q0.x * dx, r1 = q0.y * dy, r2 = q0.z * dz;
+    float s0 = q0.w * dx, s1 = q1.x * dy, s2 = q1.y * dz;
+    float t0 = q1.z * dx, t1 = q1.w * dy, t2 = q2.x * dz;
+    float r = (r0 + r1 + r2) * iv, s = (s0 + s1 + s2) * iv, t = (t0 + t1 + t2) * iv;
+    float S = (fabsf(r0) + fabsf(r1) + fabsf(r2) + fabsf(s0) + fabsf(s1) + fabsf(s2) + fabsf(t0) + fabsf(t1) +
+               fabsf(t2)) * fabsf(iv);
+    float tol = 1e-6f * (1.0f + S);
+    float w = 1.0f - r - s - t;
+    float c[4] = {r, s, t, w};
+    int k = 0;
+    float d = c[0];
+#pragma unroll
+    for (int j = 1; j < 4; j++)
+      if (c[j] < d) { d = c[j]; k = j; }
+    float second = 3.0e38f;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (j != k) second = fminf(second, c[j]);
+    if (!(d < -(1e-10f + 2.0f * tol)) || !(second - d > 1e-10f + 4.0f * tol)) return -1;
+    return k;
+  } else {
+    float4 q0 = __ldg(reinterpret_cast<const float4*>(q));
+    float iv = __ldg(q + 4);
+    const double* qd = reinterpret_cast<const double*>(q + 6);
+    double x0 = __ldg(qd), y0 = __ldg(qd + 1);
+    float dx = (float)(X[0] - x0), dy = (float)(X[1] - y0);
+    float r0 = q0.x * dx, r1 = q0.y * dy, s0 = q0.z * dx, s1 = q0.w * dy;
+    float r = (r0 + r1) * iv, s = (s0 + s1) * iv;
+    float S = (fabsf(r0) + fabsf(r1) + fabsf(s0) + fabsf(s1)) * fabsf(iv);
+    float tol = 1e-6f * (1.0f + S);
+    float w = 1.0f - r - s;
+    float c[3] = {r, s, w};
+    int k = 0;
+    float d = c[0];
+#pragma unroll
+    for (int j = 1; j < 3; j++)
+      if (c[j] < d) { d = c[j]; k = j; }
+    float second = 3.0e38f;
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      if (j != k) second = fminf(second, c[j]);
+    if (!(d < -(1e-10f + 2.0f * tol)) || !(second - d > 1e-10f + 4.0f * tol)) return -1;
+    return k;  // 2D slots: 0 r, 1 s, 2 (1 - r - s)
+  }
+}
+
+__device__ __forceinline__ int neighbour(const DevMesh& m, int e, int slot) {
+  int4 nb = __ldg(m.elem + 2 * (long)e + 1);
+  return slot == 0 ? nb.x : slot == 1 ? nb.y : slot == 2 ? nb.z : nb.w;
+}
+
+// The reference's walk (GetVelocity_Unstructured's loop, ompVC/velocity.c:
+// 480-619, with vel_rule; Get_Element_Local_Search, ompVC/mesh.c:510-609,
+// without): hops the FP32 pre-check can decide are taken first, then the
+// FP64 solve decides at the element reached, so the lanes of a warp run the
+// expensive step together.  Returns 0 with the element's coordinates, 1 when
+// the walk leaves through a boundary face (eid = -1), or a fault bit.
+template <int DIMS>
+__device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& eid, bool vel_rule, double& r,
+                                    double& s, double& t, double& wv, double& d, int4& nd) {
+  for (int hop = 0; hop < m.max_hops;) {
+    int qs;
+    while (hop < m.max_hops && (qs = quick_hop<DIMS>(m, eid, X)) >= 0) {
+      eid = neighbour(m, eid, qs);
+      hop++;
+      if (eid == -1) return 1;
+    }
+    if (hop >= m.max_hops) break;
+    Geo<DIMS> g;
+    load_geo<DIMS>(m, eid, g);
+    d = natural_from<DIMS>(g, X, r, s, t, wv);
+    nd = g.nd;
+    if (vel_rule ? ((d + FVC_TINY) >= 0) : (d > -FVC_TINY)) return 0;
+    int slot;
+    if (fabs(r - d) < FVC_TINY) slot = 0;
+    else if (fabs(s - d) < FVC_TINY) slot = 1;
+    else if (DIMS == 3 && fabs(t - d) < FVC_TINY) slot = 2;
+    else if (fabs(wv - d) < FVC_TINY) slot = DIMS == 3 ? 3 : 2;
+    else return PT_ERR_WALK;  // "Indeterminate neighbor"
+    eid = neighbour(m, eid, slot);
+    hop++;
+    if (eid == -1) return 1;
+  }
+  return PT_ERR_WALK;
+}
+
 // GetVelocity_Unstructured, ompVC/velocity.c:459-621: walk from eid until the
 // element passes (d + TINY) >= 0, then P1 in space and linear in time.
 template <int DIMS>
@@ -279,65 +385,47 @@ __device__ __forceinline__ int vel_unstruct(const DevMesh& m, const DevWindow& w
     tloc = (tq - w.tmin) / (w.tmax - w.tmin);
     if ((tloc > 1 + FVC_TINY) || (tloc < 0 - FVC_TINY)) return PT_ERR_TLOC;
   }
-  for (int hop = 0; hop < m.max_hops; hop++) {
-    double r, s, t, wv, d;
-    int4 nd;
-    NodeVel<DIMS> nv;
-    if (nc && nc->e == eid) {
-      nd = nc->nd;
-      if (tab) load_slot_nodes<DIMS>(w, tslot, nd, nv);
-      r = nc->r;
-      s = nc->s;
-      t = nc->t;
-      wv = nc->w;
-      d = nc->d;
-    } else {
-      Geo<DIMS> g;
-      load_geo<DIMS>(m, eid, g);
-      nd = g.nd;
-      if (tab) load_slot_nodes<DIMS>(w, tslot, nd, nv);
-      d = natural_from<DIMS>(g, X, r, s, t, wv);
-    }
-    if ((d + FVC_TINY) >= 0) {
-      if (!tab) {
-        // query time off the table: interpolate the two frames in time
-        const int ids[4] = {nd.x, nd.y, nd.z, nd.w};
-#pragma unroll
-        for (int c = 0; c < (DIMS == 3 ? 4 : 3); c++) {
-          double4_32a a = ldf(w.f0 + ids[c]), b = ldf(w.f1 + ids[c]);
-          nv.u[c] = (1 - tloc) * a.x + tloc * b.x;
-          nv.v[c] = (1 - tloc) * a.y + tloc * b.y;
-          nv.w[c] = (1 - tloc) * a.z + tloc * b.z;
-        }
-      }
-      if (DIMS == 3) {
-        out[0] = nv.u[0] + (nv.u[1] - nv.u[0]) * fabs(r) + (nv.u[2] - nv.u[0]) * fabs(s) + (nv.u[3] - nv.u[0]) * fabs(t);
-        out[1] = nv.v[0] + (nv.v[1] - nv.v[0]) * fabs(r) + (nv.v[2] - nv.v[0]) * fabs(s) + (nv.v[3] - nv.v[0]) * fabs(t);
-        out[2] = nv.w[0] + (nv.w[1] - nv.w[0]) * fabs(r) + (nv.w[2] - nv.w[0]) * fabs(s) + (nv.w[3] - nv.w[0]) * fabs(t);
-      } else {
-        out[0] = nv.u[0] + (nv.u[1] - nv.u[0]) * fabs(r) + (nv.u[2] - nv.u[0]) * fabs(s);
-        out[1] = nv.v[0] + (nv.v[1] - nv.v[0]) * fabs(r) + (nv.v[2] - nv.v[0]) * fabs(s);
-        out[2] = 0.0;
-      }
-      return 0;
-    }
-    // neighbour across the face of the minimal coordinate, first match in the
-    // order r, s, t, 1-r-s-t (ompVC/velocity.c:588-609)
-    int slot;
-    if (fabs(r - d) < FVC_TINY) slot = 0;
-    else if (fabs(s - d) < FVC_TINY) slot = 1;
-    else if (DIMS == 3 && fabs(t - d) < FVC_TINY) slot = 2;
-    else if (fabs(wv - d) < FVC_TINY) slot = DIMS == 3 ? 3 : 2;
-    else return PT_ERR_WALK;
-    int4 nb = __ldg(m.elem + 2 * (long)eid + 1);
-    eid = slot == 0 ? nb.x : slot == 1 ? nb.y : slot == 2 ? nb.z : nb.w;
-    if (eid == -1) {
+  double r, s, t, wv, d;
+  int4 nd;
+  if (nc && nc->e == eid) {
+    // the last locate tested this element at this position (d > -TINY)
+    nd = nc->nd;
+    r = nc->r;
+    s = nc->s;
+    t = nc->t;
+    wv = nc->w;
+  } else {
+    int st = walk<DIMS>(m, X, eid, true, r, s, t, wv, d, nd);
+    if (st == 1) {
       left = 1;
       out[0] = out[1] = out[2] = 0.0;
       return 0;
     }
+    if (st) return st;
   }
-  return PT_ERR_WALK;
+  NodeVel<DIMS> nv;
+  if (tab) {
+    load_slot_nodes<DIMS>(w, tslot, nd, nv);
+  } else {
+    const int ids[4] = {nd.x, nd.y, nd.z, nd.w};
+#pragma unroll
+    for (int c = 0; c < (DIMS == 3 ? 4 : 3); c++) {
+      double4_32a a = ldf(w.f0 + ids[c]), b = ldf(w.f1 + ids[c]);
+      nv.u[c] = (1 - tloc) * a.x + tloc * b.x;
+      nv.v[c] = (1 - tloc) * a.y + tloc * b.y;
+      nv.w[c] = (1 - tloc) * a.z + tloc * b.z;
+    }
+  }
+  if (DIMS == 3) {
+    out[0] = nv.u[0] + (nv.u[1] - nv.u[0]) * fabs(r) + (nv.u[2] - nv.u[0]) * fabs(s) + (nv.u[3] - nv.u[0]) * fabs(t);
+    out[1] = nv.v[0] + (nv.v[1] - nv.v[0]) * fabs(r) + (nv.v[2] - nv.v[0]) * fabs(s) + (nv.v[3] - nv.v[0]) * fabs(t);
+    out[2] = nv.w[0] + (nv.w[1] - nv.w[0]) * fabs(r) + (nv.w[2] - nv.w[0]) * fabs(s) + (nv.w[3] - nv.w[0]) * fabs(t);
+  } else {
+    out[0] = nv.u[0] + (nv.u[1] - nv.u[0]) * fabs(r) + (nv.u[2] - nv.u[0]) * fabs(s);
+    out[1] = nv.v[0] + (nv.v[1] - nv.v[0]) * fabs(r) + (nv.v[2] - nv.v[0]) * fabs(s);
+    out[2] = 0.0;
+  }
+  return 0;
 }
 
 // Get_Element_Local_Search, ompVC/mesh.c:496-611: containment d > -TINY;
@@ -352,38 +440,24 @@ __device__ __forceinline__ int locate_walk(const DevMesh& m, const double X[3], 
     err |= PT_ERR_WALK;
     return -1;
   }
-  for (int hop = 0; hop < m.max_hops; hop++) {
-    double r, s, t, wv;
-    Geo<DIMS> g;
-    load_geo<DIMS>(m, guess, g);
-    double d = natural_from<DIMS>(g, X, r, s, t, wv);
-    if (d > -FVC_TINY) {
-      if (nc) {
-        nc->e = guess;
-        nc->nd = g.nd;
-        nc->r = r;
-        nc->s = s;
-        nc->t = t;
-        nc->w = wv;
-        nc->d = d;
-      }
-      return guess;
-    }
-    int slot;
-    if (fabs(r - d) < FVC_TINY) slot = 0;
-    else if (fabs(s - d) < FVC_TINY) slot = 1;
-    else if (DIMS == 3 && fabs(t - d) < FVC_TINY) slot = 2;
-    else if (fabs(d - wv) < FVC_TINY) slot = DIMS == 3 ? 3 : 2;
-    else {
-      err |= PT_ERR_WALK;
-      return -1;
-    }
-    int4 nb = __ldg(m.elem + 2 * (long)guess + 1);
-    guess = slot == 0 ? nb.x : slot == 1 ? nb.y : slot == 2 ? nb.z : nb.w;
-    if (guess == -1) return -1;
+  double r, s, t, wv, d;
+  int4 nd;
+  int st = walk<DIMS>(m, X, guess, false, r, s, t, wv, d, nd);
+  if (st == 1) return -1;
+  if (st) {
+    err |= st;
+    return -1;
   }
-  err |= PT_ERR_WALK;
-  return -1;
+  if (nc) {
+    nc->e = guess;
+    nc->nd = nd;
+    nc->r = r;
+    nc->s = s;
+    nc->t = t;
+    nc->w = wv;
+    nc->d = d;
+  }
+  return guess;
 }
 
 // Containment test of one element (the predicate of

@@ -28,7 +28,7 @@ static inline unsigned nblk(long n, int bs) { return (unsigned)((n + bs - 1) / b
 // in the same record so one gather serves the containment test and the
 // interpolation (layout in fvc_device.cuh, struct Geo).
 template <int DIMS>
-__global__ void k_geometry(DevMesh m, double* geom) {
+__global__ void k_geometry(DevMesh m, double* geom, float* geo32) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m.nelem) return;
   int4 nd = m.elem[2 * (long)e];
@@ -55,6 +55,14 @@ __global__ void k_geometry(DevMesh m, double* geom) {
     g[12] = z0;
     g[13] = 0.0;
     reinterpret_cast<int4*>(g + 14)[0] = nd;
+    // FP32 map for the walk's pre-check: a11..a33, 1/V, then x0 y0 z0 (FP64)
+    float* q = geo32 + (long)e * 16;
+    for (int c = 0; c < 9; c++) q[c] = (float)g[c];
+    q[9] = (float)(1.0 / g[9]);
+    double* qd = reinterpret_cast<double*>(q + 10);
+    qd[0] = x0;
+    qd[1] = y0;
+    qd[2] = z0;
   } else {
     double* g = geom + (long)e * 12;
     g[0] = y2 - y0;  // a11
@@ -67,12 +75,21 @@ __global__ void k_geometry(DevMesh m, double* geom) {
     g[7] = 0.0;
     reinterpret_cast<int4*>(g + 8)[0] = nd;
     g[10] = g[11] = 0.0;
+    float* q = geo32 + (long)e * 16;
+    for (int c = 0; c < 4; c++) q[c] = (float)g[c];
+    q[4] = (float)(1.0 / g[4]);
+    q[5] = 0.f;
+    double* qd = reinterpret_cast<double*>(q + 6);
+    qd[0] = x0;
+    qd[1] = y0;
+    qd[2] = 0.0;
+    q[12] = q[13] = q[14] = q[15] = 0.f;
   }
 }
 
-void launch_geometry(const DevMesh& m, double* geom, cudaStream_t s) {
-  if (m.dims == 3) k_geometry<3><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom);
-  else k_geometry<2><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom);
+void launch_geometry(const DevMesh& m, double* geom, float* geo32, cudaStream_t s) {
+  if (m.dims == 3) k_geometry<3><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom, geo32);
+  else k_geometry<2><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom, geo32);
 }
 
 // =============================================================== scans
@@ -349,6 +366,7 @@ struct ChainDev {
   int* R;          // current answers
   int* Rn;         // next answers
   int* g;          // guess of every seed
+  int* gprev;      // guesses of the previous round (null in the first round)
   int* rowfirst;   // kind 0: first answer in each (i, j) row
   int* rowstart;   // kind 0: guess at the start of each row
   int* planefirst; // kind 0
@@ -471,6 +489,7 @@ __global__ void k_chain_eval(DevMesh m, ChainDev c, DevCounters* ctr) {
     int r;
     if (c.left0[p]) r = -1;
     else if (p <= c.pstar) r = c.R0[p];
+    else if (c.gprev && c.gprev[p] == c.g[p]) r = c.R[p];  // same guess, same walk
     else {
       double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
       r = locate_walk<DIMS>(m, x, c.g[p], err);
@@ -513,6 +532,8 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
   c.R = w; w += n;
   c.Rn = w; w += n;
   c.g = w; w += n;
+  int* gother = w; w += n;
+  c.gprev = nullptr;
   c.rowfirst = w; w += c.nrows + 1;
   c.rowstart = w; w += c.nrows + 1;
   c.planefirst = w; w += c.nplanes + 1;
@@ -569,6 +590,10 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
     int* t = c.R;
     c.R = c.Rn;
     c.Rn = t;
+    // next round writes its guesses over the older array
+    int* gp = c.g;
+    c.g = c.gprev ? c.gprev : gother;
+    c.gprev = gp;
     if (!changed || rounds > n + 1) break;
   }
   cudaMemcpyAsync(eid, c.R, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
@@ -640,20 +665,27 @@ void ftle_init_marks(const DevMesh& m, const FtleDev& f, const int* left0, cudaS
 // GetFTLEForPointEarly calls (ompVC/ftle.c:130-152) reach q first.
 __global__ void k_ftle_triggers(FtleDev f, DevCounters* ctr) {
   long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= f.n || f.have[q]) return;
-  int YZ = f.yr * f.zr, zr = f.zr;
-  int k = (int)(q % zr), j = (int)((q / zr) % f.yr), i = (int)(q / YZ);
-  long cand[7] = {i > 0 ? q - YZ : -1, j > 0 ? q - zr : -1, k > 0 ? q - 1 : -1, q,
-                  k < zr - 1 ? q + 1 : -1, j < f.yr - 1 ? q + zr : -1, i < f.xr - 1 ? q + YZ : -1};
   long trig = -1;
+  if (q < f.n && !f.have[q]) {
+    int YZ = f.yr * f.zr, zr = f.zr;
+    int k = (int)(q % zr), j = (int)((q / zr) % f.yr), i = (int)(q / YZ);
+    long cand[7] = {i > 0 ? q - YZ : -1, j > 0 ? q - zr : -1, k > 0 ? q - 1 : -1, q,
+                    k < zr - 1 ? q + 1 : -1, j < f.yr - 1 ? q + zr : -1, i < f.xr - 1 ? q + YZ : -1};
 #pragma unroll
-  for (int c = 0; c < 7; c++)
-    if (cand[c] >= 0 && (f.flag[cand[c]] & 2)) {
-      trig = cand[c];
-      break;
-    }
+    for (int c = 0; c < 7; c++)
+      if (cand[c] >= 0 && (f.flag[cand[c]] & 2)) {
+        trig = cand[c];
+        break;
+      }
+  }
+  // warp-aggregated append keeps a warp's served points adjacent in the list
+  unsigned b = __ballot_sync(0xffffffffu, trig >= 0);
+  if (!b) return;
+  int lane = threadIdx.x & 31, base = 0;
+  if (lane == 0) base = atomicAdd(&ctr->count, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
   if (trig < 0) return;
-  int slot = atomicAdd(&ctr->count, 1);
+  int slot = base + __popc(b & ((1u << lane) - 1u));
   f.served[slot] = (int)q;
   f.trig[slot] = (int)trig;
 }
@@ -676,10 +708,12 @@ __global__ void k_ftle_update(FtleDev f, int extrapolate, int unstructured) {
   f.X[3 * p] = f.Xn[3 * p];
   f.X[3 * p + 1] = f.Xn[3 * p + 1];
   f.X[3 * p + 2] = f.Xn[3 * p + 2];
-  f.V[3 * p] = f.Vn[3 * p];
-  f.V[3 * p + 1] = f.Vn[3 * p + 1];
-  f.V[3 * p + 2] = f.Vn[3 * p + 2];
-  if (extrapolate) f.left[p] = (fl & 4) ? 1 : 0;
+  if (extrapolate) {
+    f.V[3 * p] = f.Vn[3 * p];
+    f.V[3 * p + 1] = f.Vn[3 * p + 1];
+    f.V[3 * p + 2] = f.Vn[3 * p + 2];
+    f.left[p] = (fl & 4) ? 1 : 0;
+  }
   if (unstructured) f.eid[p] = f.en[p];
 }
 
@@ -815,6 +849,63 @@ __global__ void k_compact_scatter(TracerDev t, int always, const int* block_off)
 }
 
 __global__ void k_copy_count(const int* src, int* dst) { *dst = *src; }
+
+// Live-point compaction: warp ballots give each lane its rank among the
+// selected lanes; block counts are scanned into offsets so the list keeps the
+// points' order (neighbouring points stay in the same warp).
+__device__ __forceinline__ bool is_live(long i, int n, const double* ldt, const int* left, int extrap) {
+  return i < n && ldt[i] > -FVC_TINY && (!left[i] || extrap);
+}
+
+__global__ void k_live_count(int n, const double* ldt, const int* left, int extrap, int* block_cnt) {
+  __shared__ int warp_cnt[32];
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned b = __ballot_sync(0xffffffffu, is_live(i, n, ldt, left, extrap));
+  if ((threadIdx.x & 31) == 0) warp_cnt[threadIdx.x >> 5] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int c = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) c += warp_cnt[k];
+    block_cnt[blockIdx.x] = c;
+  }
+}
+
+__global__ void k_live_scatter(int n, const double* ldt, const int* left, int extrap, const int* block_off,
+                               int* live, unsigned char* flag, int* nlive) {
+  __shared__ int warp_off[32];
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool sel = is_live(i, n, ldt, left, extrap);
+  unsigned b = __ballot_sync(0xffffffffu, sel);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_off[wid] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int c = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+      int v = warp_off[k];
+      warp_off[k] = c;
+      c += v;
+    }
+  }
+  __syncthreads();
+  if (i < n && flag) flag[i] = 0;
+  if (sel) live[block_off[blockIdx.x] + warp_off[wid] + __popc(b & ((1u << lane) - 1u))] = (int)i;
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *nlive = block_off[gridDim.x];
+}
+
+void compact_live(int n, const double* ldt, const int* left, int extrapolate, int* live,
+                  unsigned char* flag, int* block_cnt, DevCounters* ctr, cudaStream_t s) {
+  if (n <= 0) {
+    cudaMemsetAsync(&ctr->nlive, 0, sizeof(int), s);
+    return;
+  }
+  unsigned nb = nblk(n, 1024);
+  int* off = block_cnt + nb + 1;
+  long long* tmp = reinterpret_cast<long long*>(block_cnt + ((2 * nb + 4) & ~1u));
+  k_live_count<<<nb, 1024, 0, s>>>(n, ldt, left, extrapolate, block_cnt);
+  exclusive_scan(block_cnt, off, (int)nb, tmp, s);
+  k_live_scatter<<<nb, 1024, 0, s>>>(n, ldt, left, extrapolate, off, live, flag, &ctr->nlive);
+}
 
 void tracer_compact(const TracerDev& t, int always, DevCounters* ctr, cudaStream_t s) {
   if (t.n <= 0) {

@@ -15,12 +15,14 @@ struct DevCounters {
   unsigned long long steps_early;  // accepted steps of the early-FTLE advections
   int status;
   int changed;
-  int count;
+  int count;   // points served an early FTLE this interval
+  int nlive;   // live points of the current advection call
+  int ntask;   // early-FTLE advections queued
   int pad;
 };
 
 // ---- mesh preprocessing
-void launch_geometry(const DevMesh& m, double* geom, cudaStream_t s);
+void launch_geometry(const DevMesh& m, double* geom, float* geo32, cudaStream_t s);
 
 struct BucketGrid {
   double lo[3], inv[3];   // origin and 1 / cell size
@@ -87,6 +89,9 @@ struct FtleDev {
   double* epos;          // early FTLE: 7 positions (6 neighbours, self) per served point
   double* elt;           // early FTLE: the neighbours' exit times
   double* emt;           // early FTLE: MinExitTime
+  int2* tasks;           // early FTLE: queued advections (served index, 0-5 neighbour / 6 self)
+  int* live;             // points advected this interval, in grid order
+  int* block_cnt;        // compaction scratch
   double* out;           // 2 x n, output order
 };
 void ftle_seed_grid(const DevMesh& m, const FtleDev& f, double xmin, double ymin, double zmin,
@@ -113,7 +118,14 @@ struct TracerDev {
   int* left;
   double* outX;
   int* block_cnt;
+  int* live;             // tracers advected by the current call, in seed order
 };
+
+// Compacts the indices of live points (LeftDomainTime > -TINY and, unless
+// extrapolating, not left: ompVC/ftle.c:113, tracers.c:225) in order into
+// live[], the count into ctr->nlive; clears flag[] (may be null).
+void compact_live(int n, const double* ldt, const int* left, int extrapolate, int* live,
+                  unsigned char* flag, int* block_cnt, DevCounters* ctr, cudaStream_t s);
 void tracer_launch_vel(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq,
                        DevCounters* ctr, cudaStream_t s);
 void tracer_advance(const DevMesh& m, const DevWindow& w, const DevInteg& in, const TracerDev& t,

@@ -16,6 +16,7 @@ struct DevMesh {
   // unstructured mesh
   const int4* elem;     // 2 x nelem: {Nodes[4]}, {NeighborIndex[4]}
   const double* geom;   // natural-coordinate map + node ids, 16 (3D) or 12 (2D) doubles per element
+  const float* geo32;   // FP32 copy of the map + FP64 node-0 coordinates, 64 B per element
   const double4_32a* nodes; // x, y, z, 0 per node
   int nelem, nnodes;
   // Data_MeshBounds
