@@ -6,6 +6,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -897,5 +898,144 @@ extern "C" fvc_status fvc_tracer_get_state(fvc_job* j, double* X, int* eid, int*
   if (left) FVC_CUDA(c, cudaMemcpyAsync(left, j->t.left, 4 * n, cudaMemcpyDeviceToHost, s));
   if (ldt) FVC_CUDA(c, cudaMemcpyAsync(ldt, j->t.ldt, 8 * n, cudaMemcpyDeviceToHost, s));
   FVC_CUDA(c, cudaStreamSynchronize(s));
+  return FVC_OK;
+}
+
+// ------------------------------------------------- allocation-free advection
+//
+// fvc_advect_noalloc serves callers that may not allocate device memory while
+// they run (an application whose own pool allocator owns the rest of the GPU,
+// or a code path where the device synchronisation of a cudaMalloc is not
+// allowed).  Its scratch is this one file-scope array, which every GPU that
+// loads the library holds until the process exits.  Layout, each part
+// 256-byte aligned: the step counters, then X, V, eid, left and ldt sized for
+// FVC_NOALLOC_MAX_POINTS, then the stage-time velocity table in the rest.
+// Every call on a device shares the array and finds the previous call's bytes
+// in it: the counters are cleared at the start of each call, and every other
+// byte a call reads it has written before.
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[FVC_NOALLOC_SCRATCH_BYTES];
+
+static constexpr size_t na_al(size_t b) { return (b + 255) & ~(size_t)255; }
+static constexpr size_t NA_MAXN = FVC_NOALLOC_MAX_POINTS;
+static constexpr size_t NA_CTR = na_al(sizeof(DevCounters));
+static constexpr size_t NA_X = na_al(sizeof(double) * 3 * NA_MAXN), NA_I = na_al(sizeof(int) * NA_MAXN),
+                        NA_D = na_al(sizeof(double) * NA_MAXN);
+static constexpr size_t NA_VT = NA_CTR + 2 * NA_X + 2 * NA_I + NA_D;  // start of the velocity table
+static_assert(NA_VT < (size_t)FVC_NOALLOC_SCRATCH_BYTES, "no room left for the stage-time table");
+
+#define FVC_NOALLOC_MAX_DEVICES 64
+static std::mutex g_noalloc_mu;
+static unsigned char* g_noalloc_base[FVC_NOALLOC_MAX_DEVICES];
+
+// The array's device address on the context's device (current when this is
+// called).  In host code g_noalloc_scratch only names the array; the address
+// the kernels get is the one cudaGetSymbolAddress returns, looked up on a
+// device's first call and kept.
+static fvc_status noalloc_base(fvc_ctx* c, unsigned char** base) {
+  if (c->device >= FVC_NOALLOC_MAX_DEVICES)
+    return fail(c, FVC_ERR_ARG, "fvc_advect_noalloc supports devices 0..%d", FVC_NOALLOC_MAX_DEVICES - 1);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  unsigned char*& b = g_noalloc_base[c->device];
+  if (!b) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(c, FVC_ERR_CUDA, "device address of the fvc_advect_noalloc scratch: %s", cudaGetErrorString(e));
+    b = (unsigned char*)p;
+  }
+  *base = b;
+  return FVC_OK;
+}
+
+// The stage-time slots of prepare_slots, computed the same way, with the
+// table limited to the slots that fit in vt_bytes.  Slots are hints that the
+// kernels check against the time they compute, so a shorter table gives the
+// same results.
+static void noalloc_slots(const fvc_ctx* c, DevWindow& w, double t1, double t2, double4_32a* vt,
+                          size_t vt_bytes) {
+  int cap = FVC_MAX_SLOTS;
+  if (c->mesh.mesh_type == 1) {
+    size_t per = sizeof(double4_32a) * (size_t)c->mesh.nnodes;
+    size_t fit = per ? vt_bytes / per : 0;
+    if (fit < (size_t)cap) cap = (int)fit;
+  }
+  int n = 0;
+  auto add = [&](double tq) {
+    if (n >= cap) return false;
+    double tloc = (tq - w.tmin) / (w.tmax - w.tmin);
+    if ((tloc > 1 + 1.0e-10) || (tloc < 0 - 1.0e-10)) return false;
+    w.tq[n] = tq;
+    w.tl[n] = tloc;
+    n++;
+    return true;
+  };
+  double tc = t1, h = (t2 - t1) >= 0.0 ? fabs(c->integ.h) : -fabs(c->integ.h);
+  bool ok = true;
+  while ((tc - t2) * (t2 - t1) < 0.0) {
+    if ((tc + h - t2) * (tc + h - t1) > 0.0) h = (t2 - t1) >= 0.0 ? fabs(t2 - tc) : -fabs(t2 - tc);
+    if (!add(tc) || !add(tc + h / 2)) {
+      ok = false;
+      break;
+    }
+    tc = tc + h;
+  }
+  if (ok) add(tc);
+  w.nslots = n;
+  w.vt = vt;
+  w.vt_stride = c->mesh.nnodes;
+}
+
+extern "C" fvc_status fvc_advect_noalloc(fvc_ctx* c, int n, double* X, double* V, int* eid, int* left,
+                                         double* ldt, double t0, double t1, long long* steps) {
+  fvc_status st;
+  if ((st = ready(c, true))) return st;
+  if (n < 0 || (n > 0 && (!X || !left || !ldt))) return fail(c, FVC_ERR_ARG, "bad arrays");
+  if (n > FVC_NOALLOC_MAX_POINTS)
+    return fail(c, FVC_ERR_ARG,
+                "fvc_advect_noalloc: %d points exceed its fixed scratch (at most %d points a call); "
+                "split the call or use fvc_advect", n, FVC_NOALLOC_MAX_POINTS);
+  if (c->mesh.mesh_type == 1 && n > 0 && !eid) return fail(c, FVC_ERR_ARG, "unstructured advection needs element ids");
+  if (c->integ.extrapolate && n > 0 && !V) return fail(c, FVC_ERR_ARG, "extrapolation needs V");
+  if (steps) *steps = 0;
+  if (n == 0) return FVC_OK;
+  unsigned char* base = nullptr;
+  if ((st = noalloc_base(c, &base))) return st;
+  DevCounters* ctr = (DevCounters*)base;
+  double* dX = (double*)(base + NA_CTR);
+  double* dV = (double*)(base + NA_CTR + NA_X);
+  int* de = (int*)(base + NA_CTR + 2 * NA_X);
+  int* dl = (int*)(base + NA_CTR + 2 * NA_X + NA_I);
+  double* dt = (double*)(base + NA_CTR + 2 * NA_X + 2 * NA_I);
+  double4_32a* vt = (double4_32a*)(base + NA_VT);
+  cudaStream_t s = c->stream;
+  FVC_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(DevCounters), s));
+  FVC_CUDA(c, cudaMemcpyAsync(dX, X, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  if (V) FVC_CUDA(c, cudaMemcpyAsync(dV, V, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  if (eid) FVC_CUDA(c, cudaMemcpyAsync(de, eid, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  FVC_CUDA(c, cudaMemcpyAsync(dl, left, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  FVC_CUDA(c, cudaMemcpyAsync(dt, ldt, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  DevWindow w = c->window;  // the context's window is left as it is
+  noalloc_slots(c, w, t0, t1, vt, (size_t)FVC_NOALLOC_SCRATCH_BYTES - NA_VT);
+  if (c->mesh.mesh_type == 1 && w.nslots > 0) {
+    time_fields(c->mesh, w, vt, s);
+    if ((st = check_launch(c, "time fields"))) return st;
+  }
+  launch_advect(c->mesh, w, c->integ, n, dX, V ? dV : nullptr, eid ? de : nullptr, dl, dt, t0, t1, ctr, s);
+  if ((st = check_launch(c, "advect"))) return st;
+  FVC_CUDA(c, cudaMemcpyAsync(X, dX, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+  if (V) FVC_CUDA(c, cudaMemcpyAsync(V, dV, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+  if (eid) FVC_CUDA(c, cudaMemcpyAsync(eid, de, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  FVC_CUDA(c, cudaMemcpyAsync(left, dl, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  FVC_CUDA(c, cudaMemcpyAsync(ldt, dt, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  DevCounters h{};
+  FVC_CUDA(c, cudaMemcpyAsync(&h, ctr, sizeof(h), cudaMemcpyDeviceToHost, s));
+  FVC_CUDA(c, cudaStreamSynchronize(s));
+  if (steps) *steps = (long long)(h.steps + h.steps_early);
+  if (h.status & PT_ERR_STATE)
+    return fail(c, FVC_ERR_STATE, "advect: a point that had left the domain was advected");
+  if (h.status & PT_ERR_TLOC) return fail(c, FVC_ERR_TLOC, "advect: query time outside the loaded frame interval");
+  if (h.status & PT_ERR_WALK)
+    return fail(c, FVC_ERR_WALK, "advect: neighbour walk failed (indeterminate neighbour or hop cap)");
   return FVC_OK;
 }

@@ -61,6 +61,7 @@ SIGNATURES = {
     "fvc_set_window": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_double]),
     "fvc_advect": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_double, _llp]),
     "fvc_advect_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double, _llp]),
+    "fvc_advect_noalloc": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_double, _llp]),
     "fvc_velocity": (C.c_int, [_vp, C.c_int, _dp, _ip, _ip, C.c_double, _dp]),
     "fvc_local_search": (C.c_int, [_vp, C.c_int, _dp, _ip, _ip]),
     "fvc_global_search": (C.c_int, [_vp, C.c_int, _dp, _ip]),
@@ -198,6 +199,14 @@ class Context:
         steps = C.c_longlong(0)
         self._chk(self.lib.fvc_advect(self.h, X.shape[0], _d(X), _d(V), _i(eid), _i(left), _d(ldt), t0, t1,
                                       C.byref(steps)))
+        return steps.value
+
+    def advect_noalloc(self, X, V, eid, left, ldt, t0, t1):
+        """advect() through fvc_advect_noalloc: same results, no device
+        allocation (at most NOALLOC_MAX_POINTS points a call)."""
+        steps = C.c_longlong(0)
+        self._chk(self.lib.fvc_advect_noalloc(self.h, X.shape[0], _d(X), _d(V), _i(eid), _i(left), _d(ldt), t0,
+                                              t1, C.byref(steps)))
         return steps.value
 
     def velocity(self, X, eid, left, tq):

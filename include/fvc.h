@@ -107,6 +107,33 @@ fvc_status fvc_advect(fvc_ctx *ctx, int n, double *X, double *V, int *eid, int *
 fvc_status fvc_advect_device(fvc_ctx *ctx, int n, double *dX, double *dV, int *deid, int *dleft,
                              double *dldt, double t0, double t1, long long *steps);
 
+/* fvc_advect without any device allocation.  This entry point has no
+ * counterpart in the reference: ompVC advects in host memory and never
+ * allocates on a GPU.  It is for callers that must not allocate device
+ * memory while they run, e.g. a host application that has handed the rest
+ * of the GPU's memory to its own pool allocator, or one that advects from a
+ * code path where a cudaMalloc (which can synchronise the device) is not
+ * allowed.  Arguments, results and errors are those of fvc_advect; results
+ * are identical to it.
+ *
+ * Its device scratch (the staging copies of the point arrays, the step
+ * counters and as much of the stage-time velocity table as fits) lives in
+ * one fixed array of FVC_NOALLOC_SCRATCH_BYTES that the library declares at
+ * file scope: every GPU that loads libfvc holds that much memory until the
+ * process exits, whether or not this function is called.
+ *   - n above FVC_NOALLOC_MAX_POINTS is refused with FVC_ERR_ARG.
+ *   - The first call on a device looks the array's device address up (one
+ *     cudaGetSymbolAddress, which loads the library's device code if it is
+ *     not loaded yet); make that first call before any stream capture.
+ *   - All calls, from every context on a device, share the one array and
+ *     it keeps the last call's contents.  Calls whose GPU work overlaps
+ *     (from several threads, or several contexts on other streams) race and
+ *     corrupt each other's results: serialise them. */
+#define FVC_NOALLOC_MAX_POINTS 131072
+#define FVC_NOALLOC_SCRATCH_BYTES (32u << 20)
+fvc_status fvc_advect_noalloc(fvc_ctx *ctx, int n, double *X, double *V, int *eid, int *left,
+                              double *ldt, double t0, double t1, long long *steps);
+
 /* GetVelocity (ompVC/velocity.c:236-247) at time tq for n points; eid walks
  * and left is set as the reference does.  out: n x 3. */
 fvc_status fvc_velocity(fvc_ctx *ctx, int n, const double *X, int *eid, int *left, double tq,
