@@ -17,6 +17,32 @@ namespace fvc {
 
 static inline unsigned vblk(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// Persistent launches.  Kernels whose item count is only known on the device
+// (live lists, task lists) run as many blocks as the GPU holds at once, never
+// more than the largest possible count needs; each warp takes the next 32
+// items from a cursor in the call's counters, so warps that drew short items
+// take more and no block sits idle behind a long one.
+template <typename Kern>
+static unsigned resident_blocks(Kern k, int threads) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, 0);
+  long b = (long)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  return (unsigned)b;
+}
+static inline unsigned capped(long n, int bs, unsigned resident) {
+  unsigned need = vblk(n, bs);
+  return need < resident ? (need > 0 ? need : 1) : resident;
+}
+
+// The first of the 32 items the calling warp takes next (all lanes call it).
+__device__ __forceinline__ long warp_grab(int* cursor) {
+  int base = 0;
+  if ((threadIdx.x & 31) == 0) base = atomicAdd(cursor, 32);
+  return __shfl_sync(0xffffffffu, base, 0);
+}
+
 __device__ __forceinline__ void load_pt(Pt& p, long i, const double* X, const double* V,
                                         const int* eid, const int* left, const double* ldt) {
   p.X[0] = X[3 * i];
@@ -107,15 +133,17 @@ __global__ void k_ftle_launch(DevMesh m, DevWindow w, FtleDev f, double t, DevCo
 template <int D, int M>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_pass1(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
                                                     double t1, double t2, DevCounters* ctr) {
-  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nlive = *(volatile int*)&ctr->nlive;
+  const int lane = threadIdx.x & 31;
   unsigned steps = 0;
   int err = 0;
-  if (idx < nlive) {
+  for (long base = warp_grab(&ctr->cur[0]); base < nlive; base = warp_grab(&ctr->cur[0])) {
+    const long idx = base + lane;
+    if (idx >= nlive) continue;
     long p = f.live[idx];
     Pt t;
     load_pt(t, p, f.X, in.extrapolate ? f.V : nullptr, f.eid, f.left, f.ldt);
-    err = advect<D, M>(m, w, in, t, t1, t2, steps);
+    err |= advect<D, M>(m, w, in, t, t1, t2, steps);
     f.flag[p] = 1 | ((t.left && !in.extrapolate) ? 2 : 0) | (t.left ? 4 : 0);
     f.Xn[3 * p] = t.X[0];
     f.Xn[3 * p + 1] = t.X[1];
@@ -186,28 +214,35 @@ __device__ __forceinline__ void append_task(const FtleDev& f, DevCounters* ctr, 
 }
 
 // A: queue the neighbours that exist; boundary slots keep te as exit time.
+// The queue kernels walk their items warp by warp (grid-stride, uniform per
+// warp) so append_task's ballot always sees the whole warp.
 template <int D>
 __global__ void k_ftle_queue_nb(FtleDev f, DevCounters* ctr) {
-  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nserved = *(volatile int*)&ctr->count;
-  long s = idx / 6;
-  int c = (int)(idx % 6);
-  bool want = false;
-  if (s < nserved) {
-    long nb[6];
-    int i, j, k;
-    served_geometry(f, f.served[s], nb, i, j, k);
-    want = nb[c] >= 0;
-    if (!want) f.elt[s * 6 + c] = f.te[f.trig[s]];
+  const long total = 6 * nserved, stride = (long)gridDim.x * blockDim.x;
+  for (long base = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+    long idx = base + (threadIdx.x & 31);
+    long s = idx / 6;
+    int c = (int)(idx % 6);
+    bool want = false;
+    if (s < nserved) {
+      long nb[6];
+      int i, j, k;
+      served_geometry(f, f.served[s], nb, i, j, k);
+      want = nb[c] >= 0;
+      if (!want) f.elt[s * 6 + c] = f.te[f.trig[s]];
+    }
+    append_task(f, ctr, want, (int)s, c);
   }
-  append_task(f, ctr, want, (int)s, c);
 }
 
 // B + C queue: MinExitTime, then q itself and (if it moved) the neighbours.
 template <int D>
 __global__ void k_ftle_queue_self(FtleDev f, DevCounters* ctr) {
-  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nserved = *(volatile int*)&ctr->count;
+  const long total = 7 * nserved, stride = (long)gridDim.x * blockDim.x;
+  for (long base = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+  long idx = base + (threadIdx.x & 31);
   long s = idx / 7;
   int c = (int)(idx % 7);
   bool want = false;
@@ -226,6 +261,7 @@ __global__ void k_ftle_queue_self(FtleDev f, DevCounters* ctr) {
     }
   }
   append_task(f, ctr, want, (int)s, c);
+  }
 }
 
 // The advections of A (phase 0: to te, recording exit times) and C (phase 1:
@@ -233,11 +269,13 @@ __global__ void k_ftle_queue_self(FtleDev f, DevCounters* ctr) {
 template <int D, int M>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_tasks(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
                                                                    double t1, int phase, DevCounters* ctr) {
-  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long ntask = *(volatile int*)&ctr->ntask;
+  int* cursor = &ctr->cur[1 + phase];
   unsigned steps = 0;
   int err = 0;
-  if (idx < ntask) {
+  for (long base = warp_grab(cursor); base < ntask; base = warp_grab(cursor)) {
+    const long idx = base + (threadIdx.x & 31);
+    if (idx >= ntask) continue;
     int2 tk = f.tasks[idx];
     long s = tk.x;
     int c = tk.y;
@@ -255,7 +293,7 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_tasks(DevMesh m, De
     t.left = f.left[p];
     t.eid = eid_at_trigger(f, p, trig);
     t.ldt = 0.0;
-    err = advect<D, M>(m, w, in, t, t1, tend, steps);
+    err |= advect<D, M>(m, w, in, t, t1, tend, steps);
     double* pos = f.epos + (s * 7 + c) * 3;
     pos[0] = t.X[0];
     pos[1] = t.X[1];
@@ -266,10 +304,7 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_tasks(DevMesh m, De
 }
 
 template <int D>
-__global__ void k_ftle_early_final(FtleDev f, DevCounters* ctr) {
-  long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long nserved = *(volatile int*)&ctr->count;
-  if (s >= nserved) return;
+__device__ __forceinline__ void early_final_one(const FtleDev& f, long s) {
   long q = f.served[s];
   double mt = f.emt[s];
   long nb[6];
@@ -301,6 +336,13 @@ __global__ void k_ftle_early_final(FtleDev f, DevCounters* ctr) {
   f.have[q] = 1;
 }
 
+template <int D>
+__global__ void k_ftle_early_final(FtleDev f, DevCounters* ctr) {
+  const long nserved = *(volatile int*)&ctr->count;
+  for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < nserved; s += (long)gridDim.x * blockDim.x)
+    early_final_one<D>(f, s);
+}
+
 template <int D, int M>
 __global__ void k_tracer_launch(DevMesh m, DevWindow w, TracerDev t, double tq, DevCounters* ctr) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -322,15 +364,16 @@ __global__ void k_tracer_launch(DevMesh m, DevWindow w, TracerDev t, double tq, 
 template <int D, int M>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_tracer_advance(DevMesh m, DevWindow w, DevInteg in, TracerDev t,
                                                         double t1, double t2, DevCounters* ctr) {
-  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nlive = *(volatile int*)&ctr->nlive;
   unsigned steps = 0;
   int err = 0;
-  if (idx < nlive) {
+  for (long base = warp_grab(&ctr->cur[0]); base < nlive; base = warp_grab(&ctr->cur[0])) {
+    const long idx = base + (threadIdx.x & 31);
+    if (idx >= nlive) continue;
     long i = t.live[idx];
     Pt p;
     load_pt(p, i, t.X, t.V, t.eid, t.left, t.ldt);
-    err = advect<D, M>(m, w, in, p, t1, t2, steps);
+    err |= advect<D, M>(m, w, in, p, t1, t2, steps);
     t.X[3 * i] = p.X[0];
     t.X[3 * i + 1] = p.X[1];
     t.X[3 * i + 2] = p.X[2];
@@ -363,17 +406,22 @@ struct Variant {
   }
   static void ftle_pass1(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
                          double t1, double t2, DevCounters* ctr, cudaStream_t s) {
-    k_ftle_pass1<D, M><<<vblk(f.n, 128), 128, 0, s>>>(m, w, in, f, t1, t2, ctr);
+    static const unsigned res = resident_blocks(k_ftle_pass1<D, M>, 128);
+    k_ftle_pass1<D, M><<<capped(f.n, 128, res), 128, 0, s>>>(m, w, in, f, t1, t2, ctr);
   }
   static void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
                          double t1, DevCounters* ctr, cudaStream_t s) {
+    static const unsigned res_nb = resident_blocks(k_ftle_queue_nb<D>, 256);
+    static const unsigned res_self = resident_blocks(k_ftle_queue_self<D>, 256);
+    static const unsigned res_tasks = resident_blocks(k_ftle_tasks<D, M>, 128);
+    static const unsigned res_final = resident_blocks(k_ftle_early_final<D>, 128);
     cudaMemsetAsync(&ctr->ntask, 0, sizeof(int), s);
-    k_ftle_queue_nb<D><<<vblk(6L * f.n, 256), 256, 0, s>>>(f, ctr);
-    k_ftle_tasks<D, M><<<vblk(6L * f.n, 128), 128, 0, s>>>(m, w, in, f, t1, 0, ctr);
+    k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, ctr);
+    k_ftle_tasks<D, M><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 0, ctr);
     cudaMemsetAsync(&ctr->ntask, 0, sizeof(int), s);
-    k_ftle_queue_self<D><<<vblk(7L * f.n, 256), 256, 0, s>>>(f, ctr);
-    k_ftle_tasks<D, M><<<vblk(7L * f.n, 128), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
-    k_ftle_early_final<D><<<vblk(f.n, 128), 128, 0, s>>>(f, ctr);
+    k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, ctr);
+    k_ftle_tasks<D, M><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
+    k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
   }
   static void tracer_launch(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq,
                             DevCounters* ctr, cudaStream_t s) {
@@ -381,7 +429,8 @@ struct Variant {
   }
   static void tracer_advance(const DevMesh& m, const DevWindow& w, const DevInteg& in,
                              const TracerDev& t, double t1, double t2, DevCounters* ctr, cudaStream_t s) {
-    k_tracer_advance<D, M><<<vblk(t.n, 128), 128, 0, s>>>(m, w, in, t, t1, t2, ctr);
+    static const unsigned res = resident_blocks(k_tracer_advance<D, M>, 128);
+    k_tracer_advance<D, M><<<capped(t.n, 128, res), 128, 0, s>>>(m, w, in, t, t1, t2, ctr);
   }
 };
 

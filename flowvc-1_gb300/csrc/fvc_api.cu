@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "fvc.h"
+#include "fvc_fpmath.cuh"
 #include "fvc_kernels.h"
 
 using namespace fvc;
@@ -197,6 +198,9 @@ extern "C" fvc_status fvc_set_cart_mesh(fvc_ctx* c, double xmin, double xmax, in
   } else {
     m.zmin = 0; m.zres = 1; m.dz = 0;
   }
+  m.rdx = rcp_for_div(m.dx);
+  m.rdy = rcp_for_div(m.dy);
+  m.rdz = rcp_for_div(m.dz);
   long nn = (long)m.xres * m.yres * m.zres;
   if (c->frame_nodes && c->frame_nodes != nn) {
     for (auto& kv : c->frames) cudaFree(kv.second);

@@ -16,11 +16,15 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "fvc_fpmath.cuh"
 #include "fvc_state.h"
 
 namespace fvc {
 
 #define FVC_TINY 1.0e-10
+
+// RN(1/6), for the RK4 update's division by 6 through div_rn
+constexpr double kRcp6 = 1.0 / 6.0;
 
 struct Pt {
   double X[3];
@@ -47,12 +51,14 @@ __device__ __forceinline__ int outside_domain(const DevMesh& m, const double X[3
 // TestOutsideCartVelDomain, ompVC/velocity.c:624-651
 template <int DIMS>
 __device__ __forceinline__ int outside_cart_grid(const DevMesh& m, const double X[3]) {
-  int imin = (int)floor((X[0] - m.xmin) / m.dx);
-  int jmin = (int)floor((X[1] - m.ymin) / m.dy);
-  int kmin = DIMS == 3 ? (int)floor((X[2] - m.zmin) / m.dz) : 0;
-  int imax = (int)ceil((X[0] - m.xmin) / m.dx);
-  int jmax = (int)ceil((X[1] - m.ymin) / m.dy);
-  int kmax = DIMS == 3 ? (int)ceil((X[2] - m.zmin) / m.dz) : 0;
+  const double fx = div_rn(X[0] - m.xmin, m.dx, m.rdx), fy = div_rn(X[1] - m.ymin, m.dy, m.rdy);
+  const double fz = DIMS == 3 ? div_rn(X[2] - m.zmin, m.dz, m.rdz) : 0.0;
+  int imin = (int)floor(fx);
+  int jmin = (int)floor(fy);
+  int kmin = DIMS == 3 ? (int)floor(fz) : 0;
+  int imax = (int)ceil(fx);
+  int jmax = (int)ceil(fy);
+  int kmax = DIMS == 3 ? (int)ceil(fz) : 0;
   return imin < 0 || imax > (m.xres - 1) || jmin < 0 || jmax > (m.yres - 1) || kmin < 0 ||
          kmax > (m.zres - 1);
 }
@@ -95,29 +101,29 @@ __device__ __forceinline__ int vel_cart(const DevMesh& m, const DevWindow& w, do
   double tloc;
   if (get_tloc(w, tslot, tq, tloc)) return PT_ERR_TLOC;
   double xloc, yloc;
-  int i = (int)floor((X[0] - m.xmin) / m.dx);
+  int i = (int)floor(div_rn(X[0] - m.xmin, m.dx, m.rdx));
   if (i == (m.xres - 1)) {
     i = m.xres - 2;
     xloc = 1.0;
   } else
-    xloc = (X[0] - m.xmin - i * m.dx) / m.dx;
-  int j = (int)floor((X[1] - m.ymin) / m.dy);
+    xloc = div_rn(X[0] - m.xmin - i * m.dx, m.dx, m.rdx);
+  int j = (int)floor(div_rn(X[1] - m.ymin, m.dy, m.rdy));
   if (j == (m.yres - 1)) {
     j = m.yres - 2;
     yloc = 1.0;
   } else
-    yloc = (X[1] - m.ymin - j * m.dy) / m.dy;
+    yloc = div_rn(X[1] - m.ymin - j * m.dy, m.dy, m.rdy);
   const long nx = m.xres, ny = m.yres;
   const double4_32a* A = w.f0;
   const double4_32a* B = w.f1;
   if (DIMS == 3) {
     double zloc;
-    int k = (int)floor((X[2] - m.zmin) / m.dz);
+    int k = (int)floor(div_rn(X[2] - m.zmin, m.dz, m.rdz));
     if (k == (m.zres - 1)) {
       k = m.zres - 2;
       zloc = 1.0;
     } else
-      zloc = (X[2] - m.zmin - k * m.dz) / m.dz;
+      zloc = div_rn(X[2] - m.zmin - k * m.dz, m.dz, m.rdz);
     double V1 = (tloc) * (xloc) * (yloc) * (zloc);
     double V2 = (tloc) * (xloc) * (yloc) * (1 - zloc);
     double V3 = (tloc) * (xloc) * (1 - yloc) * (zloc);
@@ -178,12 +184,13 @@ __device__ __forceinline__ int vel_cart(const DevMesh& m, const DevWindow& w, do
 // One element's record: the natural-coordinate map precomputed from its node
 // coordinates (ompVC/velocity.c:497-510 and 529-535; recomputing it gives the
 // same doubles) and its node ids.
-//   3D, 16 doubles: a11 a12 a13 a21 a22 a23 a31 a32 a33 V x0 y0 z0 - | nodes
-//   2D, 12 doubles: a11 a12 a21 a22 V x0 y0 - | nodes | -
+//   3D, 16 doubles: a11 a12 a13 a21 a22 a23 a31 a32 a33 V x0 y0 z0 rV | nodes
+//   2D, 12 doubles: a11 a12 a21 a22 V x0 y0 rV | nodes | -
+// rV is the reciprocal div_rn uses to divide by V.
 template <int DIMS>
 struct Geo {
   double a[DIMS == 3 ? 9 : 4];
-  double V, x0, y0, z0;
+  double V, rV, x0, y0, z0;
   int4 nd;
 };
 
@@ -196,13 +203,13 @@ __device__ __forceinline__ void load_geo(const DevMesh& m, int e, Geo<DIMS>& g) 
     g.nd = __ldg(reinterpret_cast<const int4*>(p + 7));
     g.a[0] = g0.x; g.a[1] = g0.y; g.a[2] = g1.x; g.a[3] = g1.y; g.a[4] = g2.x;
     g.a[5] = g2.y; g.a[6] = g3.x; g.a[7] = g3.y; g.a[8] = g4.x;
-    g.V = g4.y; g.x0 = g5.x; g.y0 = g5.y; g.z0 = g6.x;
+    g.V = g4.y; g.x0 = g5.x; g.y0 = g5.y; g.z0 = g6.x; g.rV = g6.y;
   } else {
     const double2* p = reinterpret_cast<const double2*>(m.geom + (long)e * 12);
     double2 g0 = __ldg(p + 0), g1 = __ldg(p + 1), g2 = __ldg(p + 2), g3 = __ldg(p + 3);
     g.nd = __ldg(reinterpret_cast<const int4*>(p + 4));
     g.a[0] = g0.x; g.a[1] = g0.y; g.a[2] = g1.x; g.a[3] = g1.y;
-    g.V = g2.x; g.x0 = g2.y; g.y0 = g3.x; g.z0 = 0.0;
+    g.V = g2.x; g.x0 = g2.y; g.y0 = g3.x; g.z0 = 0.0; g.rV = g3.y;
   }
 }
 
@@ -213,15 +220,15 @@ __device__ __forceinline__ double natural_from(const Geo<DIMS>& g, const double 
                                                double& s, double& t, double& wv) {
   if (DIMS == 3) {
     double dx = X[0] - g.x0, dy = X[1] - g.y0, dz = X[2] - g.z0;
-    r = (g.a[0] * dx + g.a[1] * dy + g.a[2] * dz) / g.V;
-    s = (g.a[3] * dx + g.a[4] * dy + g.a[5] * dz) / g.V;
-    t = (g.a[6] * dx + g.a[7] * dy + g.a[8] * dz) / g.V;
+    r = div_rn(g.a[0] * dx + g.a[1] * dy + g.a[2] * dz, g.V, g.rV);
+    s = div_rn(g.a[3] * dx + g.a[4] * dy + g.a[5] * dz, g.V, g.rV);
+    t = div_rn(g.a[6] * dx + g.a[7] * dy + g.a[8] * dz, g.V, g.rV);
     wv = 1 - r - s - t;
     return dmin(r, dmin(s, dmin(t, wv)));
   } else {
     double dx = X[0] - g.x0, dy = X[1] - g.y0;
-    r = (g.a[0] * dx + g.a[1] * dy) / g.V;
-    s = (g.a[2] * dx + g.a[3] * dy) / g.V;
+    r = div_rn(g.a[0] * dx + g.a[1] * dy, g.V, g.rV);
+    s = div_rn(g.a[2] * dx + g.a[3] * dy, g.V, g.rV);
     t = 0;
     wv = 1 - r - s;
     return dmin(r, dmin(s, wv));
@@ -273,18 +280,38 @@ __device__ __forceinline__ void load_slot_nodes(const DevWindow& w, int tslot, i
 // coordinates put the point outside by more than their error bound, with one
 // coordinate below all others by more than that bound, the FP64 test fails
 // and selects that face too, so the hop is taken without the FP64 solve.
-// Returns the face slot, or -1 when the FP64 test must decide.  The bound
-// tol = 1e-6 (1 + sum |a_ij dx_j / V|) covers the FP32 roundings of the map,
-// the offsets and the products and sums (each under 2^-24 relative).
+// Returns the face slot, or -1 when the FP64 test must decide.
+//
+// The FP32 offsets are Xf - x0f, with Xf the position truncated to FP32
+// (f32_trunc, no FP64 instruction) once per walk and x0f the node rounded to
+// FP32.  Per component the offset then errs by at most
+//   E = 2^-22 (|Xf| + |x0f| + |dx|) + 2^-125,
+// and each coordinate (and 1 - r - s - t) by at most A E, with A = sum |a_ij|
+// / |V| stored per element.  The FP32 map, products, sums and 1/V add at most
+// 1e-6 (1 + S), S = sum |a_ij dx_j / V|; tol is the sum of the two.
+struct PosF {
+  float x[3];
+  float m;  // max |x_j|
+};
+
+__device__ __forceinline__ PosF pos_f32(const double X[3]) {
+  PosF P;
+  P.x[0] = f32_trunc(X[0]);
+  P.x[1] = f32_trunc(X[1]);
+  P.x[2] = f32_trunc(X[2]);
+  P.m = fmaxf(fabsf(P.x[0]), fmaxf(fabsf(P.x[1]), fabsf(P.x[2])));
+  return P;
+}
+
 template <int DIMS>
-__device__ __forceinline__ int quick_hop(const DevMesh& m, int e, const double X[3]) {
+__device__ __forceinline__ int quick_hop(const DevMesh& m, int e, const PosF& P) {
   const float* q = m.geo32 + (long)e * 16;
   if (DIMS == 3) {
     float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
-    float2 q2 = __ldg(reinterpret_cast<const float2*>(q + 8));
-    const double* qd = reinterpret_cast<const double*>(q + 10);
-    double x0 = __ldg(qd), y0 = __ldg(qd + 1), z0 = __ldg(qd + 2);
-    float dx = (float)(X[0] - x0), dy = (float)(X[1] - y0), dz = (float)(X[2] - z0);
+    float4 q2 = __ldg(reinterpret_cast<const float4*>(q + 8));
+    float2 q3 = __ldg(reinterpret_cast<const float2*>(q + 12));
+    // q2 = (a33, 1/V, x0, y0), q3 = (z0, A)
+    float dx = P.x[0] - q2.z, dy = P.x[1] - q2.w, dz = P.x[2] - q3.x;
     float iv = q2.y;
     float r0 = q0.x * dx, r1 = q0.y * dy, r2 = q0.z * dz;
     float s0 = q0.w * dx, s1 = q1.x * dy, s2 = q1.y * dz;
@@ -292,7 +319,9 @@ __device__ __forceinline__ int quick_hop(const DevMesh& m, int e, const double X
     float r = (r0 + r1 + r2) * iv, s = (s0 + s1 + s2) * iv, t = (t0 + t1 + t2) * iv;
     float S = (fabsf(r0) + fabsf(r1) + fabsf(r2) + fabsf(s0) + fabsf(s1) + fabsf(s2) + fabsf(t0) + fabsf(t1) +
                fabsf(t2)) * fabsf(iv);
-    float tol = 1e-6f * (1.0f + S);
+    float E = 2.4e-7f * (P.m + fmaxf(fabsf(q2.z), fmaxf(fabsf(q2.w), fabsf(q3.x))) +
+                         fmaxf(fabsf(dx), fmaxf(fabsf(dy), fabsf(dz)))) + 1e-37f;
+    float tol = 1e-6f * (1.0f + S) + 1.01f * q3.y * E;
     float w = 1.0f - r - s - t;
     float c[4] = {r, s, t, w};
     int k = 0;
@@ -307,15 +336,16 @@ __device__ __forceinline__ int quick_hop(const DevMesh& m, int e, const double X
     if (!(d < -(1e-10f + 2.0f * tol)) || !(second - d > 1e-10f + 4.0f * tol)) return -1;
     return k;
   } else {
-    float4 q0 = __ldg(reinterpret_cast<const float4*>(q));
-    float iv = __ldg(q + 4);
-    const double* qd = reinterpret_cast<const double*>(q + 6);
-    double x0 = __ldg(qd), y0 = __ldg(qd + 1);
-    float dx = (float)(X[0] - x0), dy = (float)(X[1] - y0);
+    float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
+    // q0 = (a11, a12, a21, a22), q1 = (1/V, x0, y0, A)
+    float dx = P.x[0] - q1.y, dy = P.x[1] - q1.z;
+    float iv = q1.x;
     float r0 = q0.x * dx, r1 = q0.y * dy, s0 = q0.z * dx, s1 = q0.w * dy;
     float r = (r0 + r1) * iv, s = (s0 + s1) * iv;
     float S = (fabsf(r0) + fabsf(r1) + fabsf(s0) + fabsf(s1)) * fabsf(iv);
-    float tol = 1e-6f * (1.0f + S);
+    float E = 2.4e-7f * (fmaxf(fabsf(P.x[0]), fabsf(P.x[1])) + fmaxf(fabsf(q1.y), fabsf(q1.z)) +
+                         fmaxf(fabsf(dx), fabsf(dy))) + 1e-37f;
+    float tol = 1e-6f * (1.0f + S) + 1.01f * q1.w * E;
     float w = 1.0f - r - s;
     float c[3] = {r, s, w};
     int k = 0;
@@ -346,9 +376,10 @@ __device__ __forceinline__ int neighbour(const DevMesh& m, int e, int slot) {
 template <int DIMS>
 __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& eid, bool vel_rule, double& r,
                                     double& s, double& t, double& wv, double& d, int4& nd) {
+  const PosF P = pos_f32(X);
   for (int hop = 0; hop < m.max_hops;) {
     int qs;
-    while (hop < m.max_hops && (qs = quick_hop<DIMS>(m, eid, X)) >= 0) {
+    while (hop < m.max_hops && (qs = quick_hop<DIMS>(m, eid, P)) >= 0) {
       eid = neighbour(m, eid, qs);
       hop++;
       if (eid == -1) return 1;
@@ -540,11 +571,11 @@ __device__ __forceinline__ int rk4_stages(const DevMesh& m, const DevWindow& w, 
   M[0] = p.X[0] + 0.5 * kk[0][0] * h;
   M[1] = p.X[1] + 0.5 * kk[0][1] * h;
   M[2] = p.X[2] + 0.5 * kk[0][2] * h;
-  if ((err = velocity<DIMS, MESH>(m, w, tc + h / 2, 2 * k + 1, M, e[1], l[1], kk[1]))) return err;
+  if ((err = velocity<DIMS, MESH>(m, w, tc + h * 0.5, 2 * k + 1, M, e[1], l[1], kk[1]))) return err;
   M[0] = p.X[0] + 0.5 * kk[1][0] * h;
   M[1] = p.X[1] + 0.5 * kk[1][1] * h;
   M[2] = p.X[2] + 0.5 * kk[1][2] * h;
-  if ((err = velocity<DIMS, MESH>(m, w, tc + h / 2, 2 * k + 1, M, e[2], l[2], kk[2]))) return err;
+  if ((err = velocity<DIMS, MESH>(m, w, tc + h * 0.5, 2 * k + 1, M, e[2], l[2], kk[2]))) return err;
   M[0] = p.X[0] + kk[2][0] * h;
   M[1] = p.X[1] + kk[2][1] * h;
   M[2] = p.X[2] + kk[2][2] * h;
@@ -566,7 +597,7 @@ __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, cons
     if ((tc + h - tend) * (tc + h - tstart) > 0.0) h = dsign(tend - tc, tend - tstart);
     if ((err |= rk4_stages<DIMS, MESH>(m, w, p, tc, h, k, e, l, kk, &nc))) return tend;
 #pragma unroll
-    for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]) / 6;
+    for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + div_rn(h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]), 6.0, kRcp6);
     tc = tc + h;
     k++;
     if (MESH == 1) p.eid = locate_walk<DIMS>(m, p.X, p.eid, err, &nc);
@@ -576,7 +607,7 @@ __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, cons
       p.left = 1;
       p.ldt = tc - h;
 #pragma unroll
-      for (int q = 0; q < 3; q++) p.X[q] = p.X[q] - h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]) / 6;
+      for (int q = 0; q < 3; q++) p.X[q] = p.X[q] - div_rn(h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]), 6.0, kRcp6);
       return p.ldt;
     }
     steps++;
@@ -610,7 +641,7 @@ __device__ __noinline__ double ab2(const DevMesh& m, const DevWindow& w, const D
       if ((err |= rk4_stages<DIMS, MESH>(m, w, p, tc, h, k, e, l, kk, &nc))) return tend;
 #pragma unroll
       for (int q = 0; q < 3; q++) {
-        inc[q] = h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]) / 6;
+        inc[q] = div_rn(h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]), 6.0, kRcp6);
         f[q] = kk[0][q];
       }
       lf = l[0] || l[1] || l[2] || l[3];

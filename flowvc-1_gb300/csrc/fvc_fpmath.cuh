@@ -1,0 +1,56 @@
+// fvc_fpmath.cuh -- two helpers that keep work off the FP64 pipe (GB300's
+// FP64 rate is 1/64 of its FP32 rate) without changing a bit of any result.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace fvc {
+
+// a / b rounded to nearest, given y = RN(1/b) (the IEEE quotient 1.0 / b,
+// precomputed once per divisor).  Markstein's correction step:
+//   r = a - b q (one FMA), q' = q + r y (one FMA)
+// returns RN(a/b) exactly when y is within half an ulp of 1/b and q is
+// within one ulp of a/b (P. Markstein, "Computation of elementary functions
+// on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990; the
+// Handbook of Floating-Point Arithmetic, Muller et al., Birkhauser, treats
+// the same theorem).  q0 = RN(a y) can be up to two ulps off, so one
+// correction first brings it within 2^-104 relative (faithful), and the
+// second gives the correctly rounded quotient.  The remainder a - b q is
+// exact only without underflow, so numerators outside 2^-400 .. 2^400 in
+// magnitude (zero included: IEEE keeps its sign) and divisors without a
+// usable reciprocal (y passed as 0) take the IEEE division.  Cost: one DMUL
+// and four DFMA, against a reciprocal iteration for the IEEE division.
+__device__ __forceinline__ double div_rn(double a, double b, double y) {
+  const int ea = (__double2hiint(a) >> 20) & 0x7ff;
+  if ((unsigned)(ea - (1023 - 400)) > 800u || __double2hiint(y) == 0) return a / b;
+  double q = a * y;
+  double r = fma(-b, q, a);
+  q = fma(r, y, q);
+  r = fma(-b, q, a);
+  return fma(r, y, q);
+}
+
+// The reciprocal div_rn wants for divisor b, or 0 when b is outside
+// 2^-400 .. 2^400 in magnitude (then div_rn divides).
+__host__ __device__ __forceinline__ double rcp_for_div(double b) {
+  double ab = b < 0 ? -b : b;
+  if (!(ab >= 0x1p-400 && ab <= 0x1p400)) return 0.0;
+  return 1.0 / b;
+}
+
+// x rounded toward zero to FP32 with integer operations only (no FP64-pipe
+// conversion).  For |x| < 2^128 the result f satisfies |x - f| <= 2^-23 |x|
+// + 2^-126; larger magnitudes, infinities and NaN give NaN, which fails
+// every comparison and so leaves a decision to the FP64 path.
+__device__ __forceinline__ float f32_trunc(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
+  const int fe = (int)((hi >> 20) & 0x7ff) - 1023 + 127;
+  const unsigned man = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  unsigned bits;
+  if (fe <= 0) bits = sign;
+  else if (fe >= 255) bits = 0x7fc00000u;
+  else bits = sign | ((unsigned)fe << 23) | man;
+  return __uint_as_float(bits);
+}
+
+}  // namespace fvc

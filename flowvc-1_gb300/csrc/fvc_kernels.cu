@@ -53,16 +53,20 @@ __global__ void k_geometry(DevMesh m, double* geom, float* geo32) {
     g[10] = x0;
     g[11] = y0;
     g[12] = z0;
-    g[13] = 0.0;
+    g[13] = rcp_for_div(g[9]);
     reinterpret_cast<int4*>(g + 14)[0] = nd;
-    // FP32 map for the walk's pre-check: a11..a33, 1/V, then x0 y0 z0 (FP64)
+    // FP32 copy for the walk's pre-check: a11..a33, 1/V, x0 y0 z0, and the
+    // scale A = sum |a_ij| / |V| of the coordinates' error per unit offset error
     float* q = geo32 + (long)e * 16;
     for (int c = 0; c < 9; c++) q[c] = (float)g[c];
     q[9] = (float)(1.0 / g[9]);
-    double* qd = reinterpret_cast<double*>(q + 10);
-    qd[0] = x0;
-    qd[1] = y0;
-    qd[2] = z0;
+    q[10] = (float)x0;
+    q[11] = (float)y0;
+    q[12] = (float)z0;
+    double sa = 0.0;
+    for (int c = 0; c < 9; c++) sa += fabs(g[c]);
+    q[13] = (float)(sa / fabs(g[9]) * (1.0 + 1e-6));
+    q[14] = q[15] = 0.f;
   } else {
     double* g = geom + (long)e * 12;
     g[0] = y2 - y0;  // a11
@@ -72,18 +76,17 @@ __global__ void k_geometry(DevMesh m, double* geom, float* geo32) {
     g[4] = (x1 - x0) * (y2 - y0) - (x2 - x0) * (y1 - y0);  // V
     g[5] = x0;
     g[6] = y0;
-    g[7] = 0.0;
+    g[7] = rcp_for_div(g[4]);
     reinterpret_cast<int4*>(g + 8)[0] = nd;
     g[10] = g[11] = 0.0;
     float* q = geo32 + (long)e * 16;
     for (int c = 0; c < 4; c++) q[c] = (float)g[c];
     q[4] = (float)(1.0 / g[4]);
-    q[5] = 0.f;
-    double* qd = reinterpret_cast<double*>(q + 6);
-    qd[0] = x0;
-    qd[1] = y0;
-    qd[2] = 0.0;
-    q[12] = q[13] = q[14] = q[15] = 0.f;
+    q[5] = (float)x0;
+    q[6] = (float)y0;
+    double sa = fabs(g[0]) + fabs(g[1]) + fabs(g[2]) + fabs(g[3]);
+    q[7] = (float)(sa / fabs(g[4]) * (1.0 + 1e-6));
+    for (int c = 8; c < 16; c++) q[c] = 0.f;
   }
 }
 

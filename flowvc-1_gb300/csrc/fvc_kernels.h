@@ -19,6 +19,7 @@ struct DevCounters {
   int nlive;   // live points of the current advection call
   int ntask;   // early-FTLE advections queued
   int pad;
+  int cur[4];  // work cursors of the persistent launches: 0 live list, 1-2 task lists
 };
 
 // ---- mesh preprocessing

@@ -12,11 +12,12 @@ struct DevMesh {
   int dims, mesh_type;  // 2/3; 0 Cartesian, 1 unstructured
   // Cartesian velocity grid (Vel_CartMesh, ompVC/mesh.c:67-122)
   double xmin, ymin, zmin, dx, dy, dz;
+  double rdx, rdy, rdz;  // reciprocals for div_rn (0: divide)
   int xres, yres, zres;
   // unstructured mesh
   const int4* elem;     // 2 x nelem: {Nodes[4]}, {NeighborIndex[4]}
   const double* geom;   // natural-coordinate map + node ids, 16 (3D) or 12 (2D) doubles per element
-  const float* geo32;   // FP32 copy of the map + FP64 node-0 coordinates, 64 B per element
+  const float* geo32;   // FP32 copy of the map, node-0 coordinates and error scale, 64 B per element
   const double4_32a* nodes; // x, y, z, 0 per node
   int nelem, nnodes;
   // Data_MeshBounds

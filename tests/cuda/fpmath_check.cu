@@ -1,0 +1,78 @@
+// Checks the FP64-pipe savers of fvc_fpmath.cuh against CUDA's own IEEE
+// operations on the GPU: div_rn(a, b, rcp_for_div(b)) must equal a / b bit
+// for bit, and f32_trunc(x) must equal __double2float_rz(x), on many seeded
+// operands from several distributions.  Prints one line of counts.
+#include <cstdio>
+#include <cstdint>
+#include <cstring>
+
+#include "fvc_fpmath.cuh"
+
+using namespace fvc;
+
+__device__ __forceinline__ uint64_t mix(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// a double with a random 52-bit fraction, random sign and exponent in [lo, hi]
+__device__ __forceinline__ double rnd(uint64_t h, int lo, int hi) {
+  uint64_t e = (uint64_t)(lo + (int)((h >> 52) % (uint64_t)(hi - lo + 1))) + 1023;
+  uint64_t bits = (h & 0xfffffffffffffull) | (e << 52) | ((h >> 63) << 63);
+  return __longlong_as_double((long long)bits);
+}
+
+struct Out {
+  unsigned long long n_div, bad_div, n_cvt, bad_cvt;
+  double a, b;
+  int kind;
+};
+
+__global__ void k_div(uint64_t seed, long n, Out* o) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t h1 = mix(seed ^ (uint64_t)i), h2 = mix(h1), h3 = mix(h2);
+  int kind = (int)(h3 % 6);
+  double a, b;
+  switch (kind) {
+    case 0: a = rnd(h1, -300, 300); b = rnd(h2, -99, 99); break;      // wide exponents
+    case 1: a = rnd(h1, -30, -10); b = rnd(h2, -24, -16); break;      // cofactor sums / element volumes
+    case 2: b = rnd(h2, -24, -16); a = b * (double)(int)(h1 % 2001 - 1000); break;  // exact quotients
+    case 3: {                                                          // quotients near a rounding midpoint
+      double q = rnd(h1, -8, 8);
+      b = rnd(h2, -20, 20);
+      a = fma(b, q, b * ldexp(q, -53));
+      break;
+    }
+    case 4: a = rnd(h1, -60, 60); b = 6.0; break;                      // the RK4 update
+    default: a = rnd(h1, -400, 400); b = rnd(h2, -400, 400); break;   // the fallback edges
+  }
+  double want = a / b, got = div_rn(a, b, rcp_for_div(b));
+  bool bad = __double_as_longlong(want) != __double_as_longlong(got);
+  if (bad && atomicAdd(&o->bad_div, 1ull) == 0) {
+    o->a = a;
+    o->b = b;
+    o->kind = kind;
+  }
+  double x = rnd(h3, -126, 127);
+  float fw = __double2float_rz(x), fg = f32_trunc(x);
+  if (__float_as_uint(fw) != __float_as_uint(fg)) atomicAdd(&o->bad_cvt, 1ull);
+}
+
+int main(int argc, char** argv) {
+  long n = argc > 1 ? atol(argv[1]) : (1L << 26);
+  int reps = argc > 2 ? atoi(argv[2]) : 4;
+  Out* d = nullptr;
+  if (cudaMalloc(&d, sizeof(Out)) != cudaSuccess) return 2;
+  cudaMemset(d, 0, sizeof(Out));
+  for (int r = 0; r < reps; r++) k_div<<<(unsigned)((n + 255) / 256), 256>>>(0x1234567ull + 977ull * r, n, d);
+  Out h;
+  if (cudaMemcpy(&h, d, sizeof(Out), cudaMemcpyDeviceToHost) != cudaSuccess) return 3;
+  h.n_div = h.n_cvt = (unsigned long long)n * reps;
+  printf("{\"n_div\": %llu, \"bad_div\": %llu, \"n_cvt\": %llu, \"bad_cvt\": %llu, \"first_bad\": [%.17g, %.17g, %d]}\n",
+         h.n_div, h.bad_div, h.n_cvt, h.bad_cvt, h.a, h.b, h.kind);
+  cudaFree(d);
+  return 0;
+}
