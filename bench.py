@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--cube", type=int, default=CUBE_N, help="mesh cells per edge")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-precision", action="store_true", help="skip the BF16 / FP16 mixed forms")
     ap.add_argument("--cpu-threads", type=int, default=0)
     return ap.parse_args()
 
@@ -229,6 +230,67 @@ def run_reference(args, rank, world):
 
 # ------------------------------------------------------------------ ranks
 
+def form_errors(ref, got):
+    """Errors of a mixed-precision window against the FP64 one.  Endpoints:
+    each point's final position (for a point that left, its last position
+    inside), over the points whose exit status agrees; element ids over the
+    same points; exit-flag and exit-time mismatches; FTLE errors relative to
+    the largest FP64 value and pointwise (floor 1e-3 of the largest)."""
+    (rT, rs), (gT, gs) = ref, got
+    same = rs["left"] == gs["left"]
+    d = np.linalg.norm(gs["X"][same] - rs["X"][same], axis=1) if same.any() else np.zeros(1)
+    both_left = same & (rs["left"] == 1)
+    scale = float(np.abs(rT).max()) or 1.0
+    e = np.abs(gT - rT)
+    rel = e / np.maximum(np.abs(rT), 1e-3 * scale)
+    return {"endpoint_max": float(d.max()), "endpoint_rms": float(np.sqrt((d ** 2).mean())),
+            "ftle_max_rel_to_max": float(e.max() / scale), "ftle_rms_rel_to_max": float(np.sqrt((e ** 2).mean()) / scale),
+            "ftle_median_rel": float(np.median(rel)), "ftle_p99_rel": float(np.quantile(rel, 0.99)),
+            "ftle_max_rel": float(rel.max()),
+            "eid_mismatch_rate": float((gs["eid"][same] != rs["eid"][same]).mean()) if same.any() else 0.0,
+            "left_mismatch_rate": float((~same).mean()),
+            "exit_time_mismatch_rate": float((np.abs(gs["ldt"][both_left] - rs["ldt"][both_left]) > 1e-9).mean())
+            if both_left.any() else 0.0,
+            "points_left": float((rs["left"] == 1).mean())}
+
+
+def precision_forms(ctx, ax, grid, stream, barrier, args, fp64_value):
+    """BF16 and FP16 frames with FP32 stages (fvc_set_precision) on the same
+    context and workload: one warm-up window, then args.steps timed windows
+    with CUDA events; errors against one more FP64 window."""
+    import torch
+
+    import flow
+    ref_state = {}
+    ref_T = flow.run_ftle(ctx, ax, grid, T_WINDOW, state=ref_state)[0]
+    out = {}
+    for name in ("bf16", "fp16"):
+        ctx.set_precision(name)
+        flow.run_ftle(ctx, ax, grid, T_WINDOW)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps, stats, st_last, T_last = 0, [], {}, None
+        e0.record(stream)
+        for k in range(args.steps):
+            wT, wN, st, js = flow.run_ftle(ctx, ax, grid, T_WINDOW)
+            steps += st
+            stats.append(js)
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1)
+        got_state = {}
+        T_last = flow.run_ftle(ctx, ax, grid, T_WINDOW, state=got_state)[0]
+        value = steps / (ms / 1000.0)
+        out[name] = {"value": value, "unit": "steps/s", "ms_per_step": ms / args.steps,
+                     "ftle_points_per_s": args.grid ** 3 * args.steps / (ms / 1000.0),
+                     "speedup_vs_fp64": value / fp64_value,
+                     "phases_ms_per_step": {k: sum(s[k] for s in stats) / args.steps
+                                            for k in ("ms_setup", "ms_main", "ms_early", "ms_reduce")},
+                     "errors": form_errors((ref_T, ref_state), (T_last, got_state))}
+    ctx.set_precision("fp64")
+    return out
+
+
 def reduce_over_ranks(secs, units, world):
     """(max seconds over ranks, sum of units over ranks).  Every rank calls it;
     uses the process group's device (CUDA for NCCL, CPU for gloo)."""
@@ -309,6 +371,11 @@ def run_engine(args, rank, world, local_rank):
     traffic = traffic_per_step * steps_main / launches_main if traffic_per_step else None
     gpu_launches = int(sum(s["launches"] for s in stats))
 
+    # the mixed-precision forms on the same workload, against this FP64 run
+    forms = None
+    if not args.no_precision:
+        forms = precision_forms(ctx, ax, grid, stream, barrier, args, steps_all / secs_max)
+
     # end to end through the C ABI from pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -362,6 +429,7 @@ def run_engine(args, rank, world, local_rank):
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "k_ftle_pass1", "bytes_per_step": BYTES_PER_STEP},
             "gpu_launches": gpu_launches,
+            "precision_forms": forms,
             "phases_ms_per_step": {k: sum(s[k] for s in stats) / args.steps
                                    for k in ("ms_setup", "ms_main", "ms_early", "ms_reduce")},
             "fp64_probe": fp64,

@@ -310,7 +310,18 @@ __device__ __forceinline__ void early_final_one(const FtleDev& f, long s) {
   long nb[6];
   int i, j, k;
   served_geometry(f, q, nb, i, j, k);
-  const double* pos = f.epos + s * 21;
+  double P[21];
+  const double* E = f.epos + s * 21;
+  if (f.mixed) {
+    // (X, c) float pairs: the position is X - c
+    const float2* E2 = reinterpret_cast<const float2*>(E);
+#pragma unroll
+    for (int a = 0; a < 21; a++) P[a] = (double)E2[a].x - (double)E2[a].y;
+  } else {
+#pragma unroll
+    for (int a = 0; a < 21; a++) P[a] = E[a];
+  }
+  const double* pos = P;
   const double* self = pos + 18;
   const double *L, *R, *B, *T, *Bk, *F;
   double fx, fy, fz;

@@ -43,6 +43,20 @@ struct fvc_ctx {
   // scratch for array calls
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
+  // mixed-precision form: quantised frames by frame id, the call's step table
+  int prec = 0;
+  struct QFrame {
+    ushort4* q = nullptr;
+    float s[3] = {1.f, 1.f, 1.f};
+    int fmt = 0;
+  };
+  std::unordered_map<int, QFrame> qframes;
+  unsigned* d_qscratch = nullptr;
+  uint4* d_qpair = nullptr;  // the window's two quantised frames, interleaved
+  std::vector<StepM> h_steps;
+  StepM* d_steps = nullptr;
+  size_t steps_cap = 0;
+  int window_lo = -1, window_hi = -1;
   std::string err;
 };
 
@@ -52,6 +66,8 @@ struct fvc_job {
   FtleDev f{};
   TracerDev t{};
   void* mem = nullptr;  // one allocation for all per-job arrays
+  int prec = 0;         // arithmetic form the job was created with
+  bool packed = false;  // positions held as (X, c) float pairs
   fvc_job_stats stats{};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
@@ -128,6 +144,24 @@ static fvc_status ensure_scratch(fvc_ctx* c, size_t bytes) {
 
 static inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// Frees the quantised frames (their node count changed with the mesh).
+static void drop_quantised(fvc_ctx* c) {
+  for (auto& kv : c->qframes) cudaFree(kv.second.q);
+  c->qframes.clear();
+  cudaFree(c->d_qpair);
+  c->d_qpair = nullptr;
+  c->window_set = false;
+}
+
+// (X, c) float pairs copied to the host back to FP64 positions X - c.
+static void unpack_host(double* A, size_t n) {
+  for (size_t i = 0; i < n; i++) {
+    float p[2];
+    memcpy(p, &A[i], sizeof(p));
+    A[i] = (double)p[0] - (double)p[1];
+  }
+}
+
 // ------------------------------------------------------------------ context
 
 extern "C" int fvc_abi_version(void) { return FVC_ABI_VERSION; }
@@ -164,6 +198,10 @@ extern "C" void fvc_destroy(fvc_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto& kv : c->frames) cudaFree(kv.second);
+  for (auto& kv : c->qframes) cudaFree(kv.second.q);
+  cudaFree(c->d_qscratch);
+  cudaFree(c->d_qpair);
+  cudaFree(c->d_steps);
   cudaFree(c->d_elem);
   cudaFree(c->d_geom);
   cudaFree(c->d_geo32);
@@ -205,6 +243,7 @@ extern "C" fvc_status fvc_set_cart_mesh(fvc_ctx* c, double xmin, double xmax, in
   if (c->frame_nodes && c->frame_nodes != nn) {
     for (auto& kv : c->frames) cudaFree(kv.second);
     c->frames.clear();
+    drop_quantised(c);
   }
   c->frame_nodes = nn;
   c->mesh_set = true;
@@ -322,6 +361,7 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
   if (c->frame_nodes && c->frame_nodes != nnodes) {
     for (auto& kv : c->frames) cudaFree(kv.second);
     c->frames.clear();
+    drop_quantised(c);
   }
   c->frame_nodes = nnodes;
   c->mesh_set = true;
@@ -363,9 +403,70 @@ extern "C" fvc_status fvc_upload_frame(fvc_ctx* c, int frame_id, const double* u
     return fail(c, FVC_ERR_OOM, "frame allocation failed");
   }
   FVC_CUDA(c, cudaMemcpyAsync(c->d_stage, uvw, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  auto qf = c->qframes.find(frame_id);
+  if (qf != c->qframes.end()) qf->second.fmt = 0;  // stale: quantised again when next used
   pack_frame(c->d_stage, dst, n, c->stream);
   if ((st = check_launch(c, "pack_frame"))) return st;
   FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FVC_OK;
+}
+
+// The quantised copy of a resident frame in the context's 16-bit format,
+// made on first use after the frame was uploaded or the format changed.
+static fvc_status quantised(fvc_ctx* c, int id, fvc_ctx::QFrame** out) {
+  fvc_ctx::QFrame& q = c->qframes[id];
+  if (q.fmt != c->prec) {
+    long n = c->frame_nodes;
+    if (!q.q && cudaMalloc(&q.q, sizeof(ushort4) * (size_t)n) != cudaSuccess)
+      return fail(c, FVC_ERR_OOM, "quantised frame allocation failed");
+    if (!c->d_qscratch && cudaMalloc(&c->d_qscratch, 4 * sizeof(unsigned)) != cudaSuccess)
+      return fail(c, FVC_ERR_OOM, "quantisation scratch allocation failed");
+    if (quantize_frame(c->frames[id], n, c->prec, q.q, c->d_qscratch, q.s, c->stream))
+      return fail(c, FVC_ERR_CUDA, "frame quantisation failed");
+    q.fmt = c->prec;
+  }
+  *out = &q;
+  return FVC_OK;
+}
+
+static fvc_status quantised_window(fvc_ctx* c) {
+  fvc_ctx::QFrame *a = nullptr, *b = nullptr;
+  fvc_status st;
+  if ((st = quantised(c, c->window_lo, &a)) || (st = quantised(c, c->window_hi, &b))) return st;
+  DevWindow& w = c->window;
+  if (!c->d_qpair && cudaMalloc(&c->d_qpair, sizeof(uint4) * (size_t)c->frame_nodes) != cudaSuccess)
+    return fail(c, FVC_ERR_OOM, "quantised window allocation failed");
+  pair_frames(a->q, b->q, c->frame_nodes, c->d_qpair, c->stream);
+  if ((st = check_launch(c, "pair frames"))) return st;
+  w.qp = c->d_qpair;
+  for (int k = 0; k < 3; k++) {
+    w.qs0[k] = a->s[k];
+    w.qs1[k] = b->s[k];
+  }
+  w.qfmt = c->prec;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_set_precision(fvc_ctx* c, int precision) {
+  if (!c) return FVC_ERR_ARG;
+  if (precision != FVC_PREC_FP64 && precision != FVC_PREC_BF16 && precision != FVC_PREC_FP16)
+    return fail(c, FVC_ERR_ARG, "precision %d: use FVC_PREC_FP64, FVC_PREC_BF16 or FVC_PREC_FP16", precision);
+  if (precision != FVC_PREC_FP64 && c->mesh.mesh_type != 1)
+    return fail(c, FVC_ERR_ARG, "the mixed-precision form needs an unstructured mesh");
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  c->prec = precision;
+  c->mesh.prec = precision;
+  if (precision && c->window_set) return quantised_window(c);
+  return FVC_OK;
+}
+
+// The mixed form runs Euler and RK4 without extrapolation.
+static fvc_status mixed_ok(fvc_ctx* c) {
+  if (!c->prec) return FVC_OK;
+  if (c->integ.type != 0 && c->integ.type != 1)
+    return fail(c, FVC_ERR_ARG, "the mixed-precision form runs Euler (0) and RK4 (1), not Int_Type %d", c->integ.type);
+  if (c->integ.extrapolate) return fail(c, FVC_ERR_ARG, "the mixed-precision form does not extrapolate");
   return FVC_OK;
 }
 
@@ -379,8 +480,11 @@ extern "C" fvc_status fvc_set_window(fvc_ctx* c, int lo, int hi, double tmin, do
   c->window.tmin = tmin;
   c->window.tmax = tmax;
   c->window.nslots = 0;
+  c->window.nsteps = 0;
   c->window_set = true;
-  return FVC_OK;
+  c->window_lo = lo;
+  c->window_hi = hi;
+  return c->prec ? quantised_window(c) : FVC_OK;
 }
 
 // The stage times of an advection call from t1 to t2, computed with the
@@ -389,7 +493,10 @@ extern "C" fvc_status fvc_set_window(fvc_ctx* c, int lo, int hi, double tmin, do
 // hint: the kernels compare its time with the time they compute before using
 // it, so the table can end early (slot cap, tloc out of range) without
 // changing any result.
+static fvc_status build_steps(fvc_ctx* c, double t1, double t2);
+
 static fvc_status prepare_slots(fvc_ctx* c, double t1, double t2) {
+  if (c->prec) return build_steps(c, t1, t2);
   DevWindow& w = c->window;
   w.nslots = 0;
   int n = 0;
@@ -431,6 +538,50 @@ static fvc_status prepare_slots(fvc_ctx* c, double t1, double t2) {
   return check_launch(c, "time fields");
 }
 
+// The mixed form's step table for a call from t1 to t2: the stage times of
+// the FP64 step loop (ompVC/integration.c:345-352, 402, the same sequence as
+// prepare_slots), each step's length and the tloc of its stages.  A stage
+// time outside the window gives FVC_ERR_TLOC for the call.
+static fvc_status build_steps(fvc_ctx* c, double t1, double t2) {
+  DevWindow& w = c->window;
+  std::vector<StepM>& T = c->h_steps;
+  T.clear();
+  auto tloc = [&](double tq, float& out) {
+    double tl = (tq - w.tmin) / (w.tmax - w.tmin);
+    if ((tl > 1 + 1.0e-10) || (tl < 0 - 1.0e-10)) return false;
+    out = (float)tl;
+    return true;
+  };
+  double tc = t1, h = (t2 - t1) >= 0.0 ? fabs(c->integ.h) : -fabs(c->integ.h);
+  while ((tc - t2) * (t2 - t1) < 0.0) {
+    if ((tc + h - t2) * (tc + h - t1) > 0.0) h = (t2 - t1) >= 0.0 ? fabs(t2 - tc) : -fabs(t2 - tc);
+    StepM s{};
+    s.tc = tc;
+    s.h = (float)h;
+    if (!tloc(tc, s.tl0) || !tloc(tc + h / 2, s.tlh) || !tloc(tc + h, s.tl1))
+      return fail(c, FVC_ERR_TLOC, "advect: query time outside the loaded frame interval");
+    T.push_back(s);
+    tc = tc + h;
+  }
+  StepM e{};
+  e.tc = tc;
+  T.push_back(e);
+  if (T.size() > c->steps_cap) {
+    cudaFree(c->d_steps);
+    c->d_steps = nullptr;
+    c->steps_cap = 0;
+    size_t cap = T.size() < 64 ? 64 : 2 * T.size();
+    if (cudaMalloc(&c->d_steps, sizeof(StepM) * cap) != cudaSuccess)
+      return fail(c, FVC_ERR_OOM, "step table allocation failed");
+    c->steps_cap = cap;
+  }
+  FVC_CUDA(c, cudaMemcpyAsync(c->d_steps, T.data(), sizeof(StepM) * T.size(), cudaMemcpyHostToDevice, c->stream));
+  w.steps = c->d_steps;
+  w.nsteps = (int)T.size() - 1;
+  w.nslots = 0;
+  return FVC_OK;
+}
+
 static fvc_status ready(fvc_ctx* c, bool need_window) {
   if (!c) return FVC_ERR_ARG;
   if (!c->mesh_set) return fail(c, FVC_ERR_STATE, "mesh not set");
@@ -447,6 +598,7 @@ extern "C" fvc_status fvc_advect_device(fvc_ctx* c, int n, double* dX, double* d
   if (n < 0 || (n > 0 && (!dX || !dleft || !dldt))) return fail(c, FVC_ERR_ARG, "bad arrays");
   if (c->mesh.mesh_type == 1 && n > 0 && !deid) return fail(c, FVC_ERR_ARG, "unstructured advection needs element ids");
   if (c->integ.extrapolate && n > 0 && !dV) return fail(c, FVC_ERR_ARG, "extrapolation needs V");
+  if ((st = mixed_ok(c))) return st;
   if ((st = prepare_slots(c, t0, t1))) return st;
   launch_advect(c->mesh, c->window, c->integ, n, dX, dV, deid, dleft, dldt, t0, t1, c->d_ctr, c->stream);
   if ((st = check_launch(c, "advect"))) return st;
@@ -477,6 +629,7 @@ extern "C" fvc_status fvc_advect(fvc_ctx* c, int n, double* X, double* V, int* e
   FVC_CUDA(c, cudaMemcpyAsync(dt, ldt, sizeof(double) * n, cudaMemcpyHostToDevice, s));
   if (c->mesh.mesh_type == 1 && !eid) return fail(c, FVC_ERR_ARG, "unstructured advection needs element ids");
   if (c->integ.extrapolate && !V) return fail(c, FVC_ERR_ARG, "extrapolation needs V");
+  if ((st = mixed_ok(c))) return st;
   if ((st = prepare_slots(c, t0, t1))) return st;
   launch_advect(c->mesh, c->window, c->integ, n, dX, V ? dV : nullptr, eid ? de : nullptr, dl, dt, t0,
                 t1, c->d_ctr, s);
@@ -649,6 +802,8 @@ extern "C" fvc_status fvc_ftle_create(fvc_ctx* c, const fvc_ftle_spec* sp, fvc_j
   f.dy = (sp->ymax - sp->ymin) / (yr - 1);
   f.dz = dims == 3 ? (sp->zmax - sp->zmin) / (zr - 1) : 0.0;
   f.start = sp->start_time;
+  f.mixed = c->prec ? 1 : 0;
+  j->prec = c->prec;
   int* left0 = nullptr;
   st = carve(c, &j->mem,
              {{(void**)&f.X, 24 * n}, {(void**)&f.V, 24 * n}, {(void**)&f.ldt, 8 * n}, {(void**)&f.ftT, 8 * n},
@@ -684,6 +839,10 @@ extern "C" fvc_status fvc_ftle_create(fvc_ctx* c, const fvc_ftle_spec* sp, fvc_j
     j->stats.launches += 3;
     if ((st = check_launch(c, "ftle marks"))) { fvc_job_destroy(j); return st; }
   }
+  if (j->prec) {
+    pack_pairs(f.X, 3 * n, c->stream);
+    j->packed = true;
+  }
   cudaEventRecord(j->ev[0], c->stream);
   FVC_CUDA(c, cudaStreamSynchronize(c->stream));
   j->stats.ms_setup += ev_ms(j->ev[3], j->ev[0]);
@@ -700,7 +859,10 @@ extern "C" fvc_status fvc_ftle_set_state(fvc_job* j, const double* X, const int*
   FtleDev& f = j->f;
   size_t n = (size_t)f.n;
   cudaStream_t s = c->stream;
-  if (X) FVC_CUDA(c, cudaMemcpyAsync(f.X, X, 24 * n, cudaMemcpyHostToDevice, s));
+  if (X) {
+    FVC_CUDA(c, cudaMemcpyAsync(f.X, X, 24 * n, cudaMemcpyHostToDevice, s));
+    if (j->packed) pack_pairs(f.X, 3 * (long)n, s);
+  }
   if (eid) {
     std::vector<int> chk(eid, eid + n);
     for (size_t i = 0; i < n; i++)
@@ -734,6 +896,7 @@ extern "C" fvc_status fvc_ftle_get_state(fvc_job* j, double* X, int* eid, int* l
   if (wT) FVC_CUDA(c, cudaMemcpyAsync(wT, f.ftT, 8 * n, cudaMemcpyDeviceToHost, s));
   if (wN) FVC_CUDA(c, cudaMemcpyAsync(wN, f.ftN, 8 * n, cudaMemcpyDeviceToHost, s));
   FVC_CUDA(c, cudaStreamSynchronize(s));
+  if (X && j->packed) unpack_host(X, 3 * n);
   return FVC_OK;
 }
 
@@ -744,6 +907,12 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   if ((st = ready(c, true))) return st;
   cudaStream_t s = c->stream;
   job_events(j);
+  if (j->prec != c->prec) return fail(c, FVC_ERR_STATE, "the job was created with another precision form");
+  if ((st = mixed_ok(c))) return st;
+  if (j->prec && !j->packed) {
+    pack_pairs(j->f.X, 3L * j->f.n, s);
+    j->packed = true;
+  }
   if ((st = prepare_slots(c, t1, t2))) return st;
   if (launch) ftle_launch(c->mesh, c->window, j->f, j->f.start, c->d_ctr, s);
   compact_live(j->f.n, j->f.ldt, j->f.left, c->integ.extrapolate, j->f.live, j->f.flag, j->f.block_cnt, c->d_ctr, s);
@@ -774,6 +943,10 @@ extern "C" fvc_status fvc_ftle_reduce(fvc_job* j, double int_t, double* wT, doub
   fvc_status st;
   if ((st = use_device(c))) return st;
   job_events(j);
+  if (j->packed) {
+    unpack_pairs(j->f.X, 3L * j->f.n, c->stream);
+    j->packed = false;
+  }
   cudaEventRecord(j->ev[0], c->stream);
   ftle_final(j->f, c->mesh.dims, int_t, c->stream);
   cudaEventRecord(j->ev[1], c->stream);
@@ -799,6 +972,7 @@ extern "C" fvc_status fvc_tracer_create(fvc_ctx* c, const fvc_tracer_spec* sp, i
   fvc_job* j = new fvc_job();
   j->ctx = c;
   j->kind = 1;
+  j->prec = c->prec;
   TracerDev& t = j->t;
   t.n = n;
   long nn = n > 0 ? n : 1;
@@ -832,6 +1006,10 @@ extern "C" fvc_status fvc_tracer_create(fvc_ctx* c, const fvc_tracer_spec* sp, i
     tracer_init_marks(c->mesh, t, left0, sp->seed_chain, s);
     j->stats.launches += 2;
     if ((st = check_launch(c, "tracer init"))) { fvc_job_destroy(j); return st; }
+    if (j->prec) {
+      pack_pairs(t.X, 3L * n, s);
+      j->packed = true;
+    }
     FVC_CUDA(c, cudaStreamSynchronize(s));
   }
   *out = j;
@@ -843,6 +1021,8 @@ extern "C" fvc_status fvc_tracer_launch(fvc_job* j, double t_start) {
   fvc_ctx* c = j->ctx;
   fvc_status st;
   if ((st = ready(c, true))) return st;
+  if (j->prec != c->prec) return fail(c, FVC_ERR_STATE, "the job was created with another precision form");
+  if ((st = mixed_ok(c))) return st;
   tracer_launch_vel(c->mesh, c->window, j->t, t_start, c->d_ctr, c->stream);
   if ((st = check_launch(c, "tracer launch"))) return st;
   j->stats.launches += 1;
@@ -855,6 +1035,8 @@ extern "C" fvc_status fvc_tracer_advance(fvc_job* j, double t1, double t2, long 
   fvc_status st;
   if ((st = ready(c, true))) return st;
   job_events(j);
+  if (j->prec != c->prec) return fail(c, FVC_ERR_STATE, "the job was created with another precision form");
+  if ((st = mixed_ok(c))) return st;
   if ((st = prepare_slots(c, t1, t2))) return st;
   compact_live(j->t.n, j->t.ldt, j->t.left, c->integ.extrapolate, j->t.live, nullptr, j->t.block_cnt, c->d_ctr,
                c->stream);
@@ -886,6 +1068,7 @@ extern "C" fvc_status fvc_tracer_snapshot(fvc_job* j, int always, double* X_out,
   if (X_out && cnt > 0)
     FVC_CUDA(c, cudaMemcpyAsync(X_out, j->t.outX, 24 * (size_t)cnt, cudaMemcpyDeviceToHost, c->stream));
   FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (X_out && j->packed) unpack_host(X_out, 3 * (size_t)cnt);
   return FVC_OK;
 }
 
@@ -902,6 +1085,7 @@ extern "C" fvc_status fvc_tracer_get_state(fvc_job* j, double* X, int* eid, int*
   if (left) FVC_CUDA(c, cudaMemcpyAsync(left, j->t.left, 4 * n, cudaMemcpyDeviceToHost, s));
   if (ldt) FVC_CUDA(c, cudaMemcpyAsync(ldt, j->t.ldt, 8 * n, cudaMemcpyDeviceToHost, s));
   FVC_CUDA(c, cudaStreamSynchronize(s));
+  if (X && j->packed) unpack_host(X, 3 * n);
   return FVC_OK;
 }
 
@@ -1001,6 +1185,7 @@ extern "C" fvc_status fvc_advect_noalloc(fvc_ctx* c, int n, double* X, double* V
                 "split the call or use fvc_advect", n, FVC_NOALLOC_MAX_POINTS);
   if (c->mesh.mesh_type == 1 && n > 0 && !eid) return fail(c, FVC_ERR_ARG, "unstructured advection needs element ids");
   if (c->integ.extrapolate && n > 0 && !V) return fail(c, FVC_ERR_ARG, "extrapolation needs V");
+  if (c->prec) return fail(c, FVC_ERR_ARG, "fvc_advect_noalloc runs the FP64 form only");
   if (steps) *steps = 0;
   if (n == 0) return FVC_OK;
   unsigned char* base = nullptr;

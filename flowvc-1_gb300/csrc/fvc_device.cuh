@@ -362,27 +362,32 @@ __device__ __forceinline__ int quick_hop(const DevMesh& m, int e, const PosF& P)
   }
 }
 
-__device__ __forceinline__ int neighbour(const DevMesh& m, int e, int slot) {
-  int4 nb = __ldg(m.elem + 2 * (long)e + 1);
+__device__ __forceinline__ int pick(int4 nb, int slot) {
   return slot == 0 ? nb.x : slot == 1 ? nb.y : slot == 2 ? nb.z : nb.w;
 }
+__device__ __forceinline__ int4 neighbours(const DevMesh& m, int e) { return __ldg(m.elem + 2 * (long)e + 1); }
+__device__ __forceinline__ int neighbour(const DevMesh& m, int e, int slot) { return pick(neighbours(m, e), slot); }
 
 // The reference's walk (GetVelocity_Unstructured's loop, ompVC/velocity.c:
 // 480-619, with vel_rule; Get_Element_Local_Search, ompVC/mesh.c:510-609,
 // without): hops the FP32 pre-check can decide are taken first, then the
 // FP64 solve decides at the element reached, so the lanes of a warp run the
-// expensive step together.  Returns 0 with the element's coordinates, 1 when
-// the walk leaves through a boundary face (eid = -1), or a fault bit.
+// expensive step together.  An element's neighbours are loaded together
+// with its records, so a hop costs one memory round trip.  Returns 0 with
+// the element's coordinates, 1 when the walk leaves through a boundary face
+// (eid = -1), or a fault bit.
 template <int DIMS>
 __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& eid, bool vel_rule, double& r,
                                     double& s, double& t, double& wv, double& d, int4& nd) {
   const PosF P = pos_f32(X);
+  int4 nb = neighbours(m, eid);
   for (int hop = 0; hop < m.max_hops;) {
     int qs;
     while (hop < m.max_hops && (qs = quick_hop<DIMS>(m, eid, P)) >= 0) {
-      eid = neighbour(m, eid, qs);
+      eid = pick(nb, qs);
       hop++;
       if (eid == -1) return 1;
+      nb = neighbours(m, eid);
     }
     if (hop >= m.max_hops) break;
     Geo<DIMS> g;
@@ -396,9 +401,10 @@ __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& ei
     else if (DIMS == 3 && fabs(t - d) < FVC_TINY) slot = 2;
     else if (fabs(wv - d) < FVC_TINY) slot = DIMS == 3 ? 3 : 2;
     else return PT_ERR_WALK;  // "Indeterminate neighbor"
-    eid = neighbour(m, eid, slot);
+    eid = pick(nb, slot);
     hop++;
     if (eid == -1) return 1;
+    nb = neighbours(m, eid);
   }
   return PT_ERR_WALK;
 }

@@ -13,6 +13,7 @@
 
 #include "fvc_device.cuh"
 #include "fvc_advect_impl.cuh"
+#include "fvc_mixed_impl.cuh"
 #include "fvc_ftle_math.cuh"
 #include "fvc_kernels.h"
 
@@ -930,7 +931,9 @@ void tracer_compact(const TracerDev& t, int always, DevCounters* ctr, cudaStream
 
 #define FVC_VARIANT(m, CALL)                                          \
   do {                                                                \
-    if ((m).mesh_type == 0) {                                         \
+    if ((m).prec) {                                                   \
+      if ((m).dims == 2) VariantMx<2>::CALL; else VariantMx<3>::CALL; \
+    } else if ((m).mesh_type == 0) {                                  \
       if ((m).dims == 2) Variant<2, 0>::CALL; else Variant<3, 0>::CALL; \
     } else {                                                          \
       if ((m).dims == 2) Variant<2, 1>::CALL; else Variant<3, 1>::CALL; \

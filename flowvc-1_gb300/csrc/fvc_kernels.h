@@ -69,6 +69,7 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
 // ---- FTLE slide
 struct FtleDev {
   int n, xr, yr, zr;
+  int mixed;             // 1: X, Xn and epos hold (X, c) float pairs (mixed-precision form)
   double dx, dy, dz;     // FTLE_CartMesh deltas
   double start;          // StartTime
   double* X;             // n x 3
@@ -144,6 +145,18 @@ void tracer_init_marks(const DevMesh& m, const TracerDev& t, const int* left0, i
 
 // Time-interpolated node velocities of every slot of w (unstructured meshes).
 void time_fields(const DevMesh& m, const DevWindow& w, double4_32a* vt, cudaStream_t s);
+
+// ---- mixed-precision form
+// Quantises one frame to 16 bits a component (fmt 1 BF16, 2 FP16) with a
+// per-component scale (max |component|, returned in scale); synchronises
+// the stream.  Returns 0 on success.
+int quantize_frame(const double4_32a* f, long n, int fmt, ushort4* q, unsigned* scratch, float scale[3],
+                   cudaStream_t s);
+// The window's two quantised frames interleaved per node (DevWindow::qp).
+void pair_frames(const ushort4* a, const ushort4* b, long n, uint4* out, cudaStream_t s);
+// FP64 values <-> (X, c) float pairs in place (X = RN(v), c = RN(X - v)).
+void pack_pairs(double* A, long n, cudaStream_t s);
+void unpack_pairs(double* A, long n, cudaStream_t s);
 
 // ---- utilities
 void outside_domain_flags(const DevMesh& m, int n, const double* X, int* left0, cudaStream_t s);

@@ -1,0 +1,306 @@
+// fvc_mixed.cuh -- the mixed-precision form of unstructured advection.
+//
+// Frames are read as 16-bit values (BF16 or FP16) times a per-frame,
+// per-component FP32 scale; point location, the barycentric weights, the
+// time interpolation and the Euler / RK4 stages run in FP32; positions are
+// FP32 with a Kahan compensation term (the position is X - c).  Within
+// FVC_NEAR_FACE of an element face (in natural coordinates) the containment
+// test and the walk's face choice are ompVC's FP64 ones
+// (ompVC/velocity.c:512-617, ompVC/mesh.c:542-609) on X - c.
+//
+// The step sequence of a call (stage times, step lengths, tloc) is the FP64
+// host sequence of the call in a device table (StepM), so the step loop
+// issues no FP64 instruction: GB300 runs FP64 at 1/64 of its FP32 rate.
+// A particle that leaves records the start time of the step it left in
+// (LeftDomainTime), a table time, which later calls use as an end time.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "fvc_device.cuh"
+
+namespace fvc {
+
+#define FVC_NEAR_FACE 1.0e-5f
+enum { QF_BF16 = 1, QF_FP16 = 2 };  // the FVC_PREC_* codes of fvc.h
+
+struct PtM {
+  float X[3];
+  float c[3];
+  int eid;
+  int left;
+  double ldt;
+};
+
+// In the mixed form a job's FP64 position arrays hold, in each 8-byte slot,
+// the float pair (X, c) of one coordinate.
+__device__ __forceinline__ void load_pos_pair(const double* A, long p, float X[3], float c[3]) {
+  const float2* q = reinterpret_cast<const float2*>(A + 3 * p);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float2 v = q[k];
+    X[k] = v.x;
+    c[k] = v.y;
+  }
+}
+__device__ __forceinline__ void store_pos_pair(double* A, long p, const float X[3], const float c[3]) {
+  float2* q = reinterpret_cast<float2*>(A + 3 * p);
+#pragma unroll
+  for (int k = 0; k < 3; k++) q[k] = make_float2(X[k], c[k]);
+}
+// FP64 value <-> pair: X = RN(v), c = RN(X - v); back: X - c
+__device__ __forceinline__ float2 split_pos(double v) {
+  float x = __double2float_rn(v);
+  return make_float2(x, __double2float_rn((double)x - v));
+}
+__device__ __forceinline__ double join_pos(float2 p) { return (double)p.x - (double)p.y; }
+
+__device__ __forceinline__ float dec16(unsigned short b, int fmt) {
+  return fmt == QF_BF16 ? __uint_as_float((unsigned)b << 16) : __half2float(__ushort_as_half(b));
+}
+
+// One node's velocity at tloc tl from the two quantised frames.
+__device__ __forceinline__ void node_vel_mx(const DevWindow& w, int node, float tl, float out[3]) {
+  const uint4 p = __ldg(w.qp + node);
+  const float ua = dec16((unsigned short)(p.x & 0xffffu), w.qfmt) * w.qs0[0];
+  const float va = dec16((unsigned short)(p.x >> 16), w.qfmt) * w.qs0[1];
+  const float wa = dec16((unsigned short)(p.y & 0xffffu), w.qfmt) * w.qs0[2];
+  const float ub = dec16((unsigned short)(p.y >> 16), w.qfmt) * w.qs1[0];
+  const float vb = dec16((unsigned short)(p.z & 0xffffu), w.qfmt) * w.qs1[1];
+  const float wb = dec16((unsigned short)(p.z >> 16), w.qfmt) * w.qs1[2];
+  out[0] = fmaf(tl, ub - ua, ua);
+  out[1] = fmaf(tl, vb - va, va);
+  out[2] = fmaf(tl, wb - wa, wa);
+}
+
+// FP32 natural coordinates of X in element e from its 64-byte FP32 record
+// (a11..a33, 1/V, x0, y0, z0 in 3D; a11..a22, 1/V, x0, y0 in 2D); returns
+// their minimum.
+template <int D>
+__device__ __forceinline__ float nat32(const DevMesh& m, int e, const float X[3], float& r, float& s, float& t,
+                                       float& wv) {
+  const float* q = m.geo32 + (long)e * 16;
+  if (D == 3) {
+    float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
+    float4 q2 = __ldg(reinterpret_cast<const float4*>(q + 8));
+    float z0 = __ldg(q + 12);
+    float dx = X[0] - q2.z, dy = X[1] - q2.w, dz = X[2] - z0;
+    r = fmaf(q0.x, dx, fmaf(q0.y, dy, q0.z * dz)) * q2.y;
+    s = fmaf(q0.w, dx, fmaf(q1.x, dy, q1.y * dz)) * q2.y;
+    t = fmaf(q1.z, dx, fmaf(q1.w, dy, q2.x * dz)) * q2.y;
+    wv = 1.0f - r - s - t;
+    return fminf(fminf(r, s), fminf(t, wv));
+  } else {
+    float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
+    float dx = X[0] - q1.y, dy = X[1] - q1.z;
+    r = fmaf(q0.x, dx, q0.y * dy) * q1.x;
+    s = fmaf(q0.z, dx, q0.w * dy) * q1.x;
+    t = 0.0f;
+    wv = 1.0f - r - s;
+    return fminf(fminf(r, s), wv);
+  }
+}
+
+// The walk of GetVelocity_Unstructured (vel_rule) / Get_Element_Local_Search
+// in the mixed form.  Returns 0 with the FP32 natural coordinates of the
+// element found, 1 when the walk leaves through a boundary face (eid = -1),
+// or PT_ERR_WALK.
+// ompVC's FP64 containment test of element e at X - C and, when it fails,
+// its face choice: returns -2 when the point is inside (coordinates in
+// r, s, t, wv), the face slot to step through, or -1 ("Indeterminate
+// neighbor").  Out of line so that none of its FP64 work is hoisted into
+// the FP32 walk.
+template <int D>
+__device__ __noinline__ int near_face_fp64(const DevMesh& m, int e, const float* X, const float* C, bool vel_rule,
+                                           float* out) {
+  const double x[3] = {(double)X[0] - (double)C[0], (double)X[1] - (double)C[1], (double)X[2] - (double)C[2]};
+  double R, S, T, W;
+  const double dd = natural<D>(m, e, x, R, S, T, W);
+  if (vel_rule ? ((dd + FVC_TINY) >= 0) : (dd > -FVC_TINY)) {
+    out[0] = (float)R;
+    out[1] = (float)S;
+    out[2] = (float)T;
+    out[3] = (float)W;
+    return -2;
+  }
+  if (fabs(R - dd) < FVC_TINY) return 0;
+  if (fabs(S - dd) < FVC_TINY) return 1;
+  if (D == 3 && fabs(T - dd) < FVC_TINY) return 2;
+  if (fabs(W - dd) < FVC_TINY) return D == 3 ? 3 : 2;
+  return -1;
+}
+
+template <int D>
+__device__ __forceinline__ int walk_mx(const DevMesh& m, const float X[3], const float C[3], int& eid, bool vel_rule,
+                                       float& r, float& s, float& t, float& wv) {
+  for (int hop = 0; hop < m.max_hops; hop++) {
+    const int4 nb = neighbours(m, eid);  // loaded beside the element's record
+    const float d = nat32<D>(m, eid, X, r, s, t, wv);
+    int slot;
+    if (d > FVC_NEAR_FACE) return 0;
+    if (d < -FVC_NEAR_FACE) {
+      // the face of the smallest coordinate, first in r, s, t, 1-r-s-t order
+      slot = (r == d) ? 0 : (s == d) ? 1 : (D == 3 && t == d) ? 2 : (D == 3 ? 3 : 2);
+    } else {
+      float c4[4];
+      slot = near_face_fp64<D>(m, eid, X, C, vel_rule, c4);
+      if (slot == -2) {
+        r = c4[0];
+        s = c4[1];
+        t = c4[2];
+        wv = c4[3];
+        return 0;
+      }
+      if (slot < 0) return PT_ERR_WALK;
+    }
+    eid = pick(nb, slot);
+    if (eid == -1) return 1;
+  }
+  return PT_ERR_WALK;
+}
+
+// The last locate's element and coordinates at the current position.
+struct NatM {
+  int e;
+  float r, s, t;
+};
+
+// Velocity at X (compensation C) and tloc tl: P1 in space, linear in time.
+template <int D>
+__device__ __forceinline__ int vel_mx(const DevMesh& m, const DevWindow& w, float tl, const float X[3],
+                                      const float C[3], int& eid, int& left, float out[3], const NatM* nc) {
+  if (eid < 0 || eid >= m.nelem) return PT_ERR_WALK;
+  float r, s, t, wv;
+  if (nc && nc->e == eid) {
+    r = nc->r;
+    s = nc->s;
+    t = nc->t;
+  } else {
+    const int st = walk_mx<D>(m, X, C, eid, true, r, s, t, wv);
+    if (st == 1) {
+      left = 1;
+      out[0] = out[1] = out[2] = 0.0f;
+      return 0;
+    }
+    if (st) return st;
+  }
+  const int4 nd = __ldg(m.elem + 2 * (long)eid);
+  float u0[3], u1[3], u2[3];
+  node_vel_mx(w, nd.x, tl, u0);
+  node_vel_mx(w, nd.y, tl, u1);
+  node_vel_mx(w, nd.z, tl, u2);
+  const float ar = fabsf(r), as = fabsf(s);
+  if (D == 3) {
+    float u3[3];
+    node_vel_mx(w, nd.w, tl, u3);
+    const float at = fabsf(t);
+#pragma unroll
+    for (int c = 0; c < 3; c++) out[c] = fmaf(u3[c] - u0[c], at, fmaf(u2[c] - u0[c], as, fmaf(u1[c] - u0[c], ar, u0[c])));
+  } else {
+#pragma unroll
+    for (int c = 0; c < 2; c++) out[c] = fmaf(u2[c] - u0[c], as, fmaf(u1[c] - u0[c], ar, u0[c]));
+    out[2] = 0.0f;
+  }
+  return 0;
+}
+
+template <int D>
+__device__ __forceinline__ int locate_mx(const DevMesh& m, const float X[3], const float C[3], int guess, int& err,
+                                         NatM* nc) {
+  nc->e = -1;
+  if (guess < 0) return -1;
+  if (guess >= m.nelem) {
+    err |= PT_ERR_WALK;
+    return -1;
+  }
+  float r, s, t, wv;
+  const int st = walk_mx<D>(m, X, C, guess, false, r, s, t, wv);
+  if (st == 1) return -1;
+  if (st) {
+    err |= st;
+    return -1;
+  }
+  nc->e = guess;
+  nc->r = r;
+  nc->s = s;
+  nc->t = t;
+  return guess;
+}
+
+// Positions += inc with Kahan compensation.
+__device__ __forceinline__ void kahan_add(float X[3], float c[3], const float inc[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float y = inc[k] - c[k];
+    const float t = X[k] + y;
+    c[k] = (t - X[k]) - y;
+    X[k] = t;
+  }
+}
+
+// Euler or RK4 over table steps [0, kend) (Advect, ompVC/integration.c:
+// 22-45, with RK4's stage hints and exit rules, integration.c:317-462).  A
+// particle that leaves keeps its position before the step and records the
+// step's start time as LeftDomainTime.
+template <int D>
+__device__ __forceinline__ void advect_mx(const DevMesh& m, const DevWindow& w, int type, PtM& p, int kend,
+                                          unsigned& steps, int& err) {
+  if (p.left) return;
+  const float zero[3] = {0.0f, 0.0f, 0.0f};
+  int e[4] = {p.eid, p.eid, p.eid, p.eid};
+  int l[4] = {0, 0, 0, 0};
+  NatM nc;
+  nc.e = -1;
+  for (int k = 0; k < kend; k++) {
+    const StepM st = w.steps[k];
+    const float h = st.h;
+    float inc[3];
+    if (type == 0) {
+      float v[3];
+      if ((err |= vel_mx<D>(m, w, st.tl0, p.X, p.c, e[0], l[0], v, &nc))) return;
+#pragma unroll
+      for (int q = 0; q < 3; q++) inc[q] = h * v[q];
+    } else {
+      float k1[3], k2[3], k3[3], k4[3], M[3];
+      if ((err |= vel_mx<D>(m, w, st.tl0, p.X, p.c, e[0], l[0], k1, &nc))) return;
+#pragma unroll
+      for (int q = 0; q < 3; q++) M[q] = fmaf(0.5f * h, k1[q], p.X[q]);
+      if ((err |= vel_mx<D>(m, w, st.tlh, M, zero, e[1], l[1], k2, nullptr))) return;
+#pragma unroll
+      for (int q = 0; q < 3; q++) M[q] = fmaf(0.5f * h, k2[q], p.X[q]);
+      if ((err |= vel_mx<D>(m, w, st.tlh, M, zero, e[2], l[2], k3, nullptr))) return;
+#pragma unroll
+      for (int q = 0; q < 3; q++) M[q] = fmaf(h, k3[q], p.X[q]);
+      if ((err |= vel_mx<D>(m, w, st.tl1, M, zero, e[3], l[3], k4, nullptr))) return;
+#pragma unroll
+      for (int q = 0; q < 3; q++) inc[q] = h * ((k1[q] + 2.0f * k2[q] + 2.0f * k3[q] + k4[q]) * (1.0f / 6.0f));
+    }
+    float X0[3] = {p.X[0], p.X[1], p.X[2]}, c0[3] = {p.c[0], p.c[1], p.c[2]};
+    kahan_add(p.X, p.c, inc);
+    p.eid = locate_mx<D>(m, p.X, p.c, p.eid, err, &nc);
+    if (err) return;
+    if (p.eid < 0 || l[0] || l[1] || l[2] || l[3]) {
+      p.left = 1;
+      p.ldt = st.tc;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        p.X[q] = X0[q];
+        p.c[q] = c0[q];
+      }
+      return;
+    }
+    steps++;
+  }
+}
+
+// The number of table steps from the call's start to tend, a table time
+// (the end of the call or a LeftDomainTime recorded in it); -1 if tend is
+// not one.  Compared bit for bit, with integer instructions.
+__device__ __forceinline__ int steps_to(const DevWindow& w, double tend) {
+  const long long b = __double_as_longlong(tend);
+  for (int k = 0; k <= w.nsteps; k++)
+    if (__double_as_longlong(w.steps[k].tc) == b) return k;
+  return -1;
+}
+
+}  // namespace fvc

@@ -23,6 +23,17 @@ struct DevMesh {
   // Data_MeshBounds
   double bounds[6];
   int max_hops;
+  int prec;  // arithmetic form: FVC_PREC_FP64 (ompVC's, bit-exact) or a mixed form
+};
+
+// One step of a call's step sequence for the mixed-precision form: the
+// step's start time (exact, as the FP64 host loop computes it), its length
+// and the tloc of its three stage times.  Entry nsteps holds the end time.
+struct StepM {
+  double tc;
+  float h;
+  float tl0, tlh, tl1;
+  float pad[3];
 };
 
 // Stage times of one advection call.  Every particle of a call starts at the
@@ -45,6 +56,15 @@ struct DevWindow {
   int nslots;
   double tq[FVC_MAX_SLOTS];  // slot times
   double tl[FVC_MAX_SLOTS];  // tloc of each slot, range-checked when the table is built
+  // mixed-precision form: the two frames quantised to 16 bits a component
+  // with a per-frame, per-component FP32 scale, interleaved per node in one
+  // 16-byte record (u0 v0 | w0 u1 | v1 w1 | -) so a stage reads one sector a
+  // node; and the call's step table
+  const uint4* qp;
+  float qs0[3], qs1[3];
+  int qfmt;  // FVC_PREC_BF16 or FVC_PREC_FP16
+  const StepM* steps;
+  int nsteps;
 };
 
 struct DevInteg {

@@ -60,11 +60,12 @@ def upload_frames(ctx: fvc.Context, ax: TimeAxis, frames):
         ctx.upload_frame(i, f)
 
 
-def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, lsc=1):
+def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, lsc=1, state=None):
     """One FTLE slide over its whole integration window, frames resident.
 
     grid = (xmin, xmax, ymin, ymax, zmin, zmax, xres, yres, zres).  Returns
-    (ftle_wT, ftle_woT, steps, job stats)."""
+    (ftle_wT, ftle_woT, steps, job stats); a dict passed as state receives
+    the slide's final point state (fvc_ftle_get_state)."""
     if ax.periodic:
         stop = t_start + direction * T
     else:
@@ -86,6 +87,8 @@ def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, 
             steps += job.interval(launch, t1, t2)
             if ((stop - tmax) if direction > 0 else (tmin - stop)) < TINY:
                 out = job.reduce(T)
+                if state is not None:
+                    state.update(job.get_state())
                 break
         df += direction
     st = job.stats()

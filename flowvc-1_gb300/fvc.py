@@ -15,6 +15,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "build", "libfvc.so")
 
+PREC_FP64, PREC_BF16, PREC_FP16 = 0, 1, 2
+PRECISIONS = {"fp64": PREC_FP64, "bf16": PREC_BF16, "fp16": PREC_FP16}
 FVC_OK, FVC_ERR_IO, FVC_ERR_ARG, FVC_ERR_OOM, FVC_ERR_WALK, FVC_ERR_TIMEOUT, FVC_ERR_CUDA, FVC_ERR_STATE, FVC_ERR_TLOC = range(9)
 STATUS_NAMES = {0: "FVC_OK", 1: "FVC_ERR_IO", 2: "FVC_ERR_ARG", 3: "FVC_ERR_OOM", 4: "FVC_ERR_WALK",
                 5: "FVC_ERR_TIMEOUT", 6: "FVC_ERR_CUDA", 7: "FVC_ERR_STATE", 8: "FVC_ERR_TLOC"}
@@ -59,6 +61,7 @@ SIGNATURES = {
     "fvc_set_integrator": (C.c_int, [_vp, C.c_int, C.c_double, C.c_int]),
     "fvc_upload_frame": (C.c_int, [_vp, C.c_int, _dp]),
     "fvc_set_window": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_double]),
+    "fvc_set_precision": (C.c_int, [_vp, C.c_int]),
     "fvc_advect": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_double, _llp]),
     "fvc_advect_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double, _llp]),
     "fvc_advect_noalloc": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_double, _llp]),
@@ -192,6 +195,13 @@ class Context:
 
     def set_window(self, lo, hi, tmin, tmax):
         self._chk(self.lib.fvc_set_window(self.h, lo, hi, tmin, tmax))
+
+    def set_precision(self, precision):
+        """PREC_FP64 (ompVC's arithmetic), PREC_BF16 or PREC_FP16 (mixed form);
+        also accepts the names "fp64", "bf16", "fp16"."""
+        if isinstance(precision, str):
+            precision = PRECISIONS[precision]
+        self._chk(self.lib.fvc_set_precision(self.h, precision))
 
     # ---- step level
     def advect(self, X, V, eid, left, ldt, t0, t1):

@@ -17,6 +17,7 @@
  *     must not overlap; separate contexts may be used from separate threads.
  *   - Arithmetic is IEEE FP64 in ompVC's operation order: element ids, exit
  *     flags and positions are bit-identical to ompVC built for x86-64.
+ *     fvc_set_precision selects the mixed-precision form instead.
  *   - Point arrays are n x 3 doubles (x, y, z interleaved), as in ompVC's
  *     LagrangianPoint.X.
  */
@@ -91,6 +92,21 @@ fvc_status fvc_upload_frame(fvc_ctx *ctx, int frame_id, const double *uvw);
 /* Select the two resident frames bracketing [tmin, tmax] (Data_LoadedTMin /
  * Data_LoadedTMax, ompVC/main.c:188-195); frame_lo is the frame at tmin. */
 fvc_status fvc_set_window(fvc_ctx *ctx, int frame_lo, int frame_hi, double tmin, double tmax);
+
+/* Arithmetic form.  ompVC has FP64 only; the mixed forms are this engine's
+ * own, for unstructured meshes with Euler or RK4 and no extrapolation:
+ *   FVC_PREC_FP64  (default) ompVC's FP64 arithmetic, bit-exact.
+ *   FVC_PREC_BF16  frames stored as BF16 (FVC_PREC_FP16: FP16) with one FP32
+ *                  scale per frame and component; point location,
+ *                  interpolation and the integrator's stages in FP32;
+ *                  positions accumulated in FP32 with Kahan compensation.
+ *                  Within 1e-5 of an element face the containment test is
+ *                  the FP64 one; the FTLE eigenvalue step stays FP64.
+ * Results differ from the FP64 form by the quantisation of the frames and
+ * FP32 rounding.  Set it before creating jobs; jobs keep the form they were
+ * created with. */
+enum { FVC_PREC_FP64 = 0, FVC_PREC_BF16 = 1, FVC_PREC_FP16 = 2 };
+fvc_status fvc_set_precision(fvc_ctx *ctx, int precision);
 
 /* ---- step level ------------------------------------------------------- */
 
