@@ -367,8 +367,16 @@ def run_engine(args, rank, world, local_rank):
     launches_main = sum(s["intervals"] for s in stats)
     peak, peak_kind = measured_peak()
     achieved = (steps_main * BYTES_PER_STEP) / (ms_main / 1000.0) / 1e9 if ms_main > 0 else 0.0
-    traffic_per_step, _ = profiled_traffic()
+    traffic_per_step, prof = profiled_traffic()
     traffic = traffic_per_step * steps_main / launches_main if traffic_per_step else None
+    # the bound that applies: FP64 issue (ops per step from the committed
+    # instruction-mix profile) against the FMA rate the probe measured
+    fp64_pipe = None
+    if prof and prof.get("fp64_pipe_ops_per_step") and fp64 and ms_main > 0:
+        ops = prof["fp64_pipe_ops_per_step"] * steps_main / (ms_main / 1000.0)
+        fp64_pipe = {"ops_per_step": prof["fp64_pipe_ops_per_step"], "achieved": ops / 1e9,
+                     "peak": fp64["fma_per_s"] / 1e9, "unit": "G FP64-pipe ops/s",
+                     "frac": ops / fp64["fma_per_s"], "kernel": "k_ftle_pass1"}
     gpu_launches = int(sum(s["launches"] for s in stats))
 
     # the mixed-precision forms on the same workload, against this FP64 run
@@ -429,6 +437,7 @@ def run_engine(args, rank, world, local_rank):
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "k_ftle_pass1", "bytes_per_step": BYTES_PER_STEP},
             "gpu_launches": gpu_launches,
+            "fp64_pipe": fp64_pipe,
             "precision_forms": forms,
             "phases_ms_per_step": {k: sum(s[k] for s in stats) / args.steps
                                    for k in ("ms_setup", "ms_main", "ms_early", "ms_reduce")},
