@@ -757,8 +757,9 @@ static fvc_status run_chain(fvc_ctx* c, const ChainArgs& a, const double* dX, co
     fvc_status st = finish(c, "seed location", nullptr);
     return st ? st : fail(c, FVC_ERR_CUDA, "seed location failed");
   }
-  // global search + first-found, then per round the guess kernels and the walk
-  *launches += 2 + (long long)rounds * (a.kind == 0 ? 6 : 4);
+  // the three-level FTLE chain (rounds == 0), or the global search +
+  // first-found and per round the guess kernels and the walk
+  *launches += rounds == 0 ? 3 : 2 + (long long)rounds * (a.kind == 0 ? 6 : 4);
   return FVC_OK;
 }
 

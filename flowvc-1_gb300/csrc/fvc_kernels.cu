@@ -511,6 +511,84 @@ __global__ void k_chain_eval(DevMesh m, ChainDev c, DevCounters* ctr) {
   }
 }
 
+// The FTLE chain (kind 0) with a centre element, solved in its own order in
+// three sequential levels instead of by rounds: ompVC's answer for a seed
+// depends on its guess only when the seed lies within TINY of a shared face,
+// and on such seeds (grid points on the cube's edges, for example) the
+// rounds of the fixed point advance one seed at a time.  Level 1 (one
+// thread) follows the planes: each plane starts from the first element found
+// in the previous plane (iguess).  Level 2 (a thread per plane) follows the
+// rows of a plane from the first element found in the previous row
+// (jguess).  Level 3 (a thread per row) walks the row from the last element
+// found.  Each level evaluates the seeds it needs with the guess the serial
+// loop would hold, so the answers are the serial loop's.
+
+// One seed with the given guess (ompVC/ftle.c:520-597): a walk from the
+// guess, then from the centre seed's element, then the global search when
+// LocalSearchChecking is set.
+template <int DIMS>
+__device__ __forceinline__ int chain_one(const DevMesh& m, const BucketGrid& g, const ChainDev& c, long p,
+                                         int guess, int& err) {
+  if (c.left0[p]) return -1;
+  const double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
+  int r = locate_walk<DIMS>(m, x, guess, err);
+  if (r < 0) r = locate_walk<DIMS>(m, x, c.seed, err);
+  if (r < 0 && c.lsc) r = global_find<DIMS>(m, g, x);
+  return r;
+}
+
+template <int DIMS>
+__global__ void k_chain3_planes(DevMesh m, BucketGrid g, ChainDev c, DevCounters* ctr) {
+  if (threadIdx.x || blockIdx.x) return;
+  int err = 0, G = c.init_guess;
+  const long plane = (long)c.res[1] * c.res[2];
+  for (int i = 0; i < c.nplanes; i++) {
+    c.planestart[i] = G;
+    // before the plane's first find every seed's guess is the plane start
+    for (long q = 0; q < plane; q++) {
+      const int r = chain_one<DIMS>(m, g, c, i * plane + q, G, err);
+      if (r >= 0) {
+        G = r;
+        break;
+      }
+    }
+  }
+  if (err) atomicOr(&ctr->status, err);
+}
+
+template <int DIMS>
+__global__ void k_chain3_rows(DevMesh m, BucketGrid g, ChainDev c, DevCounters* ctr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.nplanes) return;
+  int err = 0, G = c.planestart[i];
+  for (int j = 0; j < c.res[1]; j++) {
+    const long row = (long)i * c.res[1] + j;
+    c.rowstart[row] = G;
+    for (int k = 0; k < c.res[2]; k++) {
+      const int r = chain_one<DIMS>(m, g, c, row * c.res[2] + k, G, err);
+      if (r >= 0) {
+        G = r;
+        break;
+      }
+    }
+  }
+  if (err) atomicOr(&ctr->status, err);
+}
+
+template <int DIMS>
+__global__ void k_chain3_points(DevMesh m, BucketGrid g, ChainDev c, int* eid, DevCounters* ctr) {
+  const long row = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= c.nrows) return;
+  int err = 0, cur = c.rowstart[row];
+  for (int k = 0; k < c.res[2]; k++) {
+    const long p = row * c.res[2] + k;
+    const int r = chain_one<DIMS>(m, g, c, p, cur, err);
+    eid[p] = r;
+    if (r >= 0) cur = r;
+  }
+  if (err) atomicOr(&ctr->status, err);
+}
+
 __global__ void k_first_found(int n, const int* left0, const int* R0, int* out) {
   long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p < n && !left0[p] && R0[p] >= 0) atomicMin(out, (int)p);
@@ -546,6 +624,24 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
   c.chunk_carry = w; w += c.nchunks + 1;
   int* d_first = w; w += 1;
   c.R0 = R0;
+  if (a.kind == 0 && a.center_eid >= 0) {
+    c.seed = a.center_eid;
+    c.pstar = -1;
+    c.init_guess = a.center_eid;
+    if (m.dims == 3) {
+      k_chain3_planes<3><<<1, 32, 0, s>>>(m, g, c, ctr);
+      k_chain3_rows<3><<<nblk(c.nplanes, 32), 32, 0, s>>>(m, g, c, ctr);
+      k_chain3_points<3><<<nblk(c.nrows, 64), 64, 0, s>>>(m, g, c, eid, ctr);
+    } else {
+      k_chain3_planes<2><<<1, 32, 0, s>>>(m, g, c, ctr);
+      k_chain3_rows<2><<<nblk(c.nplanes, 32), 32, 0, s>>>(m, g, c, ctr);
+      k_chain3_points<2><<<nblk(c.nrows, 64), 64, 0, s>>>(m, g, c, eid, ctr);
+    }
+    int status = 0;
+    cudaMemcpyAsync(&status, &ctr->status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess || status) return -1;
+    return 0;
+  }
   launch_global_search(m, g, n, X, left0, R0, s);
   // first seed found by the global search: the chain's start when no centre
   // element is known (and always for a tracer list)
