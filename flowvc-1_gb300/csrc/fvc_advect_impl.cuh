@@ -203,21 +203,65 @@ __device__ __forceinline__ int eid_at_trigger(const FtleDev& f, long pp, long tr
   return (pp < trig && (f.flag[pp] & 1) && !(f.flag[pp] & 2)) ? f.en[pp] : f.eid[pp];
 }
 
-// Appends (s, c) to the task list; the lanes of a warp land next to each other.
-__device__ __forceinline__ void append_task(const FtleDev& f, DevCounters* ctr, bool want, int s, int c) {
-  unsigned b = __ballot_sync(0xffffffffu, want);
-  if (!b) return;
-  int lane = threadIdx.x & 31, base = 0;
-  if (lane == 0) base = atomicAdd(&ctr->ntask, __popc(b));
+// The length bucket of an advection from t1 to tend: its number of steps,
+// capped at 7.  Only a sort key: advections of one bucket run together so a
+// warp's lanes finish their step loops at about the same time.
+__device__ __forceinline__ int length_bucket(double t1, double tend, double inv_h) {
+  const double k = fabs(tend - t1) * inv_h + 0.5;
+  return k < 7.0 ? (int)k : 7;
+}
+
+// Appends (s, c) with its bucket to the task list (the lanes of a warp land
+// next to each other) and counts it in its bucket.
+__device__ __forceinline__ void append_task(const FtleDev& f, DevCounters* ctr, bool want, int s, int c, int b) {
+  const unsigned m = __ballot_sync(0xffffffffu, want);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(&ctr->ntask, __popc(m));
   base = __shfl_sync(0xffffffffu, base, 0);
-  if (want) f.tasks[base + __popc(b & ((1u << lane) - 1u))] = make_int2(s, c);
+  if (want) f.tasks[base + __popc(m & ((1u << lane) - 1u))] = make_int2(s, c | (b << 3));
+  const unsigned peers = __match_any_sync(0xffffffffu, want ? b : -1);
+  if (want && lane == __ffs(peers) - 1) atomicAdd(&ctr->hist[b], __popc(peers));
+}
+
+// Groups the task list by bucket into f.tsorted (order within a bucket
+// follows the warps' arrival, roughly the served points' grid order).
+template <int D>
+__global__ void k_task_sort(FtleDev f, DevCounters* ctr) {
+  __shared__ int off[8];
+  if (threadIdx.x == 0) {
+    int a = 0;
+    for (int b = 0; b < 8; b++) {
+      off[b] = a;
+      a += ((volatile int*)ctr->hist)[b];
+    }
+  }
+  __syncthreads();
+  const long ntask = *(volatile int*)&ctr->ntask;
+  const int lane = threadIdx.x & 31;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long base = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < ntask; base += stride) {
+    const long i = base + lane;
+    const bool ok = i < ntask;
+    const int2 t = ok ? f.tasks[i] : make_int2(0, 0);
+    const int b = ok ? (t.y >> 3) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    if (ok) {
+      const int leader = __ffs(peers) - 1;
+      int pos = 0;
+      if (lane == leader) pos = atomicAdd(&ctr->scat[b], __popc(peers));
+      pos = __shfl_sync(peers, pos, leader);
+      f.tsorted[off[b] + pos + __popc(peers & ((1u << lane) - 1u))] = t;
+    }
+  }
 }
 
 // A: queue the neighbours that exist; boundary slots keep te as exit time.
 // The queue kernels walk their items warp by warp (grid-stride, uniform per
 // warp) so append_task's ballot always sees the whole warp.
 template <int D>
-__global__ void k_ftle_queue_nb(FtleDev f, DevCounters* ctr) {
+__global__ void k_ftle_queue_nb(FtleDev f, DevCounters* ctr, double t1, double inv_h) {
   const long nserved = *(volatile int*)&ctr->count;
   const long total = 6 * nserved, stride = (long)gridDim.x * blockDim.x;
   for (long base = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
@@ -225,20 +269,23 @@ __global__ void k_ftle_queue_nb(FtleDev f, DevCounters* ctr) {
     long s = idx / 6;
     int c = (int)(idx % 6);
     bool want = false;
+    int b = 0;
     if (s < nserved) {
       long nb[6];
       int i, j, k;
       served_geometry(f, f.served[s], nb, i, j, k);
       want = nb[c] >= 0;
-      if (!want) f.elt[s * 6 + c] = f.te[f.trig[s]];
+      const double te = f.te[f.trig[s]];
+      if (!want) f.elt[s * 6 + c] = te;
+      b = length_bucket(t1, te, inv_h);
     }
-    append_task(f, ctr, want, (int)s, c);
+    append_task(f, ctr, want, (int)s, c, b);
   }
 }
 
 // B + C queue: MinExitTime, then q itself and (if it moved) the neighbours.
 template <int D>
-__global__ void k_ftle_queue_self(FtleDev f, DevCounters* ctr) {
+__global__ void k_ftle_queue_self(FtleDev f, DevCounters* ctr, double t1, double inv_h) {
   const long nserved = *(volatile int*)&ctr->count;
   const long total = 7 * nserved, stride = (long)gridDim.x * blockDim.x;
   for (long base = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
@@ -246,10 +293,12 @@ __global__ void k_ftle_queue_self(FtleDev f, DevCounters* ctr) {
   long s = idx / 7;
   int c = (int)(idx % 7);
   bool want = false;
+  int b = 0;
   if (s < nserved) {
     double te = f.te[f.trig[s]];
     const double* lt = f.elt + s * 6;
     double mt = dmin(te, dmin(lt[5], dmin(lt[4], dmin(lt[3], dmin(lt[2], dmin(lt[1], lt[0]))))));
+    b = length_bucket(t1, mt, inv_h);
     if (c == 6) {
       f.emt[s] = mt;
       want = true;
@@ -260,7 +309,7 @@ __global__ void k_ftle_queue_self(FtleDev f, DevCounters* ctr) {
       want = nb[c] >= 0;
     }
   }
-  append_task(f, ctr, want, (int)s, c);
+  append_task(f, ctr, want, (int)s, c, b);
   }
 }
 
@@ -276,9 +325,9 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_tasks(DevMesh m, De
   for (long base = warp_grab(cursor); base < ntask; base = warp_grab(cursor)) {
     const long idx = base + (threadIdx.x & 31);
     if (idx >= ntask) continue;
-    int2 tk = f.tasks[idx];
+    int2 tk = f.tsorted[idx];
     long s = tk.x;
-    int c = tk.y;
+    int c = tk.y & 7;
     long q = f.served[s], trig = f.trig[s];
     long nb[6];
     int i, j, k;
@@ -426,11 +475,15 @@ struct Variant {
     static const unsigned res_self = resident_blocks(k_ftle_queue_self<D>, 256);
     static const unsigned res_tasks = resident_blocks(k_ftle_tasks<D, M>, 128);
     static const unsigned res_final = resident_blocks(k_ftle_early_final<D>, 128);
-    cudaMemsetAsync(&ctr->ntask, 0, sizeof(int), s);
-    k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, ctr);
+    static const unsigned res_sort = resident_blocks(k_task_sort<D>, 256);
+    const double inv_h = 1.0 / fabs(in.h);
+    cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
+    k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, ctr, t1, inv_h);
+    k_task_sort<D><<<capped(6L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
     k_ftle_tasks<D, M><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 0, ctr);
-    cudaMemsetAsync(&ctr->ntask, 0, sizeof(int), s);
-    k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, ctr);
+    cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
+    k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, ctr, t1, inv_h);
+    k_task_sort<D><<<capped(7L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
     k_ftle_tasks<D, M><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
   }

@@ -812,7 +812,7 @@ extern "C" fvc_status fvc_ftle_create(fvc_ctx* c, const fvc_ftle_spec* sp, fvc_j
               {(void**)&f.Xn, 24 * n}, {(void**)&f.Vn, 24 * n}, {(void**)&f.te, 8 * n}, {(void**)&f.en, 4 * n},
               {(void**)&f.flag, n}, {(void**)&f.served, 4 * n}, {(void**)&f.trig, 4 * n}, {(void**)&f.out, 16 * n},
               {(void**)&f.epos, 168 * n}, {(void**)&f.elt, 48 * n}, {(void**)&f.emt, 8 * n},
-              {(void**)&f.tasks, 56 * n}, {(void**)&f.live, 4 * n},
+              {(void**)&f.tasks, 56 * n}, {(void**)&f.tsorted, 56 * n}, {(void**)&f.live, 4 * n},
               {(void**)&f.block_cnt, sizeof(int) * (2 * (n / 1024 + 1) + 16) + sizeof(long long) * (n / 1048576 + 8)},
               {(void**)&left0, 4 * n}});
   if (st) {
@@ -930,7 +930,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   DevCounters h{};
   st = finish(c, "ftle interval", steps, &h);
   j->stats.intervals++;
-  j->stats.launches += (launch ? 1 : 0) + 4 + 1 + (c->integ.extrapolate ? 0 : 6) + 1 + (c->mesh.mesh_type == 1 ? 1 : 0);
+  j->stats.launches += (launch ? 1 : 0) + 4 + 1 + (c->integ.extrapolate ? 0 : 8) + 1 + (c->mesh.mesh_type == 1 && !c->prec ? 1 : 0);
   j->stats.steps_main += (long long)h.steps;
   j->stats.steps_early += (long long)h.steps_early;
   j->stats.ms_main += ev_ms(j->ev[0], j->ev[1]);

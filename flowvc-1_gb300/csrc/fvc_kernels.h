@@ -17,10 +17,14 @@ struct DevCounters {
   int changed;
   int count;   // points served an early FTLE this interval
   int nlive;   // live points of the current advection call
-  int ntask;   // early-FTLE advections queued
+  int ntask;    // early-FTLE advections queued
+  int hist[8];  // queued advections per length bucket (steps, capped at 7)
+  int scat[8];  // fill cursors of the buckets in the sorted list
   int pad;
-  int cur[4];  // work cursors of the persistent launches: 0 live list, 1-2 task lists
+  int cur[4];   // work cursors of the persistent launches: 0 live list, 1-2 task lists
 };
+// ntask, hist and scat are cleared together before each task list
+#define FVC_TASK_COUNTERS_BYTES (17 * sizeof(int))
 
 // ---- mesh preprocessing
 void launch_geometry(const DevMesh& m, double* geom, float* geo32, cudaStream_t s);
@@ -91,7 +95,8 @@ struct FtleDev {
   double* epos;          // early FTLE: 7 positions (6 neighbours, self) per served point
   double* elt;           // early FTLE: the neighbours' exit times
   double* emt;           // early FTLE: MinExitTime
-  int2* tasks;           // early FTLE: queued advections (served index, 0-5 neighbour / 6 self)
+  int2* tasks;           // early FTLE: queued advections (served index, 0-5 neighbour / 6 self | bucket << 3)
+  int2* tsorted;         // the same, grouped by length bucket
   int* live;             // points advected this interval, in grid order
   int* block_cnt;        // compaction scratch
   double* out;           // 2 x n, output order

@@ -112,9 +112,9 @@ __global__ void __launch_bounds__(128) k_ftle_tasks_mx(DevMesh m, DevWindow w, i
   for (long base = warp_grab(cursor); base < ntask; base = warp_grab(cursor)) {
     const long idx = base + (threadIdx.x & 31);
     if (idx >= ntask) continue;
-    const int2 tk = f.tasks[idx];
+    const int2 tk = f.tsorted[idx];
     const long s = tk.x;
-    const int c = tk.y;
+    const int c = tk.y & 7;
     const long q = f.served[s], trig = f.trig[s];
     long nb[6];
     int i, j, k;
@@ -211,11 +211,15 @@ struct VariantMx {
     static const unsigned res_self = resident_blocks(k_ftle_queue_self<D>, 256);
     static const unsigned res_tasks = resident_blocks(k_ftle_tasks_mx<D>, 128);
     static const unsigned res_final = resident_blocks(k_ftle_early_final<D>, 128);
-    cudaMemsetAsync(&ctr->ntask, 0, sizeof(int), s);
-    k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, ctr);
+    static const unsigned res_sort = resident_blocks(k_task_sort<D>, 256);
+    const double inv_h = 1.0 / fabs(in.h);
+    cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
+    k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, ctr, t1, inv_h);
+    k_task_sort<D><<<capped(6L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
     k_ftle_tasks_mx<D><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, f, 0, ctr);
-    cudaMemsetAsync(&ctr->ntask, 0, sizeof(int), s);
-    k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, ctr);
+    cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
+    k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, ctr, t1, inv_h);
+    k_task_sort<D><<<capped(7L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
     k_ftle_tasks_mx<D><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, f, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
   }
