@@ -132,9 +132,12 @@ __device__ __noinline__ int near_face_fp64(const DevMesh& m, int e, const float*
 
 template <int D>
 __device__ __forceinline__ int walk_mx(const DevMesh& m, const float X[3], const float C[3], int& eid, bool vel_rule,
-                                       float& r, float& s, float& t, float& wv) {
+                                       float& r, float& s, float& t, float& wv, int4& nd) {
   for (int hop = 0; hop < m.max_hops; hop++) {
-    const int4 nb = neighbours(m, eid);  // loaded beside the element's record
+    // the element's node ids and neighbours (one 32-byte sector), loaded
+    // beside its record
+    nd = __ldg(m.elem + 2 * (long)eid);
+    const int4 nb = __ldg(m.elem + 2 * (long)eid + 1);
     const float d = nat32<D>(m, eid, X, r, s, t, wv);
     int slot;
     if (d > FVC_NEAR_FACE) return 0;
@@ -162,6 +165,7 @@ __device__ __forceinline__ int walk_mx(const DevMesh& m, const float X[3], const
 // The last locate's element and coordinates at the current position.
 struct NatM {
   int e;
+  int4 nd;
   float r, s, t;
 };
 
@@ -171,12 +175,14 @@ __device__ __forceinline__ int vel_mx(const DevMesh& m, const DevWindow& w, floa
                                       const float C[3], int& eid, int& left, float out[3], const NatM* nc) {
   if (eid < 0 || eid >= m.nelem) return PT_ERR_WALK;
   float r, s, t, wv;
+  int4 nd;
   if (nc && nc->e == eid) {
+    nd = nc->nd;
     r = nc->r;
     s = nc->s;
     t = nc->t;
   } else {
-    const int st = walk_mx<D>(m, X, C, eid, true, r, s, t, wv);
+    const int st = walk_mx<D>(m, X, C, eid, true, r, s, t, wv, nd);
     if (st == 1) {
       left = 1;
       out[0] = out[1] = out[2] = 0.0f;
@@ -184,7 +190,6 @@ __device__ __forceinline__ int vel_mx(const DevMesh& m, const DevWindow& w, floa
     }
     if (st) return st;
   }
-  const int4 nd = __ldg(m.elem + 2 * (long)eid);
   float u0[3], u1[3], u2[3];
   node_vel_mx(w, nd.x, tl, u0);
   node_vel_mx(w, nd.y, tl, u1);
@@ -214,13 +219,15 @@ __device__ __forceinline__ int locate_mx(const DevMesh& m, const float X[3], con
     return -1;
   }
   float r, s, t, wv;
-  const int st = walk_mx<D>(m, X, C, guess, false, r, s, t, wv);
+  int4 nd;
+  const int st = walk_mx<D>(m, X, C, guess, false, r, s, t, wv, nd);
   if (st == 1) return -1;
   if (st) {
     err |= st;
     return -1;
   }
   nc->e = guess;
+  nc->nd = nd;
   nc->r = r;
   nc->s = s;
   nc->t = t;

@@ -205,22 +205,24 @@ struct VariantMx {
     static const unsigned res = resident_blocks(k_ftle_pass1_mx<D>, 128);
     k_ftle_pass1_mx<D><<<capped(f.n, 128, res), 128, 0, s>>>(m, w, in.type, f, ctr);
   }
+  // The mixed form runs the task lists in queue order: its advections are
+  // bound by gather latency, and grid order keeps a warp's points close
+  // together, which pays more here than grouping them by length.
   static void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f, double t1,
                          DevCounters* ctr, cudaStream_t s) {
     static const unsigned res_nb = resident_blocks(k_ftle_queue_nb<D>, 256);
     static const unsigned res_self = resident_blocks(k_ftle_queue_self<D>, 256);
     static const unsigned res_tasks = resident_blocks(k_ftle_tasks_mx<D>, 128);
     static const unsigned res_final = resident_blocks(k_ftle_early_final<D>, 128);
-    static const unsigned res_sort = resident_blocks(k_task_sort<D>, 256);
     const double inv_h = 1.0 / fabs(in.h);
+    FtleDev g = f;
+    g.tsorted = g.tasks;
     cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
     k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, ctr, t1, inv_h);
-    k_task_sort<D><<<capped(6L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
-    k_ftle_tasks_mx<D><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, f, 0, ctr);
+    k_ftle_tasks_mx<D><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, g, 0, ctr);
     cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
     k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, ctr, t1, inv_h);
-    k_task_sort<D><<<capped(7L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
-    k_ftle_tasks_mx<D><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, f, 1, ctr);
+    k_ftle_tasks_mx<D><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, g, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
   }
   static void tracer_launch(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq, DevCounters* ctr,
