@@ -22,7 +22,7 @@ struct fvc_ctx {
   cudaStream_t stream = nullptr;
   DevMesh mesh{};
   bool mesh_set = false;
-  DevInteg integ{1, 0.01, 0};
+  DevInteg integ{1, 0.01, 0, 0.0, 0.0, 0.0};
   bool integ_set = false;
   DevWindow window{};
   bool window_set = false;
@@ -374,11 +374,21 @@ extern "C" fvc_status fvc_set_bounds(fvc_ctx* c, const double b[6]) {
   return FVC_OK;
 }
 
+extern "C" fvc_status fvc_set_rkf(fvc_ctx* c, double accuracy, double min_step, double max_step) {
+  if (!c) return FVC_ERR_ARG;
+  if (!(accuracy >= 1.0e-10) || !(min_step >= 1.0e-10) || !(max_step >= 1.0e-10))
+    return fail(c, FVC_ERR_ARG, "RKF integration parameters must be positive");
+  c->integ.acc = accuracy;
+  c->integ.hmin = min_step;
+  c->integ.hmax = max_step;
+  return FVC_OK;
+}
+
 extern "C" fvc_status fvc_set_integrator(fvc_ctx* c, int int_type, double h, int extrapolate) {
   if (!c) return FVC_ERR_ARG;
-  if (int_type != 0 && int_type != 1 && int_type != 3)
-    return fail(c, FVC_ERR_ARG, "Int_Type %d not supported (0 Euler, 1 RK4, 3 AB2)", int_type);
-  if (!(h > 0)) return fail(c, FVC_ERR_ARG, "Int_TimeStep must be positive");
+  if (int_type < 0 || int_type > 3)
+    return fail(c, FVC_ERR_ARG, "Int_Type %d not supported (0 Euler, 1 RK4, 2 RKF, 3 AB2)", int_type);
+  if (!(h > 0) && int_type != 2) return fail(c, FVC_ERR_ARG, "Int_TimeStep must be positive");
   c->integ.type = int_type;
   c->integ.h = h;
   c->integ.extrapolate = extrapolate ? 1 : 0;
@@ -461,8 +471,11 @@ extern "C" fvc_status fvc_set_precision(fvc_ctx* c, int precision) {
   return FVC_OK;
 }
 
-// The mixed form runs Euler and RK4 without extrapolation.
+// RKF needs its parameters; the mixed form runs Euler and RK4 without
+// extrapolation.
 static fvc_status mixed_ok(fvc_ctx* c) {
+  if (c->integ.type == 2 && !(c->integ.acc > 0 && c->integ.hmin > 0 && c->integ.hmax > 0))
+    return fail(c, FVC_ERR_ARG, "Int_Type 2 (RKF) needs fvc_set_rkf before advecting");
   if (!c->prec) return FVC_OK;
   if (c->integ.type != 0 && c->integ.type != 1)
     return fail(c, FVC_ERR_ARG, "the mixed-precision form runs Euler (0) and RK4 (1), not Int_Type %d", c->integ.type);
@@ -479,6 +492,7 @@ extern "C" fvc_status fvc_set_window(fvc_ctx* c, int lo, int hi, double tmin, do
   c->window.f1 = b->second;
   c->window.tmin = tmin;
   c->window.tmax = tmax;
+  c->window.rspan = rcp_for_div(tmax - tmin);
   c->window.nslots = 0;
   c->window.nsteps = 0;
   c->window_set = true;
@@ -1187,6 +1201,7 @@ extern "C" fvc_status fvc_advect_noalloc(fvc_ctx* c, int n, double* X, double* V
   if (c->mesh.mesh_type == 1 && n > 0 && !eid) return fail(c, FVC_ERR_ARG, "unstructured advection needs element ids");
   if (c->integ.extrapolate && n > 0 && !V) return fail(c, FVC_ERR_ARG, "extrapolation needs V");
   if (c->prec) return fail(c, FVC_ERR_ARG, "fvc_advect_noalloc runs the FP64 form only");
+  if ((st = mixed_ok(c))) return st;
   if (steps) *steps = 0;
   if (n == 0) return FVC_OK;
   unsigned char* base = nullptr;

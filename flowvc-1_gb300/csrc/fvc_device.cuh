@@ -23,8 +23,10 @@ namespace fvc {
 
 #define FVC_TINY 1.0e-10
 
-// RN(1/6), for the RK4 update's division by 6 through div_rn
+// RN(1/6) and RN(1/13), for the RK4 update's division by 6 and RKF's stage
+// time 12h/13 through div_rn
 constexpr double kRcp6 = 1.0 / 6.0;
+constexpr double kRcp13 = 1.0 / 13.0;
 
 struct Pt {
   double X[3];
@@ -85,7 +87,7 @@ __device__ __forceinline__ int get_tloc(const DevWindow& w, int slot, double tq,
     tloc = w.tl[slot];
     return 0;
   }
-  tloc = (tq - w.tmin) / (w.tmax - w.tmin);
+  tloc = div_rn(tq - w.tmin, w.tmax - w.tmin, w.rspan);
   if ((tloc > 1 + FVC_TINY) || (tloc < 0 - FVC_TINY)) return PT_ERR_TLOC;
   return 0;
 }
@@ -419,7 +421,7 @@ __device__ __forceinline__ int vel_unstruct(const DevMesh& m, const DevWindow& w
   const bool tab = slot_hit(w, tslot, tq);
   double tloc = 0.0;
   if (!tab) {
-    tloc = (tq - w.tmin) / (w.tmax - w.tmin);
+    tloc = div_rn(tq - w.tmin, w.tmax - w.tmin, w.rspan);
     if ((tloc > 1 + FVC_TINY) || (tloc < 0 - FVC_TINY)) return PT_ERR_TLOC;
   }
   double r, s, t, wv, d;
@@ -684,6 +686,107 @@ __device__ __noinline__ double ab2(const DevMesh& m, const DevWindow& w, const D
 
 // Advect, ompVC/integration.c:22-45 (Int_Type 0 Euler, 1 RK4, 3 AB2).
 // Euler and AB2 are called out of line so that kernels inline only RK4.
+// RKF, ompVC/integration.c:464-699: Runge-Kutta-Fehlberg 4(5) with the
+// reference's coefficients, error estimate and step-size control, per
+// particle.  The stage points keep their element hints and exit flags across
+// steps (MP1 .. MP6); a stage outside the domain stops the point at tc
+// without moving it.  Stage times vary per particle, so the stages
+// interpolate the two frames in time themselves.  The step-size factor is
+// the reference's pow(x, 0.25), computed correctly rounded (rn_root4): the
+// accept / reject test makes the trajectory depend on its last bit.
+template <int DIMS, int MESH>
+__device__ __noinline__ double rkf(const DevMesh& m, const DevWindow& w, const DevInteg& in, Pt& p,
+                                   double tstart, double tend, unsigned& steps, int& err) {
+  double k[6][3], M[3];
+  int e[6], l[6];
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    e[j] = p.eid;
+    l[j] = p.left;
+  }
+  const double a3 = 3.0 / 32.0, b3 = 9.0 / 32.0;
+  const double a4 = 1932.0 / 2197.0, b4 = -7200.0 / 2197.0, c4 = 7296.0 / 2197.0;
+  const double a5 = 439.0 / 216.0, b5 = -8.0, c5 = 3680.0 / 513.0, d5 = -845.0 / 4104.0;
+  const double a6 = -8.0 / 27.0, b6 = 2.0, c6 = -3544.0 / 2565.0, d6 = 1859.0 / 4104.0, e6 = -11.0 / 40.0;
+  const double a7 = 1.0 / 360.0, b7 = -128.0 / 4275.0, c7 = -2197.0 / 75240.0, d7 = 1.0 / 50.0, e7 = 2.0 / 55.0;
+  const double a8 = 25.0 / 216.0, b8 = 1408.0 / 2565.0, c8 = 2197.0 / 4104.0, d8 = -1.0 / 5.0;
+  double h = dsign(in.hmax, tend - tstart), tc = tstart, ts, ss;
+  // the reference loops until tc reaches tend; a cap on the attempts bounds
+  // the kernel when Int_MinTimeStep is tiny against the interval
+  for (int attempt = 0; (tc - tend) * (tend - tstart) < 0.0; attempt++) {
+    if (attempt >= (1 << 24)) {
+      err |= PT_ERR_WALK;
+      return tend;
+    }
+    if ((tc + h - tend) * (tc + h - tstart) > 0.0) h = dsign(tend - tc, tend - tstart);
+#pragma unroll
+    for (int q = 0; q < 3; q++) M[q] = p.X[q];
+    if ((err |= velocity<DIMS, MESH>(m, w, tc, -1, M, e[0], l[0], k[0]))) return tend;
+#pragma unroll
+    for (int q = 0; q < 3; q++) M[q] = p.X[q] + 0.25 * k[0][q] * h;
+    ts = tc + 0.25 * h;
+    if ((err |= velocity<DIMS, MESH>(m, w, ts, -1, M, e[1], l[1], k[1]))) return tend;
+#pragma unroll
+    for (int q = 0; q < 3; q++) M[q] = p.X[q] + (a3 * k[0][q] + b3 * k[1][q]) * h;
+    ts = tc + 0.375 * h;
+    if ((err |= velocity<DIMS, MESH>(m, w, ts, -1, M, e[2], l[2], k[2]))) return tend;
+#pragma unroll
+    for (int q = 0; q < 3; q++) M[q] = p.X[q] + (a4 * k[0][q] + b4 * k[1][q] + c4 * k[2][q]) * h;
+    ts = tc + div_rn(12.0 * h, 13.0, kRcp13);
+    if ((err |= velocity<DIMS, MESH>(m, w, ts, -1, M, e[3], l[3], k[3]))) return tend;
+#pragma unroll
+    for (int q = 0; q < 3; q++) M[q] = p.X[q] + (a5 * k[0][q] + b5 * k[1][q] + c5 * k[2][q] + d5 * k[3][q]) * h;
+    ts = tc + h;
+    if ((err |= velocity<DIMS, MESH>(m, w, ts, -1, M, e[4], l[4], k[4]))) return tend;
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+      M[q] = p.X[q] + (a6 * k[0][q] + b6 * k[1][q] + c6 * k[2][q] + d6 * k[3][q] + e6 * k[4][q]) * h;
+    ts = tc + 0.5 * h;
+    if ((err |= velocity<DIMS, MESH>(m, w, ts, -1, M, e[5], l[5], k[5]))) return tend;
+    if (l[0] || l[1] || l[2] || l[3] || l[4] || l[5]) {
+      p.left = 1;
+      p.ldt = tc;
+      return p.ldt;
+    }
+    double ex[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+      ex[q] = fabs(a7 * k[0][q] + b7 * k[2][q] + c7 * k[3][q] + d7 * k[4][q] + e7 * k[5][q]);
+    const double er = fmax(fmax(ex[0], ex[1]), ex[2]);
+    if (er == 0.0) ss = 0.0;
+    else ss = rn_root4(fabs((in.acc * h) / (2 * er)));
+    if (er < in.acc || fabs(h) <= in.hmin) {
+#pragma unroll
+      for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + (a8 * k[0][q] + b8 * k[2][q] + c8 * k[3][q] + d8 * k[4][q]) * h;
+      tc = tc + h;
+      if (MESH == 1) p.eid = locate_walk<DIMS>(m, p.X, p.eid, err);
+      if (err) return tend;
+      if ((MESH == 0 && outside_domain(m, p.X)) || (MESH == 1 && p.eid < 0)) {
+        p.left = 1;
+        p.ldt = tc - h;
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+          p.X[q] = p.X[q] - (a8 * k[0][q] + b8 * k[2][q] + c8 * k[3][q] + d8 * k[4][q]) * h;
+        return p.ldt;
+      }
+      steps++;
+      if (in.extrapolate && (err |= velocity_cold<DIMS, MESH>(m, w, tc, -1, p.X, &p.eid, &p.left, p.V)))
+        return tend;
+      if (fabs(h) > in.hmin && ss > 1.0) {
+        ss = (ss > 4.0) ? 4.0 : ss;
+        h = dsign((fabs(ss * h) > in.hmax) ? in.hmax : ss * h, tend - tstart);
+      }
+    } else {
+      if (ss < 1.0) {
+        ss = (ss < 0.1) ? 0.1 : ss;
+        h = dsign((fabs(ss * h) < in.hmin) ? in.hmin : ss * h, tend - tstart);
+      } else
+        h = dsign((fabs(0.5 * h) < in.hmin) ? in.hmin : 0.5 * h, tend - tstart);
+    }
+  }
+  return tend;
+}
+
 template <int DIMS, int MESH>
 __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, const DevInteg& in,
                                       Pt& p, double tstart, double tend, unsigned& steps) {
@@ -697,6 +800,7 @@ __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, cons
   if (MESH == 1 && p.eid < 0) return PT_ERR_STATE;
   double stop;
   if (in.type == 1) stop = rk4<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
+  else if (in.type == 2) stop = rkf<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
   else if (in.type == 3) stop = ab2<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
   else stop = euler<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
   if (!err && (fabs(stop - tend) > FVC_TINY) && in.extrapolate) {

@@ -29,6 +29,25 @@ __device__ __forceinline__ double div_rn(double a, double b, double y) {
   return fma(r, y, q);
 }
 
+// x^(1/4) rounded to nearest, for RKF's step-size factor (the reference
+// calls pow(x, 0.25), which glibc rounds correctly but for inputs within
+// about 0.02 ulp of a rounding boundary).  y = sqrt(sqrt(x)) is within about
+// an ulp; its residual y^4 - x is formed with error-free products
+// (Dekker's TwoProduct by FMA: y*y = P + p, P*P = Q + q exactly, and Q - x
+// exact by Sterbenz's lemma since Q is within a few ulps of x), and one
+// Newton step t = y - (y^4 - x) / (4 y^3) lands within about 2^-104 of the
+// root, so the final subtraction rounds to RN(x^(1/4)) unless the root lies
+// within that distance of a rounding boundary.  Inputs outside
+// 2^-960 .. 2^960 (where the products could over- or underflow) use pow.
+__device__ __forceinline__ double rn_root4(double x) {
+  if (!(x >= 0x1p-960 && x <= 0x1p960)) return pow(x, 0.25);
+  const double y = sqrt(sqrt(x));
+  const double P = y * y, p = fma(y, y, -P);
+  const double Q = P * P, q = fma(P, P, -Q);
+  const double r = (Q - x) + (q + (2.0 * P * p + p * p));
+  return y - r / (4.0 * y * P);
+}
+
 // The reciprocal div_rn wants for divisor b, or 0 when b is outside
 // 2^-400 .. 2^400 in magnitude (then div_rn divides).
 __host__ __device__ __forceinline__ double rcp_for_div(double b) {

@@ -51,6 +51,7 @@ struct DevWindow {
   const double4_32a* f0;  // frame at tmin, (u, v, w, 0) per node
   const double4_32a* f1;  // frame at tmax
   double tmin, tmax;
+  double rspan;           // reciprocal of tmax - tmin for div_rn (0: divide)
   const double4_32a* vt;  // nslots x vt_stride time-interpolated node velocities
   long vt_stride;
   int nslots;
@@ -68,9 +69,10 @@ struct DevWindow {
 };
 
 struct DevInteg {
-  int type;  // 0 Euler, 1 RK4, 3 AB2
+  int type;  // 0 Euler, 1 RK4, 2 RKF, 3 AB2
   double h;  // Int_TimeStep
   int extrapolate;
+  double acc, hmin, hmax;  // Int_Accuracy, Int_MinTimeStep, Int_MaxTimeStep (RKF)
 };
 
 }  // namespace fvc

@@ -62,6 +62,7 @@ SIGNATURES = {
     "fvc_upload_frame": (C.c_int, [_vp, C.c_int, _dp]),
     "fvc_set_window": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_double]),
     "fvc_set_precision": (C.c_int, [_vp, C.c_int]),
+    "fvc_set_rkf": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double]),
     "fvc_advect": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_double, _llp]),
     "fvc_advect_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double, _llp]),
     "fvc_advect_noalloc": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_double, _llp]),
@@ -188,6 +189,10 @@ class Context:
 
     def set_integrator(self, int_type, h, extrapolate=0):
         self._chk(self.lib.fvc_set_integrator(self.h, int_type, h, extrapolate))
+
+    def set_rkf(self, accuracy, min_step, max_step):
+        """Int_Accuracy, Int_MinTimeStep, Int_MaxTimeStep for Int_Type 2."""
+        self._chk(self.lib.fvc_set_rkf(self.h, accuracy, min_step, max_step))
 
     def upload_frame(self, frame_id, uvw):
         uvw = f64(uvw)

@@ -110,7 +110,7 @@ static void fix_path(char *s)
 
 /* CheckParameters (ompVC/parameters.c:432-567) and SetDerivedParameters
  * (ompVC/parameters.c:294-430).  Options outside the engine's scope
- * (RKF, inertial particles, staggered release, side analyses) are refused. */
+ * (inertial particles, staggered release, side analyses) are refused. */
 int fvcp_check_derive(fvcp_params *p, char *err, int errlen)
 {
     if (p->dims != 2 && p->dims != 3) return perr(err, errlen, "Dimensions must be equal to 2 or 3");
@@ -123,9 +123,10 @@ int fvcp_check_derive(fvcp_params *p, char *err, int errlen)
     if (p->bounds[4] > p->bounds[5]) return perr(err, errlen, "Data_MeshBounds.ZMin > Data_MeshBounds.ZMax");
     if (p->out_tres < 1) return perr(err, errlen, "Output_TRes < 1");
     if (p->out_tdelta < P_TINY && p->out_tres > 1) return perr(err, errlen, "Output_TDelta must be positive");
-    if (p->int_type == 2) return perr(err, errlen, "Int_Type = 2 (Runge-Kutta-Fehlberg) is not supported");
-    if (p->int_type != 0 && p->int_type != 1 && p->int_type != 3) p->int_type = 0; /* as Advect's fallback */
-    if (p->int_h < P_TINY) return perr(err, errlen, "Int_TimeStep must be positive");
+    if (p->int_type < 0 || p->int_type > 3) p->int_type = 0; /* as Advect's fallback */
+    if (p->int_h < P_TINY && p->int_type != 2) return perr(err, errlen, "Int_TimeStep must be positive");
+    if ((p->int_hmin < P_TINY || p->int_hmax < P_TINY || p->int_acc < P_TINY) && p->int_type == 2)
+        return perr(err, errlen, "RKF integration parameters must be positive");
     if (p->int_dir != 1 && p->int_dir != -1) return perr(err, errlen, "Unsupported Int_TimeDirection value, must be -1 or 1");
     if (p->p_radius > P_TINY) return perr(err, errlen, "Particle_Radius > 0 (inertial particles) is not supported");
     if (p->normal_flow) return perr(err, errlen, "Int_NormalFlow is not supported");

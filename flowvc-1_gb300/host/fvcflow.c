@@ -9,7 +9,7 @@
  * Differences from ompVC, by design:
  *   - every velocity frame the run needs is uploaded once and stays resident
  *     in device memory; no per-interval temporary files are written;
- *   - out-of-scope options (RKF, inertial particles, staggered release, CET /
+ *   - out-of-scope options (inertial particles, staggered release, CET /
  *     residence-time / activation-potential analyses, velocity resampling)
  *     are refused with an error instead of being computed;
  *   - errors return a non-zero exit status with a message instead of
@@ -551,6 +551,8 @@ int main(int argc, char **argv)
     memcpy(bounds, R.P.bounds, sizeof(bounds));
     if ((rc = fvc_set_bounds(R.ctx, bounds)) || (rc = fvc_set_integrator(R.ctx, R.P.int_type, R.P.int_h, R.P.extrapolate)))
         return die("settings", R.ctx, rc);
+    if (R.P.int_type == 2 && (rc = fvc_set_rkf(R.ctx, R.P.int_acc, R.P.int_hmin, R.P.int_hmax)))
+        return die("RKF settings", R.ctx, rc);
     int bad = load_mesh(&R);
     if (!bad) bad = R.P.ftle_compute ? run_ftle(&R) : run_tracers(&R);
     if (!bad && stats)

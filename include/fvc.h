@@ -77,10 +77,15 @@ fvc_status fvc_set_unstruct_mesh(fvc_ctx *ctx, int nnodes, const double *xyz, in
  * ompVC/velocity.c:654-669). */
 fvc_status fvc_set_bounds(fvc_ctx *ctx, const double bounds[6]);
 
-/* Int_Type (0 Euler, 1 RK4, 3 two-step Adams-Bashforth), Int_TimeStep and
- * Int_Extrapolate; replaces the globals Advect reads
- * (ompVC/integration.c:22-45). */
+/* Int_Type (0 Euler, 1 RK4, 2 Runge-Kutta-Fehlberg, 3 two-step
+ * Adams-Bashforth), Int_TimeStep and Int_Extrapolate; replaces the globals
+ * Advect reads (ompVC/integration.c:22-45). */
 fvc_status fvc_set_integrator(fvc_ctx *ctx, int int_type, double h, int extrapolate);
+
+/* Int_Accuracy, Int_MinTimeStep and Int_MaxTimeStep of RKF (ompVC/
+ * integration.c:464-699, checked as CheckParameters does,
+ * ompVC/parameters.c:462-463); required before advecting with Int_Type 2. */
+fvc_status fvc_set_rkf(fvc_ctx *ctx, double accuracy, double min_step, double max_step);
 
 /* Velocity frames.  uvw is one frame as stored in a <prefix>_vel.<n>.bin file
  * after its time stamp: (u, v, w) per node, Cartesian nodes in k, j, i order

@@ -37,6 +37,8 @@ int orc_set_bounds(orc_ctx *c, const double b[6]);
  * in file order (interleaved u,v,w per node, Cartesian k,j,i i fastest). */
 int orc_set_frames(orc_ctx *c, const double *uvw0, const double *uvw1, double tmin, double tmax);
 int orc_set_integrator(orc_ctx *c, int int_type, double h, int extrapolate);
+/* Int_Accuracy, Int_MinTimeStep, Int_MaxTimeStep of RKF (Int_Type 2) */
+int orc_set_rkf(orc_ctx *c, double accuracy, double min_step, double max_step);
 
 /* Advect n points from t0 to t1 in place (ompVC Advect, integration.c:22-45).
  * X is n x 3, V n x 3 (extrapolation velocity), eid/left per point, ldt the

@@ -84,10 +84,19 @@ int orc_set_frames(orc_ctx *c, const double *uvw0, const double *uvw1, double tm
 
 int orc_set_integrator(orc_ctx *c, int int_type, double h, int extrapolate)
 {
-    if (!c || (int_type != 0 && int_type != 1 && int_type != 3) || !(h > 0)) return ORC_ERR_ARG;
+    if (!c || (int_type < 0 || int_type > 3) || !(h > 0)) return ORC_ERR_ARG;
     c->int_type = int_type;
     c->h = h;
     c->extrapolate = extrapolate;
+    return ORC_OK;
+}
+
+int orc_set_rkf(orc_ctx *c, double accuracy, double min_step, double max_step)
+{
+    if (!c || !(accuracy > 0) || !(min_step > 0) || !(max_step > 0)) return ORC_ERR_ARG;
+    c->acc = accuracy;
+    c->hmin = min_step;
+    c->hmax = max_step;
     return ORC_OK;
 }
 

@@ -382,6 +382,89 @@ static double ab2(const orc_ctx *c, orc_pt *p, double tstart, double tend, long 
 }
 
 /* Advect, ompVC/integration.c:22-45 */
+/* RKF, ompVC/integration.c:464-699: Runge-Kutta-Fehlberg 4(5) with the
+ * reference's coefficients, error estimate and step-size control; the
+ * stage points keep their element hints and exit flags across steps (MP1 ..
+ * MP6).  A stage outside the domain stops the point at tc without moving
+ * it. */
+static double rkf(const orc_ctx *c, orc_pt *p, double tstart, double tend, long long *steps, int *err)
+{
+    double k[6][3], M[3];
+    int e[6], l[6];
+    for (int j = 0; j < 6; j++) {
+        e[j] = p->eid;
+        l[j] = p->left;
+    }
+    const double a3 = 3.0 / 32.0, b3 = 9.0 / 32.0;
+    const double a4 = 1932.0 / 2197.0, b4 = -7200.0 / 2197.0, c4 = 7296.0 / 2197.0;
+    const double a5 = 439.0 / 216.0, b5 = -8.0, c5 = 3680.0 / 513.0, d5 = -845.0 / 4104.0;
+    const double a6 = -8.0 / 27.0, b6 = 2.0, c6 = -3544.0 / 2565.0, d6 = 1859.0 / 4104.0, e6 = -11.0 / 40.0;
+    const double a7 = 1.0 / 360.0, b7 = -128.0 / 4275.0, c7 = -2197.0 / 75240.0, d7 = 1.0 / 50.0, e7 = 2.0 / 55.0;
+    const double a8 = 25.0 / 216.0, b8 = 1408.0 / 2565.0, c8 = 2197.0 / 4104.0, d8 = -1.0 / 5.0;
+    double h = ORC_SIGN(c->hmax, tend - tstart), hmax = c->hmax, tol = c->acc, tc = tstart, ts, ss;
+    int unst = c->mesh_type == 1;
+    while ((tc - tend) * (tend - tstart) < 0.0) {
+        if ((tc + h - tend) * (tc + h - tstart) > 0.0) h = ORC_SIGN(tend - tc, tend - tstart);
+        for (int q = 0; q < 3; q++) M[q] = p->X[q];
+        if ((*err |= orc_vel(c, tc, M, &e[0], &l[0], k[0]))) return tend;
+        for (int q = 0; q < 3; q++) M[q] = p->X[q] + 0.25 * k[0][q] * h;
+        ts = tc + 0.25 * h;
+        if ((*err |= orc_vel(c, ts, M, &e[1], &l[1], k[1]))) return tend;
+        for (int q = 0; q < 3; q++) M[q] = p->X[q] + (a3 * k[0][q] + b3 * k[1][q]) * h;
+        ts = tc + 0.375 * h;
+        if ((*err |= orc_vel(c, ts, M, &e[2], &l[2], k[2]))) return tend;
+        for (int q = 0; q < 3; q++) M[q] = p->X[q] + (a4 * k[0][q] + b4 * k[1][q] + c4 * k[2][q]) * h;
+        ts = tc + (12.0 * h) / 13.0;
+        if ((*err |= orc_vel(c, ts, M, &e[3], &l[3], k[3]))) return tend;
+        for (int q = 0; q < 3; q++)
+            M[q] = p->X[q] + (a5 * k[0][q] + b5 * k[1][q] + c5 * k[2][q] + d5 * k[3][q]) * h;
+        ts = tc + h;
+        if ((*err |= orc_vel(c, ts, M, &e[4], &l[4], k[4]))) return tend;
+        for (int q = 0; q < 3; q++)
+            M[q] = p->X[q] + (a6 * k[0][q] + b6 * k[1][q] + c6 * k[2][q] + d6 * k[3][q] + e6 * k[4][q]) * h;
+        ts = tc + 0.5 * h;
+        if ((*err |= orc_vel(c, ts, M, &e[5], &l[5], k[5]))) return tend;
+        if (l[0] || l[1] || l[2] || l[3] || l[4] || l[5]) {
+            p->left = 1;
+            p->ldt = tc;
+            return p->ldt;
+        }
+        double ex[3];
+        for (int q = 0; q < 3; q++)
+            ex[q] = fabs(a7 * k[0][q] + b7 * k[2][q] + c7 * k[3][q] + d7 * k[4][q] + e7 * k[5][q]);
+        double er = fmax(fmax(ex[0], ex[1]), ex[2]);
+        if (er == 0.0) ss = 0.0;
+        else ss = pow(fabs((tol * h) / (2 * er)), 0.25);
+        if (er < tol || fabs(h) <= c->hmin) {
+            for (int q = 0; q < 3; q++)
+                p->X[q] = p->X[q] + (a8 * k[0][q] + b8 * k[2][q] + c8 * k[3][q] + d8 * k[4][q]) * h;
+            tc = tc + h;
+            if (unst) p->eid = orc_local(c, p->X, p->eid, err);
+            if (*err) return tend;
+            if ((!unst && orc_outside_domain(c, p->X)) || (unst && p->eid < 0)) {
+                p->left = 1;
+                p->ldt = tc - h;
+                for (int q = 0; q < 3; q++)
+                    p->X[q] = p->X[q] - (a8 * k[0][q] + b8 * k[2][q] + c8 * k[3][q] + d8 * k[4][q]) * h;
+                return p->ldt;
+            }
+            (*steps)++;
+            if (c->extrapolate && (*err |= orc_vel(c, tc, p->X, &p->eid, &p->left, p->V))) return tend;
+            if (fabs(h) > c->hmin && ss > 1.0) {
+                ss = (ss > 4.0) ? 4.0 : ss;
+                h = ORC_SIGN((fabs(ss * h) > hmax) ? hmax : ss * h, tend - tstart);
+            }
+        } else {
+            if (ss < 1.0) {
+                ss = (ss < 0.1) ? 0.1 : ss;
+                h = ORC_SIGN((fabs(ss * h) < c->hmin) ? c->hmin : ss * h, tend - tstart);
+            } else
+                h = ORC_SIGN((fabs(0.5 * h) < c->hmin) ? c->hmin : 0.5 * h, tend - tstart);
+        }
+    }
+    return tend;
+}
+
 int orc_advect_pt(const orc_ctx *c, orc_pt *p, double tstart, double tend, long long *steps)
 {
     int err = 0;
@@ -393,6 +476,7 @@ int orc_advect_pt(const orc_ctx *c, orc_pt *p, double tstart, double tend, long 
     if (c->mesh_type == 1 && p->eid < 0) return ORC_PT_ERR_WALK;
     double stop;
     if (c->int_type == 1) stop = rk4(c, p, tstart, tend, steps, &err);
+    else if (c->int_type == 2) stop = rkf(c, p, tstart, tend, steps, &err);
     else if (c->int_type == 3) stop = ab2(c, p, tstart, tend, steps, &err);
     else stop = euler(c, p, tstart, tend, steps, &err);
     if (!err && (fabs(stop - tend) > ORC_TINY) && c->extrapolate)

@@ -27,9 +27,10 @@ struct orc_ctx {
     double bounds[6];           /* Data_MeshBounds */
     const double *f0, *f1;      /* velocity slots 0 and 1, file order */
     double tmin, tmax;          /* Data_LoadedTMin / TMax */
-    int int_type;               /* 0 Euler, 1 RK4, 3 Adams-Bashforth 2 */
+    int int_type;               /* 0 Euler, 1 RK4, 2 RKF, 3 Adams-Bashforth 2 */
     double h;
     int extrapolate;
+    double acc, hmin, hmax;     /* Int_Accuracy, Int_MinTimeStep, Int_MaxTimeStep (RKF) */
 };
 
 /* One Lagrangian point as the integrators see it (the fields of

@@ -120,8 +120,11 @@ static int load_mesh(orc_run_state *S, char *err, int errlen)
     c->dims = P->dims;
     c->mesh_type = P->mesh_type;
     memcpy(c->bounds, P->bounds, sizeof(c->bounds));
-    c->int_type = P->int_type == 1 ? 1 : (P->int_type == 3 ? 3 : 0);
+    c->int_type = (P->int_type >= 1 && P->int_type <= 3) ? P->int_type : 0;
     c->h = P->int_h;
+    c->acc = P->int_acc;
+    c->hmin = P->int_hmin;
+    c->hmax = P->int_hmax;
     c->extrapolate = P->extrapolate;
     if (P->mesh_type == 0) {
         snprintf(path, sizeof(path), "%s%s_Cartesian.bin", P->path_data, P->prefix);

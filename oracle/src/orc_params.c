@@ -123,7 +123,8 @@ int orc_check_derive(orc_params *p, char *err, int errlen)
     if (p->out_tdelta < ORC_TINY && p->out_tres > 1) return fail(err, errlen, "Output_TDelta must be positive");
     if (p->int_h < ORC_TINY && p->int_type != 2) return fail(err, errlen, "Int_TimeStep must be positive");
     if (p->int_dir != 1 && p->int_dir != -1) return fail(err, errlen, "Unsupported Int_TimeDirection value, must be -1 or 1");
-    if (p->int_type == 2) return fail(err, errlen, "Int_Type 2 (RKF) is not supported by this engine");
+    if ((p->int_hmin < ORC_TINY || p->int_hmax < ORC_TINY || p->int_acc < ORC_TINY) && p->int_type == 2)
+        return fail(err, errlen, "RKF integration parameters must be positive");
     if (p->p_radius > ORC_TINY) return fail(err, errlen, "finite-size particles (Particle_Radius > 0) are not supported");
     if (p->normal_flow) return fail(err, errlen, "Int_NormalFlow is not supported");
     if (p->ftle_compute && p->tr_compute)

@@ -1,7 +1,8 @@
-// Checks the FP64-pipe savers of fvc_fpmath.cuh against CUDA's own IEEE
-// operations on the GPU: div_rn(a, b, rcp_for_div(b)) must equal a / b bit
-// for bit, and f32_trunc(x) must equal __double2float_rz(x), on many seeded
-// operands from several distributions.  Prints one line of counts.
+// Checks the helpers of fvc_fpmath.cuh on the GPU: div_rn(a, b,
+// rcp_for_div(b)) must equal CUDA's IEEE a / b bit for bit, and f32_trunc(x)
+// must equal __double2float_rz(x), on many seeded operands from several
+// distributions (one line of counts on stdout).  With a file argument it
+// also writes seeded (x, rn_root4(x)) pairs there for the host to check.
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
@@ -61,6 +62,16 @@ __global__ void k_div(uint64_t seed, long n, Out* o) {
   if (__float_as_uint(fw) != __float_as_uint(fg)) atomicAdd(&o->bad_cvt, 1ull);
 }
 
+__global__ void k_root4(uint64_t seed, long n, double* out) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t h = mix(seed ^ (uint64_t)i);
+  // RKF's factor |tol h / (2 err)| spans a few decades around 1; also wide
+  double x = (i & 1) ? fabs(rnd(h, -40, 40)) : fabs(rnd(h, -900, 900));
+  out[2 * i] = x;
+  out[2 * i + 1] = rn_root4(x);
+}
+
 int main(int argc, char** argv) {
   long n = argc > 1 ? atol(argv[1]) : (1L << 26);
   int reps = argc > 2 ? atoi(argv[2]) : 4;
@@ -74,5 +85,18 @@ int main(int argc, char** argv) {
   printf("{\"n_div\": %llu, \"bad_div\": %llu, \"n_cvt\": %llu, \"bad_cvt\": %llu, \"first_bad\": [%.17g, %.17g, %d]}\n",
          h.n_div, h.bad_div, h.n_cvt, h.bad_cvt, h.a, h.b, h.kind);
   cudaFree(d);
+  if (argc > 3) {
+    const long nr = 1L << 18;
+    double* dr = nullptr;
+    if (cudaMalloc(&dr, 16 * nr) != cudaSuccess) return 4;
+    k_root4<<<(unsigned)(nr / 256), 256>>>(0xabcdefull, nr, dr);
+    double* hr = (double*)malloc(16 * nr);
+    if (!hr || cudaMemcpy(hr, dr, 16 * nr, cudaMemcpyDeviceToHost) != cudaSuccess) return 5;
+    FILE* f = fopen(argv[3], "wb");
+    if (!f || fwrite(hr, 16, nr, f) != (size_t)nr) return 6;
+    fclose(f);
+    free(hr);
+    cudaFree(dr);
+  }
   return 0;
 }

@@ -67,6 +67,11 @@ def cases():
         "ftle_euler": dict(FTLE, FTLE_IntTLength=0.6, Int_TimeStep=0.01, Int_Type=0, **fb(0, 2, 0, 1, 0, 0, 25, 13, 1)),
         "tracer_list": dict(TRACE, Trace_InFile="seeds2d.bin", Trace_InFileFormat=4, Output_TRes=6, Output_TDelta=0.15,
                             Trace_IntTLength=0.8, Int_TimeStep=0.01),
+        "ftle_rkf": dict(FTLE, FTLE_IntTLength=0.8, Int_Type=2, Int_Accuracy=1e-6, Int_MinTimeStep=1e-4,
+                         Int_MaxTimeStep=0.05, **fb(0, 2, 0, 1, 0, 0, 25, 13, 1)),
+        "tracer_rkf": dict(TRACE, Trace_InFile="seeds2d.bin", Trace_InFileFormat=4, Output_TRes=6, Output_TDelta=0.15,
+                           Trace_IntTLength=0.8, Int_Type=2, Int_Accuracy=1e-7, Int_MinTimeStep=1e-4,
+                           Int_MaxTimeStep=0.04),
     }))
 
     def dgp(d):  # one full period of the double gyre (period 10): periodic data
@@ -112,6 +117,11 @@ def cases():
                             **tb(0.0, 1.0, 0.05, 0.95, 0.1, 0.9, 6, 5, 4)),
         "tracer_always": dict(TRACE, Trace_InFile="seeds.bin", Trace_InFileFormat=4, Output_TRes=4, Output_TDelta=0.06,
                               Trace_IntTLength=0.2, Int_TimeStep=0.005, Trace_AlwaysOutput=1),
+        "tracer_rkf": dict(TRACE, Trace_InFile="seeds.bin", Trace_InFileFormat=4, Output_TRes=6, Output_TDelta=0.03,
+                           Trace_IntTLength=0.2, Int_Type=2, Int_Accuracy=1e-7, Int_MinTimeStep=1e-4,
+                           Int_MaxTimeStep=0.01),
+        "ftle_rkf": dict(FTLE, FTLE_IntTLength=0.12, Int_Type=2, Int_Accuracy=1e-6, Int_MinTimeStep=1e-4,
+                         Int_MaxTimeStep=0.01, **fb(0, 1, 0, 1, 0, 1, 8, 7, 6)),
     }))
 
     def c3(d):

@@ -31,6 +31,7 @@ def lib():
         L.orc_set_bounds.argtypes = [C.c_void_p, _dp]
         L.orc_set_frames.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_double]
         L.orc_set_integrator.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int]
+        L.orc_set_rkf.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
         L.orc_advect.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_double,
                                  C.POINTER(C.c_longlong)]
         L.orc_velocity.argtypes = [C.c_void_p, C.c_int, _dp, _ip, _ip, C.c_double, _dp]
@@ -83,6 +84,9 @@ class Oracle:
 
     def set_integrator(self, t, h, ex=0):
         assert self.L.orc_set_integrator(self.h, t, h, ex) == 0
+
+    def set_rkf(self, acc, hmin, hmax):
+        assert self.L.orc_set_rkf(self.h, acc, hmin, hmax) == 0
 
     def advect(self, X, V, eid, left, ldt, t0, t1):
         steps = C.c_longlong(0)

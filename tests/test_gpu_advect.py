@@ -140,3 +140,56 @@ def test_searches_bit_exact(engine, kind):
     assert np.array_equal(o.global_search(P), g.global_search(P))
     guess = rng.integers(0, F["conn"].shape[0], len(P)).astype(np.int32)
     assert np.array_equal(o.local_search(P, guess), g.local_search(P, guess))
+
+
+@pytest.mark.parametrize("kind", ["cart2", "cart3", "tri", "tet"])
+@pytest.mark.parametrize("direction", [1, -1])
+def test_rkf_matches_oracle(engine, kind, direction):
+    """RKF (Int_Type 2, ompVC/integration.c:464-699) against the oracle's
+    restatement: element ids, exit flags and step counts identical, positions
+    and exit times within 1e-12 (the step-size factor is pow(x, 0.25), whose
+    last bit may differ between CUDA and the host's libm)."""
+    F = make_field(kind, seed=3)
+    rng = np.random.default_rng(zlib.crc32(f"rkf{kind}{direction}".encode()))
+    o, g = setup_pair(F, 2, 0.01, 0)
+    for x in (o, g):
+        x.set_rkf(1e-6, 1e-4, 0.02)
+    P = seeds(F, 2000, rng)
+    n = len(P)
+    left = np.zeros(n, np.int32)
+    if F["mesh"] == 1:
+        eid = o.global_search(P)
+        left[eid < 0] = 1
+    else:
+        eid = np.full(n, -1, np.int32)
+        left[(P[:, :F["dims"]] < np.array(F["lo"][:F["dims"]])).any(1) | (P[:, :F["dims"]] > np.array(F["hi"][:F["dims"]])).any(1)] = 1
+    t0, t1 = (0.3, 0.3877) if direction > 0 else (0.4, 0.3123)
+    a = [P.copy(), np.zeros_like(P), eid.copy(), left.copy(), np.zeros(n)]
+    b = [P.copy(), np.zeros_like(P), eid.copy(), left.copy(), np.zeros(n)]
+    sa = o.advect(*a, t0, t1)
+    sb = g.advect(*b, t0, t1)
+    assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])
+    assert sa == sb > 0
+    np.testing.assert_allclose(b[0], a[0], rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(b[4], a[4], rtol=1e-12, atol=1e-13)
+    # how many positions are bit-identical is reported, not required
+    print(kind, direction, "bit-identical positions:", np.mean(np.all(a[0] == b[0], axis=1)))
+
+
+def test_rkf_needs_its_parameters(engine):
+    F = make_field("tet", seed=4)
+    g = fvc.Context(3, 1)
+    g.set_unstruct_mesh(F["xyz"], F["conn"], F["adj"])
+    g.set_bounds(F["bounds"])
+    g.upload_frame(0, F["frames"][0])
+    g.upload_frame(1, F["frames"][1])
+    g.set_window(0, 1, 0.3, 0.4)
+    g.set_integrator(2, 0.0, 0)
+    P = np.full((4, 3), 0.5)
+    eid = g.global_search(P)
+    with pytest.raises(fvc.FvcError) as e:
+        g.advect(P, None, eid, np.zeros(4, np.int32), np.zeros(4), 0.3, 0.35)
+    assert e.value.status == fvc.FVC_ERR_ARG
+    with pytest.raises(fvc.FvcError):
+        g.set_rkf(0.0, 1e-4, 0.01)
+    g.close()

@@ -12,7 +12,7 @@ def _run(engine, path):
 
 
 @pytest.mark.parametrize("over,msg", [
-    (dict(Int_Type=2), "Runge-Kutta-Fehlberg"),
+    (dict(Int_Type=2, Int_Accuracy=0.0), "RKF integration parameters must be positive"),
     (dict(Particle_Radius=0.1), "inertial"),
     (dict(Trace_Compute=1, FTLE_Compute=1), "concurrently"),
     (dict(Int_TimeDirection=2), "Int_TimeDirection"),
