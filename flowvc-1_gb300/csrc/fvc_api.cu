@@ -57,6 +57,10 @@ struct fvc_ctx {
   StepM* d_steps = nullptr;
   size_t steps_cap = 0;
   int window_lo = -1, window_hi = -1;
+  // exposure time (Trace_CETCompute): per-element sums shared by all releases
+  double* d_cet_sum = nullptr;
+  int* d_cet_enc = nullptr;
+  int cet_sub = 0;  // Trace_CETSubsteps; 0 = off
   std::string err;
 };
 
@@ -128,6 +132,8 @@ static fvc_status finish(fvc_ctx* c, const char* what, long long* steps, DevCoun
     return fail(c, FVC_ERR_TLOC, "%s: query time outside the loaded frame interval", what);
   if (h.status & PT_ERR_WALK)
     return fail(c, FVC_ERR_WALK, "%s: neighbour walk failed (indeterminate neighbour or hop cap)", what);
+  if (h.status & PT_ERR_CET)
+    return fail(c, FVC_ERR_WALK, "%s: exposure time: a step started outside the velocity domain", what);
   return FVC_OK;
 }
 
@@ -212,6 +218,8 @@ extern "C" void fvc_destroy(fvc_ctx* c) {
   cudaFree(c->d_ctr);
   cudaFree(c->d_scratch);
   cudaFree(c->d_vt);
+  cudaFree(c->d_cet_sum);
+  cudaFree(c->d_cet_enc);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -257,6 +265,7 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
   if (nnodes <= 0 || nelem <= 0 || !xyz || !conn || !adj) return fail(c, FVC_ERR_ARG, "empty mesh");
   fvc_status st;
   if ((st = use_device(c))) return st;
+  if (c->cet_sub) fvc_cet_enable(c, 0);  // the accumulators belong to the old mesh
   const int nv = c->mesh.dims == 3 ? 4 : 3;
   // host-side validation keeps every device gather in bounds
   for (long e = 0; e < nelem; e++) {
@@ -975,6 +984,93 @@ extern "C" fvc_status fvc_ftle_reduce(fvc_job* j, double int_t, double* wT, doub
   return FVC_OK;
 }
 
+// ------------------------------------------------ exposure / residence time
+
+static CetDev cet_dev(const fvc_ctx* c) {
+  CetDev d{};
+  d.sum = c->d_cet_sum;
+  d.enc = c->d_cet_enc;
+  d.substeps = c->cet_sub;
+  d.g = c->grid;
+  return d;
+}
+
+// Exposure time runs in the FP64 form with Euler, RK4 or RKF, as ompVC's
+// integrators call ComputeExposureTime (integration.c:183-203, 277-299,
+// 427-447, 649-669); ompVC has no multistep integrator.
+static fvc_status cet_ok(fvc_ctx* c, const fvc_job* j) {
+  if (!c->cet_sub) return FVC_OK;
+  if (j->prec) return fail(c, FVC_ERR_ARG, "exposure time is computed in the FP64 form only");
+  if (c->integ.type == 3) return fail(c, FVC_ERR_ARG, "exposure time needs Int_Type 0, 1 or 2");
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_cet_enable(fvc_ctx* c, int substeps) {
+  if (!c) return FVC_ERR_ARG;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  if (substeps == 0) {
+    cudaFree(c->d_cet_sum);
+    cudaFree(c->d_cet_enc);
+    c->d_cet_sum = nullptr;
+    c->d_cet_enc = nullptr;
+    c->cet_sub = 0;
+    return FVC_OK;
+  }
+  if (substeps < 2) return fail(c, FVC_ERR_ARG, "Trace_CETSubsteps must be greater than 1");
+  if (c->mesh.mesh_type != 1 || !c->mesh_set)
+    return fail(c, FVC_ERR_STATE, "exposure time needs an unstructured mesh (set it first)");
+  size_t E = (size_t)c->mesh.nelem;
+  if (!c->d_cet_sum) {
+    if (cudaMalloc(&c->d_cet_sum, sizeof(double) * E) != cudaSuccess ||
+        cudaMalloc(&c->d_cet_enc, sizeof(int) * E) != cudaSuccess) {
+      cudaFree(c->d_cet_sum);
+      c->d_cet_sum = nullptr;
+      c->d_cet_enc = nullptr;
+      return fail(c, FVC_ERR_OOM, "exposure-time accumulators");
+    }
+  }
+  FVC_CUDA(c, cudaMemsetAsync(c->d_cet_sum, 0, sizeof(double) * E, c->stream));
+  FVC_CUDA(c, cudaMemsetAsync(c->d_cet_enc, 0, sizeof(int) * E, c->stream));
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->cet_sub = substeps;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_cet_results(fvc_ctx* c, int ntracers, double* cet, double* met, int* enc) {
+  if (!c) return FVC_ERR_ARG;
+  if (!c->cet_sub) return fail(c, FVC_ERR_STATE, "exposure time is not enabled");
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  size_t E = (size_t)c->mesh.nelem;
+  if ((st = ensure_scratch(c, 16 * E))) return st;
+  double* out = (double*)c->d_scratch;
+  cet_results(c->mesh, cet_dev(c), ntracers, out, c->stream);
+  if ((st = check_launch(c, "exposure-time results"))) return st;
+  if (cet) FVC_CUDA(c, cudaMemcpyAsync(cet, out, 8 * E, cudaMemcpyDeviceToHost, c->stream));
+  if (met) FVC_CUDA(c, cudaMemcpyAsync(met, out + E, 8 * E, cudaMemcpyDeviceToHost, c->stream));
+  if (enc) FVC_CUDA(c, cudaMemcpyAsync(enc, c->d_cet_enc, 4 * E, cudaMemcpyDeviceToHost, c->stream));
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_tracer_residence(fvc_job* j, double launch_time, double stop_time, double* rt) {
+  if (!j || j->kind != 1 || !rt) return FVC_ERR_ARG;
+  fvc_ctx* c = j->ctx;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  size_t n = (size_t)j->t.n;
+  if (n == 0) return FVC_OK;
+  if ((st = ensure_scratch(c, 8 * n))) return st;
+  double* d = (double*)c->d_scratch;
+  tracer_residence(j->t, launch_time, stop_time, d, c->stream);
+  if ((st = check_launch(c, "residence time"))) return st;
+  j->stats.launches += 1;
+  FVC_CUDA(c, cudaMemcpyAsync(rt, d, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FVC_OK;
+}
+
 // ---------------------------------------------------------------- tracers
 
 extern "C" fvc_status fvc_tracer_create(fvc_ctx* c, const fvc_tracer_spec* sp, int n, const double* seeds,
@@ -1038,6 +1134,11 @@ extern "C" fvc_status fvc_tracer_launch(fvc_job* j, double t_start) {
   if ((st = ready(c, true))) return st;
   if (j->prec != c->prec) return fail(c, FVC_ERR_STATE, "the job was created with another precision form");
   if ((st = mixed_ok(c))) return st;
+  if ((st = cet_ok(c, j))) return st;
+  if (c->cet_sub) {
+    cet_release(j->t, cet_dev(c), c->stream);
+    j->stats.launches += 1;
+  }
   tracer_launch_vel(c->mesh, c->window, j->t, t_start, c->d_ctr, c->stream);
   if ((st = check_launch(c, "tracer launch"))) return st;
   j->stats.launches += 1;
@@ -1052,11 +1153,13 @@ extern "C" fvc_status fvc_tracer_advance(fvc_job* j, double t1, double t2, long 
   job_events(j);
   if (j->prec != c->prec) return fail(c, FVC_ERR_STATE, "the job was created with another precision form");
   if ((st = mixed_ok(c))) return st;
+  if ((st = cet_ok(c, j))) return st;
   if ((st = prepare_slots(c, t1, t2))) return st;
   compact_live(j->t.n, j->t.ldt, j->t.left, c->integ.extrapolate, j->t.live, nullptr, j->t.block_cnt, c->d_ctr,
                c->stream);
   cudaEventRecord(j->ev[0], c->stream);
-  tracer_advance(c->mesh, c->window, c->integ, j->t, t1, t2, c->d_ctr, c->stream);
+  if (c->cet_sub) tracer_advance_cet(c->mesh, c->window, c->integ, j->t, t1, t2, cet_dev(c), c->d_ctr, c->stream);
+  else tracer_advance(c->mesh, c->window, c->integ, j->t, t1, t2, c->d_ctr, c->stream);
   cudaEventRecord(j->ev[1], c->stream);
   if ((st = check_launch(c, "tracer advance"))) return st;
   DevCounters h{};

@@ -507,6 +507,27 @@ __device__ __forceinline__ bool contains(const DevMesh& m, int e, const double X
   return natural<DIMS>(m, e, X, r, s, t, wv) > -FVC_TINY;
 }
 
+// Get_Element_Global_Search (ompVC/mesh.c:304-398): lowest element id whose
+// containment test d > -TINY passes, from the point's bucket.
+template <int DIMS>
+__device__ __forceinline__ int global_find(const DevMesh& m, const BucketGrid& g, const double X[3]) {
+  int c[3];
+  for (int a = 0; a < 3; a++) {
+    if (a == 2 && DIMS == 2) { c[a] = 0; continue; }
+    double f = (X[a] - g.lo[a]) * g.inv[a];
+    if (!(f >= 0.0) || f >= (double)g.n[a]) return -1;
+    c[a] = min(g.n[a] - 1, (int)f);
+  }
+  long cell = ((long)c[2] * g.n[1] + c[1]) * g.n[0] + c[0];
+  int b = __ldg(g.start + cell), e = __ldg(g.start + cell + 1);
+  for (int i = b; i < e; i++) {
+    int el = __ldg(g.ids + i);
+    if (contains<DIMS>(m, el, X)) return el;
+  }
+  return -1;
+}
+
+
 // GetVelocity dispatch, ompVC/velocity.c:236-247.  tslot names the stage
 // time in the call's table (-1: none); nc the last locate's coordinates.
 template <int DIMS, int MESH>
@@ -515,6 +536,49 @@ __device__ __forceinline__ int velocity(const DevMesh& m, const DevWindow& w, do
                                         const NatCache* nc = nullptr) {
   if (MESH == 0) return vel_cart<DIMS>(m, w, tq, tslot, X, left, out);
   return vel_unstruct<DIMS>(m, w, tq, tslot, X, eid, left, out, nc);
+}
+
+// ComputeExposureTime, ompVC/exposuretime.c:110-172: credits a step of
+// length h from X0 to X1 (X1 in element e1) to the elements it crossed.  If
+// both ends lie in one element the whole step goes to it; otherwise the
+// straight path is cut into substeps - 1 pieces, each credited with
+// h / (substeps - 1) to the element holding its end point (walk from the
+// previous piece's element, global search if the walk leaves the mesh;
+// pieces outside the mesh are skipped, as ompVC skips them with a warning),
+// and every change of element counts an encounter.  Accumulated with
+// atomics: the sums' rounding depends on the order the GPU adds them in.
+template <int DIMS>
+__device__ __noinline__ void cet_step(const DevMesh& m, const CetDev& c, const double* X0, const double* X1,
+                                      int e1, double h, int* err) {
+  int e0 = locate_walk<DIMS>(m, X0, e1, *err);
+  if (e0 < 0) {
+    e0 = global_find<DIMS>(m, c.g, X0);
+    if (e0 < 0) {
+      *err |= PT_ERR_CET;  // ompVC: "Point X0 ... appears to be outside of velocity domain"
+      return;
+    }
+  }
+  if (e0 == e1) {
+    atomicAdd(c.sum + e0, h);
+    return;
+  }
+  int last = e0;
+  for (int s = 1; s < c.substeps; s++) {
+    const double a = ((double)s) / ((double)(c.substeps - 1));
+    double Xt[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) Xt[q] = (1 - a) * X0[q] + a * X1[q];
+    int et = locate_walk<DIMS>(m, Xt, last, *err);
+    if (et < 0) {
+      et = global_find<DIMS>(m, c.g, Xt);
+      if (et < 0) continue;
+    }
+    atomicAdd(c.sum + et, h / (c.substeps - 1));
+    if (et != last) {
+      atomicAdd(c.enc + et, 1);
+      last = et;
+    }
+  }
 }
 
 // ---------------------------------------------------------------- integrators
@@ -532,9 +596,10 @@ __device__ __noinline__ int velocity_cold(const DevMesh& m, const DevWindow& w, 
 }
 
 // Euler, ompVC/integration.c:222-311
-template <int DIMS, int MESH>
+template <int DIMS, int MESH, bool CET = false>
 __device__ __noinline__ double euler(const DevMesh& m, const DevWindow& w, const DevInteg& in,
-                                     Pt& p, double tstart, double tend, unsigned& steps, int& err) {
+                                     Pt& p, double tstart, double tend, unsigned& steps, int& err,
+                                     const CetDev* cet = nullptr) {
   double tc = tstart, h = dsign(in.h, tend - tstart), ve[3];
   NatCache nc;
   nc.e = -1;
@@ -560,6 +625,11 @@ __device__ __noinline__ double euler(const DevMesh& m, const DevWindow& w, const
     steps++;
     if (in.extrapolate && (err |= velocity_cold<DIMS, MESH>(m, w, tc, 2 * k, p.X, &p.eid, &p.left, p.V)))
       return tend;
+    if (CET) {  // ompVC/integration.c:277-299
+      const double X0[3] = {p.X[0] - h * ve[0], p.X[1] - h * ve[1], p.X[2] - h * ve[2]};
+      cet_step<DIMS>(m, *cet, X0, p.X, p.eid, h, &err);
+      if (err) return tend;
+    }
   }
   return tend;
 }
@@ -591,9 +661,10 @@ __device__ __forceinline__ int rk4_stages(const DevMesh& m, const DevWindow& w, 
 }
 
 // RK4, ompVC/integration.c:317-462
-template <int DIMS, int MESH>
+template <int DIMS, int MESH, bool CET = false>
 __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, const DevInteg& in,
-                                      Pt& p, double tstart, double tend, unsigned& steps, int& err) {
+                                      Pt& p, double tstart, double tend, unsigned& steps, int& err,
+                                      const CetDev* cet = nullptr) {
   int e[4] = {p.eid, p.eid, p.eid, p.eid};
   int l[4] = {p.left, p.left, p.left, p.left};
   double kk[4][3];
@@ -621,6 +692,13 @@ __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, cons
     steps++;
     if (in.extrapolate && (err |= velocity_cold<DIMS, MESH>(m, w, tc, 2 * k, p.X, &p.eid, &p.left, p.V)))
       return tend;
+    if (CET) {  // ompVC/integration.c:427-447
+      double X0[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) X0[q] = p.X[q] - div_rn(h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]), 6.0, kRcp6);
+      cet_step<DIMS>(m, *cet, X0, p.X, p.eid, h, &err);
+      if (err) return tend;
+    }
   }
   return tend;
 }
@@ -694,9 +772,10 @@ __device__ __noinline__ double ab2(const DevMesh& m, const DevWindow& w, const D
 // interpolate the two frames in time themselves.  The step-size factor is
 // the reference's pow(x, 0.25), computed correctly rounded (rn_root4): the
 // accept / reject test makes the trajectory depend on its last bit.
-template <int DIMS, int MESH>
+template <int DIMS, int MESH, bool CET = false>
 __device__ __noinline__ double rkf(const DevMesh& m, const DevWindow& w, const DevInteg& in, Pt& p,
-                                   double tstart, double tend, unsigned& steps, int& err) {
+                                   double tstart, double tend, unsigned& steps, int& err,
+                                   const CetDev* cet = nullptr) {
   double k[6][3], M[3];
   int e[6], l[6];
 #pragma unroll
@@ -772,6 +851,14 @@ __device__ __noinline__ double rkf(const DevMesh& m, const DevWindow& w, const D
       steps++;
       if (in.extrapolate && (err |= velocity_cold<DIMS, MESH>(m, w, tc, -1, p.X, &p.eid, &p.left, p.V)))
         return tend;
+      if (CET) {  // ompVC/integration.c:649-669
+        double X0[3];
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+          X0[q] = p.X[q] - (a8 * k[0][q] + b8 * k[2][q] + c8 * k[3][q] + d8 * k[4][q]) * h;
+        cet_step<DIMS>(m, *cet, X0, p.X, p.eid, h, &err);
+        if (err) return tend;
+      }
       if (fabs(h) > in.hmin && ss > 1.0) {
         ss = (ss > 4.0) ? 4.0 : ss;
         h = dsign((fabs(ss * h) > in.hmax) ? in.hmax : ss * h, tend - tstart);
@@ -787,9 +874,10 @@ __device__ __noinline__ double rkf(const DevMesh& m, const DevWindow& w, const D
   return tend;
 }
 
-template <int DIMS, int MESH>
+template <int DIMS, int MESH, bool CET = false>
 __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, const DevInteg& in,
-                                      Pt& p, double tstart, double tend, unsigned& steps) {
+                                      Pt& p, double tstart, double tend, unsigned& steps,
+                                      const CetDev* cet = nullptr) {
   int err = 0;
   if (p.left && in.extrapolate) {
 #pragma unroll
@@ -799,10 +887,10 @@ __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, cons
   if (p.left) return PT_ERR_STATE;  // "integrate point that already left domain"
   if (MESH == 1 && p.eid < 0) return PT_ERR_STATE;
   double stop;
-  if (in.type == 1) stop = rk4<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
-  else if (in.type == 2) stop = rkf<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
-  else if (in.type == 3) stop = ab2<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
-  else stop = euler<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
+  if (in.type == 1) stop = rk4<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet);
+  else if (in.type == 2) stop = rkf<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet);
+  else if (in.type == 3 && !CET) stop = ab2<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
+  else stop = euler<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet);
   if (!err && (fabs(stop - tend) > FVC_TINY) && in.extrapolate) {
 #pragma unroll
     for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + p.V[q] * (tend - stop);

@@ -251,26 +251,6 @@ void scan_counts(const int* in, int* out, int n, long long* tmp, cudaStream_t s)
   exclusive_scan(in, out, n, tmp, s);
 }
 
-// Get_Element_Global_Search (ompVC/mesh.c:304-398): lowest element id whose
-// containment test d > -TINY passes, from the point's bucket.
-template <int DIMS>
-__device__ __forceinline__ int global_find(const DevMesh& m, const BucketGrid& g, const double X[3]) {
-  int c[3];
-  for (int a = 0; a < 3; a++) {
-    if (a == 2 && DIMS == 2) { c[a] = 0; continue; }
-    double f = (X[a] - g.lo[a]) * g.inv[a];
-    if (!(f >= 0.0) || f >= (double)g.n[a]) return -1;
-    c[a] = min(g.n[a] - 1, (int)f);
-  }
-  long cell = ((long)c[2] * g.n[1] + c[1]) * g.n[0] + c[0];
-  int b = __ldg(g.start + cell), e = __ldg(g.start + cell + 1);
-  for (int i = b; i < e; i++) {
-    int el = __ldg(g.ids + i);
-    if (contains<DIMS>(m, el, X)) return el;
-  }
-  return -1;
-}
-
 template <int DIMS>
 __global__ void k_global(DevMesh m, BucketGrid g, int n, const double* X, const int* skip, int* out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;

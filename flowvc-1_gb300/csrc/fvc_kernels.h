@@ -29,12 +29,6 @@ struct DevCounters {
 // ---- mesh preprocessing
 void launch_geometry(const DevMesh& m, double* geom, float* geo32, cudaStream_t s);
 
-struct BucketGrid {
-  double lo[3], inv[3];   // origin and 1 / cell size
-  int n[3];               // cells per axis
-  const int* start;       // ncells + 1 offsets
-  const int* ids;         // element ids per cell, ascending
-};
 // Builds the grid into caller-owned buffers; returns the number of entries
 // written to ids (the caller sizes ids with bucket_count first).
 long long bucket_count(const DevMesh& m, BucketGrid& g, int* cell_count, int ncells, int* d_total,
@@ -141,6 +135,17 @@ void tracer_init_ldt(const TracerDev& t, cudaStream_t s);
 // Compacts the selected tracers' positions (in seed order) into t.outX;
 // the count lands in ctr->count.
 void tracer_compact(const TracerDev& t, int always, DevCounters* ctr, cudaStream_t s);
+
+// ---- tracer side analyses (fvc_cet.cu), unstructured meshes, FP64 form
+// tracer_advance with the exposure-time accumulation after every step
+void tracer_advance_cet(const DevMesh& m, const DevWindow& w, const DevInteg& in, const TracerDev& t, double t1,
+                        double t2, const CetDev& cet, DevCounters* ctr, cudaStream_t s);
+// one encounter for the element of every tracer of a release inside the domain
+void cet_release(const TracerDev& t, const CetDev& cet, cudaStream_t s);
+// normalised exposure times: out = CET[nelem] then MET[nelem]
+void cet_results(const DevMesh& m, const CetDev& cet, int ntracers, double* out, cudaStream_t s);
+// residence time of every tracer of a release
+void tracer_residence(const TracerDev& t, double launch, double stop, double* rt, cudaStream_t s);
 
 // left = outside the domain or not placed by the seed chain; LeftDomainTime
 // as ompVC initialises it for each seeding routine

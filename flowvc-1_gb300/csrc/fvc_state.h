@@ -6,7 +6,7 @@
 namespace fvc {
 
 // per-point fault bits, OR-ed into a launch's status word
-enum : int { PT_ERR_WALK = 1, PT_ERR_TLOC = 2, PT_ERR_STATE = 4 };
+enum : int { PT_ERR_WALK = 1, PT_ERR_TLOC = 2, PT_ERR_STATE = 4, PT_ERR_CET = 8 };
 
 struct DevMesh {
   int dims, mesh_type;  // 2/3; 0 Cartesian, 1 unstructured
@@ -66,6 +66,24 @@ struct DevWindow {
   int qfmt;  // FVC_PREC_BF16 or FVC_PREC_FP16
   const StepM* steps;
   int nsteps;
+};
+
+// Uniform bucket grid over the mesh for Get_Element_Global_Search.
+struct BucketGrid {
+  double lo[3], inv[3];   // origin and 1 / cell size
+  int n[3];               // cells per axis
+  const int* start;       // ncells + 1 offsets
+  const int* ids;         // element ids per cell, ascending
+};
+
+// Exposure-time accumulators (Trace_CETArray, ompVC/exposuretime.c:110-172):
+// per element of the velocity mesh, the time tracers spent in it and the
+// number of times one entered it.  Shared by every release of a run.
+struct CetDev {
+  double* sum;   // CETsum
+  int* enc;      // Encounters
+  int substeps;  // Trace_CETSubsteps (>= 2)
+  BucketGrid g;  // global-search fallback of the sub-step walk
 };
 
 struct DevInteg {

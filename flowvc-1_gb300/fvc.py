@@ -83,6 +83,9 @@ SIGNATURES = {
     "fvc_stream": (_vp, [_vp]),
     "fvc_job_destroy": (None, [_vp]),
     "fvc_probe_fp64": (C.c_int, [C.c_int, _dp]),
+    "fvc_cet_enable": (C.c_int, [_vp, C.c_int]),
+    "fvc_cet_results": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip]),
+    "fvc_tracer_residence": (C.c_int, [_vp, C.c_double, C.c_double, _dp]),
 }
 
 _lib = None
@@ -234,6 +237,14 @@ class Context:
         self._chk(self.lib.fvc_local_search(self.h, X.shape[0], _d(f64(X)), _i(i32(guess)), _i(out)))
         return out
 
+    def cet_enable(self, substeps):
+        self._chk(self.lib.fvc_cet_enable(self.h, substeps))
+
+    def cet_results(self, ntracers, nelem):
+        cet, met, enc = np.empty(nelem), np.empty(nelem), np.empty(nelem, np.int32)
+        self._chk(self.lib.fvc_cet_results(self.h, ntracers, _d(cet), _d(met), _i(enc)))
+        return cet, met, enc
+
     def global_search(self, X):
         out = np.empty(X.shape[0], np.int32)
         self._chk(self.lib.fvc_global_search(self.h, X.shape[0], _d(f64(X)), _i(out)))
@@ -323,6 +334,11 @@ class TracerJob:
         eid, left = np.empty(n, np.int32), np.empty(n, np.int32)
         self.ctx._chk(self.lib.fvc_tracer_get_state(self.h, _d(X), _i(eid), _i(left), _d(ldt)))
         return dict(X=X, eid=eid, left=left, ldt=ldt)
+
+    def residence(self, launch_time, stop_time):
+        rt = np.empty(max(self.n, 1))
+        self.ctx._chk(self.lib.fvc_tracer_residence(self.h, launch_time, stop_time, _d(rt)))
+        return rt[: self.n].copy()
 
     def close(self):
         if self.h:

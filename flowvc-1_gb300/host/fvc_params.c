@@ -148,7 +148,17 @@ int fvcp_check_derive(fvcp_params *p, char *err, int errlen)
     }
     if (p->tr_compute) {
         if (p->tr_strategy == 1) return perr(err, errlen, "Trace_ReleaseStrategy = 1 (staggered release) is not supported");
-        if (p->tr_ap || p->tr_cet || p->tr_rt) return perr(err, errlen, "tracer side analyses (AP, CET, RT) are not supported");
+        if (p->tr_ap) return perr(err, errlen, "Trace_APCompute (activation potential) is not supported");
+        /* CheckParameters, ompVC/parameters.c:535-542 */
+        if (p->tr_cet) {
+            if (p->tr_rt) return perr(err, errlen, "Cannot compute exposure times and residence times concurrently");
+            if (p->tr_cetsub < 2) return perr(err, errlen, "Trace_CETSubsteps must be greater than 1");
+            if (p->mesh_type != 1) return perr(err, errlen, "exposure time needs an unstructured velocity mesh");
+            if (p->tr_cetaux) return perr(err, errlen, "Trace_CETAuxillaryMesh is not supported");
+            if (p->int_type == 3) return perr(err, errlen, "exposure time needs Int_Type 0, 1 or 2");
+        }
+        if ((p->tr_rt || p->tr_cet) && p->int_dir < 0)
+            return perr(err, errlen, "Residence/Exposure time computations not supported for backward time integrations");
         if (p->tr_genmesh) {
             if (p->tb[0] > p->tb[1]) return perr(err, errlen, "Trace_CartMesh.XMin > Trace_CartMesh.XMax");
             if (p->tb[2] > p->tb[3]) return perr(err, errlen, "Trace_CartMesh.YMin > Trace_CartMesh.YMax");

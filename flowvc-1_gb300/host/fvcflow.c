@@ -9,9 +9,10 @@
  * Differences from ompVC, by design:
  *   - every velocity frame the run needs is uploaded once and stays resident
  *     in device memory; no per-interval temporary files are written;
- *   - out-of-scope options (inertial particles, staggered release, CET /
- *     residence-time / activation-potential analyses, velocity resampling)
- *     are refused with an error instead of being computed;
+ *   - out-of-scope options (inertial particles, staggered release, the
+ *     activation-potential analysis, an auxiliary exposure-time mesh,
+ *     velocity resampling) are refused with an error instead of being
+ *     computed;
  *   - errors return a non-zero exit status with a message instead of
  *     exiting from inside the computation.
  *
@@ -66,6 +67,7 @@ typedef struct {
     long long steps;
     double t_compute;
     const char *dump_dir; /* --dump-state: final FTLE grid state per output */
+    long nelem;           /* elements of the unstructured mesh */
 } run_t;
 
 /* frame index -> file index with ompVC's wrap (ompVC/velocity.c:77-80) */
@@ -118,6 +120,7 @@ static int load_mesh(run_t *R)
         }
         fclose(f);
         rc = fvc_set_unstruct_mesh(R->ctx, n, xyz, e, conn, adj);
+        R->nelem = e;
         free(xyz); free(conn); free(adj);
         if (rc) return die("unstructured mesh", R->ctx, rc);
         R->frame_len = 3L * n;
@@ -422,6 +425,77 @@ static int read_seeds(run_t *R, int *nout, double **out, double center[3])
     return 0;
 }
 
+/* OutputRT, ompVC/residencetime.c:21-185 (generated grids and seed lists):
+ * <RT>_Cartesian.bin (the seed grid's bounds and resolution) or
+ * <RT>_coordinates.bin (count, then the located seeds' positions), and per
+ * release <RT>.<ss>.bin: its release time, then the residence time of each
+ * tracer in seed order (fvc_tracer_residence). */
+static int output_rt(run_t *R, int n, const double *icX, fvc_job **rel, const double *stop)
+{
+    fvcp_params *P = &R->P;
+    char path[2 * FVCP_STR];
+    FILE *f;
+    if (P->tr_genmesh) {
+        snprintf(path, sizeof(path), "%s%s_Cartesian.bin", P->path_output, P->tr_rtprefix);
+        if (!(f = fopen(path, "wb"))) { fprintf(stderr, "Could not open file %s\n", path); return 1; }
+        for (int a = 0; a < 3; a++) {
+            fwrite(&P->tb[2 * a], 8, 1, f);
+            fwrite(&P->tb[2 * a + 1], 8, 1, f);
+            fwrite(&P->tres3[a], 4, 1, f);
+        }
+        fclose(f);
+    } else {
+        snprintf(path, sizeof(path), "%s%s_coordinates.bin", P->path_output, P->tr_rtprefix);
+        if (!(f = fopen(path, "wb"))) { fprintf(stderr, "Could not open file %s\n", path); return 1; }
+        fwrite(&n, 4, 1, f);
+        fwrite(icX, 24, (size_t)n, f);
+        fclose(f);
+    }
+    double *rt = (double *)malloc(8 * (size_t)(n ? n : 1));
+    if (!rt) return 1;
+    for (int ss = 0; ss < P->tr_nlaunch; ss++) {
+        double time = P->out_tstart + ss * P->tr_spacing;
+        int rc = fvc_tracer_residence(rel[ss], time, stop[ss], rt);
+        if (rc) { free(rt); return die("residence time", R->ctx, rc); }
+        snprintf(path, sizeof(path), "%s%s.%d.bin", P->path_output, P->tr_rtprefix, ss);
+        if (!(f = fopen(path, "wb"))) { free(rt); fprintf(stderr, "Could not open file %s\n", path); return 1; }
+        fwrite(&time, 8, 1, f);
+        fwrite(rt, 8, (size_t)n, f);
+        fclose(f);
+    }
+    free(rt);
+    return 0;
+}
+
+/* OutputCET, ompVC/exposuretime.c:175-302: <RT>_CET.0.bin and <RT>_MET.0.bin
+ * (time stamp -1, then a double per element) and <RT>_ENC.0.bin (time stamp
+ * -1, then an int per element), from fvc_cet_results. */
+static int output_cet(run_t *R, int ntracers)
+{
+    fvcp_params *P = &R->P;
+    long E = R->nelem;
+    double *cet = (double *)malloc(8 * (size_t)E), *met = (double *)malloc(8 * (size_t)E);
+    int *enc = (int *)malloc(4 * (size_t)E);
+    if (!cet || !met || !enc) return 1;
+    int rc = fvc_cet_results(R->ctx, ntracers, cet, met, enc);
+    if (rc) return die("exposure time", R->ctx, rc);
+    const char *suffix[3] = {"CET", "MET", "ENC"};
+    double t = -1.0;
+    for (int k = 0; k < 3; k++) {
+        char path[2 * FVCP_STR];
+        snprintf(path, sizeof(path), "%s%s_%s.0.bin", P->path_output, P->tr_rtprefix, suffix[k]);
+        FILE *f = fopen(path, "wb");
+        if (!f) { fprintf(stderr, "Could not open %s\n", path); return 1; }
+        fwrite(&t, 8, 1, f);
+        if (k == 0) fwrite(cet, 8, (size_t)E, f);
+        else if (k == 1) fwrite(met, 8, (size_t)E, f);
+        else fwrite(enc, 4, (size_t)E, f);
+        fclose(f);
+    }
+    free(cet); free(met); free(enc);
+    return 0;
+}
+
 static int run_tracers(run_t *R)
 {
     fvcp_params *P = &R->P;
@@ -444,14 +518,18 @@ static int run_tracers(run_t *R)
         start[ss] = P->out_tstart + P->int_dir * ss * P->tr_spacing;
         stop[ss] = P->int_dir > 0 ? MIN(start[ss] + P->tr_T, P->out_tend) : MAX(start[ss] - P->tr_T, P->out_tend);
     }
+    if (P->tr_cet && (rc = fvc_cet_enable(R->ctx, P->tr_cetsub))) return die("exposure time", R->ctx, rc);
     R->t_compute += wall() - t0;
+    double *icX = (double *)malloc(24 * (size_t)(n ? n : 1));
+    if (!icX) { fprintf(stderr, "out of memory\n"); return 1; }
     {   /* the located seeds, as ompVC stores them (ompVC/tracers.c:1258-1272) */
         char path[2 * FVCP_STR];
         snprintf(path, sizeof(path), "%s%s.IC", P->path_data, P->tr_prefix);
         int *eid = (int *)malloc(4 * (size_t)(n ? n : 1)), *left = (int *)malloc(4 * (size_t)(n ? n : 1));
-        double *X = (double *)malloc(24 * (size_t)(n ? n : 1)), *ldt = (double *)malloc(8 * (size_t)(n ? n : 1));
+        double *X = icX, *ldt = (double *)malloc(8 * (size_t)(n ? n : 1));
+        if ((rc = fvc_tracer_get_state(rel[0], X, eid, left, ldt))) return die("tracer seeds", R->ctx, rc);
         FILE *f = fopen(path, "wb");
-        if (f && eid && left && X && ldt && !fvc_tracer_get_state(rel[0], X, eid, left, ldt)) {
+        if (f && eid && left && ldt) {
             fwrite(&n, 4, 1, f);
             disk_lpt r;
             for (int i = 0; i < n; i++) {
@@ -462,7 +540,7 @@ static int run_tracers(run_t *R)
             }
         }
         if (f) fclose(f);
-        free(eid); free(left); free(X); free(ldt);
+        free(eid); free(left); free(ldt);
     }
     int outputframe = 0;
     double next = P->out_tstart;
@@ -515,8 +593,10 @@ static int run_tracers(run_t *R)
             t1 = t2;
         }
     }
+    if (P->tr_rt && output_rt(R, n, icX, rel, stop)) return 1;
+    if (P->tr_cet && output_cet(R, n)) return 1;
     for (int ss = 0; ss < nl; ss++) fvc_job_destroy(rel[ss]);
-    free(rel); free(start); free(stop); free(status); free(snap); free(seeds);
+    free(rel); free(start); free(stop); free(status); free(snap); free(seeds); free(icX);
     return 0;
 }
 

@@ -227,6 +227,32 @@ fvc_status fvc_tracer_advance(fvc_job *job, double t1, double t2, long long *ste
 fvc_status fvc_tracer_snapshot(fvc_job *job, int always_output, double *X_out, long long *count);
 fvc_status fvc_tracer_get_state(fvc_job *job, double *X, int *eid, int *left, double *ldt);
 
+/* ---- tracer side analyses (unstructured meshes, FP64 form) ------------- */
+
+/* Exposure time (Trace_CETCompute, ompVC/exposuretime.c:110-172): while
+ * enabled, every accepted Euler / RK4 / RKF step of fvc_tracer_advance
+ * credits its duration to the elements its straight path crosses, sampled
+ * at `substeps` points (Trace_CETSubsteps >= 2), and every release counts
+ * one encounter for each tracer's starting element (ompVC/tracers.c:180-185).
+ * The per-element sums live on the device, shared by all releases on the
+ * context; enabling clears them, substeps = 0 disables and frees them.  The
+ * GPU adds with atomics, so sums can differ from ompVC's serial order in
+ * their last bits; encounter counts are exact.  Velocity-mesh only (ompVC's
+ * Trace_CETAuxillaryMesh is not supported). */
+fvc_status fvc_cet_enable(fvc_ctx *ctx, int substeps);
+/* OutputCET's fields (ompVC/exposuretime.c:175-246), nelem values each, any
+ * pointer may be NULL: cet = sum / xc / ntracers and met = sum / xc /
+ * encounters where sum > TINY, else 0 (xc = 1 in 3D, as the reference's
+ * pow(vol, 1/3) with integer 1/3 evaluates; sqrt(area) in 2D); enc the
+ * encounter counts. */
+fvc_status fvc_cet_results(fvc_ctx *ctx, int ntracers, double *cet, double *met, int *enc);
+
+/* Residence time of a release (OutputRT, ompVC/residencetime.c:160-178),
+ * in seed order: -1 for tracers never inside the domain, else
+ * LeftDomainTime - launch_time for tracers that left and stop_time -
+ * launch_time for the rest.  rt must hold n doubles. */
+fvc_status fvc_tracer_residence(fvc_job *job, double launch_time, double stop_time, double *rt);
+
 /* Counters of a job since its creation, from CUDA events recorded on the
  * context's stream around each launch. */
 typedef struct {

@@ -253,6 +253,41 @@ int orc_global(const orc_ctx *c, const double X[3])
     return -1;
 }
 
+/* ComputeExposureTime, ompVC/exposuretime.c:110-172: the step from X0 to X1
+ * (X1 in element e1) of length h.  Same element at both ends: all of h to
+ * it.  Otherwise the straight path is sampled at substeps points; each
+ * sample after the first credits h / (substeps - 1) to the element holding
+ * it (walk from the previous sample's element, global search when the walk
+ * leaves; samples outside the mesh are skipped) and a change of element
+ * counts an encounter. */
+static void cet_step(const orc_ctx *c, const double X0[3], const double X1[3], int e1, double h, int *err)
+{
+    int e0 = orc_local(c, X0, e1, err);
+    if (e0 < 0) {
+        e0 = orc_global(c, X0);
+        if (e0 < 0) { *err |= ORC_PT_ERR_CET; return; }
+    }
+    if (e0 == e1) {
+        c->cet_sum[e0] = c->cet_sum[e0] + h;
+        return;
+    }
+    int last = e0;
+    for (int s = 1; s < c->cet_sub; s++) {
+        double a = ((double)s) / ((double)(c->cet_sub - 1)), Xt[3];
+        for (int q = 0; q < 3; q++) Xt[q] = (1 - a) * X0[q] + a * X1[q];
+        int et = orc_local(c, Xt, last, err);
+        if (et < 0) {
+            et = orc_global(c, Xt);
+            if (et < 0) continue;
+        }
+        c->cet_sum[et] = c->cet_sum[et] + (h / (c->cet_sub - 1));
+        if (et != last) {
+            c->cet_enc[et]++;
+            last = et;
+        }
+    }
+}
+
 /* -------------------------------------------------------------- integrators */
 
 /* Euler, ompVC/integration.c:222-311 */
@@ -279,6 +314,11 @@ static double euler(const orc_ctx *c, orc_pt *p, double tstart, double tend, lon
         }
         (*steps)++;
         if (c->extrapolate && (*err |= orc_vel(c, tc, p->X, &p->eid, &p->left, p->V))) return tend;
+        if (c->cet_sub) {   /* ompVC/integration.c:277-299 */
+            double X0[3] = {p->X[0] - h * ve[0], p->X[1] - h * ve[1], p->X[2] - h * ve[2]};
+            cet_step(c, X0, p->X, p->eid, h, err);
+            if (*err) return tend;
+        }
     }
     return tend;
 }
@@ -331,6 +371,13 @@ static double rk4(const orc_ctx *c, orc_pt *p, double tstart, double tend, long 
         }
         (*steps)++;
         if (c->extrapolate && (*err |= orc_vel(c, tc, p->X, &p->eid, &p->left, p->V))) return tend;
+        if (c->cet_sub) {   /* ompVC/integration.c:427-447 */
+            double X0[3];
+            for (int q = 0; q < 3; q++)
+                X0[q] = p->X[q] - h * (k[0][q] + 2 * k[1][q] + 2 * k[2][q] + k[3][q]) / 6;
+            cet_step(c, X0, p->X, p->eid, h, err);
+            if (*err) return tend;
+        }
     }
     return tend;
 }
@@ -450,6 +497,13 @@ static double rkf(const orc_ctx *c, orc_pt *p, double tstart, double tend, long 
             }
             (*steps)++;
             if (c->extrapolate && (*err |= orc_vel(c, tc, p->X, &p->eid, &p->left, p->V))) return tend;
+            if (c->cet_sub) {   /* ompVC/integration.c:649-669 */
+                double X0[3];
+                for (int q = 0; q < 3; q++)
+                    X0[q] = p->X[q] - (a8 * k[0][q] + b8 * k[2][q] + c8 * k[3][q] + d8 * k[4][q]) * h;
+                cet_step(c, X0, p->X, p->eid, h, err);
+                if (*err) return tend;
+            }
             if (fabs(h) > c->hmin && ss > 1.0) {
                 ss = (ss > 4.0) ? 4.0 : ss;
                 h = ORC_SIGN((fabs(ss * h) > hmax) ? hmax : ss * h, tend - tstart);

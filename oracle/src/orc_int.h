@@ -31,6 +31,11 @@ struct orc_ctx {
     double h;
     int extrapolate;
     double acc, hmin, hmax;     /* Int_Accuracy, Int_MinTimeStep, Int_MaxTimeStep (RKF) */
+    /* exposure time (Trace_CETArray, ompVC/exposuretime.c): per-element sums
+     * and encounters; cet_sub = Trace_CETSubsteps, 0 when off */
+    double *cet_sum;
+    int *cet_enc;
+    int cet_sub;
 };
 
 /* One Lagrangian point as the integrators see it (the fields of
@@ -46,6 +51,7 @@ typedef struct {
 /* status bits a point can raise */
 #define ORC_PT_ERR_WALK 1
 #define ORC_PT_ERR_TLOC 2
+#define ORC_PT_ERR_CET 4
 
 int orc_outside_domain(const orc_ctx *c, const double X[3]);
 int orc_vel(const orc_ctx *c, double tq, double X[3], int *eid, int *left, double out[3]);

@@ -788,6 +788,93 @@ static int tracer_seed(orc_run_state *S, int *nout, orc_pt **out, char *err, int
     return ORC_OK;
 }
 
+/* OutputRT, ompVC/residencetime.c:21-185, for generated grids and seed
+ * lists: the seed grid's parameters (<RT>_Cartesian.bin) or the located
+ * seeds' positions (<RT>_coordinates.bin: count, then X per seed), and per
+ * release <RT>.<ss>.bin: the release time, then per tracer -1 if it never was
+ * in the domain, else (LeftDomainTime if it left, the release's stop time if
+ * not) minus the release time. */
+static int output_rt(orc_run_state *S, int n, const orc_pt *ic, orc_pt **rel, const launch_t *L, char *err,
+                     int errlen)
+{
+    const orc_params *P = &S->P;
+    char path[2 * ORC_STR];
+    FILE *f;
+    if (P->tr_genmesh) {
+        snprintf(path, sizeof(path), "%s%s_Cartesian.bin", P->path_output, P->tr_rtprefix);
+        if (!(f = fopen(path, "wb"))) return set_err(err, errlen, ORC_ERR_IO, "Could not open file %s", path);
+        for (int a = 0; a < 3; a++) {
+            fwrite(&P->tb[2 * a], 8, 1, f);
+            fwrite(&P->tb[2 * a + 1], 8, 1, f);
+            fwrite(&P->tres3[a], 4, 1, f);
+        }
+        fclose(f);
+    } else {
+        snprintf(path, sizeof(path), "%s%s_coordinates.bin", P->path_output, P->tr_rtprefix);
+        if (!(f = fopen(path, "wb"))) return set_err(err, errlen, ORC_ERR_IO, "Could not open file %s", path);
+        fwrite(&n, 4, 1, f);
+        for (int i = 0; i < n; i++) fwrite(ic[i].X, 8, 3, f);
+        fclose(f);
+    }
+    for (int ss = 0; ss < P->tr_nlaunch; ss++) {
+        snprintf(path, sizeof(path), "%s%s.%d.bin", P->path_output, P->tr_rtprefix, ss);
+        if (!(f = fopen(path, "wb"))) return set_err(err, errlen, ORC_ERR_IO, "Could not open file %s", path);
+        double time = P->out_tstart + ss * P->tr_spacing;
+        fwrite(&time, 8, 1, f);
+        for (int i = 0; i < n; i++) {
+            const orc_pt *t = &rel[ss][i];
+            double rt = fabs(t->ldt + 1) < ORC_TINY ? -1.0 : (t->left ? t->ldt : L[ss].stop) - time;
+            fwrite(&rt, 8, 1, f);
+        }
+        fclose(f);
+    }
+    return ORC_OK;
+}
+
+/* OutputCET, ompVC/exposuretime.c:175-302: per element CET = sum / xc /
+ * Trace_NumTracers and MET = sum / xc / encounters where the sum exceeds
+ * TINY, else 0, with xc = pow(vol, (1/3)) in 3D -- the integer quotient 1/3
+ * is 0, so xc = 1 -- and sqrt(triangle area) in 2D; the files
+ * <RT>_CET.0.bin, <RT>_MET.0.bin (time stamp -1, then doubles) and
+ * <RT>_ENC.0.bin (time stamp -1, then ints). */
+static int output_cet(orc_run_state *S, int ntracers, char *err, int errlen)
+{
+    const orc_params *P = &S->P;
+    const orc_ctx *c = &S->ctx;
+    long E = c->nelem;
+    double *cet = (double *)calloc((size_t)E, 8), *met = (double *)calloc((size_t)E, 8);
+    if (!cet || !met) return set_err(err, errlen, ORC_ERR_OOM, "out of memory");
+    for (long e = 0; e < E; e++) {
+        if (c->cet_sum[e] > ORC_TINY) {
+            double xc = 1.0;
+            if (c->dims == 2) {
+                const double *X1 = c->xyz + 3L * c->conn[4 * e], *X2 = c->xyz + 3L * c->conn[4 * e + 1],
+                             *X3 = c->xyz + 3L * c->conn[4 * e + 2];
+                double A0 = X2[0] - X1[0], A1 = X2[1] - X1[1], B0 = X3[0] - X1[0], B1 = X3[1] - X1[1];
+                xc = sqrt(fabs(A0 * B1 - A1 * B0) / 2);
+            }
+            cet[e] = c->cet_sum[e] / xc / ntracers;
+            met[e] = c->cet_sum[e] / xc / c->cet_enc[e];
+        }
+    }
+    const char *suffix[3] = {"CET", "MET", "ENC"};
+    double t = -1.0;
+    for (int k = 0; k < 3; k++) {
+        char path[2 * ORC_STR];
+        snprintf(path, sizeof(path), "%s%s_%s.0.bin", P->path_output, P->tr_rtprefix, suffix[k]);
+        FILE *f = fopen(path, "wb");
+        if (!f) { free(cet); free(met); return set_err(err, errlen, ORC_ERR_IO, "Could not open %s", path); }
+        fwrite(&t, 8, 1, f);
+        if (k == 0) fwrite(cet, 8, (size_t)E, f);
+        else if (k == 1) fwrite(met, 8, (size_t)E, f);
+        else fwrite(c->cet_enc, 4, (size_t)E, f);
+        fclose(f);
+    }
+    free(cet);
+    free(met);
+    return ORC_OK;
+}
+
 static int run_tracers(orc_run_state *S, double *secs, long long *steps, char *err, int errlen)
 {
     orc_params *P = &S->P;
@@ -808,6 +895,12 @@ static int run_tracers(orc_run_state *S, double *secs, long long *steps, char *e
         if (!rel[ss]) return set_err(err, errlen, ORC_ERR_OOM, "out of memory");
         memcpy(rel[ss], ic, sizeof(orc_pt) * (size_t)n);
     }
+    if (P->tr_cet) {
+        c->cet_sum = (double *)calloc((size_t)c->nelem, sizeof(double));
+        c->cet_enc = (int *)calloc((size_t)c->nelem, sizeof(int));
+        if (!c->cet_sum || !c->cet_enc) return set_err(err, errlen, ORC_ERR_OOM, "out of memory");
+        c->cet_sub = P->tr_cetsub;
+    }
     int outputframe = 0;
     double next = P->out_tstart, tsum = 0;
     for (int df = P->first_frame; df != P->last_frame; df = df + P->int_dir) {
@@ -822,6 +915,10 @@ static int run_tracers(orc_run_state *S, double *secs, long long *steps, char *e
                     orc_pt *T = rel[ss];
                     if (L[ss].status == 0) {
                         L[ss].status = 1;
+                        /* the release's first encounters, ompVC/tracers.c:180-185 */
+                        if (c->cet_sub)
+                            for (int i = 0; i < n; i++)
+                                if (!T[i].left) c->cet_enc[T[i].eid]++;
                         t1 = L[ss].start;
                         for (int i = 0; i < n; i++)
                             if (!T[i].left) {
@@ -833,7 +930,9 @@ static int run_tracers(orc_run_state *S, double *secs, long long *steps, char *e
                     }
                     long long st = 0;
                     int fault = 0;
-#pragma omp parallel for schedule(dynamic, 256) reduction(+ : st) reduction(| : fault)
+                    /* exposure-time sums are added in tracer order, as ompVC's
+                     * loop on one thread adds them */
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : st) reduction(| : fault) if (!c->cet_sub)
                     for (int i = 0; i < n; i++)
                         if (T[i].ldt > -ORC_TINY && (!T[i].left || P->extrapolate))
                             fault |= orc_advect_pt(c, &T[i], t1, t2, &st);
@@ -877,9 +976,13 @@ static int run_tracers(orc_run_state *S, double *secs, long long *steps, char *e
         fwrite(outbuf[i], 8, 3 * (size_t)cnt[i], f);
         fclose(f);
     }
+    if (P->tr_rt && (rc = output_rt(S, n, ic, rel, L, err, errlen))) return rc;
+    if (P->tr_cet && (rc = output_cet(S, n, err, errlen))) return rc;
     for (int i = 0; i < P->out_tres; i++) free(outbuf[i]);
     for (int ss = 0; ss < nl; ss++) free(rel[ss]);
     free(outbuf); free(cnt); free(rel); free(L); free(ic);
+    free(c->cet_sum); free(c->cet_enc);
+    c->cet_sum = NULL; c->cet_enc = NULL; c->cet_sub = 0;
     return ORC_OK;
 }
 

@@ -145,7 +145,17 @@ int orc_check_derive(orc_params *p, char *err, int errlen)
     }
     if (p->tr_compute) {
         if (p->tr_strategy == 1) return fail(err, errlen, "staggered tracer release is not supported");
-        if (p->tr_ap || p->tr_cet || p->tr_rt) return fail(err, errlen, "tracer side analyses (AP/CET/RT) are not supported");
+        if (p->tr_ap) return fail(err, errlen, "Trace_APCompute (activation potential) is not supported");
+        /* CheckParameters, ompVC/parameters.c:535-542 */
+        if (p->tr_cet) {
+            if (p->tr_rt) return fail(err, errlen, "Cannot compute exposure times and residence times concurrently");
+            if (p->tr_cetsub < 2) return fail(err, errlen, "Trace_CETSubsteps must be greater than 1");
+            if (p->mesh_type != 1) return fail(err, errlen, "exposure time needs an unstructured velocity mesh");
+            if (p->tr_cetaux) return fail(err, errlen, "Trace_CETAuxillaryMesh is not supported");
+            if (p->int_type == 3) return fail(err, errlen, "exposure time needs Int_Type 0, 1 or 2");
+        }
+        if ((p->tr_rt || p->tr_cet) && p->int_dir < 0)
+            return fail(err, errlen, "Residence/Exposure time computations not supported for backward time integrations");
         if (p->tr_genmesh) {
             if (p->tb[0] > p->tb[1] || p->tb[2] > p->tb[3] || p->tb[4] > p->tb[5])
                 return fail(err, errlen, "Trace_CartMesh bounds inverted");

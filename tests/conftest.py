@@ -37,6 +37,10 @@ def engine():
     return fvc_build
 
 
+def undefined_files(case, run):
+    return {f for c, r, f in REFERENCE_UNDEFINED if (c, r) == (case, run)}
+
+
 def golden_cases():
     out = []
     for name in sorted(os.listdir(GOLDEN)):
@@ -74,15 +78,41 @@ FTLE_RTOL = 1e-12
 FTLE_ATOL = 1e-13
 
 
-def compare_outputs(expected_dir, got_dir, ftle_rtol=FTLE_RTOL, ftle_atol=FTLE_ATOL):
+# Exposure-time sums (<RT>_CET / _MET files): the GPU adds each element's
+# contributions with atomics, in an order of its own, so sums of many terms
+# can differ from ompVC's serial order in their last bits.
+CET_RTOL = 1e-12
+
+# Files whose content in ompVC depends on undefined behaviour.  OutputRT
+# (ompVC/residencetime.c:154) discards the buffer ReadInTraceLaunch returns
+# and reads through the pointer that WriteOutTraceLaunch freed
+# (ompVC/tracers.c:1649-1656, 1689-1695): with glibc's reuse of freed blocks
+# release 0 comes out right and every later release repeats release 0's
+# tracer states.  The engine writes each release's own residence times; these
+# files are compared with the oracle only.
+REFERENCE_UNDEFINED = {("cube", "tracer_rt", "rt.1.bin"), ("tri", "tracer_rt", "rt.1.bin")}
+
+
+def compare_outputs(expected_dir, got_dir, ftle_rtol=FTLE_RTOL, ftle_atol=FTLE_ATOL, skip=(), cet_rtol=0.0):
     exp = sorted(os.listdir(expected_dir))
     got = sorted(f for f in os.listdir(got_dir))
     assert exp == got, f"output files differ: expected {exp}, got {got}"
     for f in exp:
+        if f in skip:
+            continue
         a = open(os.path.join(expected_dir, f), "rb").read()
         b = open(os.path.join(got_dir, f), "rb").read()
-        if f.endswith(".info") or f.endswith("_Cartesian.bin") or f.startswith("tracer"):
+        if (f.endswith((".info", "_Cartesian.bin", "_coordinates.bin", "_ENC.0.bin")) or f.startswith("tracer")
+                or f.startswith("rt.")):
             assert a == b, f"{f}: bytes differ"
+            continue
+        if f.endswith(("_CET.0.bin", "_MET.0.bin")):
+            A, B = np.frombuffer(a, "<f8"), np.frombuffer(b, "<f8")
+            assert len(A) == len(B) and A[0] == B[0], f"{f}: length or time stamp"
+            if cet_rtol == 0.0:
+                assert a == b, f"{f}: bytes differ"
+            else:
+                np.testing.assert_allclose(B[1:], A[1:], rtol=cet_rtol, atol=0, err_msg=f)
             continue
         assert len(a) == len(b), f"{f}: length {len(a)} != {len(b)}"
         A = np.frombuffer(a, "<f8")

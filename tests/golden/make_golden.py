@@ -89,6 +89,12 @@ def cases():
                          **fb(0.1, 1.9, 0.05, 0.95, 0, 0, 19, 10, 1)),
         "tracer_grid": dict(TRACE, Trace_GenerateMesh=1, Output_TRes=5, Output_TDelta=0.2, Trace_IntTLength=0.8,
                             Int_TimeStep=0.01, **tb(0.05, 1.95, 0.05, 0.95, 0, 0, 15, 8, 1)),
+        "tracer_rt": dict(TRACE, Trace_GenerateMesh=1, Output_TRes=5, Output_TDelta=0.2, Trace_IntTLength=0.8,
+                          Int_TimeStep=0.01, Trace_ComputeRT=1, Trace_NumLaunchTimes=2, Trace_LaunchTimeSpacing=0.2,
+                          **tb(0.0, 2.0, 0.05, 0.95, 0, 0, 12, 6, 1)),
+        "tracer_cet": dict(TRACE, Trace_GenerateMesh=1, Output_TRes=5, Output_TDelta=0.2, Trace_IntTLength=0.8,
+                           Int_TimeStep=0.01, Trace_ComputeCET=1, Trace_CETSubsteps=6, Num_threads=1,
+                           **tb(0.05, 1.95, 0.05, 0.95, 0, 0, 15, 8, 1)),
     }))
 
     def cube(d):
@@ -122,6 +128,26 @@ def cases():
                            Int_MaxTimeStep=0.01),
         "ftle_rkf": dict(FTLE, FTLE_IntTLength=0.12, Int_Type=2, Int_Accuracy=1e-6, Int_MinTimeStep=1e-4,
                          Int_MaxTimeStep=0.01, **fb(0, 1, 0, 1, 0, 1, 8, 7, 6)),
+        # residence time (OutputRT): seed list with points outside the mesh,
+        # two releases; and a generated seed grid
+        "tracer_rt": dict(TRACE, Trace_InFile="seeds.txt", Trace_InFileFormat=1, Output_TRes=5, Output_TDelta=0.04,
+                          Trace_IntTLength=0.12, Int_TimeStep=0.005, Trace_NumLaunchTimes=2,
+                          Trace_LaunchTimeSpacing=0.04, Trace_ComputeRT=1),
+        "tracer_rt_grid": dict(TRACE, Trace_GenerateMesh=1, Output_TRes=4, Output_TDelta=0.05, Trace_IntTLength=0.15,
+                               Int_TimeStep=0.005, Trace_ComputeRT=1, **tb(0.0, 1.0, 0.05, 0.95, 0.1, 0.9, 6, 5, 4)),
+        # exposure time (ComputeExposureTime / OutputCET) with RK4, Euler and
+        # RKF; one thread, because ompVC's OpenMP loop adds the sums without
+        # synchronisation
+        "tracer_cet": dict(TRACE, Trace_InFile="seeds.bin", Trace_InFileFormat=4, Output_TRes=4, Output_TDelta=0.05,
+                           Trace_IntTLength=0.15, Int_TimeStep=0.005, Trace_ComputeCET=1, Trace_CETSubsteps=5,
+                           Num_threads=1),
+        "tracer_cet_euler": dict(TRACE, Trace_InFile="seeds.txt", Trace_InFileFormat=1, Output_TRes=4,
+                                 Output_TDelta=0.05, Trace_IntTLength=0.15, Int_TimeStep=0.004, Int_Type=0,
+                                 Trace_NumLaunchTimes=2, Trace_LaunchTimeSpacing=0.05, Trace_ComputeCET=1,
+                                 Trace_CETSubsteps=3, Num_threads=1),
+        "tracer_cet_rkf": dict(TRACE, Trace_InFile="seeds.bin", Trace_InFileFormat=4, Output_TRes=4, Output_TDelta=0.05,
+                               Trace_IntTLength=0.15, Int_Type=2, Int_Accuracy=1e-7, Int_MinTimeStep=1e-4,
+                               Int_MaxTimeStep=0.01, Trace_ComputeCET=1, Trace_CETSubsteps=4, Num_threads=1),
     }))
 
     def c3(d):
@@ -153,8 +179,23 @@ def run_ref(case_dir, name, params):
 
 
 def main():
+    """All cases (inputs regenerated), or with arguments CASE/RUN ... only those
+    runs, on the committed inputs."""
     if not os.path.exists(REF):
         sys.exit("build the reference first: make -f oracle/Makefile.ref")
+    only = [a.split("/") for a in sys.argv[1:]]
+    if only:
+        table = {name: runs for name, _, runs in cases()}
+        for name, rn in only:
+            cd = os.path.join(HERE, name)
+            with open(os.path.join(cd, "params.json")) as f:
+                params = json.load(f)
+            params["runs"][rn] = table[name][rn]
+            with open(os.path.join(cd, "params.json"), "w") as f:
+                json.dump(params, f, indent=1, sort_keys=True)
+            run_ref(cd, rn, dict(params["base"], **params["runs"][rn]))
+            print(name, rn)
+        return
     for name, build, runs in cases():
         cd = os.path.join(HERE, name)
         shutil.rmtree(cd, ignore_errors=True)

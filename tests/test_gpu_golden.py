@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, compare_outputs, golden_cases, run_golden
+from conftest import CET_RTOL, GOLDEN, compare_outputs, golden_cases, run_golden, undefined_files
 
 pytestmark = pytest.mark.gpu
 
@@ -53,14 +53,15 @@ def test_engine_matches_reference(engine, oracle_bin, tmp_path, case, run):
             compare_outputs(os.path.join(GOLDEN, case, "expected", run), got, ftle_rtol=RKF_RTOL,
                             ftle_atol=RKF_ATOL)
         return
-    compare_outputs(os.path.join(GOLDEN, case, "expected", run), got)
+    compare_outputs(os.path.join(GOLDEN, case, "expected", run), got, skip=undefined_files(case, run),
+                    cet_rtol=CET_RTOL)
     os.environ["ORC_DUMP_STATE"] = str(dump_o)
     try:
         orc, _ = run_golden(oracle_bin, case, run, tmp_path)
     finally:
         del os.environ["ORC_DUMP_STATE"]
     # against the oracle: FTLE to a few ulps (CUDA's log vs glibc's), the rest exact
-    compare_outputs(orc, got, ftle_rtol=1e-14, ftle_atol=1e-15)
+    compare_outputs(orc, got, ftle_rtol=1e-14, ftle_atol=1e-15, cet_rtol=CET_RTOL)
     for f in sorted(os.listdir(dump_o)):
         a = np.fromfile(dump_o / f, np.uint8)
         b = np.fromfile(dump_g / f, np.uint8)
