@@ -13,75 +13,14 @@
 
 #include "fvc.h"
 #include "fvc_fpmath.cuh"
-#include "fvc_kernels.h"
+#include "fvc_internal.h"
 
-using namespace fvc;
-
-struct fvc_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  DevMesh mesh{};
-  bool mesh_set = false;
-  DevInteg integ{1, 0.01, 0, 0.0, 0.0, 0.0};
-  bool integ_set = false;
-  DevWindow window{};
-  bool window_set = false;
-  long frame_nodes = 0;  // nodes per frame
-  // device buffers
-  int4* d_elem = nullptr;
-  double* d_geom = nullptr;
-  float* d_geo32 = nullptr;
-  double4_32a* d_nodes = nullptr;
-  int* d_cell_start = nullptr;
-  int* d_cell_ids = nullptr;
-  BucketGrid grid{};
-  std::unordered_map<int, double4_32a*> frames;
-  double* d_stage = nullptr;  // frame upload staging, 3 doubles a node
-  DevCounters* d_ctr = nullptr;
-  double4_32a* d_vt = nullptr;  // stage-time node velocities
-  int vt_slots = 0;
-  // scratch for array calls
-  void* d_scratch = nullptr;
-  size_t scratch_bytes = 0;
-  // mixed-precision form: quantised frames by frame id, the call's step table
-  int prec = 0;
-  struct QFrame {
-    ushort4* q = nullptr;
-    float s[3] = {1.f, 1.f, 1.f};
-    int fmt = 0;
-  };
-  std::unordered_map<int, QFrame> qframes;
-  unsigned* d_qscratch = nullptr;
-  uint4* d_qpair = nullptr;  // the window's two quantised frames, interleaved
-  std::vector<StepM> h_steps;
-  StepM* d_steps = nullptr;
-  size_t steps_cap = 0;
-  int window_lo = -1, window_hi = -1;
-  // exposure time (Trace_CETCompute): per-element sums shared by all releases
-  double* d_cet_sum = nullptr;
-  int* d_cet_enc = nullptr;
-  int cet_sub = 0;  // Trace_CETSubsteps; 0 = off
-  std::string err;
-};
-
-struct fvc_job {
-  fvc_ctx* ctx = nullptr;
-  int kind = 0;  // 0 FTLE, 1 tracers
-  FtleDev f{};
-  TracerDev t{};
-  void* mem = nullptr;  // one allocation for all per-job arrays
-  int prec = 0;         // arithmetic form the job was created with
-  bool packed = false;  // positions held as (X, c) float pairs
-  fvc_job_stats stats{};
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-};
-
-static void job_events(fvc_job* j) {
+void job_events(fvc_job* j) {
   for (int k = 0; k < 4; k++)
     if (!j->ev[k]) cudaEventCreate(&j->ev[k]);
 }
 
-static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+float ev_ms(cudaEvent_t a, cudaEvent_t b) {
   float ms = 0.f;
   if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) ms = 0.f;
   return ms;
@@ -89,7 +28,7 @@ static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
 
 // ------------------------------------------------------------------ helpers
 
-static fvc_status fail(fvc_ctx* c, fvc_status code, const char* fmt, ...) {
+fvc_status fail(fvc_ctx* c, fvc_status code, const char* fmt, ...) {
   if (c) {
     char buf[1024];
     va_list ap;
@@ -101,18 +40,13 @@ static fvc_status fail(fvc_ctx* c, fvc_status code, const char* fmt, ...) {
   return code;
 }
 
-#define FVC_CUDA(c, x)                                                                   \
-  do {                                                                                   \
-    cudaError_t e_ = (x);                                                                \
-    if (e_ != cudaSuccess) return fail((c), FVC_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
-  } while (0)
 
-static fvc_status use_device(fvc_ctx* c) {
+fvc_status use_device(fvc_ctx* c) {
   FVC_CUDA(c, cudaSetDevice(c->device));
   return FVC_OK;
 }
 
-static fvc_status check_launch(fvc_ctx* c, const char* what) {
+fvc_status check_launch(fvc_ctx* c, const char* what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(c, FVC_ERR_CUDA, "%s launch: %s", what, cudaGetErrorString(e));
   return FVC_OK;
@@ -160,7 +94,7 @@ static void drop_quantised(fvc_ctx* c) {
 }
 
 // (X, c) float pairs copied to the host back to FP64 positions X - c.
-static void unpack_host(double* A, size_t n) {
+void unpack_host(double* A, size_t n) {
   for (size_t i = 0; i < n; i++) {
     float p[2];
     memcpy(p, &A[i], sizeof(p));
@@ -432,7 +366,7 @@ extern "C" fvc_status fvc_upload_frame(fvc_ctx* c, int frame_id, const double* u
 
 // The quantised copy of a resident frame in the context's 16-bit format,
 // made on first use after the frame was uploaded or the format changed.
-static fvc_status quantised(fvc_ctx* c, int id, fvc_ctx::QFrame** out) {
+fvc_status quantised(fvc_ctx* c, int id, fvc_ctx::QFrame** out) {
   fvc_ctx::QFrame& q = c->qframes[id];
   if (q.fmt != c->prec) {
     long n = c->frame_nodes;
@@ -482,7 +416,7 @@ extern "C" fvc_status fvc_set_precision(fvc_ctx* c, int precision) {
 
 // RKF needs its parameters; the mixed form runs Euler and RK4 without
 // extrapolation.
-static fvc_status mixed_ok(fvc_ctx* c) {
+fvc_status mixed_ok(fvc_ctx* c) {
   if (c->integ.type == 2 && !(c->integ.acc > 0 && c->integ.hmin > 0 && c->integ.hmax > 0))
     return fail(c, FVC_ERR_ARG, "Int_Type 2 (RKF) needs fvc_set_rkf before advecting");
   if (!c->prec) return FVC_OK;

@@ -1,0 +1,1132 @@
+// fvc_batch.cu -- batched and served advection: many tracer, residence-time
+// and FTLE jobs with their own seeds and integration windows, advanced
+// together over the frames resident on the device.
+//
+// Schedule.  Time advances in ticks.  In one tick every active job runs its
+// next frame interval -- exactly the interval ompVC's frame loop would give
+// it (ompVC/main.c:170-227: the window [t_k, t_k+1] of two frames, the step
+// sequence restarted at the interval's start and clipped at its end) -- so a
+// job's arithmetic does not depend on which other jobs share its ticks:
+// its results are identical alone and in any mix.  Jobs are admitted
+// between ticks as device memory allows (an HBM budget over the jobs'
+// footprints) and retired when their window ends; a fixed set of jobs can
+// instead be captured whole into one CUDA graph.
+//
+// Device work per tick: one compaction kernel appends the live points of
+// every active job to the tick's work queue (warp ballots, one atomic per
+// warp), one persistent kernel advects the queue (each warp takes 32 entries
+// at a time from a cursor), then each FTLE job runs its early-FTLE passes
+// and update (the per-interval body of ComputeFTLE, ompVC/ftle.c:109-175)
+// and, after its last interval, the FTLE reduction.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <deque>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "fvc_fpmath.cuh"
+#include "fvc_internal.h"
+#include "fvc_mixed_impl.cuh"
+
+namespace fvc {
+
+// The mixed form's view of one job's interval: the two frames' quantised
+// pair records with their scales, and the interval's step table.
+struct WinQ {
+  const uint4* qp;
+  float qs0[3], qs1[3];
+  int qfmt;
+  const StepM* steps;
+  int nsteps;
+};
+
+// One job's work in one tick, as the kernels see it.
+struct BJob {
+  int kind;             // 0 tracers (state advanced in place), 1 FTLE pass 1
+  int n;                // points
+  long long group0;     // first 32-point group of the job in the compaction grid
+  double* X;            // positions (FP64, or (X, c) float pairs in the mixed form)
+  int* eid;
+  int* left;
+  double* ldt;
+  double* Xn;           // FTLE pass-1 outputs
+  int* en;
+  double* te;
+  unsigned char* flag;
+  DevCounters* ctr;     // the job's own counters
+  double t1, t2;        // the interval's integration range
+  const double4_32a* f0;  // FP64 window
+  const double4_32a* f1;
+  double tmin, tmax, rspan;
+  WinQ q;
+  const DevWindow* w;   // FP64 form: the job's window (two frames, no stage table)
+};
+
+struct BatchCtr {
+  int nqueue;
+  int cursor;
+};
+
+// The tick's work queue: (job, point) of every live point of every job
+// (ldt > -TINY and not left, ompVC/ftle.c:113, tracers.c:225); FTLE jobs'
+// per-interval flags are cleared on the way.
+__global__ void k_batch_compact(const BJob* __restrict__ jobs, int njobs, long long ngroups, int2* queue,
+                                BatchCtr* bc) {
+  const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (g >= ngroups) return;  // uniform per warp
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].group0 <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  const BJob& J = jobs[lo];
+  const long i = (long)(g - J.group0) * 32 + lane;
+  bool live = false;
+  if (i < J.n) {
+    live = J.ldt[i] > -FVC_TINY && !J.left[i];
+    if (J.kind == 1) J.flag[i] = 0;
+  }
+  const unsigned b = __ballot_sync(0xffffffffu, live);
+  int base = 0;
+  if (lane == 0 && b) base = atomicAdd(&bc->nqueue, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (live) queue[base + __popc(b & ((1u << lane) - 1u))] = make_int2(lo, (int)i);
+}
+
+// Accepted steps and fault bits of the warp's 32 entries, added to each
+// job's counters once per job present in the warp.
+__device__ __forceinline__ void flush_jobs(const BJob* jobs, int jid, unsigned steps, int err) {
+  const unsigned grp = __match_any_sync(0xffffffffu, jid);
+  const unsigned s = __reduce_add_sync(grp, steps);
+  const int e = (int)__reduce_or_sync(grp, (unsigned)err);
+  if (jid >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) {
+    DevCounters* c = jobs[jid].ctr;
+    if (s) atomicAdd(&c->steps, (unsigned long long)s);
+    if (e) atomicOr(&c->status, e);
+  }
+}
+
+// The persistent advection of the mixed form over the tick's queue.
+template <int D>
+__global__ void __launch_bounds__(256) k_batch_advance_mx(DevMesh m, int type, const BJob* __restrict__ jobs,
+                                                         const int2* __restrict__ queue, BatchCtr* bc) {
+  const long nq = *(volatile int*)&bc->nqueue;
+  for (long base = warp_grab(&bc->cursor); base < nq; base = warp_grab(&bc->cursor)) {
+    const long idx = base + (threadIdx.x & 31);
+    int jid = -1, err = 0;
+    unsigned steps = 0;
+    if (idx < nq) {
+      const int2 e = queue[idx];
+      jid = e.x;
+      const BJob& J = jobs[jid];
+      const long p = e.y;
+      PtM t;
+      load_pos_pair(J.X, p, t.X, t.c);
+      t.eid = J.eid[p];
+      t.left = J.left[p];
+      t.ldt = J.ldt[p];
+      const WinQ w = J.q;
+      advect_mx<D>(m, w, type, t, w.nsteps, steps, err);
+      if (J.kind == 0) {
+        store_pos_pair(J.X, p, t.X, t.c);
+        J.eid[p] = t.eid;
+        J.left[p] = t.left;
+        J.ldt[p] = t.ldt;
+      } else {
+        J.flag[p] = 1 | (t.left ? 6 : 0);
+        store_pos_pair(J.Xn, p, t.X, t.c);
+        J.en[p] = t.eid;
+        J.te[p] = t.ldt;
+      }
+    }
+    flush_jobs(jobs, jid, steps, err);
+  }
+}
+
+// The same in the FP64 form (ompVC's arithmetic): each stage interpolates the
+// job's two frames itself (the window carries no stage-time table).
+template <int D>
+__global__ void __launch_bounds__(256, FVC_MINBLOCKS / 2) k_batch_advance(DevMesh m, DevInteg in,
+                                                                      const BJob* __restrict__ jobs,
+                                                                      const int2* __restrict__ queue,
+                                                                      BatchCtr* bc) {
+  const long nq = *(volatile int*)&bc->nqueue;
+  for (long base = warp_grab(&bc->cursor); base < nq; base = warp_grab(&bc->cursor)) {
+    const long idx = base + (threadIdx.x & 31);
+    int jid = -1, err = 0;
+    unsigned steps = 0;
+    if (idx < nq) {
+      const int2 e = queue[idx];
+      jid = e.x;
+      const BJob& J = jobs[jid];
+      const long p = e.y;
+      Pt t;
+      load_pt(t, p, J.X, nullptr, J.eid, J.left, J.ldt);
+      err = advect<D, 1>(m, *J.w, in, t, J.t1, J.t2, steps);
+      if (J.kind == 0) {
+        J.X[3 * p] = t.X[0];
+        J.X[3 * p + 1] = t.X[1];
+        J.X[3 * p + 2] = t.X[2];
+        J.eid[p] = t.eid;
+        J.left[p] = t.left;
+        J.ldt[p] = t.ldt;
+      } else {
+        J.flag[p] = 1 | (t.left ? 6 : 0);
+        J.Xn[3 * p] = t.X[0];
+        J.Xn[3 * p + 1] = t.X[1];
+        J.Xn[3 * p + 2] = t.X[2];
+        J.en[p] = t.eid;
+        J.te[p] = t.ldt;
+      }
+    }
+    flush_jobs(jobs, jid, steps, err);
+  }
+}
+
+// Launch geometry of the persistent advection, chosen by the autotuner.
+struct BatchLaunch {
+  int threads;  // block size
+  int blocks;   // grid (resident blocks, or fewer)
+};
+
+static unsigned batch_resident(int dims, int prec, int threads) {
+  if (prec) return dims == 3 ? resident_blocks(k_batch_advance_mx<3>, threads)
+                             : resident_blocks(k_batch_advance_mx<2>, threads);
+  return dims == 3 ? resident_blocks(k_batch_advance<3>, threads) : resident_blocks(k_batch_advance<2>, threads);
+}
+
+static void batch_advance(const DevMesh& m, const DevInteg& in, const BJob* jobs, const int2* queue, BatchCtr* bc,
+                          const BatchLaunch& L, cudaStream_t s) {
+  if (m.prec) {
+    if (m.dims == 3) k_batch_advance_mx<3><<<L.blocks, L.threads, 0, s>>>(m, in.type, jobs, queue, bc);
+    else k_batch_advance_mx<2><<<L.blocks, L.threads, 0, s>>>(m, in.type, jobs, queue, bc);
+  } else {
+    if (m.dims == 3) k_batch_advance<3><<<L.blocks, L.threads, 0, s>>>(m, in, jobs, queue, bc);
+    else k_batch_advance<2><<<L.blocks, L.threads, 0, s>>>(m, in, jobs, queue, bc);
+  }
+}
+
+}  // namespace fvc
+
+// ====================================================================== host
+
+namespace {
+
+constexpr double kTiny = 1.0e-10;
+
+enum { JQ_QUEUED = 0, JQ_ACTIVE = 1, JQ_FINISHING = 2, JQ_DONE = 3, JQ_FAILED = 4, JQ_RELEASED = 5 };
+
+struct HostJob {
+  int id = 0;
+  int kind = 0;  // FVC_JOB_*
+  int state = JQ_QUEUED;
+  fvc_batch_job_spec spec{};
+  std::vector<double> seeds;
+  fvc_job* job = nullptr;
+  int slot = -1;
+  int dir = 1;
+  double stop = 0.0, T = 0.0;
+  long long df = 0;      // next frame interval (unwrapped index), moving in dir
+  bool launched = false;
+  size_t bytes = 0;
+  cudaEvent_t done = nullptr;
+  long long ticks = 0;
+  long npts = 0;  // points (work-queue entries at most)
+  fvc_status err = FVC_OK;
+  std::string msg;
+};
+
+// A frame pair's quantised records (the mixed form's window of one interval).
+struct PairQ {
+  uint4* q = nullptr;
+  float s0[3], s1[3];
+  int fmt = 0;
+};
+
+// Per-point device bytes of a job (the carve lists of fvc_tracer_create /
+// fvc_ftle_create, rounded up) and the seed-chain scratch.
+size_t job_bytes(int kind, long n) {
+  if (kind == FVC_JOB_FTLE) return (size_t)n * 560 + (1u << 20);
+  return (size_t)n * 130 + (1u << 20);
+}
+
+}  // namespace
+
+struct fvc_batch {
+  fvc_ctx* c = nullptr;
+  fvc_batch_opts o{};
+  std::vector<std::unique_ptr<HostJob>> jobs;
+  std::deque<int> queued;
+  std::vector<int> active;
+  std::vector<int> finishing;
+  size_t used = 0;
+  int max_jobs = 1024;
+  // device state
+  DevCounters* d_ctrs = nullptr;  // one block per job slot
+  DevCounters* h_ctrs = nullptr;  // pinned copies, written after each job's last tick
+  std::vector<int> free_slots;
+  BatchCtr* d_bc = nullptr;
+  int2* d_queue = nullptr;
+  size_t queue_cap = 0;  // entries
+  size_t queue_need = 0;
+  char* d_tick = nullptr;
+  size_t tick_cap = 0;
+  char* h_tick[2] = {nullptr, nullptr};
+  size_t h_cap[2] = {0, 0};
+  cudaEvent_t h_ev[2] = {nullptr, nullptr};
+  int hbuf = 0;
+  std::map<std::pair<int, int>, PairQ> pairs;
+  std::vector<cudaEvent_t> tick_ev;  // ring of the last ticks, for the in-flight limit
+  cudaEvent_t t_start = nullptr, t_end = nullptr;
+  BatchLaunch launch{128, 0};
+  fvc_batch_stats stats{};
+};
+
+using namespace fvc;
+
+static int frame_mod(const fvc_batch* b, long long frame) {
+  long long per = b->o.tres - 1;
+  long long m = frame % per;
+  if (m < 0) m += per;
+  return (int)m;
+}
+
+static fvc_status batch_fail(fvc_batch* b, fvc_status code, const char* what) {
+  return fail(b->c, code, "%s", what);
+}
+
+// One interval of a job: (frame_lo, tmin, tmax) of interval df, the
+// integration range and whether it is the job's last (flow of
+// ompVC/main.c:170-227 with one FTLE slide or one tracer release).
+struct Interval {
+  long long lo;
+  double tmin, tmax, t1, t2;
+  bool launch, last;
+};
+
+static Interval interval_of(const fvc_batch* b, const HostJob& J) {
+  Interval I{};
+  I.lo = J.dir > 0 ? J.df : J.df - 1;
+  I.tmin = b->o.tmin + (double)I.lo * b->o.tdelta;
+  I.tmax = I.tmin + b->o.tdelta;
+  I.launch = !J.launched;
+  const double t0 = J.spec.t_start;
+  I.t1 = I.launch ? t0 : (J.dir > 0 ? I.tmin : I.tmax);
+  I.t2 = J.dir > 0 ? std::min(I.tmax, J.stop) : std::max(I.tmin, J.stop);
+  I.last = (J.dir > 0 ? (J.stop - I.tmax) : (I.tmin - J.stop)) < kTiny;
+  return I;
+}
+
+// The first frame interval of a window starting at t0 (ompVC/parameters.c:
+// 322-333 for one slide).
+static long long first_interval(const fvc_batch* b, double t0, int dir) {
+  double x = (t0 - b->o.tmin) / b->o.tdelta;
+  return dir > 0 ? (long long)floor(x) : (long long)ceil(x);
+}
+
+// The mixed form's step table of [t1, t2] in the window [tmin, tmax]: the
+// stage times of the FP64 step loop (ompVC/integration.c:345-352, 402), as
+// the single-job calls build it.
+static bool build_steps_for(double h0, double tmin, double tmax, double t1, double t2, std::vector<StepM>& T) {
+  T.clear();
+  auto tloc = [&](double tq, float& out) {
+    double tl = (tq - tmin) / (tmax - tmin);
+    if ((tl > 1 + 1.0e-10) || (tl < 0 - 1.0e-10)) return false;
+    out = (float)tl;
+    return true;
+  };
+  double tc = t1, h = (t2 - t1) >= 0.0 ? fabs(h0) : -fabs(h0);
+  while ((tc - t2) * (t2 - t1) < 0.0) {
+    if ((tc + h - t2) * (tc + h - t1) > 0.0) h = (t2 - t1) >= 0.0 ? fabs(t2 - tc) : -fabs(t2 - tc);
+    StepM s{};
+    s.tc = tc;
+    s.h = (float)h;
+    if (!tloc(tc, s.tl0) || !tloc(tc + h / 2, s.tlh) || !tloc(tc + h, s.tl1)) return false;
+    T.push_back(s);
+    tc = tc + h;
+  }
+  StepM e{};
+  e.tc = tc;
+  T.push_back(e);
+  return true;
+}
+
+static fvc_status ensure_pair(fvc_batch* b, int lo, int hi, PairQ** out) {
+  fvc_ctx* c = b->c;
+  auto key = std::make_pair(lo, hi);
+  PairQ& P = b->pairs[key];
+  if (!P.q || P.fmt != c->prec) {
+    fvc_ctx::QFrame *qa = nullptr, *qb = nullptr;
+    if (!c->frames.count(lo) || !c->frames.count(hi)) return fail(c, FVC_ERR_STATE, "frames %d / %d are not resident", lo, hi);
+    fvc_status st;
+    if ((st = quantised(c, lo, &qa)) || (st = quantised(c, hi, &qb))) return st;
+    if (!P.q && cudaMalloc(&P.q, sizeof(uint4) * (size_t)c->frame_nodes) != cudaSuccess) {
+      P.q = nullptr;
+      return fail(c, FVC_ERR_OOM, "quantised frame pair");
+    }
+    pair_frames(qa->q, qb->q, c->frame_nodes, P.q, c->stream);
+    if ((st = check_launch(c, "pair frames"))) return st;
+    for (int k = 0; k < 3; k++) {
+      P.s0[k] = qa->s[k];
+      P.s1[k] = qb->s[k];
+    }
+    P.fmt = c->prec;
+  }
+  *out = &P;
+  return FVC_OK;
+}
+
+// The host view of a job's window for the per-job kernels (launch velocity,
+// early FTLE): FP64 frames without a stage table, or the quantised pair and
+// the interval's step table at d_steps.
+static fvc_status job_window(fvc_batch* b, const Interval& I, const StepM* d_steps, int nsteps, DevWindow& w,
+                             BJob& J) {
+  fvc_ctx* c = b->c;
+  const int flo = frame_mod(b, I.lo), fhi = frame_mod(b, I.lo + 1);
+  auto a = c->frames.find(flo), z = c->frames.find(fhi);
+  if (a == c->frames.end() || z == c->frames.end())
+    return fail(c, FVC_ERR_STATE, "frames %d / %d are not resident", flo, fhi);
+  memset(&w, 0, sizeof(w));
+  w.f0 = a->second;
+  w.f1 = z->second;
+  w.tmin = I.tmin;
+  w.tmax = I.tmax;
+  w.rspan = rcp_for_div(I.tmax - I.tmin);
+  w.nslots = 0;
+  J.f0 = w.f0;
+  J.f1 = w.f1;
+  J.tmin = w.tmin;
+  J.tmax = w.tmax;
+  J.rspan = w.rspan;
+  J.t1 = I.t1;
+  J.t2 = I.t2;
+  memset(&J.q, 0, sizeof(J.q));
+  if (c->prec) {
+    PairQ* P = nullptr;
+    fvc_status st;
+    if ((st = ensure_pair(b, flo, fhi, &P))) return st;
+    w.qp = P->q;
+    for (int k = 0; k < 3; k++) {
+      w.qs0[k] = P->s0[k];
+      w.qs1[k] = P->s1[k];
+    }
+    w.qfmt = c->prec;
+    w.steps = d_steps;
+    w.nsteps = nsteps;
+    J.q.qp = w.qp;
+    memcpy(J.q.qs0, w.qs0, sizeof(w.qs0));
+    memcpy(J.q.qs1, w.qs1, sizeof(w.qs1));
+    J.q.qfmt = w.qfmt;
+    J.q.steps = d_steps;
+    J.q.nsteps = nsteps;
+  }
+  return FVC_OK;
+}
+
+// ------------------------------------------------------------ admission
+
+static fvc_status admit_one(fvc_batch* b, HostJob& J) {
+  fvc_ctx* c = b->c;
+  fvc_status st;
+  if (J.kind == FVC_JOB_FTLE) {
+    fvc_ftle_spec sp = J.spec.grid;
+    sp.start_time = J.spec.t_start;
+    sp.stop_time = J.stop;
+    sp.generate = 1;
+    st = fvc_ftle_create(c, &sp, &J.job);
+  } else {
+    fvc_tracer_spec sp{};
+    sp.local_search_checking = J.spec.local_search_checking;
+    sp.seed_chain = 0;
+    st = fvc_tracer_create(c, &sp, J.spec.n, J.seeds.data(), &J.job);
+  }
+  if (st) return st;
+  J.slot = b->free_slots.back();
+  b->free_slots.pop_back();
+  FVC_CUDA(c, cudaMemsetAsync(b->d_ctrs + J.slot, 0, sizeof(DevCounters), c->stream));
+  if (!J.done) cudaEventCreateWithFlags(&J.done, cudaEventDisableTiming);
+  J.df = first_interval(b, J.spec.t_start, J.dir);
+  J.launched = false;
+  J.state = JQ_ACTIVE;
+  b->used += J.bytes;
+  J.npts = J.kind == FVC_JOB_FTLE ? J.job->f.n : J.job->t.n;
+  b->queue_need += (size_t)J.npts;
+  b->active.push_back(J.id);
+  return FVC_OK;
+}
+
+// Admits queued jobs in submission order while their footprint fits the
+// budget (a job larger than the whole budget runs alone) and slots are free.
+static fvc_status admit(fvc_batch* b) {
+  while (!b->queued.empty()) {
+    HostJob& J = *b->jobs[b->queued.front()];
+    const bool alone = b->active.empty() && b->finishing.empty();
+    if (b->o.hbm_budget > 0 && b->used + J.bytes > (size_t)b->o.hbm_budget && !alone) break;
+    if (b->free_slots.empty()) break;
+    b->queued.pop_front();
+    fvc_status st = admit_one(b, J);
+    if (st) {
+      J.state = JQ_FAILED;
+      J.err = st;
+      J.msg = b->c->err;
+      if (J.job) {
+        fvc_job_destroy(J.job);
+        J.job = nullptr;
+      }
+    }
+  }
+  if (b->queue_need > b->queue_cap) {
+    fvc_ctx* c = b->c;
+    FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(b->d_queue);
+    b->d_queue = nullptr;
+    size_t cap = std::max(b->queue_need, (size_t)2 * b->queue_cap);
+    if (cudaMalloc(&b->d_queue, sizeof(int2) * cap) != cudaSuccess) {
+      b->queue_cap = 0;
+      return fail(c, FVC_ERR_OOM, "batch work queue (%zu entries)", cap);
+    }
+    b->queue_cap = cap;
+  }
+  return FVC_OK;
+}
+
+// ------------------------------------------------------------ one tick
+
+// The tick's descriptors (BJob array, then the step tables) in a host blob,
+// with the device address each part will have at dev_base.
+struct TickPlan {
+  std::vector<char> blob;
+  std::vector<int> ids;           // job ids in BJob order
+  std::vector<Interval> iv;
+  std::vector<DevWindow> win;     // per job (launch velocity, early FTLE)
+  long long ngroups = 0;
+};
+
+static size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+static fvc_status plan_tick(fvc_batch* b, const std::vector<int>& ids, char* dev_base, TickPlan& P) {
+  fvc_ctx* c = b->c;
+  P.ids = ids;
+  const size_t nj = ids.size();
+  P.iv.resize(nj);
+  P.win.resize(nj);
+  std::vector<BJob> J(nj);
+  std::vector<std::vector<StepM>> tabs(nj);
+  size_t off = al16(sizeof(BJob) * nj);
+  const size_t woff = off;  // FP64 form: the jobs' windows
+  if (!c->prec) off = al16(off + sizeof(DevWindow) * nj);
+  std::vector<size_t> toff(nj, 0);
+  for (size_t k = 0; k < nj; k++) {
+    HostJob& H = *b->jobs[ids[k]];
+    P.iv[k] = interval_of(b, H);
+    if (c->prec) {
+      if (!build_steps_for(c->integ.h, P.iv[k].tmin, P.iv[k].tmax, P.iv[k].t1, P.iv[k].t2, tabs[k]))
+        return fail(c, FVC_ERR_TLOC, "batch job %d: query time outside the loaded frame interval", H.id);
+      toff[k] = off;
+      off = al16(off + sizeof(StepM) * tabs[k].size());
+    }
+  }
+  P.blob.assign(off, 0);
+  long long groups = 0;
+  for (size_t k = 0; k < nj; k++) {
+    HostJob& H = *b->jobs[ids[k]];
+    BJob& B = J[k];
+    memset(&B, 0, sizeof(B));
+    const StepM* dsteps = c->prec ? (const StepM*)(dev_base + toff[k]) : nullptr;
+    fvc_status st = job_window(b, P.iv[k], dsteps, c->prec ? (int)tabs[k].size() - 1 : 0, P.win[k], B);
+    if (st) return st;
+    B.ctr = b->d_ctrs + H.slot;
+    B.group0 = groups;
+    if (H.kind == FVC_JOB_FTLE) {
+      const FtleDev& f = H.job->f;
+      B.kind = 1;
+      B.n = f.n;
+      B.X = f.X;
+      B.eid = f.eid;
+      B.left = f.left;
+      B.ldt = f.ldt;
+      B.Xn = f.Xn;
+      B.en = f.en;
+      B.te = f.te;
+      B.flag = f.flag;
+    } else {
+      const TracerDev& t = H.job->t;
+      B.kind = 0;
+      B.n = t.n;
+      B.X = t.X;
+      B.eid = t.eid;
+      B.left = t.left;
+      B.ldt = t.ldt;
+    }
+    groups += (B.n + 31) / 32;
+    if (c->prec) {
+      memcpy(P.blob.data() + toff[k], tabs[k].data(), sizeof(StepM) * tabs[k].size());
+    } else {
+      memcpy(P.blob.data() + woff + sizeof(DevWindow) * k, &P.win[k], sizeof(DevWindow));
+      B.w = (const DevWindow*)(dev_base + woff + sizeof(DevWindow) * k);
+    }
+  }
+  memcpy(P.blob.data(), J.data(), sizeof(BJob) * nj);
+  P.ngroups = groups;
+  return FVC_OK;
+}
+
+// Enqueues a planned tick whose descriptors are at d_jobs on the stream.
+static fvc_status enqueue_tick(fvc_batch* b, const TickPlan& P, const BJob* d_jobs, bool counters_cleared) {
+  fvc_ctx* c = b->c;
+  cudaStream_t s = c->stream;
+  const size_t nj = P.ids.size();
+  if (!counters_cleared) FVC_CUDA(c, cudaMemsetAsync(b->d_bc, 0, sizeof(BatchCtr), s));
+  // releases / slide launches: the velocity at the start time
+  for (size_t k = 0; k < nj; k++) {
+    HostJob& H = *b->jobs[P.ids[k]];
+    if (!P.iv[k].launch) continue;
+    if (H.kind == FVC_JOB_FTLE) ftle_launch(c->mesh, P.win[k], H.job->f, H.job->f.start, b->d_ctrs + H.slot, s);
+    else tracer_launch_vel(c->mesh, P.win[k], H.job->t, H.spec.t_start, b->d_ctrs + H.slot, s);
+    b->stats.launches++;
+  }
+  if (P.ngroups > 0) {
+    const unsigned nb = (unsigned)((P.ngroups + 7) / 8);
+    k_batch_compact<<<nb, 256, 0, s>>>(d_jobs, (int)nj, P.ngroups, b->d_queue, b->d_bc);
+    batch_advance(c->mesh, c->integ, d_jobs, b->d_queue, b->d_bc, b->launch, s);
+    b->stats.launches += 2;
+  }
+  for (size_t k = 0; k < nj; k++) {
+    HostJob& H = *b->jobs[P.ids[k]];
+    if (H.kind != FVC_JOB_FTLE) continue;
+    DevCounters* ctr = b->d_ctrs + H.slot;
+    const FtleDev& f = H.job->f;
+    // the task lists' work cursors start at 0 every interval
+    FVC_CUDA(c, cudaMemsetAsync(ctr->cur, 0, sizeof(ctr->cur), s));
+    ftle_triggers(f, ctr, s);
+    ftle_early(c->mesh, P.win[k], c->integ, f, P.iv[k].t1, ctr, s);
+    ftle_update(c->mesh, c->integ, f, s);
+    b->stats.launches += 10;
+    if (P.iv[k].last) {
+      if (H.job->packed) {
+        unpack_pairs(H.job->f.X, 3L * f.n, s);
+        H.job->packed = false;
+        b->stats.launches++;
+      }
+      ftle_final(f, c->mesh.dims, H.T, s);
+      b->stats.launches++;
+    }
+  }
+  return check_launch(c, "batch tick");
+}
+
+// Bookkeeping after a tick was planned and enqueued: interval cursors, jobs
+// whose window ended move to the finishing list with an event behind them.
+static void advance_cursors(fvc_batch* b, const TickPlan& P) {
+  std::vector<int> still;
+  for (size_t k = 0; k < P.ids.size(); k++) {
+    HostJob& H = *b->jobs[P.ids[k]];
+    H.launched = true;
+    H.df += H.dir;
+    H.ticks++;
+    if (P.iv[k].last) {
+      cudaMemcpyAsync(b->h_ctrs + H.slot, b->d_ctrs + H.slot, sizeof(DevCounters), cudaMemcpyDeviceToHost,
+                      b->c->stream);
+      cudaEventRecord(H.done, b->c->stream);
+      H.state = JQ_FINISHING;
+      b->queue_need -= (size_t)H.npts;
+      b->finishing.push_back(H.id);
+    } else {
+      still.push_back(H.id);
+    }
+  }
+  b->active.swap(still);
+}
+
+// Device room for a tick's descriptors (waits for the ticks in flight when
+// it has to grow).
+static fvc_status ensure_tick_cap(fvc_batch* b, size_t bytes) {
+  fvc_ctx* c = b->c;
+  if (bytes > b->tick_cap) {
+    FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(b->d_tick);
+    b->d_tick = nullptr;
+    size_t cap = std::max(bytes, (size_t)2 * b->tick_cap);
+    if (cudaMalloc(&b->d_tick, cap) != cudaSuccess) {
+      b->tick_cap = 0;
+      return fail(c, FVC_ERR_OOM, "batch descriptors");
+    }
+    b->tick_cap = cap;
+  }
+  return FVC_OK;
+}
+
+static fvc_status stage_upload(fvc_batch* b, const std::vector<char>& blob) {
+  fvc_ctx* c = b->c;
+  const size_t bytes = blob.size();
+  fvc_status st;
+  if ((st = ensure_tick_cap(b, bytes))) return st;
+  int k = b->hbuf;
+  b->hbuf ^= 1;
+  FVC_CUDA(c, cudaEventSynchronize(b->h_ev[k]));
+  if (bytes > b->h_cap[k]) {
+    cudaFreeHost(b->h_tick[k]);
+    b->h_tick[k] = nullptr;
+    size_t cap = std::max(bytes, (size_t)2 * b->h_cap[k]);
+    if (cudaMallocHost(&b->h_tick[k], cap) != cudaSuccess) {
+      b->h_cap[k] = 0;
+      return fail(c, FVC_ERR_OOM, "pinned batch staging");
+    }
+    b->h_cap[k] = cap;
+  }
+  memcpy(b->h_tick[k], blob.data(), bytes);
+  FVC_CUDA(c, cudaMemcpyAsync(b->d_tick, b->h_tick[k], bytes, cudaMemcpyHostToDevice, c->stream));
+  FVC_CUDA(c, cudaEventRecord(b->h_ev[k], c->stream));
+  return FVC_OK;
+}
+
+// Retires finishing jobs whose last tick has completed: reads their counters
+// and marks them done (or failed with the counters' fault).
+static void retire(fvc_batch* b, bool wait) {
+  std::vector<int> still;
+  for (int id : b->finishing) {
+    HostJob& H = *b->jobs[id];
+    cudaError_t q = wait ? cudaEventSynchronize(H.done) : cudaEventQuery(H.done);
+    if (q == cudaErrorNotReady) {
+      still.push_back(id);
+      continue;
+    }
+    const DevCounters h = b->h_ctrs[H.slot];
+    H.job->stats.steps_main += (long long)h.steps;
+    H.job->stats.steps_early += (long long)h.steps_early;
+    H.job->stats.intervals += H.ticks;
+    b->stats.steps += (long long)(h.steps + h.steps_early);
+    b->stats.jobs_done++;
+    if (q != cudaSuccess) {
+      H.state = JQ_FAILED;
+      H.err = FVC_ERR_CUDA;
+      H.msg = cudaGetErrorString(q);
+    } else if (h.status) {
+      H.state = JQ_FAILED;
+      H.err = (h.status & PT_ERR_STATE) ? FVC_ERR_STATE : (h.status & PT_ERR_TLOC) ? FVC_ERR_TLOC : FVC_ERR_WALK;
+      H.msg = "device fault while advancing the job";
+    } else {
+      H.state = JQ_DONE;
+    }
+  }
+  b->finishing.swap(still);
+}
+
+static fvc_status tick(fvc_batch* b) {
+  fvc_ctx* c = b->c;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  retire(b, false);
+  if ((st = admit(b))) return st;
+  if (b->active.empty()) return FVC_OK;
+  TickPlan P;
+  if ((st = plan_tick(b, b->active, b->d_tick, P))) return st;
+  // the step tables' device addresses depend on where the blob lands
+  if (P.blob.size() > b->tick_cap) {
+    if ((st = ensure_tick_cap(b, P.blob.size()))) return st;
+    if ((st = plan_tick(b, b->active, b->d_tick, P))) return st;
+  }
+  if ((st = stage_upload(b, P.blob))) return st;
+  if ((st = enqueue_tick(b, P, (const BJob*)b->d_tick, false))) return st;
+  advance_cursors(b, P);
+  // at most two ticks in flight: the host plans the next while one runs
+  cudaEvent_t& e = b->tick_ev[b->stats.ticks % b->tick_ev.size()];
+  if (b->stats.ticks >= (long long)b->tick_ev.size()) FVC_CUDA(c, cudaEventSynchronize(e));
+  FVC_CUDA(c, cudaEventRecord(e, c->stream));
+  b->stats.ticks++;
+  return FVC_OK;
+}
+
+// --------------------------------------------------------------- autotune
+
+// Times the persistent advection of one planned tick for each candidate
+// block size (and half occupancy) on a copy of the jobs' state and keeps the
+// fastest.  The state is restored afterwards, so tuning changes no result.
+static fvc_status autotune(fvc_batch* b) {
+  fvc_ctx* c = b->c;
+  if (b->active.empty()) return FVC_OK;
+  fvc_status st;
+  TickPlan P;
+  if ((st = plan_tick(b, b->active, b->d_tick, P))) return st;
+  if (P.blob.size() > b->tick_cap) {
+    if ((st = ensure_tick_cap(b, P.blob.size()))) return st;
+    if ((st = plan_tick(b, b->active, b->d_tick, P))) return st;
+  }
+  if ((st = stage_upload(b, P.blob))) return st;
+  // snapshot every job's mutable state
+  std::vector<std::pair<void*, size_t>> regions;
+  size_t total = 0;
+  for (int id : b->active) {
+    HostJob& H = *b->jobs[id];
+    size_t n = H.kind == FVC_JOB_FTLE ? (size_t)H.job->f.n : (size_t)H.job->t.n;
+    if (H.kind == FVC_JOB_FTLE) {
+      regions.push_back({H.job->f.Xn, 24 * n});
+      regions.push_back({H.job->f.en, 4 * n});
+      regions.push_back({H.job->f.te, 8 * n});
+      regions.push_back({H.job->f.flag, n});
+    } else {
+      regions.push_back({H.job->t.X, 24 * n});
+      regions.push_back({H.job->t.eid, 4 * n});
+      regions.push_back({H.job->t.left, 4 * n});
+      regions.push_back({H.job->t.ldt, 8 * n});
+    }
+    regions.push_back({b->d_ctrs + H.slot, sizeof(DevCounters)});
+  }
+  for (auto& r : regions) total += r.second;
+  char* save = nullptr;
+  if (cudaMalloc(&save, total) != cudaSuccess) return FVC_OK;  // no room to tune: keep the default
+  size_t o = 0;
+  for (auto& r : regions) {
+    cudaMemcpyAsync(save + o, r.first, r.second, cudaMemcpyDeviceToDevice, c->stream);
+    o += r.second;
+  }
+  const BJob* dj = (const BJob*)b->d_tick;
+  const int cand_threads[3] = {64, 128, 256};
+  float best = 1e30f;
+  BatchLaunch bestL = b->launch;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int ti = 0; ti < 3; ti++) {
+    const unsigned res = batch_resident(c->mesh.dims, c->prec, cand_threads[ti]);
+    for (int half = 0; half < 2; half++) {
+      BatchLaunch L{cand_threads[ti], (int)std::max(1u, half ? res / 2 : res)};
+      cudaMemsetAsync(b->d_bc, 0, sizeof(BatchCtr), c->stream);
+      const unsigned nb = (unsigned)((P.ngroups + 7) / 8);
+      k_batch_compact<<<nb, 256, 0, c->stream>>>(dj, (int)P.ids.size(), P.ngroups, b->d_queue, b->d_bc);
+      cudaEventRecord(e0, c->stream);
+      batch_advance(c->mesh, c->integ, dj, b->d_queue, b->d_bc, L, c->stream);
+      cudaEventRecord(e1, c->stream);
+      // restore before the next candidate
+      o = 0;
+      for (auto& r : regions) {
+        cudaMemcpyAsync(r.first, save + o, r.second, cudaMemcpyDeviceToDevice, c->stream);
+        o += r.second;
+      }
+      if (cudaStreamSynchronize(c->stream) != cudaSuccess) break;
+      float ms = ev_ms(e0, e1);
+      if (ms > 0 && ms < best) {
+        best = ms;
+        bestL = L;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(save);
+  b->launch = bestL;
+  b->stats.tuned_threads = bestL.threads;
+  b->stats.tuned_blocks = bestL.blocks;
+  return check_launch(c, "batch autotune");
+}
+
+// ============================================================== C ABI
+
+extern "C" fvc_status fvc_batch_create(fvc_ctx* c, const fvc_batch_opts* o, fvc_batch** out) {
+  if (!c || !o || !out) return FVC_ERR_ARG;
+  *out = nullptr;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  if (!c->mesh_set || c->mesh.mesh_type != 1) return fail(c, FVC_ERR_STATE, "the batch form needs an unstructured mesh");
+  if (o->tres < 2 || !(o->tdelta > 0)) return fail(c, FVC_ERR_ARG, "batch time axis: tres >= 2 and tdelta > 0");
+  if (c->integ.type != 0 && c->integ.type != 1) return fail(c, FVC_ERR_ARG, "the batch form runs Euler (0) or RK4 (1)");
+  if (c->integ.extrapolate) return fail(c, FVC_ERR_ARG, "the batch form does not extrapolate");
+  if ((st = mixed_ok(c))) return st;
+  fvc_batch* b = new fvc_batch();
+  b->c = c;
+  b->o = *o;
+  b->max_jobs = o->max_jobs > 0 ? o->max_jobs : 1024;
+  if (cudaMalloc(&b->d_ctrs, sizeof(DevCounters) * (size_t)b->max_jobs) != cudaSuccess ||
+      cudaMallocHost(&b->h_ctrs, sizeof(DevCounters) * (size_t)b->max_jobs) != cudaSuccess ||
+      cudaMalloc(&b->d_bc, sizeof(BatchCtr)) != cudaSuccess) {
+    fvc_batch_destroy(b);
+    return fail(c, FVC_ERR_OOM, "batch counters");
+  }
+  for (int k = b->max_jobs - 1; k >= 0; k--) b->free_slots.push_back(k);
+  for (int k = 0; k < 2; k++) cudaEventCreateWithFlags(&b->h_ev[k], cudaEventDisableTiming);
+  b->tick_ev.resize(2);
+  for (auto& e : b->tick_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  cudaEventCreate(&b->t_start);
+  cudaEventCreate(&b->t_end);
+  b->launch.threads = 128;
+  b->launch.blocks = (int)batch_resident(c->mesh.dims, c->prec, 128);
+  *out = b;
+  return check_launch(c, "batch create");
+}
+
+extern "C" void fvc_batch_destroy(fvc_batch* b) {
+  if (!b) return;
+  fvc_ctx* c = b->c;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& J : b->jobs) {
+    if (J->job) fvc_job_destroy(J->job);
+    if (J->done) cudaEventDestroy(J->done);
+  }
+  for (auto& kv : b->pairs) cudaFree(kv.second.q);
+  cudaFree(b->d_ctrs);
+  cudaFreeHost(b->h_ctrs);
+  cudaFree(b->d_bc);
+  cudaFree(b->d_queue);
+  cudaFree(b->d_tick);
+  for (int k = 0; k < 2; k++) {
+    cudaFreeHost(b->h_tick[k]);
+    if (b->h_ev[k]) cudaEventDestroy(b->h_ev[k]);
+  }
+  for (auto& e : b->tick_ev) cudaEventDestroy(e);
+  if (b->t_start) cudaEventDestroy(b->t_start);
+  if (b->t_end) cudaEventDestroy(b->t_end);
+  delete b;
+}
+
+extern "C" fvc_status fvc_batch_submit(fvc_batch* b, const fvc_batch_job_spec* sp, int* id) {
+  if (!b || !sp || !id) return FVC_ERR_ARG;
+  fvc_ctx* c = b->c;
+  if (sp->kind != FVC_JOB_TRACERS && sp->kind != FVC_JOB_RESIDENCE && sp->kind != FVC_JOB_FTLE)
+    return fail(c, FVC_ERR_ARG, "unknown job kind %d", sp->kind);
+  if (!(sp->t_stop != sp->t_start)) return fail(c, FVC_ERR_ARG, "empty integration window");
+  if (sp->kind == FVC_JOB_RESIDENCE && sp->t_stop < sp->t_start)
+    return fail(c, FVC_ERR_ARG, "residence time is computed forward in time (ompVC/parameters.c:541-542)");
+  if (sp->kind != FVC_JOB_FTLE && (sp->n < 0 || (sp->n > 0 && !sp->seeds)))
+    return fail(c, FVC_ERR_ARG, "bad seed array");
+  std::unique_ptr<HostJob> J(new HostJob());
+  J->id = (int)b->jobs.size();
+  J->kind = sp->kind;
+  J->spec = *sp;
+  J->dir = sp->t_stop > sp->t_start ? 1 : -1;
+  J->T = fabs(sp->t_stop - sp->t_start);
+  const double tmax = b->o.tmin + (b->o.tres - 1) * b->o.tdelta;
+  J->stop = sp->t_stop;
+  if (!b->o.periodic) {
+    if (sp->t_start < b->o.tmin || sp->t_start > tmax) return fail(c, FVC_ERR_ARG, "start time outside the data range");
+    J->stop = std::max(std::min(sp->t_stop, tmax), b->o.tmin);
+  }
+  long n;
+  if (sp->kind == FVC_JOB_FTLE) {
+    const fvc_ftle_spec& g = sp->grid;
+    n = (long)g.xres * g.yres * (c->mesh.dims == 3 ? g.zres : 1);
+    if (g.xres < 2 || g.yres < 2 || (c->mesh.dims == 3 && g.zres < 2)) return fail(c, FVC_ERR_ARG, "FTLE grid too small");
+  } else {
+    n = sp->n;
+    J->seeds.assign(sp->seeds, sp->seeds + 3 * (size_t)sp->n);
+  }
+  J->spec.seeds = nullptr;
+  J->bytes = job_bytes(sp->kind, n);
+  *id = J->id;
+  b->queued.push_back(J->id);
+  b->jobs.push_back(std::move(J));
+  b->stats.jobs_submitted++;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_batch_tick(fvc_batch* b, int* pending) {
+  if (!b) return FVC_ERR_ARG;
+  fvc_status st = tick(b);
+  if (pending) *pending = (int)(b->queued.size() + b->active.size() + b->finishing.size());
+  return st;
+}
+
+extern "C" fvc_status fvc_batch_autotune(fvc_batch* b) {
+  if (!b) return FVC_ERR_ARG;
+  fvc_status st;
+  if ((st = use_device(b->c))) return st;
+  if ((st = admit(b))) return st;
+  return autotune(b);
+}
+
+extern "C" fvc_status fvc_batch_run(fvc_batch* b, int graph) {
+  if (!b) return FVC_ERR_ARG;
+  fvc_ctx* c = b->c;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  cudaEventRecord(b->t_start, c->stream);
+  if ((st = admit(b))) return st;
+  if (graph && b->queued.empty() && !b->active.empty()) {
+    // the whole remaining schedule is fixed: plan every tick, upload all
+    // descriptors once, capture the ticks into one graph and launch it
+    std::vector<TickPlan> plans;
+    std::vector<size_t> offs;
+    size_t total = 0;
+    // plan with cursors moved on a copy of the host state
+    std::vector<HostJob> saved;
+    for (int id : b->active) saved.push_back(*b->jobs[id]);
+    std::vector<int> act = b->active;
+    while (!act.empty()) {
+      plans.emplace_back();
+      offs.push_back(total);
+      if ((st = plan_tick(b, act, nullptr, plans.back()))) break;  // sizes and pairs
+      total = al16(total + plans.back().blob.size());
+      std::vector<int> still;
+      for (size_t k = 0; k < act.size(); k++) {
+        HostJob& H = *b->jobs[act[k]];
+        H.launched = true;
+        H.df += H.dir;
+        if (!plans.back().iv[k].last) still.push_back(act[k]);
+      }
+      act.swap(still);
+    }
+    for (size_t k = 0; k < saved.size(); k++) {  // restore the cursors
+      HostJob& H = *b->jobs[saved[k].id];
+      H.df = saved[k].df;
+      H.launched = saved[k].launched;
+    }
+    if (st) return st;
+    char* d_all = nullptr;
+    if (cudaMalloc(&d_all, total ? total : 16) != cudaSuccess) return fail(c, FVC_ERR_OOM, "graph descriptors");
+    std::vector<char> all(total);
+    act = b->active;
+    for (size_t t = 0; t < plans.size(); t++) {
+      if ((st = plan_tick(b, act, d_all + offs[t], plans[t]))) break;
+      memcpy(all.data() + offs[t], plans[t].blob.data(), plans[t].blob.size());
+      std::vector<int> still;
+      for (size_t k = 0; k < act.size(); k++) {
+        HostJob& H = *b->jobs[act[k]];
+        H.launched = true;
+        H.df += H.dir;
+        if (!plans[t].iv[k].last) still.push_back(act[k]);
+      }
+      act.swap(still);
+    }
+    for (size_t k = 0; k < saved.size(); k++) {
+      HostJob& H = *b->jobs[saved[k].id];
+      H.df = saved[k].df;
+      H.launched = saved[k].launched;
+    }
+    if (st) {
+      cudaFree(d_all);
+      return st;
+    }
+    FVC_CUDA(c, cudaMemcpyAsync(d_all, all.data(), total, cudaMemcpyHostToDevice, c->stream));
+    FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    FVC_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+    fvc_status cst = FVC_OK;
+    for (size_t t = 0; t < plans.size() && !cst; t++) {
+      cst = enqueue_tick(b, plans[t], (const BJob*)(d_all + offs[t]), false);
+      if (!cst) advance_cursors(b, plans[t]);
+    }
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    if (cst || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaFree(d_all);
+      return cst ? cst : fail(c, FVC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    }
+    ce = cudaGraphInstantiate(&ge, g, 0);
+    if (ce == cudaSuccess) ce = cudaGraphLaunch(ge, c->stream);
+    // the done events recorded during capture are graph nodes; record them again after the graph
+    for (int id : b->finishing) cudaEventRecord(b->jobs[id]->done, c->stream);
+    b->stats.ticks += (long long)plans.size();
+    b->stats.graphs++;
+    cudaError_t se = cudaStreamSynchronize(c->stream);
+    if (ge) cudaGraphExecDestroy(ge);
+    cudaGraphDestroy(g);
+    cudaFree(d_all);
+    if (ce != cudaSuccess || se != cudaSuccess)
+      return fail(c, FVC_ERR_CUDA, "graph launch: %s", cudaGetErrorString(ce != cudaSuccess ? ce : se));
+  }
+  while (!b->queued.empty() || !b->active.empty()) {
+    if ((st = tick(b))) return st;
+  }
+  retire(b, true);
+  cudaEventRecord(b->t_end, c->stream);
+  FVC_CUDA(c, cudaEventSynchronize(b->t_end));
+  b->stats.ms_run += ev_ms(b->t_start, b->t_end);
+  return FVC_OK;
+}
+
+static HostJob* job_of(fvc_batch* b, int id) {
+  if (!b || id < 0 || id >= (int)b->jobs.size()) return nullptr;
+  return b->jobs[id].get();
+}
+
+extern "C" fvc_status fvc_batch_poll(fvc_batch* b, int id, int* state) {
+  HostJob* J = job_of(b, id);
+  if (!J || !state) return FVC_ERR_ARG;
+  if (J->state == JQ_FINISHING) retire(b, false);
+  *state = J->state == JQ_DONE ? FVC_BATCH_DONE
+         : J->state == JQ_FAILED ? FVC_BATCH_FAILED
+         : J->state == JQ_RELEASED ? FVC_BATCH_RELEASED
+         : J->state == JQ_QUEUED ? FVC_BATCH_QUEUED : FVC_BATCH_RUNNING;
+  if (J->state == JQ_FAILED) return fail(b->c, J->err, "batch job %d: %s", id, J->msg.c_str());
+  return FVC_OK;
+}
+
+static fvc_status job_ready(fvc_batch* b, HostJob* J, int kind_ok) {
+  if (!J) return FVC_ERR_ARG;
+  if (J->state == JQ_FINISHING) retire(b, true);
+  if (J->state == JQ_FAILED) return fail(b->c, J->err, "batch job %d: %s", J->id, J->msg.c_str());
+  if (J->state != JQ_DONE) return fail(b->c, FVC_ERR_STATE, "batch job %d has not finished", J->id);
+  if (!(kind_ok & (1 << J->kind))) return fail(b->c, FVC_ERR_ARG, "batch job %d is of another kind", J->id);
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_batch_tracer_result(fvc_batch* b, int id, double* X, int* eid, int* left, double* ldt) {
+  HostJob* J = job_of(b, id);
+  fvc_status st = job_ready(b, J, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE));
+  if (st) return st;
+  return fvc_tracer_get_state(J->job, X, eid, left, ldt);
+}
+
+extern "C" fvc_status fvc_batch_residence_result(fvc_batch* b, int id, double* rt) {
+  HostJob* J = job_of(b, id);
+  fvc_status st = job_ready(b, J, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE));
+  if (st) return st;
+  return fvc_tracer_residence(J->job, J->spec.t_start, J->stop, rt);
+}
+
+extern "C" fvc_status fvc_batch_ftle_result(fvc_batch* b, int id, double* wT, double* wN) {
+  HostJob* J = job_of(b, id);
+  fvc_status st = job_ready(b, J, 1 << FVC_JOB_FTLE);
+  if (st) return st;
+  fvc_ctx* c = b->c;
+  if ((st = use_device(c))) return st;
+  size_t n = (size_t)J->job->f.n;
+  if (wT) FVC_CUDA(c, cudaMemcpyAsync(wT, J->job->f.out, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  if (wN) FVC_CUDA(c, cudaMemcpyAsync(wN, J->job->f.out + n, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_batch_job_stats(fvc_batch* b, int id, fvc_job_stats* out) {
+  HostJob* J = job_of(b, id);
+  if (!J || !out) return FVC_ERR_ARG;
+  if (J->state == JQ_FINISHING) retire(b, true);
+  memset(out, 0, sizeof(*out));
+  if (J->job) *out = J->job->stats;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_batch_release(fvc_batch* b, int id) {
+  HostJob* J = job_of(b, id);
+  if (!J) return FVC_ERR_ARG;
+  if (J->state == JQ_QUEUED || J->state == JQ_ACTIVE)
+    return fail(b->c, FVC_ERR_STATE, "batch job %d is still running", id);
+  if (J->state == JQ_FINISHING) retire(b, true);
+  if (J->job) {
+    fvc_job_destroy(J->job);
+    J->job = nullptr;
+    b->used -= J->bytes;
+  }
+  if (J->slot >= 0) {
+    b->free_slots.push_back(J->slot);
+    J->slot = -1;
+  }
+  J->seeds.clear();
+  J->seeds.shrink_to_fit();
+  if (J->state != JQ_FAILED) J->state = JQ_RELEASED;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_batch_get_stats(fvc_batch* b, fvc_batch_stats* out) {
+  if (!b || !out) return FVC_ERR_ARG;
+  *out = b->stats;
+  out->hbm_used = (long long)b->used;
+  return FVC_OK;
+}

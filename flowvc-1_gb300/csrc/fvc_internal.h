@@ -1,0 +1,93 @@
+// fvc_internal.h -- library-internal state shared by the C-ABI translation
+// units (fvc_api.cu, fvc_batch.cu): the context and job structures and the
+// helpers both use.  Not part of the public interface (include/fvc.h).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "fvc.h"
+#include "fvc_kernels.h"
+
+using namespace fvc;
+
+struct fvc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DevMesh mesh{};
+  bool mesh_set = false;
+  DevInteg integ{1, 0.01, 0, 0.0, 0.0, 0.0};
+  bool integ_set = false;
+  DevWindow window{};
+  bool window_set = false;
+  long frame_nodes = 0;  // nodes per frame
+  // device buffers
+  int4* d_elem = nullptr;
+  double* d_geom = nullptr;
+  float* d_geo32 = nullptr;
+  double4_32a* d_nodes = nullptr;
+  int* d_cell_start = nullptr;
+  int* d_cell_ids = nullptr;
+  BucketGrid grid{};
+  std::unordered_map<int, double4_32a*> frames;
+  double* d_stage = nullptr;  // frame upload staging, 3 doubles a node
+  DevCounters* d_ctr = nullptr;
+  double4_32a* d_vt = nullptr;  // stage-time node velocities
+  int vt_slots = 0;
+  // scratch for array calls
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  // mixed-precision form: quantised frames by frame id, the call's step table
+  int prec = 0;
+  struct QFrame {
+    ushort4* q = nullptr;
+    float s[3] = {1.f, 1.f, 1.f};
+    int fmt = 0;
+  };
+  std::unordered_map<int, QFrame> qframes;
+  unsigned* d_qscratch = nullptr;
+  uint4* d_qpair = nullptr;  // the window's two quantised frames, interleaved
+  std::vector<StepM> h_steps;
+  StepM* d_steps = nullptr;
+  size_t steps_cap = 0;
+  int window_lo = -1, window_hi = -1;
+  // exposure time (Trace_CETCompute): per-element sums shared by all releases
+  double* d_cet_sum = nullptr;
+  int* d_cet_enc = nullptr;
+  int cet_sub = 0;  // Trace_CETSubsteps; 0 = off
+  std::string err;
+};
+
+struct fvc_job {
+  fvc_ctx* ctx = nullptr;
+  int kind = 0;  // 0 FTLE, 1 tracers
+  FtleDev f{};
+  TracerDev t{};
+  void* mem = nullptr;  // one allocation for all per-job arrays
+  int prec = 0;         // arithmetic form the job was created with
+  bool packed = false;  // positions held as (X, c) float pairs
+  fvc_job_stats stats{};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+// ---- helpers defined in fvc_api.cu
+// records the message on the context and returns code
+fvc_status fail(fvc_ctx* c, fvc_status code, const char* fmt, ...);
+fvc_status use_device(fvc_ctx* c);
+fvc_status check_launch(fvc_ctx* c, const char* what);
+// the quantised copy of resident frame `id` in the context's 16-bit format
+fvc_status quantised(fvc_ctx* c, int id, fvc_ctx::QFrame** out);
+// the integrator / precision combination is one the form supports
+fvc_status mixed_ok(fvc_ctx* c);
+void job_events(fvc_job* j);
+float ev_ms(cudaEvent_t a, cudaEvent_t b);
+// (X, c) float pairs copied to the host back to FP64 positions X - c
+void unpack_host(double* A, size_t n);
+
+#define FVC_CUDA(c, x)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (x);                                                                \
+    if (e_ != cudaSuccess) return fail((c), FVC_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
+  } while (0)

@@ -59,8 +59,10 @@ __device__ __forceinline__ float dec16(unsigned short b, int fmt) {
   return fmt == QF_BF16 ? __uint_as_float((unsigned)b << 16) : __half2float(__ushort_as_half(b));
 }
 
-// One node's velocity at tloc tl from the two quantised frames.
-__device__ __forceinline__ void node_vel_mx(const DevWindow& w, int node, float tl, float out[3]) {
+// One node's velocity at tloc tl from the two quantised frames.  W is a
+// DevWindow or any view with its qp, qs0, qs1 and qfmt members.
+template <class W>
+__device__ __forceinline__ void node_vel_mx(const W& w, int node, float tl, float out[3]) {
   const uint4 p = __ldg(w.qp + node);
   const float ua = dec16((unsigned short)(p.x & 0xffffu), w.qfmt) * w.qs0[0];
   const float va = dec16((unsigned short)(p.x >> 16), w.qfmt) * w.qs0[1];
@@ -170,8 +172,8 @@ struct NatM {
 };
 
 // Velocity at X (compensation C) and tloc tl: P1 in space, linear in time.
-template <int D>
-__device__ __forceinline__ int vel_mx(const DevMesh& m, const DevWindow& w, float tl, const float X[3],
+template <int D, class W>
+__device__ __forceinline__ int vel_mx(const DevMesh& m, const W& w, float tl, const float X[3],
                                       const float C[3], int& eid, int& left, float out[3], const NatM* nc) {
   if (eid < 0 || eid >= m.nelem) return PT_ERR_WALK;
   float r, s, t, wv;
@@ -249,8 +251,8 @@ __device__ __forceinline__ void kahan_add(float X[3], float c[3], const float in
 // 22-45, with RK4's stage hints and exit rules, integration.c:317-462).  A
 // particle that leaves keeps its position before the step and records the
 // step's start time as LeftDomainTime.
-template <int D>
-__device__ __forceinline__ void advect_mx(const DevMesh& m, const DevWindow& w, int type, PtM& p, int kend,
+template <int D, class W>
+__device__ __forceinline__ void advect_mx(const DevMesh& m, const W& w, int type, PtM& p, int kend,
                                           unsigned& steps, int& err) {
   if (p.left) return;
   const float zero[3] = {0.0f, 0.0f, 0.0f};

@@ -49,6 +49,26 @@ class JobStats(C.Structure):
                 ("ms_setup", C.c_double), ("launches", C.c_longlong)]
 
 
+class BatchOpts(C.Structure):
+    _fields_ = [("tmin", C.c_double), ("tdelta", C.c_double), ("tres", C.c_int), ("periodic", C.c_int),
+                ("hbm_budget", C.c_longlong), ("max_jobs", C.c_int)]
+
+
+class BatchJobSpec(C.Structure):
+    _fields_ = [("kind", C.c_int), ("t_start", C.c_double), ("t_stop", C.c_double), ("n", C.c_int),
+                ("seeds", C.POINTER(C.c_double)), ("local_search_checking", C.c_int), ("grid", FtleSpec)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("ticks", C.c_longlong), ("graphs", C.c_longlong), ("launches", C.c_longlong),
+                ("steps", C.c_longlong), ("jobs_submitted", C.c_longlong), ("jobs_done", C.c_longlong),
+                ("ms_run", C.c_double), ("tuned_threads", C.c_int), ("tuned_blocks", C.c_int),
+                ("hbm_used", C.c_longlong)]
+
+
+JOB_TRACERS, JOB_RESIDENCE, JOB_FTLE = 0, 1, 2
+BATCH_QUEUED, BATCH_RUNNING, BATCH_DONE, BATCH_FAILED, BATCH_RELEASED = range(5)
+
 SIGNATURES = {
     "fvc_abi_version": (C.c_int, []),
     "fvc_create": (C.c_int, [C.POINTER(_vp), C.POINTER(Opts)]),
@@ -86,6 +106,19 @@ SIGNATURES = {
     "fvc_cet_enable": (C.c_int, [_vp, C.c_int]),
     "fvc_cet_results": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip]),
     "fvc_tracer_residence": (C.c_int, [_vp, C.c_double, C.c_double, _dp]),
+    "fvc_batch_create": (C.c_int, [_vp, C.POINTER(BatchOpts), C.POINTER(_vp)]),
+    "fvc_batch_destroy": (None, [_vp]),
+    "fvc_batch_submit": (C.c_int, [_vp, C.POINTER(BatchJobSpec), _ip]),
+    "fvc_batch_tick": (C.c_int, [_vp, _ip]),
+    "fvc_batch_run": (C.c_int, [_vp, C.c_int]),
+    "fvc_batch_autotune": (C.c_int, [_vp]),
+    "fvc_batch_poll": (C.c_int, [_vp, C.c_int, _ip]),
+    "fvc_batch_tracer_result": (C.c_int, [_vp, C.c_int, _dp, _ip, _ip, _dp]),
+    "fvc_batch_residence_result": (C.c_int, [_vp, C.c_int, _dp]),
+    "fvc_batch_ftle_result": (C.c_int, [_vp, C.c_int, _dp, _dp]),
+    "fvc_batch_job_stats": (C.c_int, [_vp, C.c_int, C.POINTER(JobStats)]),
+    "fvc_batch_release": (C.c_int, [_vp, C.c_int]),
+    "fvc_batch_get_stats": (C.c_int, [_vp, C.POINTER(BatchStats)]),
 }
 
 _lib = None
@@ -343,6 +376,97 @@ class TracerJob:
     def close(self):
         if self.h:
             self.lib.fvc_job_destroy(self.h)
+            self.h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Batched / served jobs on one context (fvc_batch_*): submit jobs, then
+    run them all (run) or advance tick by tick (tick) while submitting more."""
+
+    def __init__(self, ctx: Context, tmin, tdelta, tres, periodic=0, hbm_budget=0, max_jobs=0):
+        self.ctx, self.lib = ctx, ctx.lib
+        self.h = _vp()
+        self.sizes = {}
+        o = BatchOpts(tmin, tdelta, tres, periodic, int(hbm_budget), max_jobs)
+        ctx._chk(self.lib.fvc_batch_create(ctx.h, C.byref(o), C.byref(self.h)))
+
+    def _submit(self, spec, keep=None):
+        jid = C.c_int(0)
+        self.ctx._chk(self.lib.fvc_batch_submit(self.h, C.byref(spec), C.byref(jid)))
+        return jid.value
+
+    def submit_tracers(self, seeds, t_start, t_stop, residence=False, lsc=1):
+        seeds = f64(seeds)
+        spec = BatchJobSpec(JOB_RESIDENCE if residence else JOB_TRACERS, t_start, t_stop, seeds.shape[0],
+                            _d(seeds), lsc, FtleSpec())
+        jid = self._submit(spec)
+        self.sizes[jid] = seeds.shape[0]
+        return jid
+
+    def submit_ftle(self, grid, t_start, t_stop, lsc=1):
+        g = FtleSpec(*grid[:6], *grid[6:9], lsc, t_start, t_stop, 1)
+        spec = BatchJobSpec(JOB_FTLE, t_start, t_stop, 0, C.POINTER(C.c_double)(), lsc, g)
+        jid = self._submit(spec)
+        self.sizes[jid] = int(grid[6]) * int(grid[7]) * int(grid[8])
+        return jid
+
+    def tick(self):
+        pend = C.c_int(0)
+        self.ctx._chk(self.lib.fvc_batch_tick(self.h, C.byref(pend)))
+        return pend.value
+
+    def run(self, graph=False):
+        self.ctx._chk(self.lib.fvc_batch_run(self.h, 1 if graph else 0))
+
+    def autotune(self):
+        self.ctx._chk(self.lib.fvc_batch_autotune(self.h))
+
+    def poll(self, jid):
+        st = C.c_int(0)
+        self.ctx._chk(self.lib.fvc_batch_poll(self.h, jid, C.byref(st)))
+        return st.value
+
+    def tracer_result(self, jid):
+        n = self.sizes[jid]
+        X, ldt = np.empty((max(n, 1), 3)), np.empty(max(n, 1))
+        eid, left = np.empty(max(n, 1), np.int32), np.empty(max(n, 1), np.int32)
+        self.ctx._chk(self.lib.fvc_batch_tracer_result(self.h, jid, _d(X), _i(eid), _i(left), _d(ldt)))
+        return dict(X=X[:n], eid=eid[:n], left=left[:n], ldt=ldt[:n])
+
+    def residence_result(self, jid):
+        n = self.sizes[jid]
+        rt = np.empty(max(n, 1))
+        self.ctx._chk(self.lib.fvc_batch_residence_result(self.h, jid, _d(rt)))
+        return rt[:n]
+
+    def ftle_result(self, jid):
+        n = self.sizes[jid]
+        wT, wN = np.empty(n), np.empty(n)
+        self.ctx._chk(self.lib.fvc_batch_ftle_result(self.h, jid, _d(wT), _d(wN)))
+        return wT, wN
+
+    def job_stats(self, jid):
+        st = JobStats()
+        self.ctx._chk(self.lib.fvc_batch_job_stats(self.h, jid, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in JobStats._fields_}
+
+    def release(self, jid):
+        self.ctx._chk(self.lib.fvc_batch_release(self.h, jid))
+
+    def stats(self):
+        st = BatchStats()
+        self.ctx._chk(self.lib.fvc_batch_get_stats(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in BatchStats._fields_}
+
+    def close(self):
+        if self.h:
+            self.lib.fvc_batch_destroy(self.h)
             self.h = _vp()
 
     def __del__(self):

@@ -445,3 +445,143 @@ def uniform_seeds(n, dims=3, seed=0, lo=0.0, hi=1.0):
     if dims == 2:
         pts[:, 2] = 0.0
     return pts
+
+
+# ---------------------------------------------------------------- bent tube
+
+def _kuhn_conn(nx, ny, nz):
+    """Kuhn 6-tet split of an nx x ny x nz grid of hexahedral cells, nodes
+    numbered (i * (ny+1) + j) * (nz+1) + k; conforming across cells."""
+    my, mz = ny + 1, nz + 1
+    CI, CJ, CK = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    base = np.stack([CI, CJ, CK], axis=-1).reshape(-1, 3).astype(np.int64)
+    unit = np.eye(3, dtype=np.int64)
+    tets = []
+    for (a, b, c) in [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]:
+        v0 = base
+        v1 = v0 + unit[a]
+        v2 = v1 + unit[b]
+        v3 = v2 + unit[c]
+        tets.append(np.stack([(v[:, 0] * my + v[:, 1]) * mz + v[:, 2] for v in (v0, v1, v2, v3)], axis=-1))
+    return np.stack(tets, axis=1).reshape(-1, 4)
+
+
+def _disc_map(u, v):
+    """Shirley-Chiu concentric map of the square [-1, 1]^2 onto the unit disc
+    (area preserving: constant Jacobian pi/4, so no cell degenerates)."""
+    x, y = np.zeros_like(u), np.zeros_like(v)
+    a = np.abs(u) >= np.abs(v)
+    nz = (u != 0) | (v != 0)
+    m = a & nz
+    r = u[m]
+    phi = (math.pi / 4) * v[m] / u[m]
+    x[m], y[m] = r * np.cos(phi), r * np.sin(phi)
+    m = ~a & nz
+    r = v[m]
+    phi = math.pi / 2 - (math.pi / 4) * u[m] / v[m]
+    x[m], y[m] = r * np.cos(phi), r * np.sin(phi)
+    return x, y
+
+
+def tube_centreline(s, length=20.0, bend_radius=4.0):
+    """Centre C(s), tangent T(s) and normal N(s) of a tube axis of the given
+    length: straight, a 90-degree arc of bend_radius in the x-z plane, then
+    straight again, with the two straight legs equally long.  The binormal
+    is +y throughout."""
+    s = np.asarray(s, dtype=np.float64)
+    arc = 0.5 * math.pi * bend_radius
+    ls = 0.5 * (length - arc)
+    C = np.zeros(s.shape + (3,))
+    T = np.zeros(s.shape + (3,))
+    N = np.zeros(s.shape + (3,))
+    m1 = s <= ls
+    C[m1] = np.stack([0 * s[m1], 0 * s[m1], s[m1]], -1)
+    T[m1] = (0.0, 0.0, 1.0)
+    N[m1] = (1.0, 0.0, 0.0)
+    m2 = (s > ls) & (s <= ls + arc)
+    th = (s[m2] - ls) / bend_radius
+    C[m2] = np.stack([bend_radius * (1 - np.cos(th)), 0 * th, ls + bend_radius * np.sin(th)], -1)
+    T[m2] = np.stack([np.sin(th), 0 * th, np.cos(th)], -1)
+    N[m2] = np.stack([np.cos(th), 0 * th, -np.sin(th)], -1)
+    m3 = s > ls + arc
+    d = s[m3] - (ls + arc)
+    C[m3] = np.stack([bend_radius + d, 0 * d, ls + bend_radius + 0 * d], -1)
+    T[m3] = (1.0, 0.0, 0.0)
+    N[m3] = (0.0, 0.0, -1.0)
+    return C, T, N
+
+
+@dataclass
+class Tube:
+    """A tet-meshed bent tube: mesh arrays plus, per node, its axial position
+    s, its radius r / R and the unit axial direction (for the velocity)."""
+    xyz: np.ndarray
+    conn: np.ndarray
+    adj: np.ndarray
+    s: np.ndarray
+    r: np.ndarray
+    tangent: np.ndarray
+    radius: float
+    length: float
+    bend_radius: float
+
+    def bounds(self):
+        lo, hi = self.xyz.min(0), self.xyz.max(0)
+        return [float(lo[0]), float(hi[0]), float(lo[1]), float(hi[1]), float(lo[2]), float(hi[2])]
+
+
+def bent_tube_mesh(nc=40, nax=320, radius=1.0, bend_radius=4.0, length=20.0):
+    """Tube of radius R with a 90-degree bend of radius bend_radius and axial
+    length `length`: nc x nc cross-section cells (the square mapped onto the
+    disc) x nax axial layers, each hexahedral cell split into 6 Kuhn
+    tetrahedra (nc = 40, nax = 320: 3,072,000 tets, 539,601 nodes)."""
+    t = np.linspace(-1.0, 1.0, nc + 1)
+    U, V, S = np.meshgrid(t, t, np.linspace(0.0, length, nax + 1), indexing="ij")
+    x, y = _disc_map(U.reshape(-1), V.reshape(-1))
+    s = S.reshape(-1)
+    C, T, N = tube_centreline(s, length, bend_radius)
+    B = np.array([0.0, 1.0, 0.0])
+    xyz = C + radius * (x[:, None] * N + y[:, None] * B)
+    conn = _orient_tets(xyz, _kuhn_conn(nc, nc, nax))
+    adj = tet_adjacency(conn)
+    r = np.minimum(np.hypot(x, y), 1.0)
+    return Tube(xyz, conn.astype(np.int32), adj, s, r, T, radius, length, bend_radius)
+
+
+def womersley_profile(r, alpha=4.0):
+    """Complex Womersley shape 1 - J0(i^{3/2} alpha r) / J0(i^{3/2} alpha) of
+    the first harmonic at radius r / R (zero at the wall)."""
+    from scipy.special import jv
+    k = alpha * np.exp(0.75j * math.pi)
+    return 1.0 - jv(0, k * r) / jv(0, k)
+
+
+def womersley_frames(tube, nframes=101, period=1.0, peak=1.0, amp=0.5, alpha=4.0):
+    """Pulsatile axial flow along the tube: a Poiseuille profile of centre-line
+    speed `peak` plus a first harmonic of centre-line amplitude `amp` with
+    Womersley number alpha, u(r, t) = peak (1 - r^2) + Re(a W(r) e^{2 pi i t / period}),
+    directed along the local axis; no slip at the wall.  Frames at
+    t = k period / (nframes - 1), k = 0 .. nframes - 1 (the last repeats the
+    first, for Data_TPeriodic = 1).  Returns (times, list of N x 3 arrays)."""
+    W = womersley_profile(tube.r, alpha)
+    a = amp / abs(womersley_profile(np.zeros(1), alpha)[0])
+    pois = peak * (1.0 - tube.r ** 2)
+    times, frames = [], []
+    for k in range(nframes):
+        tk = k * period / (nframes - 1)
+        ph = np.exp(2j * math.pi * (k % (nframes - 1)) / (nframes - 1))
+        u = pois + np.real(a * W * ph)
+        frames.append(u[:, None] * tube.tangent)
+        times.append(tk)
+    return times, frames
+
+
+def tube_cross_section_seeds(tube, n, s, seed=0, margin=0.02):
+    """n seeds uniformly distributed over the tube's cross-section at axial
+    position s (radius up to (1 - margin) R)."""
+    rng = np.random.default_rng(seed)
+    rr = np.sqrt(rng.uniform(0.0, (1.0 - margin) ** 2, n))
+    th = rng.uniform(0.0, 2 * math.pi, n)
+    C, T, N = tube_centreline(np.full(n, float(s)), tube.length, tube.bend_radius)
+    B = np.array([0.0, 1.0, 0.0])
+    return C + tube.radius * ((rr * np.cos(th))[:, None] * N + (rr * np.sin(th))[:, None] * B)

@@ -267,6 +267,95 @@ typedef struct {
 } fvc_job_stats;
 fvc_status fvc_job_get_stats(fvc_job *job, fvc_job_stats *out);
 
+/* ---- batched and served form ------------------------------------------ */
+
+/* Many tracer, residence-time and FTLE jobs, each with its own seeds and
+ * integration window, advanced together over velocity frames resident on
+ * the device.  No counterpart in ompVC, which runs one window per process;
+ * each job is computed exactly as the single-job calls above compute it (the
+ * same frame intervals, step sequences and kernels' arithmetic), so its
+ * results are identical alone and in any mix of jobs, in either arithmetic
+ * form of the context.
+ *
+ * Time advances in ticks; in one tick every active job runs its next frame
+ * interval: one kernel builds the tick's work queue from all jobs' live
+ * points, one persistent kernel advects it, then FTLE jobs run their
+ * per-interval early-FTLE passes.  Jobs are admitted between ticks, in
+ * submission order, while their device footprint fits hbm_budget; results
+ * stay on the device until read or released.  Unstructured meshes, Euler or
+ * RK4, no extrapolation.  Frames 0 .. tres-1 must be resident
+ * (fvc_upload_frame) under their file index, frame k at tmin + k tdelta;
+ * with periodic data frame indices wrap modulo tres - 1 as ompVC wraps them
+ * (ompVC/velocity.c:77-80). */
+typedef struct fvc_batch fvc_batch;
+typedef struct {
+  double tmin;           /* Data_TMin: time of frame 0 */
+  double tdelta;         /* Data_TDelta */
+  int tres;              /* Data_TRes */
+  int periodic;          /* Data_TPeriodic */
+  long long hbm_budget;  /* device bytes the admitted jobs may hold; 0 = no limit */
+  int max_jobs;          /* jobs admitted at once; 0 = 1024 */
+} fvc_batch_opts;
+
+enum { FVC_JOB_TRACERS = 0, FVC_JOB_RESIDENCE = 1, FVC_JOB_FTLE = 2 };
+typedef struct {
+  int kind;                  /* FVC_JOB_* */
+  double t_start, t_stop;    /* integration window; backward when t_stop < t_start
+                                (residence time: forward only) */
+  /* tracers / residence time: n seeds (n x 3), located with ompVC's list chain */
+  int n;
+  const double *seeds;
+  int local_search_checking;
+  /* FTLE: the seed grid (start_time, stop_time and generate are set from
+     the window) */
+  fvc_ftle_spec grid;
+} fvc_batch_job_spec;
+
+enum { FVC_BATCH_QUEUED = 0, FVC_BATCH_RUNNING = 1, FVC_BATCH_DONE = 2, FVC_BATCH_FAILED = 3,
+       FVC_BATCH_RELEASED = 4 };
+
+typedef struct {
+  long long ticks;           /* ticks run (graph ticks included) */
+  long long graphs;          /* CUDA graphs launched */
+  long long launches;        /* kernels launched by ticks */
+  long long steps;           /* accepted steps of retired jobs */
+  long long jobs_submitted;
+  long long jobs_done;
+  double ms_run;             /* device time inside fvc_batch_run */
+  int tuned_threads;         /* block size the autotuner chose (0 = not tuned) */
+  int tuned_blocks;          /* grid the autotuner chose */
+  long long hbm_used;        /* footprint of the jobs holding device memory */
+} fvc_batch_stats;
+
+fvc_status fvc_batch_create(fvc_ctx *ctx, const fvc_batch_opts *opts, fvc_batch **batch);
+void fvc_batch_destroy(fvc_batch *batch);
+/* Queues a job (the seeds are copied); returns its id. */
+fvc_status fvc_batch_submit(fvc_batch *batch, const fvc_batch_job_spec *spec, int *id);
+/* Admits what fits, then enqueues one tick and returns without waiting for
+ * the GPU (at most two ticks in flight).  *pending = jobs not yet finished. */
+fvc_status fvc_batch_tick(fvc_batch *batch, int *pending);
+/* Runs until every submitted job has finished.  graph = 1: when every job
+ * fits at once, the whole schedule is captured into one CUDA graph and
+ * launched as one. */
+fvc_status fvc_batch_run(fvc_batch *batch, int graph);
+/* Times the persistent kernel's launch shapes on the next tick of the
+ * admitted jobs (their state restored after each trial) and keeps the
+ * fastest. */
+fvc_status fvc_batch_autotune(fvc_batch *batch);
+/* *state = FVC_BATCH_*; a failed job returns its error. */
+fvc_status fvc_batch_poll(fvc_batch *batch, int id, int *state);
+/* Results of a finished job (waits for it): tracer state in seed order
+ * (as fvc_tracer_get_state), residence times (as fvc_tracer_residence with
+ * the job's window), FTLE fields in output order (as fvc_ftle_reduce). */
+fvc_status fvc_batch_tracer_result(fvc_batch *batch, int id, double *X, int *eid, int *left, double *ldt);
+fvc_status fvc_batch_residence_result(fvc_batch *batch, int id, double *rt);
+fvc_status fvc_batch_ftle_result(fvc_batch *batch, int id, double *ftle_wT, double *ftle_woT);
+fvc_status fvc_batch_job_stats(fvc_batch *batch, int id, fvc_job_stats *out);
+/* Frees a finished job's device memory (its results become unavailable). */
+fvc_status fvc_batch_release(fvc_batch *batch, int id);
+fvc_status fvc_batch_get_stats(fvc_batch *batch, fvc_batch_stats *out);
+
+
 /* The context's CUDA stream (a cudaStream_t), for callers that record their
  * own events on it or order their work after the engine's. */
 void *fvc_stream(fvc_ctx *ctx);
