@@ -6,7 +6,9 @@
 // FP32 with a Kahan compensation term (the position is X - c).  Within
 // FVC_NEAR_FACE of an element face (in natural coordinates) the containment
 // test and the walk's face choice are ompVC's FP64 ones
-// (ompVC/velocity.c:512-617, ompVC/mesh.c:542-609) on X - c.
+// (ompVC/velocity.c:512-617, ompVC/mesh.c:542-609) on X - c; so is every
+// decision whose FP32 coordinates lie within their own error bound of a face
+// (nat32's tol, from the element's conditioning).
 //
 // The step sequence of a call (stage times, step lengths, tloc) is the FP64
 // host sequence of the call in a device table (StepM), so the step loop
@@ -76,29 +78,45 @@ __device__ __forceinline__ void node_vel_mx(const W& w, int node, float tl, floa
 }
 
 // FP32 natural coordinates of X in element e from its 64-byte FP32 record
-// (a11..a33, 1/V, x0, y0, z0 in 3D; a11..a22, 1/V, x0, y0 in 2D); returns
-// their minimum.
+// (a11..a33, 1/V, x0, y0, z0, A in 3D; a11..a22, 1/V, x0, y0, A in 2D);
+// returns their minimum.  tol bounds the coordinates' FP32 error: the
+// offsets X - x0 err by at most E = 2^-23 (|X| + |x0| + |dx|) per component
+// (half an ulp each for X against X - c, for the rounded x0 and for the
+// difference, with a factor 2 to spare), which moves each coordinate by at
+// most A E with A = sum |a_ij| / |V|, and the FP32 products and sums add at
+// most 1e-6 (1 + S) with S <= A max |dx| -- the bound of the FP64 form's
+// pre-check (fvc_device.cuh, quick_hop).  Ill-conditioned (sliver) elements
+// have a large A, so their walk decisions fall to the FP64 test.
 template <int D>
 __device__ __forceinline__ float nat32(const DevMesh& m, int e, const float X[3], float& r, float& s, float& t,
-                                       float& wv) {
+                                       float& wv, float& tol) {
   const float* q = m.geo32 + (long)e * 16;
   if (D == 3) {
     float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
     float4 q2 = __ldg(reinterpret_cast<const float4*>(q + 8));
-    float z0 = __ldg(q + 12);
-    float dx = X[0] - q2.z, dy = X[1] - q2.w, dz = X[2] - z0;
+    float2 q3 = __ldg(reinterpret_cast<const float2*>(q + 12));  // (z0, A)
+    float dx = X[0] - q2.z, dy = X[1] - q2.w, dz = X[2] - q3.x;
     r = fmaf(q0.x, dx, fmaf(q0.y, dy, q0.z * dz)) * q2.y;
     s = fmaf(q0.w, dx, fmaf(q1.x, dy, q1.y * dz)) * q2.y;
     t = fmaf(q1.z, dx, fmaf(q1.w, dy, q2.x * dz)) * q2.y;
     wv = 1.0f - r - s - t;
+    const float dm = fmaxf(fabsf(dx), fmaxf(fabsf(dy), fabsf(dz)));
+    const float xm = fmaxf(fabsf(X[0]), fmaxf(fabsf(X[1]), fabsf(X[2])));
+    const float om = fmaxf(fabsf(q2.z), fmaxf(fabsf(q2.w), fabsf(q3.x)));
+    tol = fmaf(q3.y, fmaf(1.2e-7f, xm + om + dm, 1e-6f * dm), 1e-6f);
     return fminf(fminf(r, s), fminf(t, wv));
   } else {
     float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
+    // q1 = (1/V, x0, y0, A)
     float dx = X[0] - q1.y, dy = X[1] - q1.z;
     r = fmaf(q0.x, dx, q0.y * dy) * q1.x;
     s = fmaf(q0.z, dx, q0.w * dy) * q1.x;
     t = 0.0f;
     wv = 1.0f - r - s;
+    const float dm = fmaxf(fabsf(dx), fabsf(dy));
+    const float xm = fmaxf(fabsf(X[0]), fabsf(X[1]));
+    const float om = fmaxf(fabsf(q1.y), fabsf(q1.z));
+    tol = fmaf(q1.w, fmaf(1.2e-7f, xm + om + dm, 1e-6f * dm), 1e-6f);
     return fminf(fminf(r, s), wv);
   }
 }
@@ -140,10 +158,13 @@ __device__ __forceinline__ int walk_mx(const DevMesh& m, const float X[3], const
     // beside its record
     nd = __ldg(m.elem + 2 * (long)eid);
     const int4 nb = __ldg(m.elem + 2 * (long)eid + 1);
-    const float d = nat32<D>(m, eid, X, r, s, t, wv);
+    float tol;
+    const float d = nat32<D>(m, eid, X, r, s, t, wv, tol);
+    // FP32 decides only outside the band its error bound leaves open
+    const float band = fmaxf(FVC_NEAR_FACE, 2.0f * tol);
     int slot;
-    if (d > FVC_NEAR_FACE) return 0;
-    if (d < -FVC_NEAR_FACE) {
+    if (d > band) return 0;
+    if (d < -band) {
       // the face of the smallest coordinate, first in r, s, t, 1-r-s-t order
       slot = (r == d) ? 0 : (s == d) ? 1 : (D == 3 && t == d) ? 2 : (D == 3 ? 3 : 2);
     } else {
