@@ -24,6 +24,11 @@ cpu_baseline  the CPU oracle (the reference's algorithm restated in C,
            OpenMP over all host cores) on a bounded sample: the same grid and
            mesh over the first 5 frame intervals (T = 0.1).
 
+batched    the bent-tube batch of 64 tracer releases (uneven seed counts and
+           windows) in the BF16 form and the FP64 form, one CUDA graph each.
+served     a Poisson request stream over the tube and the cube, served in the
+           BF16 and FP64 forms: p50 / p95 / p99 latency and steps/s.
+
 --impl reference runs that CPU implementation alone, every step one bounded
 sample, on the same metric.  Multi-GPU (torchrun, N > 1): every rank runs the
 whole workload on its own GPU (replicas; the window has no exchange step),
@@ -70,6 +75,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the BF16 / FP16 mixed forms")
     ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--no-batched", action="store_true", help="skip the bent-tube batch")
+    ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
+    ap.add_argument("--batch-jobs", type=int, default=64)
+    ap.add_argument("--served-rate", type=float, default=200.0, help="requests / s")
+    ap.add_argument("--served-seconds", type=float, default=10.0, help="arrival window, s")
     return ap.parse_args()
 
 
@@ -226,6 +236,69 @@ def run_reference(args, rank, world):
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ batched / served
+
+SERVED_BUDGET = 150 * 10 ** 9   # device bytes for frames plus job state, both sites
+
+
+def bench_batched(args, tube, frames):
+    """The bent-tube batch: 64 tracer releases (seed counts log-uniform in
+    [1e3, 1e6] on random cross-sections, windows U[0.2, 2] periods, forward or
+    backward), one persistent launch per tick, the whole schedule one CUDA
+    graph, launch shape autotuned; BF16 frames with FP32 stages against the
+    FP64 form on the same jobs."""
+    import serve
+    jobs = serve.tube_batch_jobs(tube, args.batch_jobs)
+    out = {"workload": f"{len(jobs)} tracer releases on the bent tube ({len(tube.conn)} tets, "
+                       f"{len(tube.xyz)} nodes, Womersley alpha=4, {serve.TUBE_FRAMES} frames a period), "
+                       "seeds log-uniform in [1e3, 1e6], T in U[0.2, 2] periods, +-direction, RK4 h=0.002",
+           "particles": int(sum(len(j[1]) for j in jobs)), "graph": True}
+    res = {}
+    for prec in ("bf16", "fp64"):
+        site = serve.tube_site(prec, tube=tube, frames=frames)
+        serve.warm_pairs(site)
+        steps, secs, wall, st, r = serve.run_batched(site, jobs, graph=True, tune=True, results=True)
+        res[prec] = r
+        out[prec] = {"value": steps / wall, "unit": "steps/s", "steps": int(steps), "wall_s": wall,
+                     "device_s": secs, "device_value": steps / secs if secs > 0 else None,
+                     "tuned": {"threads": st["tuned_threads"], "blocks": st["tuned_blocks"]}}
+        site.close()
+    out["speedup_vs_fp64"] = out["bf16"]["value"] / out["fp64"]["value"]
+    import serve as _s
+    out["bf16"]["errors_vs_fp64"] = _s.endpoint_errors(res["fp64"], res["bf16"])
+    return out
+
+
+def bench_served(args, tube, frames, cube_inputs):
+    """A request stream over both resident data sets: Poisson arrivals for
+    args.served_seconds, 50% tracer releases on the tube, 40% FTLE grids on
+    the cube, 10% residence-time releases on the tube; admission by an HBM
+    budget; latency from arrival to results on the host.  The same stream is
+    served in the BF16 form and in the FP64 form."""
+    import serve
+    xyz, conn, adj, cframes = cube_inputs
+    kw = dict(rate=args.served_rate, duration=args.served_seconds, seed=7)
+    out = {"workload": f"Poisson {args.served_rate:g} requests/s for {args.served_seconds:g} s: 50% tracer releases "
+                       "(tube, 1e3-1e5 seeds log-uniform, 0.2-2 periods), 40% FTLE grids (cube, 16^3-48^3, T=1), "
+                       "10% residence time (tube, 1e4 seeds, 3 periods)",
+           "hbm_budget_bytes": SERVED_BUDGET}
+    for prec in ("bf16", "fp64"):
+        reqs = serve.poisson_requests(tube, **kw)
+        frame_bytes = 32 * (len(tube.xyz) * serve.TUBE_FRAMES + len(xyz) * len(cframes))
+        budget = max((SERVED_BUDGET - frame_bytes) // 2, 1)
+        sites = {"tube": serve.tube_site(prec, tube=tube, frames=frames, hbm_budget=budget),
+                 "cube": serve.cube_site(prec, mesh=(xyz, conn, adj), frames=cframes, hbm_budget=budget)}
+        serve.warm_pairs(sites["tube"])
+        serve.run_batched(sites["cube"], [("ftle", (0, 1, 0, 1, 0, 1, 8, 8, 8), 0.0, 1.0)], graph=False, tune=False)
+        r = serve.serve(sites, reqs)
+        out[prec] = r
+        out["requests"] = r["requests"]
+        for st in sites.values():
+            st.close()
+    out["speedup_vs_fp64"] = out["bf16"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    return out
 
 
 # ------------------------------------------------------------------ ranks
@@ -412,6 +485,18 @@ def run_engine(args, rank, world, local_rank):
     else:
         ctx.close()
 
+    batched = served = None
+    if not (args.no_batched and args.no_served):
+        import serve
+        import synth
+        tube = synth.bent_tube_mesh()
+        _, tframes = synth.womersley_frames(tube, nframes=serve.TUBE_FRAMES)
+        if not args.no_batched:
+            batched = bench_batched(args, tube, tframes)
+        if not args.no_served:
+            served = bench_served(args, tube, tframes, inputs)
+        del tube, tframes
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         with tempfile.TemporaryDirectory() as td:
@@ -439,6 +524,8 @@ def run_engine(args, rank, world, local_rank):
             "gpu_launches": gpu_launches,
             "fp64_pipe": fp64_pipe,
             "precision_forms": forms,
+            "batched": batched,
+            "served": served,
             "phases_ms_per_step": {k: sum(s[k] for s in stats) / args.steps
                                    for k in ("ms_setup", "ms_main", "ms_early", "ms_reduce")},
             "fp64_probe": fp64,
