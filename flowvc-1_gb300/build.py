@@ -84,7 +84,7 @@ def build_host(force=False):
     hdrs = [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]
     if force or _newer(FVCFLOW, srcs + hdrs + [LIB, os.path.join(INCLUDE, "fvc.h")]):
         _run(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-Wall", "-Wno-format-truncation", "-I" + INCLUDE, *srcs,
-              "-L" + BUILD, "-lfvc", "-Wl,-rpath,$ORIGIN", "-lm", "-o", FVCFLOW])
+              "-L" + BUILD, "-lfvc", "-Wl,-rpath,$ORIGIN", "-lm", "-pthread", "-o", FVCFLOW])
     return FVCFLOW
 
 

@@ -154,6 +154,14 @@ extern "C" void fvc_destroy(fvc_ctx* c) {
   cudaFree(c->d_vt);
   cudaFree(c->d_cet_sum);
   cudaFree(c->d_cet_enc);
+  if (c->up_stream) {
+    cudaStreamSynchronize(c->up_stream);
+    cudaStreamDestroy(c->up_stream);
+  }
+  for (auto& kv : c->frame_ev) cudaEventDestroy(kv.second);
+  if (c->up_after) cudaEventDestroy(c->up_after);
+  cudaFree(c->d_up_stage[0]);
+  cudaFree(c->d_up_stage[1]);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -355,6 +363,7 @@ extern "C" fvc_status fvc_upload_frame(fvc_ctx* c, int frame_id, const double* u
     c->frames.erase(frame_id);
     return fail(c, FVC_ERR_OOM, "frame allocation failed");
   }
+  frame_dep(c, frame_id);
   FVC_CUDA(c, cudaMemcpyAsync(c->d_stage, uvw, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
   auto qf = c->qframes.find(frame_id);
   if (qf != c->qframes.end()) qf->second.fmt = 0;  // stale: quantised again when next used
@@ -364,11 +373,96 @@ extern "C" fvc_status fvc_upload_frame(fvc_ctx* c, int frame_id, const double* u
   return FVC_OK;
 }
 
+void frame_dep(fvc_ctx* c, int id) {
+  auto e = c->frame_ev.find(id);
+  if (e != c->frame_ev.end()) cudaStreamWaitEvent(c->stream, e->second, 0);
+}
+
+extern "C" fvc_status fvc_host_alloc(void** p, size_t bytes) {
+  if (!p) return FVC_ERR_ARG;
+  *p = nullptr;
+  if (cudaMallocHost(p, bytes ? bytes : 1) != cudaSuccess) {
+    *p = nullptr;
+    return FVC_ERR_OOM;
+  }
+  return FVC_OK;
+}
+
+extern "C" void fvc_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+extern "C" fvc_status fvc_upload_frame_async(fvc_ctx* c, int frame_id, const double* uvw) {
+  if (!c || !uvw) return FVC_ERR_ARG;
+  if (!c->mesh_set) return fail(c, FVC_ERR_STATE, "set the mesh before uploading frames");
+  if (frame_id < 0 || frame_id >= 65536) return fail(c, FVC_ERR_ARG, "frame id %d out of range", frame_id);
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  const long n = c->frame_nodes;
+  const size_t bytes = sizeof(double) * 3 * (size_t)n;
+  if (!c->up_stream) {
+    FVC_CUDA(c, cudaStreamCreateWithFlags(&c->up_stream, cudaStreamNonBlocking));
+    FVC_CUDA(c, cudaEventCreateWithFlags(&c->up_after, cudaEventDisableTiming));
+  }
+  for (int k = 0; k < 2; k++)
+    if (!c->d_up_stage[k] && cudaMalloc(&c->d_up_stage[k], bytes) != cudaSuccess)
+      return fail(c, FVC_ERR_OOM, "frame staging allocation failed");
+  double4_32a*& dst = c->frames[frame_id];
+  if (!dst && cudaMalloc(&dst, sizeof(double4_32a) * (size_t)n) != cudaSuccess) {
+    c->frames.erase(frame_id);
+    return fail(c, FVC_ERR_OOM, "frame allocation failed");
+  }
+  cudaEvent_t& ev = c->frame_ev[frame_id];
+  if (!ev) FVC_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  // work already queued on the context's stream may still read the frame
+  // this upload replaces
+  FVC_CUDA(c, cudaEventRecord(c->up_after, c->stream));
+  FVC_CUDA(c, cudaStreamWaitEvent(c->up_stream, c->up_after, 0));
+  // two staging buffers: an upload reuses one after the pack that read it,
+  // which the side stream orders before it
+  double* stage = c->d_up_stage[c->up_k];
+  c->up_k ^= 1;
+  FVC_CUDA(c, cudaMemcpyAsync(stage, uvw, bytes, cudaMemcpyHostToDevice, c->up_stream));
+  pack_frame(stage, dst, n, c->up_stream);
+  if ((st = check_launch(c, "pack_frame"))) return st;
+  auto qf = c->qframes.find(frame_id);
+  if (qf != c->qframes.end()) qf->second.fmt = 0;
+  FVC_CUDA(c, cudaEventRecord(ev, c->up_stream));
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_frame_ready(fvc_ctx* c, int frame_id, int* ready) {
+  if (!c || !ready) return FVC_ERR_ARG;
+  auto e = c->frame_ev.find(frame_id);
+  if (e == c->frame_ev.end()) {
+    *ready = c->frames.count(frame_id) ? 1 : 0;
+    return FVC_OK;
+  }
+  cudaError_t q = cudaEventQuery(e->second);
+  if (q == cudaErrorNotReady) {
+    *ready = 0;
+    return FVC_OK;
+  }
+  if (q != cudaSuccess) return fail(c, FVC_ERR_CUDA, "frame %d upload: %s", frame_id, cudaGetErrorString(q));
+  *ready = 1;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_frame_wait(fvc_ctx* c, int frame_id) {
+  if (!c) return FVC_ERR_ARG;
+  auto e = c->frame_ev.find(frame_id);
+  if (e == c->frame_ev.end()) return FVC_OK;
+  cudaError_t q = cudaEventSynchronize(e->second);
+  if (q != cudaSuccess) return fail(c, FVC_ERR_CUDA, "frame %d upload: %s", frame_id, cudaGetErrorString(q));
+  return FVC_OK;
+}
+
 // The quantised copy of a resident frame in the context's 16-bit format,
 // made on first use after the frame was uploaded or the format changed.
 fvc_status quantised(fvc_ctx* c, int id, fvc_ctx::QFrame** out) {
   fvc_ctx::QFrame& q = c->qframes[id];
   if (q.fmt != c->prec) {
+    frame_dep(c, id);
     long n = c->frame_nodes;
     if (!q.q && cudaMalloc(&q.q, sizeof(ushort4) * (size_t)n) != cudaSuccess)
       return fail(c, FVC_ERR_OOM, "quantised frame allocation failed");
@@ -431,6 +525,8 @@ extern "C" fvc_status fvc_set_window(fvc_ctx* c, int lo, int hi, double tmin, do
   auto a = c->frames.find(lo), b = c->frames.find(hi);
   if (a == c->frames.end() || b == c->frames.end())
     return fail(c, FVC_ERR_STATE, "frames %d / %d are not resident", lo, hi);
+  frame_dep(c, lo);
+  frame_dep(c, hi);
   c->window.f0 = a->second;
   c->window.f1 = b->second;
   c->window.tmin = tmin;

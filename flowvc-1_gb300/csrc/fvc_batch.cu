@@ -392,6 +392,8 @@ static fvc_status job_window(fvc_batch* b, const Interval& I, const StepM* d_ste
   auto a = c->frames.find(flo), z = c->frames.find(fhi);
   if (a == c->frames.end() || z == c->frames.end())
     return fail(c, FVC_ERR_STATE, "frames %d / %d are not resident", flo, fhi);
+  frame_dep(c, flo);
+  frame_dep(c, fhi);
   memset(&w, 0, sizeof(w));
   w.f0 = a->second;
   w.f1 = z->second;

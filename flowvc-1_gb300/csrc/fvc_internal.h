@@ -53,6 +53,13 @@ struct fvc_ctx {
   StepM* d_steps = nullptr;
   size_t steps_cap = 0;
   int window_lo = -1, window_hi = -1;
+  // asynchronous frame uploads: a side stream, a two-buffer staging ring and
+  // per frame the event its upload recorded
+  cudaStream_t up_stream = nullptr;
+  double* d_up_stage[2] = {nullptr, nullptr};
+  int up_k = 0;
+  cudaEvent_t up_after = nullptr;  // compute-stream point an upload must follow
+  std::unordered_map<int, cudaEvent_t> frame_ev;
   // exposure time (Trace_CETCompute): per-element sums shared by all releases
   double* d_cet_sum = nullptr;
   int* d_cet_enc = nullptr;
@@ -82,6 +89,8 @@ fvc_status quantised(fvc_ctx* c, int id, fvc_ctx::QFrame** out);
 // the integrator / precision combination is one the form supports
 fvc_status mixed_ok(fvc_ctx* c);
 void job_events(fvc_job* j);
+// orders the context's stream after a pending asynchronous upload of frame id
+void frame_dep(fvc_ctx* c, int id);
 float ev_ms(cudaEvent_t a, cudaEvent_t b);
 // (X, c) float pairs copied to the host back to FP64 positions X - c
 void unpack_host(double* A, size_t n);

@@ -106,6 +106,11 @@ SIGNATURES = {
     "fvc_cet_enable": (C.c_int, [_vp, C.c_int]),
     "fvc_cet_results": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip]),
     "fvc_tracer_residence": (C.c_int, [_vp, C.c_double, C.c_double, _dp]),
+    "fvc_upload_frame_async": (C.c_int, [_vp, C.c_int, _dp]),
+    "fvc_frame_ready": (C.c_int, [_vp, C.c_int, _ip]),
+    "fvc_frame_wait": (C.c_int, [_vp, C.c_int]),
+    "fvc_host_alloc": (C.c_int, [C.POINTER(_vp), C.c_size_t]),
+    "fvc_host_free": (None, [_vp]),
     "fvc_batch_create": (C.c_int, [_vp, C.POINTER(BatchOpts), C.POINTER(_vp)]),
     "fvc_batch_destroy": (None, [_vp]),
     "fvc_batch_submit": (C.c_int, [_vp, C.POINTER(BatchJobSpec), _ip]),
@@ -149,6 +154,30 @@ def probe_fp64(device=0):
     if st:
         raise FvcError(st, "fvc_probe_fp64 failed")
     return float(r[0]), float(r[1])
+
+
+class PinnedArray:
+    """A float64 numpy array in page-locked host memory (fvc_host_alloc),
+    freed with the object."""
+
+    def __init__(self, shape):
+        lib = load()
+        self.lib = lib
+        n = int(np.prod(shape))
+        self.p = _vp()
+        st = lib.fvc_host_alloc(C.byref(self.p), max(n, 1) * 8)
+        if st:
+            raise FvcError(st, "fvc_host_alloc failed")
+        buf = (C.c_double * max(n, 1)).from_address(self.p.value)
+        self.a = np.frombuffer(buf, dtype=np.float64, count=n).reshape(shape)
+
+    def __del__(self):
+        try:
+            if self.p:
+                self.lib.fvc_host_free(self.p)
+                self.p = _vp()
+        except Exception:
+            pass
 
 
 class FvcError(RuntimeError):
@@ -233,6 +262,20 @@ class Context:
     def upload_frame(self, frame_id, uvw):
         uvw = f64(uvw)
         self._chk(self.lib.fvc_upload_frame(self.h, frame_id, _d(uvw)))
+
+    def upload_frame_async(self, frame_id, uvw):
+        """Starts the upload; uvw (a C-contiguous float64 array, pinned for
+        overlap) must stay alive and unchanged until frame_wait / frame_ready."""
+        assert uvw.dtype == np.float64 and uvw.flags.c_contiguous
+        self._chk(self.lib.fvc_upload_frame_async(self.h, frame_id, _d(uvw)))
+
+    def frame_ready(self, frame_id):
+        r = C.c_int(0)
+        self._chk(self.lib.fvc_frame_ready(self.h, frame_id, C.byref(r)))
+        return bool(r.value)
+
+    def frame_wait(self, frame_id):
+        self._chk(self.lib.fvc_frame_wait(self.h, frame_id))
 
     def set_window(self, lo, hi, tmin, tmax):
         self._chk(self.lib.fvc_set_window(self.h, lo, hi, tmin, tmax))

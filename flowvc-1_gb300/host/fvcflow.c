@@ -21,6 +21,7 @@
  * grid state of every output: n, X, element ids, left flags, have flags).
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -68,6 +69,7 @@ typedef struct {
     double t_compute;
     const char *dump_dir; /* --dump-state: final FTLE grid state per output */
     long nelem;           /* elements of the unstructured mesh */
+    struct frame_pipe *pipe;  /* frame reader ahead of the computation */
 } run_t;
 
 /* frame index -> file index with ompVC's wrap (ompVC/velocity.c:77-80) */
@@ -130,6 +132,153 @@ static int load_mesh(run_t *R)
     return (!R->frame_buf || !R->resident) ? (fprintf(stderr, "out of memory\n"), 1) : 0;
 }
 
+/* ---- frame pipeline: a reader thread reads the frame files in the order
+ * the frame loop first needs them into a ring of page-locked buffers, and
+ * the main thread uploads each one asynchronously (fvc_upload_frame_async)
+ * as soon as it is read, so file reads and host-to-device copies overlap
+ * the kernels of earlier intervals.  A ring slot returns to the reader once
+ * its upload has completed (fvc_frame_ready / fvc_frame_wait). */
+#define PIPE_SLOTS 4
+
+typedef struct frame_pipe {
+    run_t *R;
+    int n;            /* frames in first-use order */
+    int *seq;         /* file index of each */
+    int *pos;         /* file index -> position in seq, -1 if unused */
+    double *buf;      /* PIPE_SLOTS page-locked frames */
+    int nread, up, rel, err, stop;
+    pthread_mutex_t mu;
+    pthread_cond_t cv;
+    pthread_t th;
+    int started;
+} frame_pipe;
+
+static int read_frame_file(const fvcp_params *P, int mod, double *dst, long len)
+{
+    char path[2 * FVCP_STR];
+    snprintf(path, sizeof(path), "%s%s_vel.%d.bin", P->path_data, P->prefix, P->suffix_tmin + mod * P->suffix_tdelta);
+    FILE *f = fopen(path, "rb");
+    double ts;
+    if (!f) { fprintf(stderr, "Could not open file %s\n", path); return 1; }
+    if (fread(&ts, 8, 1, f) != 1 || (long)fread(dst, 8, (size_t)len, f) != len) {
+        fclose(f);
+        fprintf(stderr, "Could not load velocity data from %s\n", path);
+        return 1;
+    }
+    fclose(f);
+    return 0;
+}
+
+static void *pipe_reader(void *arg)
+{
+    frame_pipe *F = (frame_pipe *)arg;
+    for (int i = 0; i < F->n; i++) {
+        pthread_mutex_lock(&F->mu);
+        while (!F->stop && i - F->rel >= PIPE_SLOTS) pthread_cond_wait(&F->cv, &F->mu);
+        int stop = F->stop;
+        pthread_mutex_unlock(&F->mu);
+        if (stop) break;
+        int bad = read_frame_file(&F->R->P, F->seq[i], F->buf + (long)(i % PIPE_SLOTS) * F->R->frame_len,
+                                  F->R->frame_len);
+        pthread_mutex_lock(&F->mu);
+        if (bad) F->err = 1;
+        else F->nread = i + 1;
+        pthread_cond_broadcast(&F->cv);
+        pthread_mutex_unlock(&F->mu);
+        if (bad) break;
+    }
+    return NULL;
+}
+
+/* The frame files of intervals first .. last (exclusive) in first-use order. */
+static int pipe_start(run_t *R)
+{
+    fvcp_params *P = &R->P;
+    frame_pipe *F = (frame_pipe *)calloc(1, sizeof(frame_pipe));
+    if (!F) return 1;
+    F->R = R;
+    int nfiles = P->tres;
+    F->pos = (int *)malloc(sizeof(int) * (size_t)nfiles);
+    F->seq = (int *)malloc(sizeof(int) * (size_t)nfiles);
+    if (!F->pos || !F->seq) return 1;
+    for (int k = 0; k < nfiles; k++) F->pos[k] = -1;
+    for (int df = P->first_frame; df != P->last_frame; df += P->int_dir) {
+        int lo = P->int_dir > 0 ? df : df - 1;
+        for (int e = 0; e < 2; e++) {
+            int mod = frame_mod(P, lo + e);
+            if (F->pos[mod] < 0) { F->pos[mod] = F->n; F->seq[F->n++] = mod; }
+        }
+    }
+    if (fvc_host_alloc((void **)&F->buf, sizeof(double) * (size_t)R->frame_len * PIPE_SLOTS)) {
+        fprintf(stderr, "could not allocate page-locked frame buffers\n");
+        return 1;
+    }
+    pthread_mutex_init(&F->mu, NULL);
+    pthread_cond_init(&F->cv, NULL);
+    if (pthread_create(&F->th, NULL, pipe_reader, F)) return 1;
+    F->started = 1;
+    R->pipe = F;
+    return 0;
+}
+
+static void pipe_stop(run_t *R)
+{
+    frame_pipe *F = R->pipe;
+    if (!F) return;
+    if (F->started) {
+        pthread_mutex_lock(&F->mu);
+        F->stop = 1;
+        pthread_cond_broadcast(&F->cv);
+        pthread_mutex_unlock(&F->mu);
+        pthread_join(F->th, NULL);
+        pthread_mutex_destroy(&F->mu);
+        pthread_cond_destroy(&F->cv);
+    }
+    /* page-locked buffers may still be read by uploads in flight */
+    for (int i = F->rel; i < F->up; i++) fvc_frame_wait(R->ctx, F->seq[i]);
+    fvc_host_free(F->buf);
+    free(F->seq);
+    free(F->pos);
+    free(F);
+    R->pipe = NULL;
+}
+
+/* Uploads every frame read so far, returns slots whose uploads finished, and
+ * returns once the frame at position `need` is uploaded (need < 0: no wait). */
+static int pipe_pump(run_t *R, int need)
+{
+    frame_pipe *F = R->pipe;
+    pthread_mutex_lock(&F->mu);
+    for (;;) {
+        int ready = 1;
+        while (F->rel < F->up && !fvc_frame_ready(R->ctx, F->seq[F->rel], &ready) && ready) {
+            F->rel++;
+            pthread_cond_broadcast(&F->cv);
+        }
+        while (F->up < F->nread) {
+            int rc = fvc_upload_frame_async(R->ctx, F->seq[F->up], F->buf + (long)(F->up % PIPE_SLOTS) * R->frame_len);
+            if (rc) { pthread_mutex_unlock(&F->mu); return die("frame upload", R->ctx, rc); }
+            F->up++;
+        }
+        if (need < 0 || F->up > need) break;
+        if (F->err) { pthread_mutex_unlock(&F->mu); return 1; }
+        if (F->nread - F->rel >= PIPE_SLOTS) {
+            /* the reader waits for a slot: free the oldest */
+            int mod = F->seq[F->rel];
+            pthread_mutex_unlock(&F->mu);
+            int rc = fvc_frame_wait(R->ctx, mod);
+            pthread_mutex_lock(&F->mu);
+            if (rc) { pthread_mutex_unlock(&F->mu); return die("frame upload", R->ctx, rc); }
+            F->rel++;
+            pthread_cond_broadcast(&F->cv);
+            continue;
+        }
+        pthread_cond_wait(&F->cv, &F->mu);
+    }
+    pthread_mutex_unlock(&F->mu);
+    return 0;
+}
+
 /* Upload the file behind frame index `frame` once; it stays resident under
  * its file index (Load*VelDataFrame, ompVC/velocity.c:61-234). */
 static int ensure_frame(run_t *R, int frame)
@@ -137,6 +286,11 @@ static int ensure_frame(run_t *R, int frame)
     fvcp_params *P = &R->P;
     int mod = frame_mod(P, frame);
     if (R->resident[mod]) return 0;
+    if (R->pipe && R->pipe->pos[mod] >= 0) {
+        if (pipe_pump(R, R->pipe->pos[mod])) return 1;
+        R->resident[mod] = 1;
+        return 0;
+    }
     char path[2 * FVCP_STR];
     snprintf(path, sizeof(path), "%s%s_vel.%d.bin", P->path_data, P->prefix, P->suffix_tmin + mod * P->suffix_tdelta);
     FILE *f = fopen(path, "rb");
@@ -634,7 +788,9 @@ int main(int argc, char **argv)
     if (R.P.int_type == 2 && (rc = fvc_set_rkf(R.ctx, R.P.int_acc, R.P.int_hmin, R.P.int_hmax)))
         return die("RKF settings", R.ctx, rc);
     int bad = load_mesh(&R);
+    if (!bad) bad = pipe_start(&R);
     if (!bad) bad = R.P.ftle_compute ? run_ftle(&R) : run_tracers(&R);
+    pipe_stop(&R);
     if (!bad && stats)
         printf("{\"steps\": %lld, \"compute_seconds\": %.6f, \"total_seconds\": %.6f}\n", R.steps, R.t_compute, wall() - t_start);
     free(R.frame_buf);

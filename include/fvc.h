@@ -24,6 +24,8 @@
 #ifndef FVC_H
 #define FVC_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -93,6 +95,24 @@ fvc_status fvc_set_rkf(fvc_ctx *ctx, double accuracy, double min_step, double ma
  * frame_id (0 <= frame_id < 65536) until replaced; replaces
  * Load{Cart,Unstruct}VelDataFrame (ompVC/velocity.c:61-234). */
 fvc_status fvc_upload_frame(fvc_ctx *ctx, int frame_id, const double *uvw);
+
+/* The frame pipeline: fvc_upload_frame without waiting.  The copy and the
+ * repacking run on a side stream while the context's stream computes; every
+ * later use of the frame (fvc_set_window, the mixed form's quantiser, batch
+ * ticks) waits for it on the device, in stream order, and work already queued
+ * that reads the frame id being replaced finishes first.  uvw must stay
+ * unchanged until fvc_frame_ready reports 1 or fvc_frame_wait returns; from
+ * pinned memory (fvc_host_alloc) the copy overlaps the computation, from
+ * pageable memory it does not.  Replaces the blocking read-and-load of
+ * Load{Cart,Unstruct}VelDataFrame (ompVC/velocity.c:61-234) in the frame loop
+ * (ompVC/main.c:188-199). */
+fvc_status fvc_upload_frame_async(fvc_ctx *ctx, int frame_id, const double *uvw);
+fvc_status fvc_frame_ready(fvc_ctx *ctx, int frame_id, int *ready);
+fvc_status fvc_frame_wait(fvc_ctx *ctx, int frame_id);
+/* Page-locked host memory for frame staging (cudaMallocHost); no reference
+ * counterpart. */
+fvc_status fvc_host_alloc(void **ptr, size_t bytes);
+void fvc_host_free(void *ptr);
 
 /* Select the two resident frames bracketing [tmin, tmax] (Data_LoadedTMin /
  * Data_LoadedTMax, ompVC/main.c:188-195); frame_lo is the frame at tmin. */
