@@ -212,6 +212,67 @@ static void batch_advance(const DevMesh& m, const DevInteg& in, const BJob* jobs
   }
 }
 
+// ---- spatial ordering of a release's tracers (Z-order of 64^3 cells over
+// the seeds' box): a warp's 32 tracers then walk neighbouring elements and
+// share their records and frame nodes in cache.  Advection is independent
+// per tracer, so the order changes no result; results are read back in seed
+// order through the permutation.
+
+__device__ __forceinline__ unsigned spread6(unsigned v) {  // 6 bits -> every third bit
+  unsigned r = 0;
+#pragma unroll
+  for (int b = 0; b < 6; b++) r |= ((v >> b) & 1u) << (3 * b);
+  return r;
+}
+
+__global__ void k_zkeys(const double* X, int n, int packed, double3 lo, double3 inv, int* key, int* hist) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const double v = X[3 * i + a];
+    if (packed) {
+      const float2 p = *reinterpret_cast<const float2*>(&X[3 * i + a]);
+      x[a] = (double)p.x - (double)p.y;
+    } else {
+      x[a] = v;
+    }
+  }
+  const double l[3] = {lo.x, lo.y, lo.z}, s[3] = {inv.x, inv.y, inv.z};
+  unsigned c[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const double f = (x[a] - l[a]) * s[a];
+    c[a] = f < 0.0 ? 0u : f > 63.0 ? 63u : (unsigned)f;
+  }
+  const int k = (int)(spread6(c[0]) | (spread6(c[1]) << 1) | (spread6(c[2]) << 2));
+  key[i] = k;
+  atomicAdd(hist + k, 1);
+}
+
+__global__ void k_zscatter(const int* key, int n, const int* off, int* cur, int* perm) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k = key[i];
+  perm[off[k] + atomicAdd(cur + k, 1)] = (int)i;
+}
+
+// out[j] = in[perm[j]] for the tracer state (X, V as 3 doubles, eid, left, ldt)
+__global__ void k_zgather(TracerDev t, const int* perm, double* X2, double* V2, int* e2, int* l2, double* d2) {
+  long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= t.n) return;
+  const long i = perm[j];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    X2[3 * j + a] = t.X[3 * i + a];
+    V2[3 * j + a] = t.V[3 * i + a];
+  }
+  e2[j] = t.eid[i];
+  l2[j] = t.left[i];
+  d2[j] = t.ldt[i];
+}
+
 }  // namespace fvc
 
 // ====================================================================== host
@@ -238,6 +299,7 @@ struct HostJob {
   cudaEvent_t done = nullptr;
   long long ticks = 0;
   long npts = 0;  // points (work-queue entries at most)
+  std::vector<int> perm;  // tracers: device position -> seed index (empty: seed order)
   fvc_status err = FVC_OK;
   std::string msg;
 };
@@ -433,6 +495,65 @@ static fvc_status job_window(fvc_batch* b, const Interval& I, const StepM* d_ste
 
 // ------------------------------------------------------------ admission
 
+// Reorders a located release's tracers along the Z-order curve of 64^3 cells
+// over the seeds' bounding box (counting sort: key histogram, scan, scatter,
+// gather) and keeps the permutation for reading results in seed order.
+static fvc_status zorder_tracers(fvc_batch* b, HostJob& J) {
+  fvc_ctx* c = b->c;
+  TracerDev& t = J.job->t;
+  const int n = t.n;
+  if (n < 64) return FVC_OK;
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (long i = 0; i < n; i++)
+    for (int a = 0; a < 3; a++) {
+      lo[a] = std::min(lo[a], J.seeds[3 * i + a]);
+      hi[a] = std::max(hi[a], J.seeds[3 * i + a]);
+    }
+  double3 dlo = make_double3(lo[0], lo[1], lo[2]), inv;
+  double* ip = &inv.x;
+  for (int a = 0; a < 3; a++) ip[a] = hi[a] > lo[a] ? 64.0 / (hi[a] - lo[a]) : 0.0;
+  const int K = 1 << 18;
+  const size_t nb = (size_t)n;
+  char* mem = nullptr;
+  const size_t bytes = 4 * nb * 2 + 4 * (3 * (size_t)K + 2) + 8 * ((size_t)K / 1024 + 2) + 64 * nb + 256 * 16;
+  if (cudaMalloc(&mem, bytes) != cudaSuccess) return FVC_OK;  // no room: keep seed order
+  char* q = mem;
+  auto take = [&](size_t sz) { char* r = q; q += (sz + 255) & ~(size_t)255; return r; };
+  int* key = (int*)take(4 * nb);
+  int* perm = (int*)take(4 * nb);
+  int* hist = (int*)take(4 * (size_t)K);
+  int* off = (int*)take(4 * ((size_t)K + 1));
+  int* cur = (int*)take(4 * (size_t)K);
+  long long* tmp = (long long*)take(8 * ((size_t)K / 1024 + 2));
+  double* X2 = (double*)take(24 * nb);
+  double* V2 = (double*)take(24 * nb);
+  int* e2 = (int*)take(4 * nb);
+  int* l2 = (int*)take(4 * nb);
+  double* d2 = (double*)take(8 * nb);
+  cudaStream_t s = c->stream;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  cudaMemsetAsync(hist, 0, 4 * (size_t)K, s);
+  cudaMemsetAsync(cur, 0, 4 * (size_t)K, s);
+  k_zkeys<<<g, 256, 0, s>>>(t.X, n, J.job->packed ? 1 : 0, dlo, inv, key, hist);
+  scan_counts(hist, off, K, tmp, s);
+  k_zscatter<<<g, 256, 0, s>>>(key, n, off, cur, perm);
+  k_zgather<<<g, 256, 0, s>>>(t, perm, X2, V2, e2, l2, d2);
+  cudaMemcpyAsync(t.X, X2, 24 * nb, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(t.V, V2, 24 * nb, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(t.eid, e2, 4 * nb, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(t.left, l2, 4 * nb, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(t.ldt, d2, 8 * nb, cudaMemcpyDeviceToDevice, s);
+  J.perm.resize(nb);
+  cudaMemcpyAsync(J.perm.data(), perm, 4 * nb, cudaMemcpyDeviceToHost, s);
+  fvc_status st = check_launch(c, "z-order");
+  cudaError_t e = cudaStreamSynchronize(s);
+  cudaFree(mem);
+  if (st) return st;
+  if (e != cudaSuccess) return fail(c, FVC_ERR_CUDA, "z-order: %s", cudaGetErrorString(e));
+  b->stats.launches += 6;
+  return FVC_OK;
+}
+
 static fvc_status admit_one(fvc_batch* b, HostJob& J) {
   fvc_ctx* c = b->c;
   fvc_status st;
@@ -447,6 +568,7 @@ static fvc_status admit_one(fvc_batch* b, HostJob& J) {
     sp.local_search_checking = J.spec.local_search_checking;
     sp.seed_chain = 0;
     st = fvc_tracer_create(c, &sp, J.spec.n, J.seeds.data(), &J.job);
+    if (!st) st = zorder_tracers(b, J);
   }
   if (st) return st;
   J.slot = b->free_slots.back();
@@ -1069,18 +1191,34 @@ static fvc_status job_ready(fvc_batch* b, HostJob* J, int kind_ok) {
   return FVC_OK;
 }
 
+// v (count items of w elements each, in device order) back to seed order
+template <class T>
+static void unpermute(const std::vector<int>& perm, T* v, size_t w) {
+  if (!v || perm.empty()) return;
+  std::vector<T> tmp(v, v + perm.size() * w);
+  for (size_t j = 0; j < perm.size(); j++)
+    for (size_t a = 0; a < w; a++) v[(size_t)perm[j] * w + a] = tmp[j * w + a];
+}
+
 extern "C" fvc_status fvc_batch_tracer_result(fvc_batch* b, int id, double* X, int* eid, int* left, double* ldt) {
   HostJob* J = job_of(b, id);
   fvc_status st = job_ready(b, J, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE));
   if (st) return st;
-  return fvc_tracer_get_state(J->job, X, eid, left, ldt);
+  if ((st = fvc_tracer_get_state(J->job, X, eid, left, ldt))) return st;
+  unpermute(J->perm, X, 3);
+  unpermute(J->perm, eid, 1);
+  unpermute(J->perm, left, 1);
+  unpermute(J->perm, ldt, 1);
+  return FVC_OK;
 }
 
 extern "C" fvc_status fvc_batch_residence_result(fvc_batch* b, int id, double* rt) {
   HostJob* J = job_of(b, id);
   fvc_status st = job_ready(b, J, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE));
   if (st) return st;
-  return fvc_tracer_residence(J->job, J->spec.t_start, J->stop, rt);
+  if ((st = fvc_tracer_residence(J->job, J->spec.t_start, J->stop, rt))) return st;
+  unpermute(J->perm, rt, 1);
+  return FVC_OK;
 }
 
 extern "C" fvc_status fvc_batch_ftle_result(fvc_batch* b, int id, double* wT, double* wN) {
@@ -1122,6 +1260,8 @@ extern "C" fvc_status fvc_batch_release(fvc_batch* b, int id) {
   }
   J->seeds.clear();
   J->seeds.shrink_to_fit();
+  J->perm.clear();
+  J->perm.shrink_to_fit();
   if (J->state != JQ_FAILED) J->state = JQ_RELEASED;
   return FVC_OK;
 }

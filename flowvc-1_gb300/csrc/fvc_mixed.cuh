@@ -80,9 +80,9 @@ __device__ __forceinline__ void node_vel_mx(const W& w, int node, float tl, floa
 // FP32 natural coordinates of X in element e from its 64-byte FP32 record
 // (a11..a33, 1/V, x0, y0, z0, A in 3D; a11..a22, 1/V, x0, y0, A in 2D);
 // returns their minimum.  tol bounds the coordinates' FP32 error: the
-// offsets X - x0 err by at most E = 2^-23 (|X| + |x0| + |dx|) per component
+// offsets X - x0 err by at most E = 2^-24 (|X| + |x0| + |dx|) per component
 // (half an ulp each for X against X - c, for the rounded x0 and for the
-// difference, with a factor 2 to spare), which moves each coordinate by at
+// difference), which moves each coordinate by at
 // most A E with A = sum |a_ij| / |V|, and the FP32 products and sums add at
 // most 1e-6 (1 + S) with S <= A max |dx| -- the bound of the FP64 form's
 // pre-check (fvc_device.cuh, quick_hop).  Ill-conditioned (sliver) elements
@@ -103,7 +103,7 @@ __device__ __forceinline__ float nat32(const DevMesh& m, int e, const float X[3]
     const float dm = fmaxf(fabsf(dx), fmaxf(fabsf(dy), fabsf(dz)));
     const float xm = fmaxf(fabsf(X[0]), fmaxf(fabsf(X[1]), fabsf(X[2])));
     const float om = fmaxf(fabsf(q2.z), fmaxf(fabsf(q2.w), fabsf(q3.x)));
-    tol = fmaf(q3.y, fmaf(1.2e-7f, xm + om + dm, 1e-6f * dm), 1e-6f);
+    tol = fmaf(q3.y, fmaf(6.0e-8f, xm + om + dm, 1e-6f * dm), 1e-6f);
     return fminf(fminf(r, s), fminf(t, wv));
   } else {
     float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
@@ -116,7 +116,49 @@ __device__ __forceinline__ float nat32(const DevMesh& m, int e, const float X[3]
     const float dm = fmaxf(fabsf(dx), fabsf(dy));
     const float xm = fmaxf(fabsf(X[0]), fabsf(X[1]));
     const float om = fmaxf(fabsf(q1.y), fabsf(q1.z));
-    tol = fmaf(q1.w, fmaf(1.2e-7f, xm + om + dm, 1e-6f * dm), 1e-6f);
+    tol = fmaf(q1.w, fmaf(6.0e-8f, xm + om + dm, 1e-6f * dm), 1e-6f);
+    return fminf(fminf(r, s), wv);
+  }
+}
+
+// The same coordinates with exact offsets: (X - C) - x0 formed in FP64 from
+// the element's FP64 node (6 FP64 adds, no FP64 solve) and rounded once to
+// FP32, then the FP32 map.  The offsets then err by 2^-24 |dx| instead of by
+// the FP32 positions' rounding, so tol shrinks to the map's own rounding,
+// 1e-6 (1 + S) + 6e-8 A max |dx|, about 1e-5 for a well-shaped element.
+template <int D>
+__device__ __forceinline__ float nat32_fine(const DevMesh& m, int e, const float X[3], const float C[3], float& r,
+                                            float& s, float& t, float& wv, float& tol) {
+  const float* q = m.geo32 + (long)e * 16;
+  if (D == 3) {
+    const double* g = m.geom + (long)e * 16;
+    const double2 gxy = __ldg(reinterpret_cast<const double2*>(g + 10));
+    const double gz = __ldg(g + 12);
+    const float dx = (float)(((double)X[0] - (double)C[0]) - gxy.x);
+    const float dy = (float)(((double)X[1] - (double)C[1]) - gxy.y);
+    const float dz = (float)(((double)X[2] - (double)C[2]) - gz);
+    float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
+    float4 q2 = __ldg(reinterpret_cast<const float4*>(q + 8));
+    const float A = __ldg(q + 13);
+    r = fmaf(q0.x, dx, fmaf(q0.y, dy, q0.z * dz)) * q2.y;
+    s = fmaf(q0.w, dx, fmaf(q1.x, dy, q1.y * dz)) * q2.y;
+    t = fmaf(q1.z, dx, fmaf(q1.w, dy, q2.x * dz)) * q2.y;
+    wv = 1.0f - r - s - t;
+    const float dm = fmaxf(fabsf(dx), fmaxf(fabsf(dy), fabsf(dz)));
+    tol = fmaf(A, 1.06e-6f * dm, 1e-6f);
+    return fminf(fminf(r, s), fminf(t, wv));
+  } else {
+    const double* g = m.geom + (long)e * 12;
+    const double gx = __ldg(g + 5), gy = __ldg(g + 6);
+    const float dx = (float)(((double)X[0] - (double)C[0]) - gx);
+    const float dy = (float)(((double)X[1] - (double)C[1]) - gy);
+    float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
+    r = fmaf(q0.x, dx, q0.y * dy) * q1.x;
+    s = fmaf(q0.z, dx, q0.w * dy) * q1.x;
+    t = 0.0f;
+    wv = 1.0f - r - s;
+    const float dm = fmaxf(fabsf(dx), fabsf(dy));
+    tol = fmaf(q1.w, 1.06e-6f * dm, 1e-6f);
     return fminf(fminf(r, s), wv);
   }
 }
@@ -159,9 +201,15 @@ __device__ __forceinline__ int walk_mx(const DevMesh& m, const float X[3], const
     nd = __ldg(m.elem + 2 * (long)eid);
     const int4 nb = __ldg(m.elem + 2 * (long)eid + 1);
     float tol;
-    const float d = nat32<D>(m, eid, X, r, s, t, wv, tol);
-    // FP32 decides only outside the band its error bound leaves open
-    const float band = fmaxf(FVC_NEAR_FACE, 2.0f * tol);
+    float d = nat32<D>(m, eid, X, r, s, t, wv, tol);
+    // FP32 decides only outside the band its error bound leaves open; inside
+    // it, the coordinates are recomputed from exact offsets first, and the
+    // FP64 test decides only inside that narrower band
+    float band = fmaxf(FVC_NEAR_FACE, 2.0f * tol);
+    if (fabsf(d) <= band) {
+      d = nat32_fine<D>(m, eid, X, C, r, s, t, wv, tol);
+      band = fmaxf(FVC_NEAR_FACE, 2.0f * tol);
+    }
     int slot;
     if (d > band) return 0;
     if (d < -band) {
