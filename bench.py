@@ -13,7 +13,10 @@ here with fixed seeds (no dataset is involved).
 value      accepted RK4 steps / s with mesh and frames resident in HBM; each
            step seeds and locates the grid, advects every interval
            (including the early-FTLE advections of points that leave) and
-           reduces the FTLE field.
+           reduces the FTLE field.  Early-FTLE advections that repeat the
+           main pass exactly are read from its per-step record; their steps
+           are counted (ompVC performs them) and also reported on their own
+           (steps_early_recorded).  ftle_points_per_s counts no steps.
 e2e        the same through the C ABI from pinned host buffers: mesh and all
            frames copied host->device inside each step, FTLE fields copied back.
 roofline   the main advection kernel (k_ftle_pass1) against the measured HBM
@@ -357,6 +360,7 @@ def precision_forms(ctx, ax, grid, stream, barrier, args, fp64_value):
         out[name] = {"value": value, "unit": "steps/s", "ms_per_step": ms / args.steps,
                      "ftle_points_per_s": args.grid ** 3 * args.steps / (ms / 1000.0),
                      "speedup_vs_fp64": value / fp64_value,
+                     "steps_early_recorded_per_step": sum(x["steps_early_recorded"] for x in stats) / args.steps,
                      "phases_ms_per_step": {k: sum(s[k] for s in stats) / args.steps
                                             for k in ("ms_setup", "ms_main", "ms_early", "ms_reduce")},
                      "errors": form_errors((ref_T, ref_state), (T_last, got_state))}
@@ -518,6 +522,7 @@ def run_engine(args, rank, world, local_rank):
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "ftle_points_per_s": npts * args.steps * world / secs_max,
             "steps_main": int(steps_main), "steps_early": int(sum(s["steps_early"] for s in stats)),
+            "steps_early_recorded": int(sum(s["steps_early_recorded"] for s in stats)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "k_ftle_pass1", "bytes_per_step": BYTES_PER_STEP},

@@ -143,7 +143,10 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_pass1(DevMesh m, De
     long p = f.live[idx];
     Pt t;
     load_pt(t, p, f.X, in.extrapolate ? f.V : nullptr, f.eid, f.left, f.ldt);
-    err |= advect<D, M>(m, w, in, t, t1, t2, steps);
+    const unsigned before = steps;
+    const RecOut r{f.rec + 3 * p, 3L * f.n, f.rec_steps};
+    err |= advect<D, M>(m, w, in, t, t1, t2, steps, nullptr, f.rec ? &r : nullptr);
+    if (f.rec) f.kacc[p] = (unsigned char)(steps - before);
     f.flag[p] = 1 | ((t.left && !in.extrapolate) ? 2 : 0) | (t.left ? 4 : 0);
     f.Xn[3 * p] = t.X[0];
     f.Xn[3 * p + 1] = t.X[1];
@@ -257,13 +260,67 @@ __global__ void k_task_sort(FtleDev f, DevCounters* ctr) {
   }
 }
 
+// Steps of advections read from the record: counted with the early-FTLE
+// steps (they are the advections ompVC performs) and on their own.
+__device__ __forceinline__ void flush_rec(DevCounters* ctr, unsigned steps) {
+  unsigned long long s = steps;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0 && s) {
+    atomicAdd(&ctr->steps_early, s);
+    atomicAdd(&ctr->steps_rec, s);
+  }
+}
+
+// The index k of a step-start time T in the interval's step sequence (the
+// position after k steps is the main pass's record k), or -1: FP64 form, the
+// slot table's exact times tc_k = slot 2k; mixed form, the step table.
+__device__ __forceinline__ int step_of(const DevWindow& w, int mixed, double T) {
+  const long long b = __double_as_longlong(T);
+  if (mixed) {
+    for (int k = 0; k <= w.nsteps; k++)
+      if (__double_as_longlong(w.steps[k].tc) == b) return k;
+    return -1;
+  }
+  for (int k = 0; 2 * k < w.nslots; k++)
+    if (__double_as_longlong(w.tq[2 * k]) == b) return k;
+  return -1;
+}
+
+// An early-FTLE advection of point p to the step-start time of step kend
+// repeats the main pass exactly when p was advected this interval, starts
+// from its frame-start element (the hint eid_at_trigger gives it: not a point
+// the serial loop has already moved, ompVC/ftle.c:167-168) and the record
+// reaches kend: then it stops where the main pass stood after
+// min(kend, its own accepted steps), and it exits on the way exactly when p
+// exited before kend.  Returns 1 and the result (position copied to pos, exit
+// or end time, accepted steps) or 0 when it must be recomputed.
+__device__ __forceinline__ int recorded(const FtleDev& f, long p, long trig, int kend, double tend, double* pos,
+                                        double* lt, unsigned* nsteps) {
+  if (!f.rec || kend < 0 || kend > f.rec_steps) return 0;
+  const unsigned char fl = f.flag[p];
+  if (!(fl & 1) || f.left[p]) return 0;
+  if (p < trig && !(fl & 2)) return 0;  // the hint would be the interval's end element
+  const int kx = f.kacc[p];
+  const bool exits = (fl & 2) && kx < kend;
+  const int k = exits ? kx : kend;
+  const double* src = k == 0 ? f.X + 3 * p : f.rec + (long)(k - 1) * 3 * f.n + 3 * p;
+  pos[0] = src[0];
+  pos[1] = src[1];
+  pos[2] = src[2];
+  if (lt) *lt = exits ? f.te[p] : tend;
+  *nsteps += (unsigned)k;
+  return 1;
+}
+
 // A: queue the neighbours that exist; boundary slots keep te as exit time.
 // The queue kernels walk their items warp by warp (grid-stride, uniform per
 // warp) so append_task's ballot always sees the whole warp.
 template <int D>
-__global__ void k_ftle_queue_nb(FtleDev f, DevCounters* ctr, double t1, double inv_h) {
+__global__ void k_ftle_queue_nb(FtleDev f, DevWindow w, int mixed, DevCounters* ctr, double t1, double inv_h) {
   const long nserved = *(volatile int*)&ctr->count;
   const long total = 6 * nserved, stride = (long)gridDim.x * blockDim.x;
+  unsigned rsteps = 0;
   for (long base = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
     long idx = base + (threadIdx.x & 31);
     long s = idx / 6;
@@ -275,17 +332,23 @@ __global__ void k_ftle_queue_nb(FtleDev f, DevCounters* ctr, double t1, double i
       int i, j, k;
       served_geometry(f, f.served[s], nb, i, j, k);
       want = nb[c] >= 0;
-      const double te = f.te[f.trig[s]];
+      const long trig = f.trig[s];
+      const double te = f.te[trig];
       if (!want) f.elt[s * 6 + c] = te;
+      else if (f.rec &&
+               recorded(f, nb[c], trig, step_of(w, mixed, te), te, f.epos + (s * 7 + c) * 3, f.elt + s * 6 + c, &rsteps))
+        want = false;
       b = length_bucket(t1, te, inv_h);
     }
     append_task(f, ctr, want, (int)s, c, b);
   }
+  flush_rec(ctr, rsteps);
 }
 
 // B + C queue: MinExitTime, then q itself and (if it moved) the neighbours.
 template <int D>
-__global__ void k_ftle_queue_self(FtleDev f, DevCounters* ctr, double t1, double inv_h) {
+__global__ void k_ftle_queue_self(FtleDev f, DevWindow w, int mixed, DevCounters* ctr, double t1, double inv_h) {
+  unsigned rsteps = 0;
   const long nserved = *(volatile int*)&ctr->count;
   const long total = 7 * nserved, stride = (long)gridDim.x * blockDim.x;
   for (long base = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
@@ -299,18 +362,25 @@ __global__ void k_ftle_queue_self(FtleDev f, DevCounters* ctr, double t1, double
     const double* lt = f.elt + s * 6;
     double mt = dmin(te, dmin(lt[5], dmin(lt[4], dmin(lt[3], dmin(lt[2], dmin(lt[1], lt[0]))))));
     b = length_bucket(t1, mt, inv_h);
+    long p = -1;
     if (c == 6) {
       f.emt[s] = mt;
       want = true;
+      p = f.served[s];
     } else if (mt != te) {
       long nb[6];
       int i, j, k;
       served_geometry(f, f.served[s], nb, i, j, k);
       want = nb[c] >= 0;
+      p = nb[c];
     }
+    if (want && f.rec &&
+        recorded(f, p, f.trig[s], step_of(w, mixed, mt), mt, f.epos + (s * 7 + c) * 3, nullptr, &rsteps))
+      want = false;
   }
   append_task(f, ctr, want, (int)s, c, b);
   }
+  flush_rec(ctr, rsteps);
 }
 
 // The advections of A (phase 0: to te, recording exit times) and C (phase 1:
@@ -478,11 +548,11 @@ struct Variant {
     static const unsigned res_sort = resident_blocks(k_task_sort<D>, 256);
     const double inv_h = 1.0 / fabs(in.h);
     cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
-    k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, ctr, t1, inv_h);
+    k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, w, 0, ctr, t1, inv_h);
     k_task_sort<D><<<capped(6L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
     k_ftle_tasks<D, M><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 0, ctr);
     cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
-    k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, ctr, t1, inv_h);
+    k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, w, 0, ctr, t1, inv_h);
     k_task_sort<D><<<capped(7L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
     k_ftle_tasks<D, M><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);

@@ -770,6 +770,7 @@ extern "C" void fvc_job_destroy(fvc_job* j) {
     cudaStreamSynchronize(j->ctx->stream);
   }
   cudaFree(j->mem);
+  cudaFree(j->rec_mem);
   for (int k = 0; k < 4; k++)
     if (j->ev[k]) cudaEventDestroy(j->ev[k]);
   delete j;
@@ -968,6 +969,27 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
     j->packed = true;
   }
   if ((st = prepare_slots(c, t1, t2))) return st;
+  // the main pass's per-step record, from which early-FTLE advections that
+  // repeat it are read (Euler and RK4 with a fixed step sequence)
+  j->f.rec = nullptr;
+  j->f.kacc = nullptr;
+  j->f.rec_steps = 0;
+  if ((c->integ.type == 0 || c->integ.type == 1) && !c->integ.extrapolate) {
+    const int ns = j->prec ? c->window.nsteps : (c->window.nslots > 0 ? (c->window.nslots - 1) / 2 : 0);
+    const int want = ns < 32 ? ns : 32;
+    if (want > 0 && want > j->rec_cap) {
+      cudaFree(j->rec_mem);
+      j->rec_mem = nullptr;
+      j->rec_cap = 0;
+      const size_t n = (size_t)j->f.n;
+      if (cudaMalloc(&j->rec_mem, al256(24 * n * (size_t)want) + n) == cudaSuccess) j->rec_cap = want;
+    }
+    if (want > 0 && j->rec_cap >= want) {
+      j->f.rec = (double*)j->rec_mem;
+      j->f.kacc = (unsigned char*)j->rec_mem + al256(24 * (size_t)j->f.n * (size_t)j->rec_cap);
+      j->f.rec_steps = want;
+    }
+  }
   if (launch) ftle_launch(c->mesh, c->window, j->f, j->f.start, c->d_ctr, s);
   compact_live(j->f.n, j->f.ldt, j->f.left, c->integ.extrapolate, j->f.live, j->f.flag, j->f.block_cnt, c->d_ctr, s);
   cudaEventRecord(j->ev[0], s);
@@ -986,6 +1008,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   j->stats.launches += (launch ? 1 : 0) + 4 + 1 + (c->integ.extrapolate ? 0 : 8) + 1 + (c->mesh.mesh_type == 1 && !c->prec ? 1 : 0);
   j->stats.steps_main += (long long)h.steps;
   j->stats.steps_early += (long long)h.steps_early;
+  j->stats.steps_early_recorded += (long long)h.steps_rec;
   j->stats.ms_main += ev_ms(j->ev[0], j->ev[1]);
   j->stats.ms_early += ev_ms(j->ev[1], j->ev[2]);
   return st;

@@ -599,7 +599,7 @@ __device__ __noinline__ int velocity_cold(const DevMesh& m, const DevWindow& w, 
 template <int DIMS, int MESH, bool CET = false>
 __device__ __noinline__ double euler(const DevMesh& m, const DevWindow& w, const DevInteg& in,
                                      Pt& p, double tstart, double tend, unsigned& steps, int& err,
-                                     const CetDev* cet = nullptr) {
+                                     const CetDev* cet = nullptr, const RecOut* rec = nullptr) {
   double tc = tstart, h = dsign(in.h, tend - tstart), ve[3];
   NatCache nc;
   nc.e = -1;
@@ -623,6 +623,12 @@ __device__ __noinline__ double euler(const DevMesh& m, const DevWindow& w, const
       return p.ldt;
     }
     steps++;
+    if (rec && k <= rec->max) {
+      double* o = rec->base + (long)(k - 1) * rec->stride;
+      o[0] = p.X[0];
+      o[1] = p.X[1];
+      o[2] = p.X[2];
+    }
     if (in.extrapolate && (err |= velocity_cold<DIMS, MESH>(m, w, tc, 2 * k, p.X, &p.eid, &p.left, p.V)))
       return tend;
     if (CET) {  // ompVC/integration.c:277-299
@@ -664,7 +670,7 @@ __device__ __forceinline__ int rk4_stages(const DevMesh& m, const DevWindow& w, 
 template <int DIMS, int MESH, bool CET = false>
 __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, const DevInteg& in,
                                       Pt& p, double tstart, double tend, unsigned& steps, int& err,
-                                      const CetDev* cet = nullptr) {
+                                      const CetDev* cet = nullptr, const RecOut* rec = nullptr) {
   int e[4] = {p.eid, p.eid, p.eid, p.eid};
   int l[4] = {p.left, p.left, p.left, p.left};
   double kk[4][3];
@@ -690,6 +696,12 @@ __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, cons
       return p.ldt;
     }
     steps++;
+    if (rec && k <= rec->max) {
+      double* o = rec->base + (long)(k - 1) * rec->stride;
+      o[0] = p.X[0];
+      o[1] = p.X[1];
+      o[2] = p.X[2];
+    }
     if (in.extrapolate && (err |= velocity_cold<DIMS, MESH>(m, w, tc, 2 * k, p.X, &p.eid, &p.left, p.V)))
       return tend;
     if (CET) {  // ompVC/integration.c:427-447
@@ -877,7 +889,7 @@ __device__ __noinline__ double rkf(const DevMesh& m, const DevWindow& w, const D
 template <int DIMS, int MESH, bool CET = false>
 __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, const DevInteg& in,
                                       Pt& p, double tstart, double tend, unsigned& steps,
-                                      const CetDev* cet = nullptr) {
+                                      const CetDev* cet = nullptr, const RecOut* rec = nullptr) {
   int err = 0;
   if (p.left && in.extrapolate) {
 #pragma unroll
@@ -887,10 +899,10 @@ __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, cons
   if (p.left) return PT_ERR_STATE;  // "integrate point that already left domain"
   if (MESH == 1 && p.eid < 0) return PT_ERR_STATE;
   double stop;
-  if (in.type == 1) stop = rk4<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet);
+  if (in.type == 1) stop = rk4<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet, rec);
   else if (in.type == 2) stop = rkf<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet);
   else if (in.type == 3 && !CET) stop = ab2<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
-  else stop = euler<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet);
+  else stop = euler<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet, rec);
   if (!err && (fabs(stop - tend) > FVC_TINY) && in.extrapolate) {
 #pragma unroll
     for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + p.V[q] * (tend - stop);

@@ -77,6 +77,8 @@ struct fvc_job {
   bool packed = false;  // positions held as (X, c) float pairs
   fvc_job_stats stats{};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  void* rec_mem = nullptr;  // FTLE: the main pass's per-step record
+  int rec_cap = 0;          // steps it has room for
 };
 
 // ---- helpers defined in fvc_api.cu

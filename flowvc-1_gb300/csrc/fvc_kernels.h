@@ -22,6 +22,7 @@ struct DevCounters {
   int scat[8];  // fill cursors of the buckets in the sorted list
   int pad;
   int cur[4];   // work cursors of the persistent launches: 0 live list, 1-2 task lists
+  unsigned long long steps_rec;  // early-FTLE steps read from the main pass's record
 };
 // ntask, hist and scat are cleared together before each task list
 #define FVC_TASK_COUNTERS_BYTES (17 * sizeof(int))
@@ -94,7 +95,14 @@ struct FtleDev {
   int* live;             // points advected this interval, in grid order
   int* block_cnt;        // compaction scratch
   double* out;           // 2 x n, output order
+  // the main pass's record of the interval (null: not kept): the position
+  // after k accepted steps at rec + (k - 1) 3n (k = 1 .. rec_steps; k = 0 is
+  // X), and each point's accepted steps in kacc
+  double* rec;
+  unsigned char* kacc;
+  int rec_steps;
 };
+
 void ftle_seed_grid(const DevMesh& m, const FtleDev& f, double xmin, double ymin, double zmin,
                     int* left0, cudaStream_t s);
 void ftle_mark_outside(const FtleDev& f, cudaStream_t s);

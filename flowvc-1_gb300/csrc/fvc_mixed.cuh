@@ -322,7 +322,7 @@ __device__ __forceinline__ void kahan_add(float X[3], float c[3], const float in
 // step's start time as LeftDomainTime.
 template <int D, class W>
 __device__ __forceinline__ void advect_mx(const DevMesh& m, const W& w, int type, PtM& p, int kend,
-                                          unsigned& steps, int& err) {
+                                          unsigned& steps, int& err, const RecOut* rec = nullptr) {
   if (p.left) return;
   const float zero[3] = {0.0f, 0.0f, 0.0f};
   int e[4] = {p.eid, p.eid, p.eid, p.eid};
@@ -368,6 +368,12 @@ __device__ __forceinline__ void advect_mx(const DevMesh& m, const W& w, int type
       return;
     }
     steps++;
+    if (rec && k < rec->max) {
+      float2* o = reinterpret_cast<float2*>(rec->base + (long)k * rec->stride);
+      o[0] = make_float2(p.X[0], p.c[0]);
+      o[1] = make_float2(p.X[1], p.c[1]);
+      o[2] = make_float2(p.X[2], p.c[2]);
+    }
   }
 }
 

@@ -93,7 +93,10 @@ __global__ void __launch_bounds__(128) k_ftle_pass1_mx(DevMesh m, DevWindow w, i
     t.eid = f.eid[p];
     t.left = f.left[p];
     t.ldt = f.ldt[p];
-    advect_mx<D>(m, w, type, t, w.nsteps, steps, err);
+    const unsigned before = steps;
+    const RecOut r{f.rec + 3 * p, 3L * f.n, f.rec_steps};
+    advect_mx<D>(m, w, type, t, w.nsteps, steps, err, f.rec ? &r : nullptr);
+    if (f.rec) f.kacc[p] = (unsigned char)(steps - before);
     f.flag[p] = 1 | (t.left ? 6 : 0);
     store_pos_pair(f.Xn, p, t.X, t.c);
     f.en[p] = t.eid;
@@ -218,10 +221,10 @@ struct VariantMx {
     FtleDev g = f;
     g.tsorted = g.tasks;
     cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
-    k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, ctr, t1, inv_h);
+    k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, w, 1, ctr, t1, inv_h);
     k_ftle_tasks_mx<D><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, g, 0, ctr);
     cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
-    k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, ctr, t1, inv_h);
+    k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, w, 1, ctr, t1, inv_h);
     k_ftle_tasks_mx<D><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, g, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
   }

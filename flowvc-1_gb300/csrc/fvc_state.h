@@ -86,6 +86,15 @@ struct CetDev {
   BucketGrid g;  // global-search fallback of the sub-step walk
 };
 
+// Where an integrator writes the position after each accepted step: after
+// its k-th accepted step (k = 1 .. max) at base + (k - 1) stride (FP64 form:
+// 3 doubles; mixed form: 3 (X, c) float pairs).
+struct RecOut {
+  double* base;
+  long stride;
+  int max;
+};
+
 struct DevInteg {
   int type;  // 0 Euler, 1 RK4, 2 RKF, 3 AB2
   double h;  // Int_TimeStep

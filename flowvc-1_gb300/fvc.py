@@ -46,7 +46,7 @@ class TracerSpec(C.Structure):
 class JobStats(C.Structure):
     _fields_ = [("intervals", C.c_longlong), ("steps_main", C.c_longlong), ("steps_early", C.c_longlong),
                 ("ms_main", C.c_double), ("ms_early", C.c_double), ("ms_reduce", C.c_double),
-                ("ms_setup", C.c_double), ("launches", C.c_longlong)]
+                ("ms_setup", C.c_double), ("launches", C.c_longlong), ("steps_early_recorded", C.c_longlong)]
 
 
 class BatchOpts(C.Structure):

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define FVC_ABI_VERSION 1
+#define FVC_ABI_VERSION 2
 
 typedef int fvc_status;
 enum {
@@ -284,6 +284,9 @@ typedef struct {
   double ms_reduce;        /* device time of the FTLE reduction */
   double ms_setup;         /* device time of seeding and seed location */
   long long launches;      /* kernels launched on the job's behalf */
+  long long steps_early_recorded; /* of steps_early, those read from the main
+                                     pass's per-step record instead of
+                                     recomputed (identical results) */
 } fvc_job_stats;
 fvc_status fvc_job_get_stats(fvc_job *job, fvc_job_stats *out);
 
