@@ -290,8 +290,8 @@ __device__ __forceinline__ int step_of(const DevWindow& w, int mixed, double T) 
 // An early-FTLE advection of point p to the step-start time of step kend
 // repeats the main pass exactly when p was advected this interval, starts
 // from its frame-start element (the hint eid_at_trigger gives it: not a point
-// the serial loop has already moved, ompVC/ftle.c:167-168) and the record
-// reaches kend: then it stops where the main pass stood after
+// the serial loop has already moved, ompVC/ftle.c:167-168; the mixed form
+// does not require this) and the record reaches kend: then it stops where the main pass stood after
 // min(kend, its own accepted steps), and it exits on the way exactly when p
 // exited before kend.  Returns 1 and the result (position copied to pos, exit
 // or end time, accepted steps) or 0 when it must be recomputed.
@@ -300,7 +300,11 @@ __device__ __forceinline__ int recorded(const FtleDev& f, long p, long trig, int
   if (!f.rec || kend < 0 || kend > f.rec_steps) return 0;
   const unsigned char fl = f.flag[p];
   if (!(fl & 1) || f.left[p]) return 0;
-  if (p < trig && !(fl & 2)) return 0;  // the hint would be the interval's end element
+  // the hint would be the interval's end element: in the FP64 form the walk
+  // from there may settle a tie on a shared face differently, so recompute;
+  // the mixed form reads the record (on a shared face the P1 velocity is
+  // continuous, so the two differ by rounding only)
+  if (!f.mixed && p < trig && !(fl & 2)) return 0;
   const int kx = f.kacc[p];
   const bool exits = (fl & 2) && kx < kend;
   const int k = exits ? kx : kend;
