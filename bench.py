@@ -266,7 +266,8 @@ def bench_batched(args, tube, frames):
         res[prec] = r
         out[prec] = {"value": steps / wall, "unit": "steps/s", "steps": int(steps), "wall_s": wall,
                      "device_s": secs, "device_value": steps / secs if secs > 0 else None,
-                     "tuned": {"threads": st["tuned_threads"], "blocks": st["tuned_blocks"]}}
+                     "tuned": {"threads": st["tuned_threads"], "blocks": st["tuned_blocks"],
+                               "resort_every": st["tuned_resort"]}}
         site.close()
     out["speedup_vs_fp64"] = out["bf16"]["value"] / out["fp64"]["value"]
     import serve as _s

@@ -217,6 +217,16 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
       if (nb < -1 || nb >= nelem) return fail(c, FVC_ERR_ARG, "element %ld: neighbour %d out of range", e, nb);
     }
   }
+  for (int a = 0; a < 3; a++) {
+    c->node_lo[a] = 1e300;
+    c->node_hi[a] = -1e300;
+  }
+  for (long k = 0; k < nnodes; k++)
+    for (int a = 0; a < 3; a++) {
+      const double v = xyz[3 * k + a];
+      c->node_lo[a] = v < c->node_lo[a] ? v : c->node_lo[a];
+      c->node_hi[a] = v > c->node_hi[a] ? v : c->node_hi[a];
+    }
   std::vector<int4> he(2 * (size_t)nelem);
   for (long e = 0; e < nelem; e++) {
     const int* n = conn + 4 * e;

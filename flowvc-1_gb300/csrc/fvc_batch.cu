@@ -212,6 +212,50 @@ static void batch_advance(const DevMesh& m, const DevInteg& in, const BJob* jobs
   }
 }
 
+// ---- the tick's work queue ordered by job, then by a Z-order of the
+// entries' current positions over the mesh's box (2^(3 bits) cells): a
+// counting sort, key histogram, scan, scatter.  Entries of one job and cell
+// stay together, so warps walk neighbouring elements and read one frame pair
+// even after a release has dispersed; the particle arrays are not moved.
+
+__global__ void k_qkeys(const BJob* __restrict__ jobs, const int2* queue, const BatchCtr* bc, int mixed, int bits,
+                        double3 lo, double3 inv, int* key, int* hist) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *(volatile const int*)&bc->nqueue) return;
+  const int2 e = queue[i];
+  const double* X = jobs[e.x].X + 3L * e.y;
+  double x[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    if (mixed) {
+      const float2 p = *reinterpret_cast<const float2*>(X + a);
+      x[a] = (double)p.x;
+    } else {
+      x[a] = X[a];
+    }
+  }
+  const double l[3] = {lo.x, lo.y, lo.z}, sc[3] = {inv.x, inv.y, inv.z};
+  const unsigned top = (1u << bits) - 1u;
+  unsigned code = 0;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const double f = (x[a] - l[a]) * sc[a];
+    const unsigned c = f < 0.0 ? 0u : f >= (double)top ? top : (unsigned)f;
+    for (int b = 0; b < bits; b++) code |= ((c >> b) & 1u) << (3 * b + a);
+  }
+  const int k = (int)(((unsigned)e.x << (3 * bits)) | code);
+  key[i] = k;
+  atomicAdd(hist + k, 1);
+}
+
+__global__ void k_qscatter(const int2* queue, const BatchCtr* bc, const int* key, const int* off, int* cur,
+                           int2* out) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *(volatile const int*)&bc->nqueue) return;
+  const int k = key[i];
+  out[off[k] + atomicAdd(cur + k, 1)] = queue[i];
+}
+
 // ---- spatial ordering of a release's tracers (Z-order of 64^3 cells over
 // the seeds' box): a warp's 32 tracers then walk neighbouring elements and
 // share their records and frame nodes in cache.  Advection is independent
@@ -348,7 +392,17 @@ struct fvc_batch {
   cudaEvent_t t_start = nullptr, t_end = nullptr;
   BatchLaunch launch{128, 0};
   fvc_batch_stats stats{};
+  // queue ordering (resort_every > 0): sorted copy of the queue, keys and
+  // the counting sort's arrays (room for QSORT_KEYS keys)
+  int resort = 0;
+  int2* d_queue2 = nullptr;
+  int* d_qkey = nullptr;
+  size_t qsort_cap = 0;  // entries
+  int* d_qhist = nullptr;  // hist, off (+1), cur
+  long long* d_qtmp = nullptr;
 };
+
+static constexpr int QSORT_KEYS = 1 << 22;
 
 using namespace fvc;
 
@@ -630,6 +684,7 @@ struct TickPlan {
   std::vector<Interval> iv;
   std::vector<DevWindow> win;     // per job (launch velocity, early FTLE)
   long long ngroups = 0;
+  long long npts = 0;             // points of the tick's jobs (queue entries at most)
 };
 
 static size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -689,6 +744,7 @@ static fvc_status plan_tick(fvc_batch* b, const std::vector<int>& ids, char* dev
       B.ldt = t.ldt;
     }
     groups += (B.n + 31) / 32;
+    P.npts += B.n;
     if (c->prec) {
       memcpy(P.blob.data() + toff[k], tabs[k].data(), sizeof(StepM) * tabs[k].size());
     } else {
@@ -702,7 +758,64 @@ static fvc_status plan_tick(fvc_batch* b, const std::vector<int>& ids, char* dev
 }
 
 // Enqueues a planned tick whose descriptors are at d_jobs on the stream.
-static fvc_status enqueue_tick(fvc_batch* b, const TickPlan& P, const BJob* d_jobs, bool counters_cleared) {
+// Room for ordering a queue of `need` entries (outside capture only).
+static fvc_status ensure_qsort(fvc_batch* b, size_t need) {
+  fvc_ctx* c = b->c;
+  if (!b->d_qhist) {
+    if (cudaMalloc(&b->d_qhist, sizeof(int) * (3 * (size_t)QSORT_KEYS + 2)) != cudaSuccess ||
+        cudaMalloc(&b->d_qtmp, sizeof(long long) * ((size_t)QSORT_KEYS / 1024 + 2)) != cudaSuccess)
+      return fail(c, FVC_ERR_OOM, "queue ordering arrays");
+  }
+  if (need > b->qsort_cap) {
+    FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(b->d_queue2);
+    cudaFree(b->d_qkey);
+    b->d_queue2 = nullptr;
+    b->d_qkey = nullptr;
+    b->qsort_cap = 0;
+    if (cudaMalloc(&b->d_queue2, sizeof(int2) * need) != cudaSuccess ||
+        cudaMalloc(&b->d_qkey, sizeof(int) * need) != cudaSuccess)
+      return fail(c, FVC_ERR_OOM, "queue ordering (%zu entries)", need);
+    b->qsort_cap = need;
+  }
+  return FVC_OK;
+}
+
+// Whether tick `t` orders its queue.
+static bool resorts(const fvc_batch* b, long long t) { return b->resort > 0 && t % b->resort == 0; }
+
+// Orders the tick's queue (in d_queue) into d_queue2 by job and position.
+static bool order_queue(fvc_batch* b, const TickPlan& P, const BJob* d_jobs, cudaStream_t s) {
+  fvc_ctx* c = b->c;
+  const int nj = (int)P.ids.size();
+  int jb = 0;
+  while ((1 << jb) < nj) jb++;
+  int bits = (22 - jb) / 3;
+  if (bits < 1) return false;  // too many jobs for the key range: leave the order
+  bits = bits > 6 ? 6 : bits;
+  const long long K = (long long)nj << (3 * bits);
+  if (K > QSORT_KEYS) return false;
+  double3 lo = make_double3(c->node_lo[0], c->node_lo[1], c->node_lo[2]), inv;
+  double* ip = &inv.x;
+  for (int a = 0; a < 3; a++) {
+    const double ext = c->node_hi[a] - c->node_lo[a];
+    ip[a] = ext > 0 ? (double)(1 << bits) / ext : 0.0;
+  }
+  int* hist = b->d_qhist;
+  int* off = hist + QSORT_KEYS;
+  int* cur = off + QSORT_KEYS + 1;
+  cudaMemsetAsync(hist, 0, sizeof(int) * (size_t)K, s);
+  cudaMemsetAsync(cur, 0, sizeof(int) * (size_t)K, s);
+  const unsigned g = (unsigned)((P.npts + 255) / 256);
+  k_qkeys<<<g, 256, 0, s>>>(d_jobs, b->d_queue, b->d_bc, c->prec ? 1 : 0, bits, lo, inv, b->d_qkey, hist);
+  scan_counts(hist, off, (int)K, b->d_qtmp, s);
+  k_qscatter<<<g, 256, 0, s>>>(b->d_queue, b->d_bc, b->d_qkey, off, cur, b->d_queue2);
+  b->stats.launches += 5;
+  return true;
+}
+
+static fvc_status enqueue_tick(fvc_batch* b, const TickPlan& P, const BJob* d_jobs, bool counters_cleared,
+                               long long tick) {
   fvc_ctx* c = b->c;
   cudaStream_t s = c->stream;
   const size_t nj = P.ids.size();
@@ -718,7 +831,9 @@ static fvc_status enqueue_tick(fvc_batch* b, const TickPlan& P, const BJob* d_jo
   if (P.ngroups > 0) {
     const unsigned nb = (unsigned)((P.ngroups + 7) / 8);
     k_batch_compact<<<nb, 256, 0, s>>>(d_jobs, (int)nj, P.ngroups, b->d_queue, b->d_bc);
-    batch_advance(c->mesh, c->integ, d_jobs, b->d_queue, b->d_bc, b->launch, s);
+    const int2* q = b->d_queue;
+    if (resorts(b, tick) && b->qsort_cap >= (size_t)P.npts && order_queue(b, P, d_jobs, s)) q = b->d_queue2;
+    batch_advance(c->mesh, c->integ, d_jobs, q, b->d_bc, b->launch, s);
     b->stats.launches += 2;
   }
   for (size_t k = 0; k < nj; k++) {
@@ -857,7 +972,8 @@ static fvc_status tick(fvc_batch* b) {
     if ((st = plan_tick(b, b->active, b->d_tick, P))) return st;
   }
   if ((st = stage_upload(b, P.blob))) return st;
-  if ((st = enqueue_tick(b, P, (const BJob*)b->d_tick, false))) return st;
+  if (b->resort > 0 && (st = ensure_qsort(b, (size_t)P.npts))) return st;
+  if ((st = enqueue_tick(b, P, (const BJob*)b->d_tick, false, b->stats.ticks))) return st;
   advance_cursors(b, P);
   // at most two ticks in flight: the host plans the next while one runs
   cudaEvent_t& e = b->tick_ev[b->stats.ticks % b->tick_ev.size()];
@@ -941,6 +1057,32 @@ static fvc_status autotune(fvc_batch* b) {
       }
     }
   }
+  // the re-sort interval, when left to the tuner: the best shape once more
+  // with the queue ordered (ordering included in the time); ordering every
+  // tick is kept only if that is faster
+  if (b->o.resort_every == -1) {
+    fvc_status qs = ensure_qsort(b, (size_t)P.npts);
+    b->resort = 0;
+    if (!qs) {
+      cudaMemsetAsync(b->d_bc, 0, sizeof(BatchCtr), c->stream);
+      const unsigned nb = (unsigned)((P.ngroups + 7) / 8);
+      k_batch_compact<<<nb, 256, 0, c->stream>>>(dj, (int)P.ids.size(), P.ngroups, b->d_queue, b->d_bc);
+      cudaEventRecord(e0, c->stream);
+      const bool ordered = order_queue(b, P, dj, c->stream);
+      batch_advance(c->mesh, c->integ, dj, ordered ? b->d_queue2 : b->d_queue, b->d_bc, bestL, c->stream);
+      cudaEventRecord(e1, c->stream);
+      o = 0;
+      for (auto& r : regions) {
+        cudaMemcpyAsync(r.first, save + o, r.second, cudaMemcpyDeviceToDevice, c->stream);
+        o += r.second;
+      }
+      if (cudaStreamSynchronize(c->stream) == cudaSuccess && ordered) {
+        const float ms = ev_ms(e0, e1);
+        if (ms > 0 && ms < 0.97f * best) b->resort = 1;
+      }
+    }
+    b->stats.tuned_resort = b->resort;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(save);
@@ -980,6 +1122,8 @@ extern "C" fvc_status fvc_batch_create(fvc_ctx* c, const fvc_batch_opts* o, fvc_
   cudaEventCreate(&b->t_end);
   b->launch.threads = 128;
   b->launch.blocks = (int)batch_resident(c->mesh.dims, c->prec, 128);
+  b->resort = o->resort_every > 0 ? o->resort_every : 0;
+  b->stats.tuned_resort = b->resort;
   *out = b;
   return check_launch(c, "batch create");
 }
@@ -994,6 +1138,10 @@ extern "C" void fvc_batch_destroy(fvc_batch* b) {
     if (J->done) cudaEventDestroy(J->done);
   }
   for (auto& kv : b->pairs) cudaFree(kv.second.q);
+  cudaFree(b->d_queue2);
+  cudaFree(b->d_qkey);
+  cudaFree(b->d_qhist);
+  cudaFree(b->d_qtmp);
   cudaFree(b->d_ctrs);
   cudaFreeHost(b->h_ctrs);
   cudaFree(b->d_bc);
@@ -1126,6 +1274,14 @@ extern "C" fvc_status fvc_batch_run(fvc_batch* b, int graph) {
       cudaFree(d_all);
       return st;
     }
+    if (b->resort > 0) {
+      long long most = 0;
+      for (auto& pl : plans) most = std::max(most, pl.npts);
+      if ((st = ensure_qsort(b, (size_t)most))) {
+        cudaFree(d_all);
+        return st;
+      }
+    }
     FVC_CUDA(c, cudaMemcpyAsync(d_all, all.data(), total, cudaMemcpyHostToDevice, c->stream));
     FVC_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaGraph_t g = nullptr;
@@ -1133,7 +1289,7 @@ extern "C" fvc_status fvc_batch_run(fvc_batch* b, int graph) {
     FVC_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
     fvc_status cst = FVC_OK;
     for (size_t t = 0; t < plans.size() && !cst; t++) {
-      cst = enqueue_tick(b, plans[t], (const BJob*)(d_all + offs[t]), false);
+      cst = enqueue_tick(b, plans[t], (const BJob*)(d_all + offs[t]), false, (long long)t);
       if (!cst) advance_cursors(b, plans[t]);
     }
     cudaError_t ce = cudaStreamEndCapture(c->stream, &g);

@@ -23,6 +23,7 @@ struct fvc_ctx {
   DevWindow window{};
   bool window_set = false;
   long frame_nodes = 0;  // nodes per frame
+  double node_lo[3] = {0, 0, 0}, node_hi[3] = {0, 0, 0};  // bounding box of the mesh nodes
   // device buffers
   int4* d_elem = nullptr;
   double* d_geom = nullptr;

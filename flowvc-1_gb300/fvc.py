@@ -51,7 +51,7 @@ class JobStats(C.Structure):
 
 class BatchOpts(C.Structure):
     _fields_ = [("tmin", C.c_double), ("tdelta", C.c_double), ("tres", C.c_int), ("periodic", C.c_int),
-                ("hbm_budget", C.c_longlong), ("max_jobs", C.c_int)]
+                ("hbm_budget", C.c_longlong), ("max_jobs", C.c_int), ("resort_every", C.c_int)]
 
 
 class BatchJobSpec(C.Structure):
@@ -63,7 +63,7 @@ class BatchStats(C.Structure):
     _fields_ = [("ticks", C.c_longlong), ("graphs", C.c_longlong), ("launches", C.c_longlong),
                 ("steps", C.c_longlong), ("jobs_submitted", C.c_longlong), ("jobs_done", C.c_longlong),
                 ("ms_run", C.c_double), ("tuned_threads", C.c_int), ("tuned_blocks", C.c_int),
-                ("hbm_used", C.c_longlong)]
+                ("tuned_resort", C.c_int), ("hbm_used", C.c_longlong)]
 
 
 JOB_TRACERS, JOB_RESIDENCE, JOB_FTLE = 0, 1, 2
@@ -432,11 +432,11 @@ class Batch:
     """Batched / served jobs on one context (fvc_batch_*): submit jobs, then
     run them all (run) or advance tick by tick (tick) while submitting more."""
 
-    def __init__(self, ctx: Context, tmin, tdelta, tres, periodic=0, hbm_budget=0, max_jobs=0):
+    def __init__(self, ctx: Context, tmin, tdelta, tres, periodic=0, hbm_budget=0, max_jobs=0, resort_every=0):
         self.ctx, self.lib = ctx, ctx.lib
         self.h = _vp()
         self.sizes = {}
-        o = BatchOpts(tmin, tdelta, tres, periodic, int(hbm_budget), max_jobs)
+        o = BatchOpts(tmin, tdelta, tres, periodic, int(hbm_budget), max_jobs, resort_every)
         ctx._chk(self.lib.fvc_batch_create(ctx.h, C.byref(o), C.byref(self.h)))
 
     def _submit(self, spec, keep=None):

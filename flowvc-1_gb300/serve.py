@@ -42,7 +42,7 @@ class Site:
         self.ctx.close()
 
 
-def tube_site(prec="bf16", nc=40, nax=320, h=0.002, hbm_budget=0, tube=None, frames=None):
+def tube_site(prec="bf16", nc=40, nax=320, h=0.002, hbm_budget=0, tube=None, frames=None, resort_every=-1):
     """The bent tube (3,072,000 tets at nc = 40, nax = 320) with Womersley
     frames over one period, resident on a new context."""
     if tube is None:
@@ -57,7 +57,8 @@ def tube_site(prec="bf16", nc=40, nax=320, h=0.002, hbm_budget=0, tube=None, fra
     ax = flow.TimeAxis(0.0, TUBE_PERIOD / (TUBE_FRAMES - 1), TUBE_FRAMES, 1)
     flow.upload_frames(ctx, ax, frames)
     site = Site("tube", ctx, ax, tube=tube)
-    site.batch = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, ax.periodic, hbm_budget=hbm_budget)
+    site.batch = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, ax.periodic, hbm_budget=hbm_budget,
+                           resort_every=resort_every)
     return site
 
 

@@ -318,6 +318,11 @@ typedef struct {
   int periodic;          /* Data_TPeriodic */
   long long hbm_budget;  /* device bytes the admitted jobs may hold; 0 = no limit */
   int max_jobs;          /* jobs admitted at once; 0 = 1024 */
+  int resort_every;      /* order each tick's work queue by job and position
+                            (Z-order over the mesh's box) every this many
+                            ticks, so a warp's tracers walk neighbouring
+                            elements after releases disperse; 0 = never,
+                            -1 = chosen by fvc_batch_autotune (default 0) */
 } fvc_batch_opts;
 
 enum { FVC_JOB_TRACERS = 0, FVC_JOB_RESIDENCE = 1, FVC_JOB_FTLE = 2 };
@@ -347,6 +352,7 @@ typedef struct {
   double ms_run;             /* device time inside fvc_batch_run */
   int tuned_threads;         /* block size the autotuner chose (0 = not tuned) */
   int tuned_blocks;          /* grid the autotuner chose */
+  int tuned_resort;          /* re-sort interval in use (ticks; 0 = never) */
   long long hbm_used;        /* footprint of the jobs holding device memory */
 } fvc_batch_stats;
 

@@ -116,13 +116,14 @@ def check(b, jid, spec, ref):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "bf16"])
-@pytest.mark.parametrize("mode", ["eager", "graph", "budget", "served", "tuned"])
+@pytest.mark.parametrize("mode", ["eager", "graph", "budget", "served", "tuned", "resort", "resort_graph"])
 def test_batch_matches_single_jobs(case, prec, mode):
     ctx, ax = make_ctx(case, prec)
     specs = jobs_spec()
     ref = single_results(ctx, ax, specs)
     budget = 2_500_000 if mode == "budget" else 0
-    b = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, 0, hbm_budget=budget)
+    resort = 1 if mode.startswith("resort") else (-1 if mode == "tuned" else 0)
+    b = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, 0, hbm_budget=budget, resort_every=resort)
     if mode == "served":
         # half the jobs first, the rest arriving while those run
         ids = [submit(b, s) for s in specs[::2]]
@@ -138,15 +139,18 @@ def test_batch_matches_single_jobs(case, prec, mode):
         order = list(range(len(specs)))
         if mode == "tuned":
             b.autotune()
-        b.run(graph=mode == "graph")
+        b.run(graph=mode in ("graph", "resort_graph"))
     for jid, k in zip(ids, order):
         check(b, jid, specs[k], ref[k])
     st = b.stats()
     assert st["jobs_done"] == len(specs)
-    if mode == "graph":
+    if mode in ("graph", "resort_graph"):
         assert st["graphs"] == 1
     if mode == "tuned":
         assert st["tuned_threads"] in (64, 128, 256)
+        assert st["tuned_resort"] in (0, 1)
+    if mode.startswith("resort"):
+        assert st["tuned_resort"] == 1
     b.close()
     ctx.close()
 
