@@ -781,15 +781,47 @@ extern "C" void fvc_job_destroy(fvc_job* j) {
   }
   cudaFree(j->mem);
   cudaFree(j->rec_mem);
+  cudaFree(j->d_ctr);
   for (int k = 0; k < 4; k++)
     if (j->ev[k]) cudaEventDestroy(j->ev[k]);
+  for (cudaEvent_t e : j->pend) cudaEventDestroy(e);
+  for (cudaEvent_t e : j->spare) cudaEventDestroy(e);
   delete j;
+}
+
+// Waits for the job's asynchronous FTLE intervals and accounts them: steps
+// and device times into the stats, fault bits into the returned status.
+static fvc_status job_sync(fvc_job* j, const char* what) {
+  if (!j->d_ctr) return FVC_OK;
+  fvc_ctx* c = j->ctx;
+  DevCounters h{};
+  FVC_CUDA(c, cudaMemcpyAsync(&h, j->d_ctr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  FVC_CUDA(c, cudaMemsetAsync(j->d_ctr, 0, sizeof(DevCounters), c->stream));
+  j->stats.steps_main += (long long)h.steps;
+  j->stats.steps_early += (long long)h.steps_early;
+  j->stats.steps_early_recorded += (long long)h.steps_rec;
+  for (size_t k = 0; k + 2 < j->pend.size(); k += 3) {
+    j->stats.ms_main += ev_ms(j->pend[k], j->pend[k + 1]);
+    j->stats.ms_early += ev_ms(j->pend[k + 1], j->pend[k + 2]);
+  }
+  j->spare.insert(j->spare.end(), j->pend.begin(), j->pend.end());
+  j->pend.clear();
+  if (h.status & PT_ERR_STATE)
+    return fail(c, FVC_ERR_STATE, "%s: a point that had left the domain was advected", what);
+  if (h.status & PT_ERR_TLOC)
+    return fail(c, FVC_ERR_TLOC, "%s: query time outside the loaded frame interval", what);
+  if (h.status & PT_ERR_WALK)
+    return fail(c, FVC_ERR_WALK, "%s: neighbour walk failed (indeterminate neighbour or hop cap)", what);
+  return FVC_OK;
 }
 
 extern "C" fvc_status fvc_job_get_stats(fvc_job* j, fvc_job_stats* out) {
   if (!j || !out) return FVC_ERR_ARG;
+  fvc_status st = FVC_OK;
+  if (j->d_ctr && use_device(j->ctx) == FVC_OK) st = job_sync(j, "ftle interval");
   *out = j->stats;
-  return FVC_OK;
+  return st;
 }
 
 extern "C" void* fvc_stream(fvc_ctx* c) { return c ? (void*)c->stream : nullptr; }
@@ -921,6 +953,7 @@ extern "C" fvc_status fvc_ftle_set_state(fvc_job* j, const double* X, const int*
   fvc_ctx* c = j->ctx;
   fvc_status st;
   if ((st = use_device(c))) return st;
+  if ((st = job_sync(j, "ftle interval"))) return st;
   FtleDev& f = j->f;
   size_t n = (size_t)f.n;
   cudaStream_t s = c->stream;
@@ -950,6 +983,7 @@ extern "C" fvc_status fvc_ftle_get_state(fvc_job* j, double* X, int* eid, int* l
   fvc_ctx* c = j->ctx;
   fvc_status st;
   if ((st = use_device(c))) return st;
+  if ((st = job_sync(j, "ftle interval"))) return st;
   FtleDev& f = j->f;
   size_t n = (size_t)f.n;
   cudaStream_t s = c->stream;
@@ -1000,27 +1034,41 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
       j->f.rec_steps = want;
     }
   }
-  if (launch) ftle_launch(c->mesh, c->window, j->f, j->f.start, c->d_ctr, s);
-  compact_live(j->f.n, j->f.ldt, j->f.left, c->integ.extrapolate, j->f.live, j->f.flag, j->f.block_cnt, c->d_ctr, s);
-  cudaEventRecord(j->ev[0], s);
-  ftle_pass1(c->mesh, c->window, c->integ, j->f, t1, t2, c->d_ctr, s);
-  cudaEventRecord(j->ev[1], s);
-  if (!c->integ.extrapolate) {
-    ftle_triggers(j->f, c->d_ctr, s);
-    ftle_early(c->mesh, c->window, c->integ, j->f, t1, c->d_ctr, s);
+  if (!j->d_ctr) {
+    if (cudaMalloc(&j->d_ctr, sizeof(DevCounters)) != cudaSuccess) return fail(c, FVC_ERR_OOM, "job counters");
+    FVC_CUDA(c, cudaMemsetAsync(j->d_ctr, 0, sizeof(DevCounters), s));
   }
-  cudaEventRecord(j->ev[2], s);
+  DevCounters* ctr = j->d_ctr;
+  cudaEvent_t ev[3];
+  for (int k = 0; k < 3; k++) {
+    if (!j->spare.empty()) {
+      ev[k] = j->spare.back();
+      j->spare.pop_back();
+    } else if (cudaEventCreate(&ev[k]) != cudaSuccess) {
+      return fail(c, FVC_ERR_CUDA, "event creation failed");
+    }
+    j->pend.push_back(ev[k]);
+  }
+  // the persistent launches' work cursors start at 0 every interval
+  FVC_CUDA(c, cudaMemsetAsync(ctr->cur, 0, sizeof(ctr->cur), s));
+  if (launch) ftle_launch(c->mesh, c->window, j->f, j->f.start, ctr, s);
+  compact_live(j->f.n, j->f.ldt, j->f.left, c->integ.extrapolate, j->f.live, j->f.flag, j->f.block_cnt, ctr, s);
+  cudaEventRecord(ev[0], s);
+  ftle_pass1(c->mesh, c->window, c->integ, j->f, t1, t2, ctr, s);
+  cudaEventRecord(ev[1], s);
+  if (!c->integ.extrapolate) {
+    ftle_triggers(j->f, ctr, s);
+    ftle_early(c->mesh, c->window, c->integ, j->f, t1, ctr, s);
+  }
+  cudaEventRecord(ev[2], s);
   ftle_update(c->mesh, c->integ, j->f, s);
   if ((st = check_launch(c, "ftle interval"))) return st;
-  DevCounters h{};
-  st = finish(c, "ftle interval", steps, &h);
   j->stats.intervals++;
   j->stats.launches += (launch ? 1 : 0) + 4 + 1 + (c->integ.extrapolate ? 0 : 8) + 1 + (c->mesh.mesh_type == 1 && !c->prec ? 1 : 0);
-  j->stats.steps_main += (long long)h.steps;
-  j->stats.steps_early += (long long)h.steps_early;
-  j->stats.steps_early_recorded += (long long)h.steps_rec;
-  j->stats.ms_main += ev_ms(j->ev[0], j->ev[1]);
-  j->stats.ms_early += ev_ms(j->ev[1], j->ev[2]);
+  if (!steps) return FVC_OK;  // asynchronous: accounted by the next call that waits
+  const long long before = j->stats.steps_main + j->stats.steps_early;
+  st = job_sync(j, "ftle interval");
+  *steps = j->stats.steps_main + j->stats.steps_early - before;
   return st;
 }
 
@@ -1029,6 +1077,7 @@ extern "C" fvc_status fvc_ftle_reduce(fvc_job* j, double int_t, double* wT, doub
   fvc_ctx* c = j->ctx;
   fvc_status st;
   if ((st = use_device(c))) return st;
+  if ((st = job_sync(j, "ftle interval"))) return st;
   job_events(j);
   if (j->packed) {
     unpack_pairs(j->f.X, 3L * j->f.n, c->stream);

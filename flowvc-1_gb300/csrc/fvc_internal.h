@@ -80,6 +80,12 @@ struct fvc_job {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   void* rec_mem = nullptr;  // FTLE: the main pass's per-step record
   int rec_cap = 0;          // steps it has room for
+  // FTLE intervals run asynchronously on the job's own counters; the
+  // events of each interval not yet accounted (main start, main end, early
+  // end) and recycled events
+  DevCounters* d_ctr = nullptr;
+  std::vector<cudaEvent_t> pend;
+  std::vector<cudaEvent_t> spare;
 };
 
 // ---- helpers defined in fvc_api.cu

@@ -84,7 +84,7 @@ def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, 
             t1 = t_start if launch else (tmin if direction > 0 else tmax)
             t2 = min(tmax, stop) if direction > 0 else max(tmin, stop)
             status = 1
-            steps += job.interval(launch, t1, t2)
+            job.interval(launch, t1, t2, wait=False)
             if ((stop - tmax) if direction > 0 else (tmin - stop)) < TINY:
                 out = job.reduce(T)
                 if state is not None:
@@ -92,6 +92,7 @@ def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, 
                 break
         df += direction
     st = job.stats()
+    steps = st["steps_main"] + st["steps_early"]
     job.close()
     if out is None:
         raise RuntimeError("FTLE window did not complete")

@@ -336,7 +336,12 @@ class FtleJob:
         self.shape = (spec.xres, spec.yres, spec.zres if d == 3 else 1)
         self.n = int(np.prod(self.shape))
 
-    def interval(self, launch, t1, t2):
+    def interval(self, launch, t1, t2, wait=True):
+        """One frame interval; wait=False only queues it (steps: None; faults
+        surface at the next call that waits: reduce, get_state, stats)."""
+        if not wait:
+            self.ctx._chk(self.lib.fvc_ftle_interval(self.h, int(launch), t1, t2, None))
+            return None
         steps = C.c_longlong(0)
         self.ctx._chk(self.lib.fvc_ftle_interval(self.h, int(launch), t1, t2, C.byref(steps)))
         return steps.value

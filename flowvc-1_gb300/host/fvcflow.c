@@ -503,11 +503,11 @@ static int run_ftle(run_t *R)
             double t1 = launch ? s->start : (P->int_dir > 0 ? tmin : tmax);
             double t2 = P->int_dir > 0 ? MIN(tmax, s->stop) : MAX(tmin, s->stop);
             s->status = 1;
-            long long st = 0;
             t0 = wall();
-            if ((rc = fvc_ftle_interval(s->job, launch, t1, t2, &st))) return die("FTLE interval", R->ctx, rc);
+            /* queued without waiting; the slide's output (or the stats
+               below) waits for it and reports device faults */
+            if ((rc = fvc_ftle_interval(s->job, launch, t1, t2, NULL))) return die("FTLE interval", R->ctx, rc);
             R->t_compute += wall() - t0;
-            R->steps += st;
             if (((P->int_dir > 0) ? (s->stop - tmax) : (tmin - s->stop)) < TINY) {
                 if (output_ftle(R, s, ss, P->ftle_T, &numout, buf)) return 1;
                 s->status = 2;
@@ -516,7 +516,12 @@ static int run_ftle(run_t *R)
             }
         }
     }
-    for (int ss = 0; ss < nsl; ss++) fvc_job_destroy(sl[ss].job);
+    for (int ss = 0; ss < nsl; ss++) {
+        fvc_job_stats js;
+        if ((rc = fvc_job_get_stats(sl[ss].job, &js))) return die("FTLE interval", R->ctx, rc);
+        R->steps += js.steps_main + js.steps_early;
+        fvc_job_destroy(sl[ss].job);
+    }
     free(sl); free(X); free(ldt); free(wT); free(wN); free(eid); free(left); free(have); free(buf);
     return 0;
 }

@@ -215,7 +215,12 @@ fvc_status fvc_ftle_get_state(fvc_job *job, double *X, int *eid, int *left, doub
  * (ompVC/ftle.c:72-176) on the context's current window.  launch = 1 on the
  * slide's first interval (evaluates the launch velocity, ftle.c:80-99).
  * Points that leave get their FTLE early (GetFTLEForPointEarly,
- * ftle.c:788-1048) with the result of ompVC's serial loop order. */
+ * ftle.c:788-1048) with the result of ompVC's serial loop order.
+ * With steps != NULL the call waits for the interval and returns its
+ * accepted steps; with steps == NULL it returns once the work is queued on
+ * the context's stream, and device faults of such intervals are returned by
+ * the job's next call that waits (fvc_ftle_reduce, fvc_ftle_get_state,
+ * fvc_ftle_set_state, fvc_job_get_stats). */
 fvc_status fvc_ftle_interval(fvc_job *job, int launch, double t1, double t2, long long *steps);
 
 /* FTLE of every point still without one (GetFTLEForPoint, ftle.c:1050-1203)
