@@ -27,6 +27,8 @@ cpu_baseline  the CPU oracle (the reference's algorithm restated in C,
            OpenMP over all host cores) on a bounded sample: the same grid and
            mesh over the first 5 frame intervals (T = 0.1).
 
+tracers    the cube's second workload: 1M tracers released at t = 0, outputs
+           every 10 steps, FP64 and BF16 forms.
 batched    the bent-tube batch of 64 tracer releases (uneven seed counts and
            windows) in the BF16 form and the FP64 form, one CUDA graph each.
 served     a Poisson request stream over the tube and the cube, served in the
@@ -78,6 +80,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the BF16 / FP16 mixed forms")
     ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--no-tracers", action="store_true", help="skip the 1M-tracer release on the cube")
+    ap.add_argument("--tracers", type=int, default=1_000_000)
     ap.add_argument("--no-batched", action="store_true", help="skip the bent-tube batch")
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
     ap.add_argument("--batch-jobs", type=int, default=64)
@@ -239,6 +243,56 @@ def run_reference(args, rank, world):
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ tracers
+
+def bench_tracers(args, inputs):
+    """The cube's tracer workload: args.tracers tracers released uniformly at
+    t = 0 (seed 0), RK4 h = 0.005 over T = 1, positions output every 10 steps
+    (t = 0, 0.05, ..., 1: 21 outputs, each copied to the host), through the
+    single-release loop of ompVC's Compute_Tracer (flow.run_tracers), in the
+    FP64 form and the BF16 form; endpoint errors of BF16 against FP64."""
+    import flow
+    import fvc
+    import synth
+    xyz, conn, adj, frames = inputs
+    ax = flow.TimeAxis(0.0, DT, NFRAMES, 0)
+    seeds = synth.uniform_seeds(args.tracers, 3, seed=0)
+    out = {"workload": f"{args.tracers} tracers uniform in the cube at t=0, T={T_WINDOW}, RK4 h={H}, "
+                       "positions output every 10 steps (21 outputs copied to the host)"}
+    finals = {}
+    for prec in ("fp64", "bf16"):
+        ctx = fvc.Context(3, 1)
+        ctx.set_unstruct_mesh(xyz, conn, adj)
+        ctx.set_bounds([0, 1, 0, 1, 0, 1])
+        ctx.set_integrator(1, H, 0)
+        ctx.set_precision(prec)
+        flow.upload_frames(ctx, ax, frames)
+        flow.run_tracers(ctx, ax, seeds[:4096], 0.0, 0.05, 21)          # warm-up
+        t0 = time.perf_counter()
+        fin = {}
+        outs, steps, st = flow.run_tracers(ctx, ax, seeds, 0.0, 0.05, 21, state=fin)
+        wall = time.perf_counter() - t0
+        finals[prec] = fin
+        out[prec] = {"value": steps / wall, "unit": "steps/s", "steps": int(steps), "wall_s": wall,
+                     "kernel_value": st["steps_main"] / (st["ms_main"] / 1e3) if st["ms_main"] > 0 else None,
+                     "outputs": len(outs), "written": int(sum(len(o) for o in outs))}
+        ctx.close()
+    # final tracer states: endpoints (the last position inside for tracers that
+    # left) over tracers whose exit status agrees, exit-time and id mismatches
+    a, b = finals["fp64"], finals["bf16"]
+    same = a["left"] == b["left"]
+    d = np.linalg.norm(b["X"][same] - a["X"][same], axis=1) if same.any() else np.zeros(1)
+    both = same & (a["left"] == 1)
+    out["bf16"]["errors_vs_fp64"] = {
+        "endpoint_max": float(d.max()), "endpoint_rms": float(np.sqrt((d ** 2).mean())),
+        "eid_mismatch_rate": float((a["eid"][same] != b["eid"][same]).mean()) if same.any() else 0.0,
+        "left_mismatch_rate": float((~same).mean()),
+        "exit_time_mismatch_rate": float((np.abs(a["ldt"][both] - b["ldt"][both]) > 1e-9).mean()) if both.any() else 0.0,
+        "left_fraction": float((a["left"] == 1).mean())}
+    out["speedup_vs_fp64"] = out["bf16"]["value"] / out["fp64"]["value"]
+    return out
 
 
 # ------------------------------------------------------------------ batched / served
@@ -490,6 +544,7 @@ def run_engine(args, rank, world, local_rank):
     else:
         ctx.close()
 
+    tracers = None if args.no_tracers else bench_tracers(args, inputs)
     batched = served = None
     if not (args.no_batched and args.no_served):
         import serve
@@ -530,6 +585,7 @@ def run_engine(args, rank, world, local_rank):
             "gpu_launches": gpu_launches,
             "fp64_pipe": fp64_pipe,
             "precision_forms": forms,
+            "tracers": tracers,
             "batched": batched,
             "served": served,
             "phases_ms_per_step": {k: sum(s[k] for s in stats) / args.steps

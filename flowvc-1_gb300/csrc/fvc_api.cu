@@ -142,6 +142,10 @@ extern "C" void fvc_destroy(fvc_ctx* c) {
   cudaFree(c->d_qscratch);
   cudaFree(c->d_qpair);
   cudaFree(c->d_steps);
+  cudaFreeHost(c->h_ring);
+  cudaFree(c->d_ring);
+  for (auto& kv : c->pool) cudaFree(kv.second);
+  for (auto& ev : c->ring_ev) cudaEventDestroy(ev);
   cudaFree(c->d_elem);
   cudaFree(c->d_geom);
   cudaFree(c->d_geo32);
@@ -381,6 +385,41 @@ extern "C" fvc_status fvc_upload_frame(fvc_ctx* c, int frame_id, const double* u
   if ((st = check_launch(c, "pack_frame"))) return st;
   FVC_CUDA(c, cudaStreamSynchronize(c->stream));
   return FVC_OK;
+}
+
+static constexpr size_t POOL_LIMIT = (size_t)16 << 30;
+
+void* pool_get(fvc_ctx* c, size_t bytes) {
+  auto it = c->pool.lower_bound(bytes);
+  if (it != c->pool.end() && it->first <= 2 * bytes) {
+    void* p = it->second;
+    c->pool_bytes -= it->first;
+    c->pool.erase(it);
+    return p;
+  }
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    // give the pool back to the device and try once more
+    for (auto& kv : c->pool) cudaFree(kv.second);
+    c->pool.clear();
+    c->pool_bytes = 0;
+    cudaGetLastError();
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+  }
+  return p;
+}
+
+void pool_put(fvc_ctx* c, void* p, size_t bytes) {
+  if (!p) return;
+  if (c->pool_bytes + bytes > POOL_LIMIT) {
+    cudaFree(p);
+    return;
+  }
+  c->pool.emplace(bytes, p);
+  c->pool_bytes += bytes;
 }
 
 void frame_dep(fvc_ctx* c, int id) {
@@ -629,6 +668,31 @@ static fvc_status build_steps(fvc_ctx* c, double t1, double t2) {
   StepM e{};
   e.tc = tc;
   T.push_back(e);
+  constexpr int RING = 64, RING_STEPS = 128;
+  if (T.size() <= (size_t)RING_STEPS) {
+    if (!c->h_ring) {
+      if (cudaMallocHost(&c->h_ring, sizeof(StepM) * RING * RING_STEPS) != cudaSuccess ||
+          cudaMalloc(&c->d_ring, sizeof(StepM) * RING * RING_STEPS) != cudaSuccess) {
+        cudaFreeHost(c->h_ring);
+        c->h_ring = nullptr;
+        return fail(c, FVC_ERR_OOM, "step table ring allocation failed");
+      }
+      c->ring_ev.assign(RING, nullptr);
+      for (auto& ev : c->ring_ev) FVC_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    const int k = c->ring_k;
+    c->ring_k = (c->ring_k + 1) % RING;
+    FVC_CUDA(c, cudaEventSynchronize(c->ring_ev[k]));
+    StepM* h = c->h_ring + (size_t)k * RING_STEPS;
+    StepM* d = c->d_ring + (size_t)k * RING_STEPS;
+    memcpy(h, T.data(), sizeof(StepM) * T.size());
+    FVC_CUDA(c, cudaMemcpyAsync(d, h, sizeof(StepM) * T.size(), cudaMemcpyHostToDevice, c->stream));
+    FVC_CUDA(c, cudaEventRecord(c->ring_ev[k], c->stream));
+    w.steps = d;
+    w.nsteps = (int)T.size() - 1;
+    w.nslots = 0;
+    return FVC_OK;
+  }
   if (T.size() > c->steps_cap) {
     cudaFree(c->d_steps);
     c->d_steps = nullptr;
@@ -779,8 +843,13 @@ extern "C" void fvc_job_destroy(fvc_job* j) {
     cudaSetDevice(j->ctx->device);
     cudaStreamSynchronize(j->ctx->stream);
   }
-  cudaFree(j->mem);
-  cudaFree(j->rec_mem);
+  if (j->ctx) {
+    pool_put(j->ctx, j->mem, j->mem_bytes);
+    pool_put(j->ctx, j->rec_mem, j->rec_bytes);
+  } else {
+    cudaFree(j->mem);
+    cudaFree(j->rec_mem);
+  }
   cudaFree(j->d_ctr);
   for (int k = 0; k < 4; k++)
     if (j->ev[k]) cudaEventDestroy(j->ev[k]);
@@ -827,11 +896,14 @@ extern "C" fvc_status fvc_job_get_stats(fvc_job* j, fvc_job_stats* out) {
 extern "C" void* fvc_stream(fvc_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 // Carves one allocation into the arrays listed in sizes (bytes each).
-static fvc_status carve(fvc_ctx* c, void** mem, std::vector<std::pair<void**, size_t>> parts) {
+static fvc_status carve(fvc_ctx* c, void** mem, std::vector<std::pair<void**, size_t>> parts,
+                        size_t* bytes = nullptr) {
   size_t total = 0;
   for (auto& p : parts) total += al256(p.second);
-  if (cudaMalloc(mem, total ? total : 256) != cudaSuccess)
-    return fail(c, FVC_ERR_OOM, "could not allocate %zu bytes for the job", total);
+  if (!total) total = 256;
+  *mem = pool_get(c, total);
+  if (!*mem) return fail(c, FVC_ERR_OOM, "could not allocate %zu bytes for the job", total);
+  if (bytes) *bytes = total;
   char* q = (char*)*mem;
   for (auto& p : parts) {
     *p.first = q;
@@ -844,11 +916,11 @@ static fvc_status run_chain(fvc_ctx* c, const ChainArgs& a, const double* dX, co
                             long long* launches) {
   size_t words = 5 * (size_t)a.n + 2 * ((size_t)a.res[0] * a.res[1] + 1) + 2 * ((size_t)a.res[0] + 1) +
                  2 * ((size_t)a.n / 1024 + 2) + 16;
-  int* work = nullptr;
-  if (cudaMalloc(&work, sizeof(int) * words) != cudaSuccess) return fail(c, FVC_ERR_OOM, "seed-chain scratch");
+  int* work = (int*)pool_get(c, sizeof(int) * words);
+  if (!work) return fail(c, FVC_ERR_OOM, "seed-chain scratch");
   int rounds = locate_chain(c->mesh, c->grid, a, dX, dleft0, deid, work, c->d_ctr, c->stream);
   cudaStreamSynchronize(c->stream);
-  cudaFree(work);
+  pool_put(c, work, sizeof(int) * words);
   if (rounds < 0) {
     fvc_status st = finish(c, "seed location", nullptr);
     return st ? st : fail(c, FVC_ERR_CUDA, "seed location failed");
@@ -860,19 +932,16 @@ static fvc_status run_chain(fvc_ctx* c, const ChainArgs& a, const double* dX, co
 }
 
 static int center_element(fvc_ctx* c, const double X[3]) {
-  double* dX = nullptr;
-  int* dO = nullptr;
   int r = -1;
-  if (cudaMalloc(&dX, 3 * sizeof(double)) != cudaSuccess || cudaMalloc(&dO, sizeof(int)) != cudaSuccess) {
-    cudaFree(dX);
-    return -2;
-  }
+  char* buf = (char*)pool_get(c, 256);
+  if (!buf) return -2;
+  double* dX = (double*)buf;
+  int* dO = (int*)(buf + 64);
   cudaMemcpyAsync(dX, X, 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
   launch_global_search(c->mesh, c->grid, 1, dX, nullptr, dO, c->stream);
   cudaMemcpyAsync(&r, dO, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) r = -2;
-  cudaFree(dX);
-  cudaFree(dO);
+  pool_put(c, buf, 256);
   return r;
 }
 
@@ -910,7 +979,8 @@ extern "C" fvc_status fvc_ftle_create(fvc_ctx* c, const fvc_ftle_spec* sp, fvc_j
               {(void**)&f.epos, 168 * n}, {(void**)&f.elt, 48 * n}, {(void**)&f.emt, 8 * n},
               {(void**)&f.tasks, 56 * n}, {(void**)&f.tsorted, 56 * n}, {(void**)&f.live, 4 * n},
               {(void**)&f.block_cnt, sizeof(int) * (2 * (n / 1024 + 1) + 16) + sizeof(long long) * (n / 1048576 + 8)},
-              {(void**)&left0, 4 * n}});
+              {(void**)&left0, 4 * n}},
+             &j->mem_bytes);
   if (st) {
     delete j;
     return st;
@@ -1022,11 +1092,13 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
     const int ns = j->prec ? c->window.nsteps : (c->window.nslots > 0 ? (c->window.nslots - 1) / 2 : 0);
     const int want = ns < 32 ? ns : 32;
     if (want > 0 && want > j->rec_cap) {
-      cudaFree(j->rec_mem);
+      pool_put(c, j->rec_mem, j->rec_bytes);
       j->rec_mem = nullptr;
       j->rec_cap = 0;
       const size_t n = (size_t)j->f.n;
-      if (cudaMalloc(&j->rec_mem, al256(24 * n * (size_t)want) + n) == cudaSuccess) j->rec_cap = want;
+      j->rec_bytes = al256(24 * n * (size_t)want) + n;
+      j->rec_mem = pool_get(c, j->rec_bytes);
+      if (j->rec_mem) j->rec_cap = want;
     }
     if (want > 0 && j->rec_cap >= want) {
       j->f.rec = (double*)j->rec_mem;
@@ -1206,7 +1278,8 @@ extern "C" fvc_status fvc_tracer_create(fvc_ctx* c, const fvc_tracer_spec* sp, i
               {(void**)&t.left, 4 * nn}, {(void**)&t.outX, 24 * nn},
               {(void**)&t.block_cnt, sizeof(int) * (2 * nb + 16) + sizeof(long long) * (nb / 1024 + 8)},
               {(void**)&t.live, 4 * nn},
-              {(void**)&left0, 4 * nn}});
+              {(void**)&left0, 4 * nn}},
+             &j->mem_bytes);
   if (st) {
     delete j;
     return st;

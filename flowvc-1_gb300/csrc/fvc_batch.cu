@@ -570,7 +570,8 @@ static fvc_status zorder_tracers(fvc_batch* b, HostJob& J) {
   const size_t nb = (size_t)n;
   char* mem = nullptr;
   const size_t bytes = 4 * nb * 2 + 4 * (3 * (size_t)K + 2) + 8 * ((size_t)K / 1024 + 2) + 64 * nb + 256 * 16;
-  if (cudaMalloc(&mem, bytes) != cudaSuccess) return FVC_OK;  // no room: keep seed order
+  mem = (char*)pool_get(c, bytes);
+  if (!mem) return FVC_OK;  // no room: keep seed order
   char* q = mem;
   auto take = [&](size_t sz) { char* r = q; q += (sz + 255) & ~(size_t)255; return r; };
   int* key = (int*)take(4 * nb);
@@ -601,7 +602,7 @@ static fvc_status zorder_tracers(fvc_batch* b, HostJob& J) {
   cudaMemcpyAsync(J.perm.data(), perm, 4 * nb, cudaMemcpyDeviceToHost, s);
   fvc_status st = check_launch(c, "z-order");
   cudaError_t e = cudaStreamSynchronize(s);
-  cudaFree(mem);
+  pool_put(c, mem, bytes);
   if (st) return st;
   if (e != cudaSuccess) return fail(c, FVC_ERR_CUDA, "z-order: %s", cudaGetErrorString(e));
   b->stats.launches += 6;

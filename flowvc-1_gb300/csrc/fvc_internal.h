@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -53,6 +54,13 @@ struct fvc_ctx {
   std::vector<StepM> h_steps;
   StepM* d_steps = nullptr;
   size_t steps_cap = 0;
+  // step tables staged through page-locked memory (a pageable copy would
+  // synchronise the stream): a ring of tables, each slot reused after the
+  // event of its last upload
+  StepM* h_ring = nullptr;
+  StepM* d_ring = nullptr;
+  int ring_k = 0;
+  std::vector<cudaEvent_t> ring_ev;
   int window_lo = -1, window_hi = -1;
   // asynchronous frame uploads: a side stream, a two-buffer staging ring and
   // per frame the event its upload recorded
@@ -61,6 +69,11 @@ struct fvc_ctx {
   int up_k = 0;
   cudaEvent_t up_after = nullptr;  // compute-stream point an upload must follow
   std::unordered_map<int, cudaEvent_t> frame_ev;
+  // device blocks freed by jobs, kept for later jobs on this context: a
+  // cudaFree synchronises the device, and FTLE windows allocate the same
+  // sizes again and again; reuse is ordered by the context's stream
+  std::multimap<size_t, void*> pool;
+  size_t pool_bytes = 0;
   // exposure time (Trace_CETCompute): per-element sums shared by all releases
   double* d_cet_sum = nullptr;
   int* d_cet_enc = nullptr;
@@ -70,6 +83,8 @@ struct fvc_ctx {
 
 struct fvc_job {
   fvc_ctx* ctx = nullptr;
+  size_t mem_bytes = 0;     // size of mem (returned to the context's pool)
+  size_t rec_bytes = 0;     // size of rec_mem
   int kind = 0;  // 0 FTLE, 1 tracers
   FtleDev f{};
   TracerDev t{};
@@ -98,6 +113,10 @@ fvc_status quantised(fvc_ctx* c, int id, fvc_ctx::QFrame** out);
 // the integrator / precision combination is one the form supports
 fvc_status mixed_ok(fvc_ctx* c);
 void job_events(fvc_job* j);
+// device memory from / back to the context's pool of freed blocks (a block
+// of at least `bytes` and at most twice that, else cudaMalloc)
+void* pool_get(fvc_ctx* c, size_t bytes);
+void pool_put(fvc_ctx* c, void* p, size_t bytes);
 // orders the context's stream after a pending asynchronous upload of frame id
 void frame_dep(fvc_ctx* c, int id);
 float ev_ms(cudaEvent_t a, cudaEvent_t b);

@@ -100,10 +100,11 @@ def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, 
 
 
 def run_tracers(ctx: fvc.Context, ax: TimeAxis, seeds, t_start, out_delta, out_res, direction=1, lsc=1,
-                always=0, snapshots=True):
+                always=0, snapshots=True, state=None):
     """One tracer release from t_start with outputs every out_delta (ompVC's
     Compute_Tracer loop, ompVC/tracers.c:25-289).  Returns (list of output
-    arrays, steps, job stats)."""
+    arrays, steps, job stats); a dict passed as state receives the release's
+    final tracer state (fvc_tracer_get_state)."""
     t_end = t_start + (out_res - 1) * direction * out_delta
     first = int(math.floor((t_start - ax.tmin) / ax.tdelta)) if direction > 0 else int(math.ceil((t_start - ax.tmin) / ax.tdelta))
     last = int(math.ceil((t_end - ax.tmin) / ax.tdelta)) if direction > 0 else int(math.floor((t_end - ax.tmin) / ax.tdelta))
@@ -136,5 +137,7 @@ def run_tracers(ctx: fvc.Context, ax: TimeAxis, seeds, t_start, out_delta, out_r
             t1 = t2
         df += direction
     st = job.stats()
+    if state is not None:
+        state.update(job.get_state())
     job.close()
     return outs, steps, st
