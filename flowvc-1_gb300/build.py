@@ -32,6 +32,7 @@ CU_SOURCES = ["fvc_kernels.cu", "fvc_api.cu", "fvc_variant_c2.cu", "fvc_variant_
 # resident 128-thread blocks per SM the integrator kernels are compiled for
 # (register budget 65536 / (128 * n)); FVC_MINBLOCKS overrides it for sweeps
 MINBLOCKS = os.environ.get("FVC_MINBLOCKS", "4")
+MX_MINBLOCKS = os.environ.get("FVC_MX_MINBLOCKS", "4")
 
 
 def _run(cmd):
@@ -66,7 +67,7 @@ def build_lib(force=False, verbose=False):
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(obj)
         if force or _newer(obj, deps):
-            jobs.append([NVCC, *ARCH, *NVFLAGS, "-DFVC_MINBLOCKS=" + MINBLOCKS, "-c", os.path.join(CSRC, src),
+            jobs.append([NVCC, *ARCH, *NVFLAGS, "-DFVC_MINBLOCKS=" + MINBLOCKS, "-DFVC_MX_MINBLOCKS=" + MX_MINBLOCKS, "-c", os.path.join(CSRC, src),
                          "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for r in ex.map(_run, jobs):

@@ -114,7 +114,7 @@ __device__ __forceinline__ void flush_jobs(const BJob* jobs, int jid, unsigned s
 
 // The persistent advection of the mixed form over the tick's queue.
 template <int D>
-__global__ void __launch_bounds__(256) k_batch_advance_mx(DevMesh m, int type, const BJob* __restrict__ jobs,
+__global__ void __launch_bounds__(256, (FVC_MX_MINBLOCKS + 1) / 2) k_batch_advance_mx(DevMesh m, int type, const BJob* __restrict__ jobs,
                                                          const int2* __restrict__ queue, BatchCtr* bc) {
   const long nq = *(volatile int*)&bc->nqueue;
   for (long base = warp_grab(&bc->cursor); base < nq; base = warp_grab(&bc->cursor)) {

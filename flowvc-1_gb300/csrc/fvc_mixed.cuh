@@ -24,6 +24,10 @@
 namespace fvc {
 
 #define FVC_NEAR_FACE 1.0e-5f
+// resident 128-thread blocks per SM the mixed-form kernels are compiled for
+#ifndef FVC_MX_MINBLOCKS
+#define FVC_MX_MINBLOCKS 4
+#endif
 enum { QF_BF16 = 1, QF_FP16 = 2 };  // the FVC_PREC_* codes of fvc.h
 
 struct PtM {

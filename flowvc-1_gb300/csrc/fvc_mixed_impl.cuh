@@ -10,7 +10,7 @@
 namespace fvc {
 
 template <int D>
-__global__ void __launch_bounds__(128) k_advect_mx(DevMesh m, DevWindow w, int type, int n, double* X, int* eid,
+__global__ void __launch_bounds__(128, FVC_MX_MINBLOCKS) k_advect_mx(DevMesh m, DevWindow w, int type, int n, double* X, int* eid,
                                                    int* left, double* ldt, DevCounters* ctr) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned steps = 0;
@@ -79,7 +79,7 @@ __global__ void k_ftle_launch_mx(DevMesh m, DevWindow w, FtleDev f, float tl, De
 }
 
 template <int D>
-__global__ void __launch_bounds__(128) k_ftle_pass1_mx(DevMesh m, DevWindow w, int type, FtleDev f,
+__global__ void __launch_bounds__(128, FVC_MX_MINBLOCKS) k_ftle_pass1_mx(DevMesh m, DevWindow w, int type, FtleDev f,
                                                        DevCounters* ctr) {
   const long nlive = *(volatile int*)&ctr->nlive;
   unsigned steps = 0;
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(128) k_ftle_pass1_mx(DevMesh m, DevWindow w, i
 }
 
 template <int D>
-__global__ void __launch_bounds__(128) k_ftle_tasks_mx(DevMesh m, DevWindow w, int type, FtleDev f, int phase,
+__global__ void __launch_bounds__(128, FVC_MX_MINBLOCKS) k_ftle_tasks_mx(DevMesh m, DevWindow w, int type, FtleDev f, int phase,
                                                        DevCounters* ctr) {
   const long ntask = *(volatile int*)&ctr->ntask;
   int* cursor = &ctr->cur[1 + phase];
@@ -157,7 +157,7 @@ __global__ void k_tracer_launch_mx(DevMesh m, DevWindow w, TracerDev t, float tl
 }
 
 template <int D>
-__global__ void __launch_bounds__(128) k_tracer_advance_mx(DevMesh m, DevWindow w, int type, TracerDev t,
+__global__ void __launch_bounds__(128, FVC_MX_MINBLOCKS) k_tracer_advance_mx(DevMesh m, DevWindow w, int type, TracerDev t,
                                                            DevCounters* ctr) {
   const long nlive = *(volatile int*)&ctr->nlive;
   unsigned steps = 0;
