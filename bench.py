@@ -533,7 +533,7 @@ def run_engine(args, rank, world, local_rank):
             c2.set_unstruct_mesh(pxyz, pconn, padj)
             c2.set_bounds([0, 1, 0, 1, 0, 1])
             c2.set_integrator(1, H, 0)
-            flow.upload_frames(c2, ax, pframes)
+            flow.upload_frames(c2, ax, pframes, asynchronous=True)
             wT, wN, st, _ = flow.run_ftle(c2, ax, grid, T_WINDOW)
             e2e_steps += st
             c2.close()

@@ -96,7 +96,7 @@ __global__ void k_velocity(DevMesh m, DevWindow w, int n, const double* X, int* 
   if (i < n) {
     double x[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]}, v[3] = {0, 0, 0};
     int e = eid ? eid[i] : -1, l = left[i];
-    err = velocity<D, M>(m, w, tq, -1, x, e, l, v);
+    err = velocity<D, M>(m, w, tq, -1, x, e, l, v) | (M == 1 ? walk_fault(e) : 0);
     out[3 * i] = v[0];
     out[3 * i + 1] = v[1];
     out[3 * i + 2] = v[2];
@@ -117,7 +117,7 @@ __global__ void k_ftle_launch(DevMesh m, DevWindow w, FtleDev f, double t, DevCo
   if (p < f.n && !f.left[p]) {
     double x[3] = {f.X[3 * p], f.X[3 * p + 1], f.X[3 * p + 2]}, v[3];
     int e = f.eid[p], l = 0;
-    err = velocity<D, M>(m, w, t, -1, x, e, l, v);
+    err = velocity<D, M>(m, w, t, -1, x, e, l, v) | (M == 1 ? walk_fault(e) : 0);
     f.V[3 * p] = v[0];
     f.V[3 * p + 1] = v[1];
     f.V[3 * p + 2] = v[2];
@@ -484,7 +484,7 @@ __global__ void k_tracer_launch(DevMesh m, DevWindow w, TracerDev t, double tq, 
   if (i < t.n && !t.left[i]) {
     double x[3] = {t.X[3 * i], t.X[3 * i + 1], t.X[3 * i + 2]}, v[3];
     int e = t.eid[i], l = 0;
-    err = velocity<D, M>(m, w, tq, -1, x, e, l, v);
+    err = velocity<D, M>(m, w, tq, -1, x, e, l, v) | (M == 1 ? walk_fault(e) : 0);
     t.V[3 * i] = v[0];
     t.V[3 * i + 1] = v[1];
     t.V[3 * i + 2] = v[2];

@@ -376,8 +376,8 @@ __device__ __forceinline__ int neighbour(const DevMesh& m, int e, int slot) { re
 // FP64 solve decides at the element reached, so the lanes of a warp run the
 // expensive step together.  An element's neighbours are loaded together
 // with its records, so a hop costs one memory round trip.  Returns 0 with
-// the element's coordinates, 1 when the walk leaves through a boundary face
-// (eid = -1), or a fault bit.
+// the element's coordinates, or 1 when the walk stops: eid = -1 when it left
+// through a boundary face, EID_FAULT when it failed.
 template <int DIMS>
 __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& eid, bool vel_rule, double& r,
                                     double& s, double& t, double& wv, double& d, int4& nd) {
@@ -402,14 +402,18 @@ __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& ei
     else if (fabs(s - d) < FVC_TINY) slot = 1;
     else if (DIMS == 3 && fabs(t - d) < FVC_TINY) slot = 2;
     else if (fabs(wv - d) < FVC_TINY) slot = DIMS == 3 ? 3 : 2;
-    else return PT_ERR_WALK;  // "Indeterminate neighbor"
+    else break;  // "Indeterminate neighbor"
     eid = pick(nb, slot);
     hop++;
     if (eid == -1) return 1;
     nb = neighbours(m, eid);
   }
-  return PT_ERR_WALK;
+  eid = EID_FAULT;
+  return 1;
 }
+
+// PT_ERR_WALK for the element id a failed walk leaves behind
+__device__ __forceinline__ int walk_fault(int eid) { return eid == EID_FAULT ? PT_ERR_WALK : 0; }
 
 // GetVelocity_Unstructured, ompVC/velocity.c:459-621: walk from eid until the
 // element passes (d + TINY) >= 0, then P1 in space and linear in time.
@@ -434,13 +438,12 @@ __device__ __forceinline__ int vel_unstruct(const DevMesh& m, const DevWindow& w
     t = nc->t;
     wv = nc->w;
   } else {
-    int st = walk<DIMS>(m, X, eid, true, r, s, t, wv, d, nd);
-    if (st == 1) {
+    if (walk<DIMS>(m, X, eid, true, r, s, t, wv, d, nd)) {
+      // out of the domain, or a failed walk (eid = EID_FAULT): the point stops
       left = 1;
       out[0] = out[1] = out[2] = 0.0;
       return 0;
     }
-    if (st) return st;
   }
   NodeVel<DIMS> nv;
   if (tab) {
@@ -468,8 +471,9 @@ __device__ __forceinline__ int vel_unstruct(const DevMesh& m, const DevWindow& w
 }
 
 // Get_Element_Local_Search, ompVC/mesh.c:496-611: containment d > -TINY;
-// returns -1 when the walk leaves through a boundary face.  On success nc
-// (if given) receives the natural coordinates of the element found.
+// returns -1 when the walk leaves through a boundary face (or guess < 0) and
+// EID_FAULT when it fails.  On success nc (if given) receives the natural
+// coordinates of the element found.
 template <int DIMS>
 __device__ __forceinline__ int locate_walk(const DevMesh& m, const double X[3], int guess, int& err,
                                            NatCache* nc = nullptr) {
@@ -481,12 +485,7 @@ __device__ __forceinline__ int locate_walk(const DevMesh& m, const double X[3], 
   }
   double r, s, t, wv, d;
   int4 nd;
-  int st = walk<DIMS>(m, X, guess, false, r, s, t, wv, d, nd);
-  if (st == 1) return -1;
-  if (st) {
-    err |= st;
-    return -1;
-  }
+  if (walk<DIMS>(m, X, guess, false, r, s, t, wv, d, nd)) return guess == EID_FAULT ? EID_FAULT : -1;
   if (nc) {
     nc->e = guess;
     nc->nd = nd;
@@ -497,6 +496,16 @@ __device__ __forceinline__ int locate_walk(const DevMesh& m, const double X[3], 
     nc->d = d;
   }
   return guess;
+}
+
+// locate_walk for a one-off locate: a failed walk is reported in err and
+// answers -1
+template <int DIMS>
+__device__ __forceinline__ int locate_once(const DevMesh& m, const double X[3], int guess, int& err) {
+  const int r = locate_walk<DIMS>(m, X, guess, err);
+  if (r != EID_FAULT) return r;
+  err |= PT_ERR_WALK;
+  return -1;
 }
 
 // Containment test of one element (the predicate of
@@ -550,7 +559,7 @@ __device__ __forceinline__ int velocity(const DevMesh& m, const DevWindow& w, do
 template <int DIMS>
 __device__ __noinline__ void cet_step(const DevMesh& m, const CetDev& c, const double* X0, const double* X1,
                                       int e1, double h, int* err) {
-  int e0 = locate_walk<DIMS>(m, X0, e1, *err);
+  int e0 = locate_once<DIMS>(m, X0, e1, *err);
   if (e0 < 0) {
     e0 = global_find<DIMS>(m, c.g, X0);
     if (e0 < 0) {
@@ -568,7 +577,7 @@ __device__ __noinline__ void cet_step(const DevMesh& m, const CetDev& c, const d
     double Xt[3];
 #pragma unroll
     for (int q = 0; q < 3; q++) Xt[q] = (1 - a) * X0[q] + a * X1[q];
-    int et = locate_walk<DIMS>(m, Xt, last, *err);
+    int et = locate_once<DIMS>(m, Xt, last, *err);
     if (et < 0) {
       et = global_find<DIMS>(m, c.g, Xt);
       if (et < 0) continue;
@@ -592,7 +601,8 @@ __device__ __noinline__ void cet_step(const DevMesh& m, const CetDev& c, const d
 template <int DIMS, int MESH>
 __device__ __noinline__ int velocity_cold(const DevMesh& m, const DevWindow& w, double tq, int tslot,
                                           const double* X, int* eid, int* left, double* out) {
-  return velocity<DIMS, MESH>(m, w, tq, tslot, X, *eid, *left, out);
+  const int r = velocity<DIMS, MESH>(m, w, tq, tslot, X, *eid, *left, out);
+  return MESH == 1 ? r | walk_fault(*eid) : r;
 }
 
 // Euler, ompVC/integration.c:222-311
@@ -606,7 +616,9 @@ __device__ __noinline__ double euler(const DevMesh& m, const DevWindow& w, const
   int k = 0;
   while ((tc - tend) * (tend - tstart) < 0.0) {
     if ((tc + h - tend) * (tc + h - tstart) > 0.0) h = dsign(tend - tc, tend - tstart);
-    if ((err |= velocity<DIMS, MESH>(m, w, tc, 2 * k, p.X, p.eid, p.left, ve, &nc))) return tend;
+    if ((err |= velocity<DIMS, MESH>(m, w, tc, 2 * k, p.X, p.eid, p.left, ve, &nc) |
+                (MESH == 1 ? walk_fault(p.eid) : 0)))
+      return tend;
     p.X[0] = p.X[0] + h * ve[0];
     p.X[1] = p.X[1] + h * ve[1];
     p.X[2] = p.X[2] + h * ve[2];
@@ -689,6 +701,7 @@ __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, cons
     if (err) return tend;
     if ((MESH == 0 && outside_domain(m, p.X)) || (MESH == 1 && p.eid < 0) || l[0] || l[1] || l[2] ||
         l[3]) {
+      if (MESH == 1) err |= walk_fault(e[0]) | walk_fault(e[1]) | walk_fault(e[2]) | walk_fault(e[3]);
       p.left = 1;
       p.ldt = tc - h;
 #pragma unroll
@@ -734,7 +747,7 @@ __device__ __noinline__ double ab2(const DevMesh& m, const DevWindow& w, const D
   while ((tc - tend) * (tend - tstart) < 0.0) {
     if ((tc + h - tend) * (tc + h - tstart) > 0.0) h = dsign(tend - tc, tend - tstart);
     double inc[3], f[3];
-    int lf = 0;
+    int lf = 0, ef = p.eid;
     if (first) {
       if ((err |= rk4_stages<DIMS, MESH>(m, w, p, tc, h, k, e, l, kk, &nc))) return tend;
 #pragma unroll
@@ -744,7 +757,6 @@ __device__ __noinline__ double ab2(const DevMesh& m, const DevWindow& w, const D
       }
       lf = l[0] || l[1] || l[2] || l[3];
     } else {
-      int ef = p.eid;
       if ((err |= velocity<DIMS, MESH>(m, w, tc, 2 * k, p.X, ef, lf, f, &nc))) return tend;
       double c0 = h / (2.0 * hprev), c1 = 1.0 + c0;
 #pragma unroll
@@ -757,6 +769,8 @@ __device__ __noinline__ double ab2(const DevMesh& m, const DevWindow& w, const D
     if (MESH == 1) p.eid = locate_walk<DIMS>(m, p.X, p.eid, err, &nc);
     if (err) return tend;
     if ((MESH == 0 && outside_domain(m, p.X)) || (MESH == 1 && p.eid < 0) || lf) {
+      if (MESH == 1)
+        err |= walk_fault(ef) | walk_fault(e[0]) | walk_fault(e[1]) | walk_fault(e[2]) | walk_fault(e[3]);
       p.left = 1;
       p.ldt = tc - h;
 #pragma unroll
@@ -835,6 +849,9 @@ __device__ __noinline__ double rkf(const DevMesh& m, const DevWindow& w, const D
     ts = tc + 0.5 * h;
     if ((err |= velocity<DIMS, MESH>(m, w, ts, -1, M, e[5], l[5], k[5]))) return tend;
     if (l[0] || l[1] || l[2] || l[3] || l[4] || l[5]) {
+      if (MESH == 1)
+        err |= walk_fault(e[0]) | walk_fault(e[1]) | walk_fault(e[2]) | walk_fault(e[3]) | walk_fault(e[4]) |
+               walk_fault(e[5]);
       p.left = 1;
       p.ldt = tc;
       return p.ldt;
@@ -903,6 +920,7 @@ __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, cons
   else if (in.type == 2) stop = rkf<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet);
   else if (in.type == 3 && !CET) stop = ab2<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
   else stop = euler<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet, rec);
+  if (MESH == 1) err |= walk_fault(p.eid);
   if (!err && (fabs(stop - tend) > FVC_TINY) && in.extrapolate) {
 #pragma unroll
     for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + p.V[q] * (tend - stop);

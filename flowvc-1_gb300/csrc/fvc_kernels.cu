@@ -278,7 +278,7 @@ __global__ void k_local(DevMesh m, int n, const double* X, const int* guess, int
   int err = 0;
   if (i < n) {
     double x[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
-    out[i] = locate_walk<D>(m, x, guess[i], err);
+    out[i] = locate_once<D>(m, x, guess[i], err);
   }
   flush_counters(&ctr->steps, &ctr->status, 0, err);
 }
@@ -476,8 +476,8 @@ __global__ void k_chain_eval(DevMesh m, ChainDev c, DevCounters* ctr) {
     else if (c.gprev && c.gprev[p] == c.g[p]) r = c.R[p];  // same guess, same walk
     else {
       double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
-      r = locate_walk<DIMS>(m, x, c.g[p], err);
-      if (r < 0 && c.kind != 1) r = locate_walk<DIMS>(m, x, c.seed, err);
+      r = locate_once<DIMS>(m, x, c.g[p], err);
+      if (r < 0 && c.kind != 1) r = locate_once<DIMS>(m, x, c.seed, err);
       if (r < 0 && c.lsc) r = c.R0[p];
     }
     c.Rn[p] = r;
@@ -511,8 +511,8 @@ __device__ __forceinline__ int chain_one(const DevMesh& m, const BucketGrid& g, 
                                          int guess, int& err) {
   if (c.left0[p]) return -1;
   const double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
-  int r = locate_walk<DIMS>(m, x, guess, err);
-  if (r < 0) r = locate_walk<DIMS>(m, x, c.seed, err);
+  int r = locate_once<DIMS>(m, x, guess, err);
+  if (r < 0) r = locate_once<DIMS>(m, x, c.seed, err);
   if (r < 0 && c.lsc) r = global_find<DIMS>(m, g, x);
   return r;
 }

@@ -169,8 +169,8 @@ __device__ __forceinline__ float nat32_fine(const DevMesh& m, int e, const float
 
 // The walk of GetVelocity_Unstructured (vel_rule) / Get_Element_Local_Search
 // in the mixed form.  Returns 0 with the FP32 natural coordinates of the
-// element found, 1 when the walk leaves through a boundary face (eid = -1),
-// or PT_ERR_WALK.
+// element found, or 1 when the walk stops: eid = -1 when it left through a
+// boundary face, EID_FAULT when it failed.
 // ompVC's FP64 containment test of element e at X - C and, when it fails,
 // its face choice: returns -2 when the point is inside (coordinates in
 // r, s, t, wv), the face slot to step through, or -1 ("Indeterminate
@@ -229,12 +229,13 @@ __device__ __forceinline__ int walk_mx(const DevMesh& m, const float X[3], const
         wv = c4[3];
         return 0;
       }
-      if (slot < 0) return PT_ERR_WALK;
+      if (slot < 0) break;
     }
     eid = pick(nb, slot);
     if (eid == -1) return 1;
   }
-  return PT_ERR_WALK;
+  eid = EID_FAULT;
+  return 1;
 }
 
 // The last locate's element and coordinates at the current position.
@@ -257,13 +258,12 @@ __device__ __forceinline__ int vel_mx(const DevMesh& m, const W& w, float tl, co
     s = nc->s;
     t = nc->t;
   } else {
-    const int st = walk_mx<D>(m, X, C, eid, true, r, s, t, wv, nd);
-    if (st == 1) {
+    if (walk_mx<D>(m, X, C, eid, true, r, s, t, wv, nd)) {
+      // out of the domain, or a failed walk (eid = EID_FAULT): the point stops
       left = 1;
       out[0] = out[1] = out[2] = 0.0f;
       return 0;
     }
-    if (st) return st;
   }
   float u0[3], u1[3], u2[3];
   node_vel_mx(w, nd.x, tl, u0);
@@ -295,12 +295,7 @@ __device__ __forceinline__ int locate_mx(const DevMesh& m, const float X[3], con
   }
   float r, s, t, wv;
   int4 nd;
-  const int st = walk_mx<D>(m, X, C, guess, false, r, s, t, wv, nd);
-  if (st == 1) return -1;
-  if (st) {
-    err |= st;
-    return -1;
-  }
+  if (walk_mx<D>(m, X, C, guess, false, r, s, t, wv, nd)) return guess == EID_FAULT ? EID_FAULT : -1;
   nc->e = guess;
   nc->nd = nd;
   nc->r = r;
@@ -362,6 +357,7 @@ __device__ __forceinline__ void advect_mx(const DevMesh& m, const W& w, int type
     p.eid = locate_mx<D>(m, p.X, p.c, p.eid, err, &nc);
     if (err) return;
     if (p.eid < 0 || l[0] || l[1] || l[2] || l[3]) {
+      err |= walk_fault(p.eid) | walk_fault(e[0]) | walk_fault(e[1]) | walk_fault(e[2]) | walk_fault(e[3]);
       p.left = 1;
       p.ldt = st.tc;
 #pragma unroll

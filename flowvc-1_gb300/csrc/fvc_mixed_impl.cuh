@@ -50,7 +50,7 @@ __global__ void k_velocity_mx(DevMesh m, DevWindow w, int n, const double* X, in
       c[k] = q.y;
     }
     int e = eid[i], l = left[i];
-    err = isnan(tl) ? PT_ERR_TLOC : vel_mx<D>(m, w, tl, x, c, e, l, v, nullptr);
+    err = isnan(tl) ? PT_ERR_TLOC : vel_mx<D>(m, w, tl, x, c, e, l, v, nullptr) | walk_fault(e);
     out[3 * i] = v[0];
     out[3 * i + 1] = v[1];
     out[3 * i + 2] = v[2];
@@ -68,7 +68,7 @@ __global__ void k_ftle_launch_mx(DevMesh m, DevWindow w, FtleDev f, float tl, De
     float x[3], c[3], v[3];
     load_pos_pair(f.X, p, x, c);
     int e = f.eid[p], l = 0;
-    err = isnan(tl) ? PT_ERR_TLOC : vel_mx<D>(m, w, tl, x, c, e, l, v, nullptr);
+    err = isnan(tl) ? PT_ERR_TLOC : vel_mx<D>(m, w, tl, x, c, e, l, v, nullptr) | walk_fault(e);
     f.V[3 * p] = v[0];
     f.V[3 * p + 1] = v[1];
     f.V[3 * p + 2] = v[2];
@@ -146,7 +146,7 @@ __global__ void k_tracer_launch_mx(DevMesh m, DevWindow w, TracerDev t, float tl
     float x[3], c[3], v[3];
     load_pos_pair(t.X, i, x, c);
     int e = t.eid[i], l = 0;
-    err = isnan(tl) ? PT_ERR_TLOC : vel_mx<D>(m, w, tl, x, c, e, l, v, nullptr);
+    err = isnan(tl) ? PT_ERR_TLOC : vel_mx<D>(m, w, tl, x, c, e, l, v, nullptr) | walk_fault(e);
     t.V[3 * i] = v[0];
     t.V[3 * i + 1] = v[1];
     t.V[3 * i + 2] = v[2];

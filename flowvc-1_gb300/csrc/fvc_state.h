@@ -7,6 +7,11 @@ namespace fvc {
 
 // per-point fault bits, OR-ed into a launch's status word
 enum : int { PT_ERR_WALK = 1, PT_ERR_TLOC = 2, PT_ERR_STATE = 4, PT_ERR_CET = 8 };
+// the element id a neighbour walk leaves behind when it fails (the hop cap,
+// or ompVC's "Indeterminate neighbor"); a boundary exit leaves -1.  The walk
+// stops either way, and the fault becomes PT_ERR_WALK where the callers
+// handle a point's stop, outside the stepping loop.
+enum : int { EID_FAULT = -2 };
 
 struct DevMesh {
   int dims, mesh_type;  // 2/3; 0 Cartesian, 1 unstructured

@@ -54,10 +54,16 @@ def ftle_frame_range(ax: TimeAxis, t_start, T, direction):
     return int(math.ceil((tmaxreq - ax.tmin) / ax.tdelta)), int(math.floor((tminreq - ax.tmin) / ax.tdelta))
 
 
-def upload_frames(ctx: fvc.Context, ax: TimeAxis, frames):
-    """Upload every frame file once, under its file index."""
+def upload_frames(ctx: fvc.Context, ax: TimeAxis, frames, asynchronous=False):
+    """Upload every frame file once, under its file index.  asynchronous:
+    through the frame pipeline (fvc_upload_frame_async; the arrays must be
+    C-contiguous float64, page-locked for overlap, and stay alive and
+    unchanged until the context has used them or frame_wait returned)."""
     for i, f in enumerate(frames):
-        ctx.upload_frame(i, f)
+        if asynchronous:
+            ctx.upload_frame_async(i, f)
+        else:
+            ctx.upload_frame(i, f)
 
 
 def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, lsc=1, state=None):

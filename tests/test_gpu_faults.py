@@ -1,0 +1,93 @@
+"""Failure detection without a GPU fault: failures are made on the host
+(arguments, states, limits) and must come back as the documented statuses,
+with the context still usable afterwards."""
+import numpy as np
+import pytest
+
+import flow
+import fvc
+import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def cube_ctx(max_hops=0, prec="fp64", n=6):
+    xyz, conn, adj = synth.kuhn_cube_mesh(n, jitter=0.2, seed=0)
+    ctx = fvc.Context(3, 1, max_hops=max_hops)
+    ctx.set_unstruct_mesh(xyz, conn, adj)
+    ctx.set_bounds([0, 1, 0, 1, 0, 1])
+    ctx.set_integrator(1, 0.005, 0)
+    ctx.set_precision(prec)
+    frames = [synth.abc_flow(xyz, k * 0.02) for k in range(6)]
+    ax = flow.TimeAxis(0.0, 0.02, 6, 0)
+    flow.upload_frames(ctx, ax, frames)
+    return ctx, ax
+
+
+def advect_args(P, eid):
+    return [P.copy(), np.zeros_like(P), eid.copy(), np.zeros(len(P), np.int32), np.zeros(len(P))]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "bf16"])
+def test_query_time_outside_the_window(prec):
+    ctx, ax = cube_ctx(prec=prec)
+    ctx.set_window(1, 2, 0.02, 0.04)
+    P = synth.uniform_seeds(64, 3, seed=1)
+    eid = ctx.global_search(P)
+    with pytest.raises(fvc.FvcError) as e:
+        ctx.advect(*advect_args(P, eid), 0.02, 0.07)  # ends past the window's 0.04
+    assert e.value.status == fvc.FVC_ERR_TLOC
+    # the context still works
+    a = advect_args(P, eid)
+    assert ctx.advect(*a, 0.02, 0.04) > 0
+    ctx.close()
+
+
+def test_walk_hop_cap():
+    ctx, ax = cube_ctx(max_hops=1)
+    ctx.set_window(0, 1, 0.0, 0.02)
+    P = synth.uniform_seeds(256, 3, seed=2)
+    eid = np.zeros(len(P), np.int32)  # every walk starts far away in element 0
+    with pytest.raises(fvc.FvcError) as e:
+        ctx.advect(*advect_args(P, eid), 0.0, 0.02)
+    assert e.value.status == fvc.FVC_ERR_WALK
+    ctx.close()
+
+
+def test_ftle_fault_reported_by_the_call_that_waits():
+    ctx, ax = cube_ctx()
+    ctx.set_window(0, 1, 0.0, 0.02)
+    spec = fvc.FtleSpec(0, 1, 0, 1, 0, 1, 6, 6, 6, 1, 0.0, 0.02, 1)
+    job = fvc.FtleJob(ctx, spec)
+    st = job.get_state()
+    eid = st["eid"].copy()
+    eid[7] = -1  # a live point without an element: "integrate point that already left"
+    ctx.lib.fvc_ftle_set_state(job.h, None, fvc._i(eid), None, None, None, None, None)
+    job.interval(0, 0.0, 0.02, wait=False)  # queued: no status yet
+    with pytest.raises(fvc.FvcError) as e:
+        job.reduce(0.02)
+    assert e.value.status == fvc.FVC_ERR_STATE
+    job.close()
+    # a fresh job on the same context completes
+    wT, wN, steps, _ = flow.run_ftle(ctx, ax, (0, 1, 0, 1, 0, 1, 5, 5, 5), 0.04)
+    assert steps > 0 and np.isfinite(wT).all()
+    ctx.close()
+
+
+def test_batch_reports_failed_jobs_and_keeps_the_rest():
+    """A hop cap of 1 lets no walk cross a face: a release that moves fails
+    (at seed location or while advecting), a release of tracers outside the
+    domain has nothing to walk and completes; one job's fault is its own."""
+    ctx, ax = cube_ctx(max_hops=1)
+    b = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, 0)
+    bad = b.submit_tracers(synth.uniform_seeds(500, 3, seed=5), 0.0, 0.06)
+    good = b.submit_tracers(np.full((8, 3), 1.5), 0.0, 0.06)
+    b.run()
+    with pytest.raises(fvc.FvcError) as e:
+        b.poll(bad)
+    assert e.value.status in (fvc.FVC_ERR_WALK, fvc.FVC_ERR_CUDA, fvc.FVC_ERR_STATE)
+    assert b.poll(good) == fvc.BATCH_DONE
+    r = b.tracer_result(good)
+    assert (r["left"] == 1).all()
+    b.close()
+    ctx.close()
