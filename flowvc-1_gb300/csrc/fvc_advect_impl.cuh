@@ -426,8 +426,12 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_tasks(DevMesh m, De
   flush_counters(&ctr->steps_early, &ctr->status, steps, err);
 }
 
+// GetFTLEForPointEarly's reduction (ompVC/ftle.c:900-1047) for served point
+// s.  The eigenvalue comes from the closed form; where that is not accurate
+// enough (jacobi false) the point is left for the Jacobi pass and false
+// returned.
 template <int D>
-__device__ __forceinline__ void early_final_one(const FtleDev& f, long s) {
+__device__ __forceinline__ bool early_final_one(const FtleDev& f, long s, bool jacobi) {
   long q = f.served[s];
   double mt = f.emt[s];
   long nb[6];
@@ -459,22 +463,38 @@ __device__ __forceinline__ void early_final_one(const FtleDev& f, long s) {
     else if (k == f.zr - 1) { Bk = pos + 12; F = self; fz = 1.0; }
     else { Bk = pos + 12; F = pos + 15; fz = 2.0; }
   } else { Bk = F = self; fz = 1.0; }
-  double lam = stencil_lambda(D, L, R, B, T, Bk, F, fx, fy, fz, f.dx, f.dy, f.dz);
+  double C[3][3], lm1;  // C - I and lambda - 1
+  stencil_tensor(D, L, R, B, T, Bk, F, fx, fy, fz, f.dx, f.dy, f.dz, C);
+  if (jacobi) lm1 = max_eig(C);
+  else if (!max_eig_closed(C, lm1)) return false;
   double wT = 0.0, wN = 0.0;
-  if (lam > 1.0 - FVC_TINY && !(fabs(mt - f.start) < FVC_TINY)) {
-    wT = (0.5 * log(lam)) / fabs(mt - f.start);
-    wN = 0.5 * log(lam);
+  if (lm1 > -FVC_TINY && !(fabs(mt - f.start) < FVC_TINY)) {
+    wN = 0.5 * log1p(lm1);
+    wT = wN / fabs(mt - f.start);
   }
   f.ftT[q] = wT;
   f.ftN[q] = wN;
   f.have[q] = 1;
+  return true;
 }
 
+// The served points' FTLE by the closed-form eigenvalue; the few it leaves
+// are listed (in the task array, free once the task kernels are done) for
+// k_ftle_early_jacobi.
 template <int D>
 __global__ void k_ftle_early_final(FtleDev f, DevCounters* ctr) {
   const long nserved = *(volatile int*)&ctr->count;
+  int* fall = reinterpret_cast<int*>(f.tasks);
   for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < nserved; s += (long)gridDim.x * blockDim.x)
-    early_final_one<D>(f, s);
+    if (!early_final_one<D>(f, s, false)) fall[atomicAdd(&ctr->nfall, 1)] = (int)s;
+}
+
+template <int D>
+__global__ void k_ftle_early_jacobi(FtleDev f, DevCounters* ctr) {
+  const long nfall = *(volatile int*)&ctr->nfall;
+  const int* fall = reinterpret_cast<const int*>(f.tasks);
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nfall; i += (long)gridDim.x * blockDim.x)
+    early_final_one<D>(f, fall[i], true);
 }
 
 template <int D, int M>
@@ -549,6 +569,7 @@ struct Variant {
     static const unsigned res_self = resident_blocks(k_ftle_queue_self<D>, 256);
     static const unsigned res_tasks = resident_blocks(k_ftle_tasks<D, M>, 128);
     static const unsigned res_final = resident_blocks(k_ftle_early_final<D>, 128);
+    static const unsigned res_jacobi = resident_blocks(k_ftle_early_jacobi<D>, 64);
     static const unsigned res_sort = resident_blocks(k_task_sort<D>, 256);
     const double inv_h = 1.0 / fabs(in.h);
     cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
@@ -560,6 +581,7 @@ struct Variant {
     k_task_sort<D><<<capped(7L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
     k_ftle_tasks<D, M><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
+    k_ftle_early_jacobi<D><<<capped(f.n, 64, res_jacobi), 64, 0, s>>>(f, ctr);
   }
   static void tracer_launch(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq,
                             DevCounters* ctr, cudaStream_t s) {

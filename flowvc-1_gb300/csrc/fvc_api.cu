@@ -519,6 +519,7 @@ fvc_status quantised(fvc_ctx* c, int id, fvc_ctx::QFrame** out) {
       return fail(c, FVC_ERR_OOM, "quantisation scratch allocation failed");
     if (quantize_frame(c->frames[id], n, c->prec, q.q, c->d_qscratch, q.s, c->stream))
       return fail(c, FVC_ERR_CUDA, "frame quantisation failed");
+    c->aux_launches += 2;
     q.fmt = c->prec;
   }
   *out = &q;
@@ -533,6 +534,7 @@ static fvc_status quantised_window(fvc_ctx* c) {
   if (!c->d_qpair && cudaMalloc(&c->d_qpair, sizeof(uint4) * (size_t)c->frame_nodes) != cudaSuccess)
     return fail(c, FVC_ERR_OOM, "quantised window allocation failed");
   pair_frames(a->q, b->q, c->frame_nodes, c->d_qpair, c->stream);
+  c->aux_launches++;
   if ((st = check_launch(c, "pair frames"))) return st;
   w.qp = c->d_qpair;
   for (int k = 0; k < 3; k++) {
@@ -637,6 +639,7 @@ static fvc_status prepare_slots(fvc_ctx* c, double t1, double t2) {
   w.vt = c->d_vt;
   w.vt_stride = c->mesh.nnodes;
   time_fields(c->mesh, w, c->d_vt, c->stream);
+  c->aux_launches++;
   return check_launch(c, "time fields");
 }
 
@@ -1081,6 +1084,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   if (j->prec && !j->packed) {
     pack_pairs(j->f.X, 3L * j->f.n, s);
     j->packed = true;
+    j->stats.launches++;
   }
   if ((st = prepare_slots(c, t1, t2))) return st;
   // the main pass's per-step record, from which early-FTLE advections that
@@ -1136,7 +1140,11 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   ftle_update(c->mesh, c->integ, j->f, s);
   if ((st = check_launch(c, "ftle interval"))) return st;
   j->stats.intervals++;
-  j->stats.launches += (launch ? 1 : 0) + 4 + 1 + (c->integ.extrapolate ? 0 : 8) + 1 + (c->mesh.mesh_type == 1 && !c->prec ? 1 : 0);
+  // launch, compaction (count, three scan steps, scatter), the main pass,
+  // triggers and the early-FTLE kernels, the update
+  j->stats.launches += (launch ? 1 : 0) + 5 + 1 + (c->integ.extrapolate ? 0 : 1 + (j->prec ? 6 : 8)) + 1 +
+                       c->aux_launches;
+  c->aux_launches = 0;
   if (!steps) return FVC_OK;  // asynchronous: accounted by the next call that waits
   const long long before = j->stats.steps_main + j->stats.steps_early;
   st = job_sync(j, "ftle interval");
@@ -1154,6 +1162,7 @@ extern "C" fvc_status fvc_ftle_reduce(fvc_job* j, double int_t, double* wT, doub
   if (j->packed) {
     unpack_pairs(j->f.X, 3L * j->f.n, c->stream);
     j->packed = false;
+    j->stats.launches++;
   }
   cudaEventRecord(j->ev[0], c->stream);
   ftle_final(j->f, c->mesh.dims, int_t, c->stream);

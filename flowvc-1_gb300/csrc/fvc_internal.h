@@ -24,6 +24,9 @@ struct fvc_ctx {
   DevWindow window{};
   bool window_set = false;
   long frame_nodes = 0;  // nodes per frame
+  // window-level launches (stage-time fields, quantised frame pairs) not yet
+  // counted in a job's statistics; the next FTLE interval takes them over
+  long long aux_launches = 0;
   double node_lo[3] = {0, 0, 0}, node_hi[3] = {0, 0, 0};  // bounding box of the mesh nodes
   // device buffers
   int4* d_elem = nullptr;

@@ -828,10 +828,10 @@ __global__ void k_ftle_final(FtleDev f, int dims, double int_t) {
         else if (k == zr - 1) { Bk = X + 3 * (q - 1); F = X + 3 * q; fz = 1.0; }
         else { Bk = X + 3 * (q - 1); F = X + 3 * (q + 1); fz = 2.0; }
       } else { Bk = F = X + 3 * q; fz = 1.0; }
-      double lam = stencil_lambda(dims, L, R, B, T, Bk, F, fx, fy, fz, f.dx, f.dy, f.dz);
-      if (lam > 1.0 - FVC_TINY) {
-        wT = (0.5 * log(lam)) / int_t;
-        wN = 0.5 * log(lam);
+      const double lm1 = stencil_lambda_m1(dims, L, R, B, T, Bk, F, fx, fy, fz, f.dx, f.dy, f.dz);
+      if (lm1 > -FVC_TINY) {
+        wN = 0.5 * log1p(lm1);
+        wT = wN / int_t;
       } else {
         wT = 0.0;
         wN = 0.0;

@@ -20,12 +20,12 @@ struct DevCounters {
   int ntask;    // early-FTLE advections queued
   int hist[8];  // queued advections per length bucket (steps, capped at 7)
   int scat[8];  // fill cursors of the buckets in the sorted list
-  int pad;
+  int nfall;    // served points whose eigenvalue falls back to the Jacobi solver
   int cur[4];   // work cursors of the persistent launches: 0 live list, 1-2 task lists
   unsigned long long steps_rec;  // early-FTLE steps read from the main pass's record
 };
-// ntask, hist and scat are cleared together before each task list
-#define FVC_TASK_COUNTERS_BYTES (17 * sizeof(int))
+// ntask, hist, scat and nfall are cleared together before each task list
+#define FVC_TASK_COUNTERS_BYTES (18 * sizeof(int))
 
 // ---- mesh preprocessing
 void launch_geometry(const DevMesh& m, double* geom, float* geo32, cudaStream_t s);

@@ -217,6 +217,7 @@ struct VariantMx {
     static const unsigned res_self = resident_blocks(k_ftle_queue_self<D>, 256);
     static const unsigned res_tasks = resident_blocks(k_ftle_tasks_mx<D>, 128);
     static const unsigned res_final = resident_blocks(k_ftle_early_final<D>, 128);
+    static const unsigned res_jacobi = resident_blocks(k_ftle_early_jacobi<D>, 64);
     const double inv_h = 1.0 / fabs(in.h);
     FtleDev g = f;
     g.tsorted = g.tasks;
@@ -227,6 +228,7 @@ struct VariantMx {
     k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, w, 1, ctr, t1, inv_h);
     k_ftle_tasks_mx<D><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, g, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
+    k_ftle_early_jacobi<D><<<capped(f.n, 64, res_jacobi), 64, 0, s>>>(f, ctr);
   }
   static void tracer_launch(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq, DevCounters* ctr,
                             cudaStream_t s) {

@@ -71,9 +71,11 @@ def run_golden(exe, case, run, tmp_path, extra_args=()):
 
 
 # FTLE fields: the engine computes the Cauchy-Green eigenvalue with its own
-# Jacobi solver (the reference uses Householder + QL), so FTLE values agree to
-# a few ulps of lambda; log(lambda) amplifies that near lambda = 1.  Positions
-# and tracer outputs are compared bit for bit.
+# solvers (the trigonometric closed form on C - I, Jacobi where that is
+# ill-conditioned; the reference uses Householder + QL on C), so FTLE values
+# agree to a few ulps of lambda; log(lambda) amplifies the reference's
+# rounding near lambda = 1.  Positions and tracer outputs are compared bit
+# for bit.
 FTLE_RTOL = 1e-12
 FTLE_ATOL = 1e-13
 
