@@ -1030,6 +1030,7 @@ extern "C" fvc_status fvc_ftle_set_state(fvc_job* j, const double* X, const int*
   FtleDev& f = j->f;
   size_t n = (size_t)f.n;
   cudaStream_t s = c->stream;
+  j->live_ready = false;  // the next interval compacts the live points afresh
   if (X) {
     FVC_CUDA(c, cudaMemcpyAsync(f.X, X, 24 * n, cudaMemcpyHostToDevice, s));
     if (j->packed) pack_pairs(f.X, 3 * (long)n, s);
@@ -1128,7 +1129,11 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   // the persistent launches' work cursors start at 0 every interval
   FVC_CUDA(c, cudaMemsetAsync(ctr->cur, 0, sizeof(ctr->cur), s));
   if (launch) ftle_launch(c->mesh, c->window, j->f, j->f.start, ctr, s);
-  compact_live(j->f.n, j->f.ldt, j->f.left, c->integ.extrapolate, j->f.live, j->f.flag, j->f.block_cnt, ctr, s);
+  // the previous interval's update built the live list, unless the state
+  // was set from the host since
+  const bool compact = launch || !j->live_ready;
+  if (compact)
+    compact_live(j->f.n, j->f.ldt, j->f.left, c->integ.extrapolate, j->f.live, j->f.flag, j->f.block_cnt, ctr, s);
   cudaEventRecord(ev[0], s);
   ftle_pass1(c->mesh, c->window, c->integ, j->f, t1, t2, ctr, s);
   cudaEventRecord(ev[1], s);
@@ -1137,13 +1142,14 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
     ftle_early(c->mesh, c->window, c->integ, j->f, t1, ctr, s);
   }
   cudaEventRecord(ev[2], s);
-  ftle_update(c->mesh, c->integ, j->f, s);
+  ftle_update(c->mesh, c->integ, j->f, ctr, s);
+  j->live_ready = true;
   if ((st = check_launch(c, "ftle interval"))) return st;
   j->stats.intervals++;
   // launch, compaction (count, three scan steps, scatter), the main pass,
   // triggers and the early-FTLE kernels, the update
-  j->stats.launches += (launch ? 1 : 0) + 5 + 1 + (c->integ.extrapolate ? 0 : 1 + (j->prec ? 6 : 8)) + 1 +
-                       c->aux_launches;
+  j->stats.launches += (launch ? 1 : 0) + (compact ? 5 : 0) + 1 +
+                       (c->integ.extrapolate ? 0 : 1 + (j->prec ? 6 : 8)) + 1 + c->aux_launches;
   c->aux_launches = 0;
   if (!steps) return FVC_OK;  // asynchronous: accounted by the next call that waits
   const long long before = j->stats.steps_main + j->stats.steps_early;

@@ -846,8 +846,8 @@ static fvc_status enqueue_tick(fvc_batch* b, const TickPlan& P, const BJob* d_jo
     FVC_CUDA(c, cudaMemsetAsync(ctr->cur, 0, sizeof(ctr->cur), s));
     ftle_triggers(f, ctr, s);
     ftle_early(c->mesh, P.win[k], c->integ, f, P.iv[k].t1, ctr, s);
-    ftle_update(c->mesh, c->integ, f, s);
-    b->stats.launches += 10;
+    ftle_update(c->mesh, c->integ, f, nullptr, s);
+    b->stats.launches += 2 + (H.job->prec ? 6 : 8);
     if (P.iv[k].last) {
       if (H.job->packed) {
         unpack_pairs(H.job->f.X, 3L * f.n, s);

@@ -775,30 +775,61 @@ void ftle_triggers(const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
   k_ftle_triggers<<<nblk(f.n, 256), 256, 0, s>>>(f, ctr);
 }
 
-// UpdateFTLELocations and the per-point writes of ompVC/ftle.c:155-169, 175
-__global__ void k_ftle_update(FtleDev f, int extrapolate, int unstructured) {
-  long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= f.n) return;
-  unsigned char fl = f.flag[p];
-  if (!(fl & 1)) return;
-  if (fl & 2) {
-    f.left[p] = 1;
-    return;
+// UpdateFTLELocations and the per-point writes of ompVC/ftle.c:155-169, 175.
+// Every point's flag is cleared for the next interval, and with nlive the
+// next interval's live list is built here (the points compact_live would
+// select), appended a block at a time: a block's points keep their order,
+// and blocks, which start roughly in index order, mostly keep theirs.
+__global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, int extrapolate, int unstructured, int* nlive) {
+  __shared__ int warp_off[8];
+  __shared__ int block_base;
+  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool live = false;
+  if (p < f.n) {
+    const unsigned char fl = f.flag[p];
+    int left = f.left[p];
+    if (fl & 1) {
+      if (fl & 2) {
+        left = 1;
+        f.left[p] = 1;
+      } else {
+        f.X[3 * p] = f.Xn[3 * p];
+        f.X[3 * p + 1] = f.Xn[3 * p + 1];
+        f.X[3 * p + 2] = f.Xn[3 * p + 2];
+        if (extrapolate) {
+          f.V[3 * p] = f.Vn[3 * p];
+          f.V[3 * p + 1] = f.Vn[3 * p + 1];
+          f.V[3 * p + 2] = f.Vn[3 * p + 2];
+          left = (fl & 4) ? 1 : 0;
+          f.left[p] = left;
+        }
+        if (unstructured) f.eid[p] = f.en[p];
+      }
+    }
+    if (fl) f.flag[p] = 0;
+    live = nlive && f.ldt[p] > -FVC_TINY && (!left || extrapolate);
   }
-  f.X[3 * p] = f.Xn[3 * p];
-  f.X[3 * p + 1] = f.Xn[3 * p + 1];
-  f.X[3 * p + 2] = f.Xn[3 * p + 2];
-  if (extrapolate) {
-    f.V[3 * p] = f.Vn[3 * p];
-    f.V[3 * p + 1] = f.Vn[3 * p + 1];
-    f.V[3 * p + 2] = f.Vn[3 * p + 2];
-    f.left[p] = (fl & 4) ? 1 : 0;
+  if (!nlive) return;
+  const unsigned b = __ballot_sync(0xffffffffu, live);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_off[wid] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int c = 0;
+    for (int k = 0; k < 8; k++) {
+      const int v = warp_off[k];
+      warp_off[k] = c;
+      c += v;
+    }
+    block_base = c ? atomicAdd(nlive, c) : 0;
   }
-  if (unstructured) f.eid[p] = f.en[p];
+  __syncthreads();
+  if (live) f.live[block_base + warp_off[wid] + __popc(b & ((1u << lane) - 1u))] = (int)p;
 }
 
-void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, cudaStream_t s) {
-  k_ftle_update<<<nblk(f.n, 256), 256, 0, s>>>(f, in.extrapolate, m.mesh_type == 1);
+void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
+  if (ctr) cudaMemsetAsync(&ctr->nlive, 0, sizeof(int), s);
+  k_ftle_update<<<nblk(f.n, 256), 256, 0, s>>>(f, in.extrapolate, m.mesh_type == 1, ctr ? &ctr->nlive : nullptr);
 }
 
 // GetFTLEForPoint (ompVC/ftle.c:1050-1203) for points without a value, and

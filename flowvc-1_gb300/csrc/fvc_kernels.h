@@ -114,7 +114,8 @@ void ftle_triggers(const FtleDev& f, DevCounters* ctr, cudaStream_t s);
 // the number of served points is read on the device from ctr->count
 void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
                 double t1, DevCounters* ctr, cudaStream_t s);
-void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, cudaStream_t s);
+// ctr: also build the next interval's live list (f.live, ctr->nlive)
+void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s);
 void ftle_final(const FtleDev& f, int dims, double int_t, cudaStream_t s);
 
 // ---- tracers
