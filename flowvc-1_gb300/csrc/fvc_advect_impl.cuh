@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_pass1(DevMesh m, De
     Pt t;
     load_pt(t, p, f.X, in.extrapolate ? f.V : nullptr, f.eid, f.left, f.ldt);
     const unsigned before = steps;
-    const RecOut r{f.rec + 3 * p, 3L * f.n, f.rec_steps};
+    const RecOut r{f.rec + 3 * p, 3L * f.n, f.rec_steps, f.rec_e1 ? f.rec_e1 + p : nullptr, t.eid};
     err |= advect<D, M>(m, w, in, t, t1, t2, steps, nullptr, f.rec ? &r : nullptr);
     if (f.rec) f.kacc[p] = (unsigned char)(steps - before);
     f.flag[p] = 1 | ((t.left && !in.extrapolate) ? 2 : 0) | (t.left ? 4 : 0);
@@ -287,24 +287,14 @@ __device__ __forceinline__ int step_of(const DevWindow& w, int mixed, double T) 
   return -1;
 }
 
-// An early-FTLE advection of point p to the step-start time of step kend
-// repeats the main pass exactly when p was advected this interval, starts
-// from its frame-start element (the hint eid_at_trigger gives it: not a point
-// the serial loop has already moved, ompVC/ftle.c:167-168; the mixed form
-// does not require this) and the record reaches kend: then it stops where the main pass stood after
-// min(kend, its own accepted steps), and it exits on the way exactly when p
-// exited before kend.  Returns 1 and the result (position copied to pos, exit
-// or end time, accepted steps) or 0 when it must be recomputed.
-__device__ __forceinline__ int recorded(const FtleDev& f, long p, long trig, int kend, double tend, double* pos,
-                                        double* lt, unsigned* nsteps) {
-  if (!f.rec || kend < 0 || kend > f.rec_steps) return 0;
+// The record's answer for an advection of point p from the interval's start
+// to the step-start time of step kend (kend within the record; p advected
+// this interval and not left before it): the position after min(kend, p's
+// accepted steps), exiting on the way exactly when p exited before kend.
+// Copies the position to pos, the exit or end time to lt, counts the steps.
+__device__ __forceinline__ void from_record(const FtleDev& f, long p, int kend, double tend, double* pos,
+                                            double* lt, unsigned* nsteps) {
   const unsigned char fl = f.flag[p];
-  if (!(fl & 1) || f.left[p]) return 0;
-  // the hint would be the interval's end element: in the FP64 form the walk
-  // from there may settle a tie on a shared face differently, so recompute;
-  // the mixed form reads the record (on a shared face the P1 velocity is
-  // continuous, so the two differ by rounding only)
-  if (!f.mixed && p < trig && !(fl & 2)) return 0;
   const int kx = f.kacc[p];
   const bool exits = (fl & 2) && kx < kend;
   const int k = exits ? kx : kend;
@@ -314,7 +304,33 @@ __device__ __forceinline__ int recorded(const FtleDev& f, long p, long trig, int
   pos[2] = src[2];
   if (lt) *lt = exits ? f.te[p] : tend;
   *nsteps += (unsigned)k;
+}
+
+// Whether an early-FTLE advection of point p to the step-start time of step
+// kend can be read from the main pass's record.  It repeats the main pass
+// exactly when p was advected this interval, starts from its frame-start
+// element (the hint eid_at_trigger gives it: not a point the serial loop has
+// already moved, ompVC/ftle.c:167-168) and the record reaches kend.  Returns
+// 1 with the result (from_record), 0 when it must be computed, and 2 when it
+// starts from the interval's end element instead and everything else holds:
+// in the FP64 form the walks from there may settle a tie on a shared face
+// differently, so it is computed until its step-1 element state can be
+// compared with the main pass's (FP64 RK4 with rec_e1; else 0).  The mixed
+// form reads the record in that case too (on a shared face the P1 velocity is
+// continuous, so the two differ by rounding only).
+__device__ __forceinline__ int record_state(const FtleDev& f, long p, long trig, int kend) {
+  if (!f.rec || kend < 0 || kend > f.rec_steps) return 0;
+  const unsigned char fl = f.flag[p];
+  if (!(fl & 1) || f.left[p]) return 0;
+  if (!f.mixed && p < trig && !(fl & 2)) return (f.rec_e1 && kend >= 1) ? 2 : 0;
   return 1;
+}
+
+__device__ __forceinline__ int recorded(const FtleDev& f, long p, long trig, int kend, double tend, double* pos,
+                                        double* lt, unsigned* nsteps) {
+  const int r = record_state(f, p, trig, kend);
+  if (r == 1) from_record(f, p, kend, tend, pos, lt, nsteps);
+  return r;
 }
 
 // A: queue the neighbours that exist; boundary slots keep te as exit time.
@@ -338,11 +354,13 @@ __global__ void k_ftle_queue_nb(FtleDev f, DevWindow w, int mixed, DevCounters* 
       want = nb[c] >= 0;
       const long trig = f.trig[s];
       const double te = f.te[trig];
+      int r = 0;
       if (!want) f.elt[s * 6 + c] = te;
-      else if (f.rec &&
-               recorded(f, nb[c], trig, step_of(w, mixed, te), te, f.epos + (s * 7 + c) * 3, f.elt + s * 6 + c, &rsteps))
-        want = false;
-      b = length_bucket(t1, te, inv_h);
+      else if (f.rec)
+        r = recorded(f, nb[c], trig, step_of(w, mixed, te), te, f.epos + (s * 7 + c) * 3, f.elt + s * 6 + c, &rsteps);
+      if (r == 1) want = false;
+      // an advection checked after its first step mostly ends there
+      b = r == 2 ? 1 : length_bucket(t1, te, inv_h);
     }
     append_task(f, ctr, want, (int)s, c, b);
   }
@@ -378,9 +396,11 @@ __global__ void k_ftle_queue_self(FtleDev f, DevWindow w, int mixed, DevCounters
       want = nb[c] >= 0;
       p = nb[c];
     }
-    if (want && f.rec &&
-        recorded(f, p, f.trig[s], step_of(w, mixed, mt), mt, f.epos + (s * 7 + c) * 3, nullptr, &rsteps))
-      want = false;
+    if (want && f.rec) {
+      const int r = recorded(f, p, f.trig[s], step_of(w, mixed, mt), mt, f.epos + (s * 7 + c) * 3, nullptr, &rsteps);
+      if (r == 1) want = false;
+      if (r == 2) b = 1;
+    }
   }
   append_task(f, ctr, want, (int)s, c, b);
   }
@@ -394,7 +414,7 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_tasks(DevMesh m, De
                                                                    double t1, int phase, DevCounters* ctr) {
   const long ntask = *(volatile int*)&ctr->ntask;
   int* cursor = &ctr->cur[1 + phase];
-  unsigned steps = 0;
+  unsigned steps = 0, rsteps = 0;
   int err = 0;
   for (long base = warp_grab(cursor); base < ntask; base = warp_grab(cursor)) {
     const long idx = base + (threadIdx.x & 31);
@@ -416,14 +436,37 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_tasks(DevMesh m, De
     t.left = f.left[p];
     t.eid = eid_at_trigger(f, p, trig);
     t.ldt = 0.0;
-    err |= advect<D, M>(m, w, in, t, t1, tend, steps);
     double* pos = f.epos + (s * 7 + c) * 3;
+    // started from the interval's end element (recorded() == 2): checked
+    // against the main pass after step 1, and read from its record on a match
+    const int kend = f.rec_e1 ? step_of(w, 0, tend) : -1;
+    Chk1 chk;
+    chk.hit = 0;
+    const bool check = kend >= 1 && record_state(f, p, trig, kend) == 2;
+    if (check) {
+      chk.e0 = f.eid[p];
+      chk.e1 = f.rec_e1[p];
+    }
+    unsigned st = 0;
+    err |= advect<D, M>(m, w, in, t, t1, tend, st, nullptr, nullptr, check ? &chk : nullptr);
+    if (chk.hit) {
+      // step 1 was computed (st = 1); the record has the rest
+      double lt;
+      unsigned k = 0;
+      from_record(f, p, kend, tend, pos, &lt, &k);
+      steps += 1;
+      rsteps += k - 1;
+      if (phase == 0) f.elt[s * 6 + c] = lt;
+      continue;
+    }
+    steps += st;
     pos[0] = t.X[0];
     pos[1] = t.X[1];
     pos[2] = t.X[2];
     if (phase == 0) f.elt[s * 6 + c] = t.left ? t.ldt : tend;
   }
   flush_counters(&ctr->steps_early, &ctr->status, steps, err);
+  flush_rec(ctr, rsteps);
 }
 
 // GetFTLEForPointEarly's reduction (ompVC/ftle.c:900-1047) for served point

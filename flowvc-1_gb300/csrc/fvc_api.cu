@@ -1092,6 +1092,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   // repeat it are read (Euler and RK4 with a fixed step sequence)
   j->f.rec = nullptr;
   j->f.kacc = nullptr;
+  j->f.rec_e1 = nullptr;
   j->f.rec_steps = 0;
   if ((c->integ.type == 0 || c->integ.type == 1) && !c->integ.extrapolate) {
     const int ns = j->prec ? c->window.nsteps : (c->window.nslots > 0 ? (c->window.nslots - 1) / 2 : 0);
@@ -1101,13 +1102,16 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
       j->rec_mem = nullptr;
       j->rec_cap = 0;
       const size_t n = (size_t)j->f.n;
-      j->rec_bytes = al256(24 * n * (size_t)want) + n;
+      // positions, accepted steps, step-1 element states
+      j->rec_bytes = al256(24 * n * (size_t)want) + al256(n) + 16 * n;
       j->rec_mem = pool_get(c, j->rec_bytes);
       if (j->rec_mem) j->rec_cap = want;
     }
     if (want > 0 && j->rec_cap >= want) {
       j->f.rec = (double*)j->rec_mem;
-      j->f.kacc = (unsigned char*)j->rec_mem + al256(24 * (size_t)j->f.n * (size_t)j->rec_cap);
+      const size_t n = (size_t)j->f.n, pos_bytes = al256(24 * n * (size_t)j->rec_cap);
+      j->f.kacc = (unsigned char*)j->rec_mem + pos_bytes;
+      if (!j->prec && c->integ.type == 1) j->f.rec_e1 = (int4*)((char*)j->rec_mem + pos_bytes + al256(n));
       j->f.rec_steps = want;
     }
   }

@@ -682,7 +682,8 @@ __device__ __forceinline__ int rk4_stages(const DevMesh& m, const DevWindow& w, 
 template <int DIMS, int MESH, bool CET = false>
 __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, const DevInteg& in,
                                       Pt& p, double tstart, double tend, unsigned& steps, int& err,
-                                      const CetDev* cet = nullptr, const RecOut* rec = nullptr) {
+                                      const CetDev* cet = nullptr, const RecOut* rec = nullptr,
+                                      Chk1* chk = nullptr) {
   int e[4] = {p.eid, p.eid, p.eid, p.eid};
   int l[4] = {p.left, p.left, p.left, p.left};
   double kk[4][3];
@@ -714,6 +715,12 @@ __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, cons
       o[0] = p.X[0];
       o[1] = p.X[1];
       o[2] = p.X[2];
+      if (k == 1 && rec->e1) *rec->e1 = make_int4(e[0] == rec->eid0 ? e[1] : -3, e[2], e[3], p.eid);
+    }
+    if (chk && k == 1) {
+      chk->hit = e[0] == chk->e0 && e[1] == chk->e1.x && e[2] == chk->e1.y && e[3] == chk->e1.z &&
+                 p.eid == chk->e1.w;
+      if (chk->hit) return tend;
     }
     if (in.extrapolate && (err |= velocity_cold<DIMS, MESH>(m, w, tc, 2 * k, p.X, &p.eid, &p.left, p.V)))
       return tend;
@@ -906,7 +913,8 @@ __device__ __noinline__ double rkf(const DevMesh& m, const DevWindow& w, const D
 template <int DIMS, int MESH, bool CET = false>
 __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, const DevInteg& in,
                                       Pt& p, double tstart, double tend, unsigned& steps,
-                                      const CetDev* cet = nullptr, const RecOut* rec = nullptr) {
+                                      const CetDev* cet = nullptr, const RecOut* rec = nullptr,
+                                      Chk1* chk = nullptr) {
   int err = 0;
   if (p.left && in.extrapolate) {
 #pragma unroll
@@ -916,7 +924,7 @@ __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, cons
   if (p.left) return PT_ERR_STATE;  // "integrate point that already left domain"
   if (MESH == 1 && p.eid < 0) return PT_ERR_STATE;
   double stop;
-  if (in.type == 1) stop = rk4<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet, rec);
+  if (in.type == 1) stop = rk4<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet, rec, chk);
   else if (in.type == 2) stop = rkf<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet);
   else if (in.type == 3 && !CET) stop = ab2<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
   else stop = euler<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet, rec);

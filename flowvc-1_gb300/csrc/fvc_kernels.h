@@ -101,6 +101,10 @@ struct FtleDev {
   double* rec;
   unsigned char* kacc;
   int rec_steps;
+  // FP64 RK4: each point's element state after step 1 of the main pass
+  // (RecOut::e1), against which early-FTLE advections that start from
+  // another element hint are checked (null: not kept)
+  int4* rec_e1;
 };
 
 void ftle_seed_grid(const DevMesh& m, const FtleDev& f, double xmin, double ymin, double zmin,

@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(128, FVC_MX_MINBLOCKS) k_ftle_pass1_mx(DevMesh
     t.left = f.left[p];
     t.ldt = f.ldt[p];
     const unsigned before = steps;
-    const RecOut r{f.rec + 3 * p, 3L * f.n, f.rec_steps};
+    const RecOut r{f.rec + 3 * p, 3L * f.n, f.rec_steps, nullptr, 0};
     advect_mx<D>(m, w, type, t, w.nsteps, steps, err, f.rec ? &r : nullptr);
     if (f.rec) f.kacc[p] = (unsigned char)(steps - before);
     f.flag[p] = 1 | (t.left ? 6 : 0);

@@ -98,6 +98,20 @@ struct RecOut {
   double* base;
   long stride;
   int max;
+  // RK4: the element state after step 1 (stage hints 1-3 and the located
+  // element), when stage 1 stayed in the start element eid0 (else x = -3)
+  int4* e1;
+  int eid0;
+};
+
+// An early-FTLE advection that started from another element hint than the
+// main pass: after its step 1 it stops (hit = 1) if its element state is the
+// main pass's (stage hints e0 and e1.xyz, located element e1.w), from where
+// the rest of its steps are the main pass's record.
+struct Chk1 {
+  int e0;
+  int4 e1;
+  int hit;
 };
 
 struct DevInteg {
