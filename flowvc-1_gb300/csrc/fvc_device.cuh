@@ -517,7 +517,9 @@ __device__ __forceinline__ bool contains(const DevMesh& m, int e, const double X
 }
 
 // Get_Element_Global_Search (ompVC/mesh.c:304-398): lowest element id whose
-// containment test d > -TINY passes, from the point's bucket.
+// containment test d > -TINY passes, from the point's bucket.  Candidates the
+// walk's FP32 pre-check puts outside beyond its error bound are skipped
+// without the FP64 test (they would fail it).
 template <int DIMS>
 __device__ __forceinline__ int global_find(const DevMesh& m, const BucketGrid& g, const double X[3]) {
   int c[3];
@@ -529,8 +531,10 @@ __device__ __forceinline__ int global_find(const DevMesh& m, const BucketGrid& g
   }
   long cell = ((long)c[2] * g.n[1] + c[1]) * g.n[0] + c[0];
   int b = __ldg(g.start + cell), e = __ldg(g.start + cell + 1);
+  const PosF P = pos_f32(X);
   for (int i = b; i < e; i++) {
     int el = __ldg(g.ids + i);
+    if (quick_hop<DIMS>(m, el, P) >= 0) continue;
     if (contains<DIMS>(m, el, X)) return el;
   }
   return -1;
