@@ -778,14 +778,43 @@ void ftle_triggers(const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
 // UpdateFTLELocations and the per-point writes of ompVC/ftle.c:155-169, 175.
 // Every point's flag is cleared for the next interval, and with nlive the
 // next interval's live list is built here (the points compact_live would
-// select), appended a block at a time: a block's points keep their order,
-// and blocks, which start roughly in index order, mostly keep theirs.
-__global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, int extrapolate, int unstructured, int* nlive) {
+// select), appended a block at a time.  Its threads then take the points in
+// bricks of 32 (2 x 4 x 4 in i, j, k; 4 x 8 in 2D), so that a warp of the
+// main pass, which takes 32 entries of the list, advects a compact piece of
+// the grid whose walks share elements.
+struct Bricks {
+  int bi, bj, bk, nj, nk;
+  long count;  // threads: bricks x 32
+};
+
+static Bricks bricks_of(const FtleDev& f) {
+  Bricks b;
+  b.bk = f.zr > 1 ? 4 : 1;
+  b.bi = f.zr > 1 ? 2 : 4;
+  b.bj = 32 / (b.bi * b.bk);
+  b.nj = (f.yr + b.bj - 1) / b.bj;
+  b.nk = (f.zr + b.bk - 1) / b.bk;
+  b.count = 32L * ((f.xr + b.bi - 1) / b.bi) * b.nj * b.nk;
+  return b;
+}
+
+__device__ __forceinline__ long brick_point(const FtleDev& f, const Bricks& b, long t) {
+  const long T = t >> 5;
+  const int l = (int)(t & 31);
+  const long Tk = T % b.nk, Tj = (T / b.nk) % b.nj, Ti = T / ((long)b.nk * b.nj);
+  const long i = Ti * b.bi + l / (b.bj * b.bk), j = Tj * b.bj + (l / b.bk) % b.bj, k = Tk * b.bk + l % b.bk;
+  if (i >= f.xr || j >= f.yr || k >= f.zr) return -1;
+  return (i * f.yr + j) * f.zr + k;
+}
+
+__global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, Bricks br, int extrapolate, int unstructured,
+                                                     int* nlive) {
   __shared__ int warp_off[8];
   __shared__ int block_base;
-  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long p = nlive ? (t < br.count ? brick_point(f, br, t) : -1) : t;
   bool live = false;
-  if (p < f.n) {
+  if (p >= 0 && p < f.n) {
     const unsigned char fl = f.flag[p];
     int left = f.left[p];
     if (fl & 1) {
@@ -828,8 +857,10 @@ __global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, int extrapolate,
 }
 
 void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
+  const Bricks br = bricks_of(f);
   if (ctr) cudaMemsetAsync(&ctr->nlive, 0, sizeof(int), s);
-  k_ftle_update<<<nblk(f.n, 256), 256, 0, s>>>(f, in.extrapolate, m.mesh_type == 1, ctr ? &ctr->nlive : nullptr);
+  k_ftle_update<<<nblk(ctr ? br.count : f.n, 256), 256, 0, s>>>(f, br, in.extrapolate, m.mesh_type == 1,
+                                                                 ctr ? &ctr->nlive : nullptr);
 }
 
 // GetFTLEForPoint (ompVC/ftle.c:1050-1203) for points without a value, and
