@@ -1136,8 +1136,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   // the previous interval's update built the live list, unless the state
   // was set from the host since
   const bool compact = launch || !j->live_ready;
-  if (compact)
-    compact_live(j->f.n, j->f.ldt, j->f.left, c->integ.extrapolate, j->f.live, j->f.flag, j->f.block_cnt, ctr, s);
+  if (compact) ftle_live(c->integ, j->f, ctr, s);
   cudaEventRecord(ev[0], s);
   ftle_pass1(c->mesh, c->window, c->integ, j->f, t1, t2, ctr, s);
   cudaEventRecord(ev[1], s);
@@ -1150,9 +1149,9 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   j->live_ready = true;
   if ((st = check_launch(c, "ftle interval"))) return st;
   j->stats.intervals++;
-  // launch, compaction (count, three scan steps, scatter), the main pass,
+  // launch, the live list, the main pass,
   // triggers and the early-FTLE kernels, the update
-  j->stats.launches += (launch ? 1 : 0) + (compact ? 5 : 0) + 1 +
+  j->stats.launches += (launch ? 1 : 0) + (compact ? 1 : 0) + 1 +
                        (c->integ.extrapolate ? 0 : 1 + (j->prec ? 6 : 8)) + 1 + c->aux_launches;
   c->aux_launches = 0;
   if (!steps) return FVC_OK;  // asynchronous: accounted by the next call that waits

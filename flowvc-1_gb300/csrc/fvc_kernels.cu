@@ -807,17 +807,19 @@ __device__ __forceinline__ long brick_point(const FtleDev& f, const Bricks& b, l
   return (i * f.yr + j) * f.zr + k;
 }
 
-__global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, Bricks br, int extrapolate, int unstructured,
-                                                     int* nlive) {
+// update 0: only the live list (and the cleared flags) for the state as it
+// stands, the interval's first step after a launch or a host state change.
+__global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, Bricks br, int update, int extrapolate,
+                                                     int unstructured, int* nlive) {
   __shared__ int warp_off[8];
   __shared__ int block_base;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long p = nlive ? (t < br.count ? brick_point(f, br, t) : -1) : t;
   bool live = false;
   if (p >= 0 && p < f.n) {
-    const unsigned char fl = f.flag[p];
+    const unsigned char fl = update ? f.flag[p] : 1;
     int left = f.left[p];
-    if (fl & 1) {
+    if (update && (fl & 1)) {
       if (fl & 2) {
         left = 1;
         f.left[p] = 1;
@@ -859,8 +861,14 @@ __global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, Bricks br, int e
 void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
   const Bricks br = bricks_of(f);
   if (ctr) cudaMemsetAsync(&ctr->nlive, 0, sizeof(int), s);
-  k_ftle_update<<<nblk(ctr ? br.count : f.n, 256), 256, 0, s>>>(f, br, in.extrapolate, m.mesh_type == 1,
+  k_ftle_update<<<nblk(ctr ? br.count : f.n, 256), 256, 0, s>>>(f, br, 1, in.extrapolate, m.mesh_type == 1,
                                                                  ctr ? &ctr->nlive : nullptr);
+}
+
+void ftle_live(const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
+  const Bricks br = bricks_of(f);
+  cudaMemsetAsync(&ctr->nlive, 0, sizeof(int), s);
+  k_ftle_update<<<nblk(br.count, 256), 256, 0, s>>>(f, br, 0, in.extrapolate, 0, &ctr->nlive);
 }
 
 // GetFTLEForPoint (ompVC/ftle.c:1050-1203) for points without a value, and

@@ -120,6 +120,8 @@ void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const 
                 double t1, DevCounters* ctr, cudaStream_t s);
 // ctr: also build the next interval's live list (f.live, ctr->nlive)
 void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s);
+// the live list of the current state (and every flag cleared)
+void ftle_live(const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s);
 void ftle_final(const FtleDev& f, int dims, double int_t, cudaStream_t s);
 
 // ---- tracers
