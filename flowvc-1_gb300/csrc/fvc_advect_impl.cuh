@@ -216,32 +216,32 @@ __device__ __forceinline__ int length_bucket(double t1, double tend, double inv_
 
 // Appends (s, c) with its bucket to the task list (the lanes of a warp land
 // next to each other) and counts it in its bucket.
-__device__ __forceinline__ void append_task(const FtleDev& f, DevCounters* ctr, bool want, int s, int c, int b) {
+__device__ __forceinline__ void append_task(const FtleDev& f, TaskCounters* tc, bool want, int s, int c, int b) {
   const unsigned m = __ballot_sync(0xffffffffu, want);
   if (!m) return;
   const int lane = threadIdx.x & 31;
   int base = 0;
-  if (lane == 0) base = atomicAdd(&ctr->ntask, __popc(m));
+  if (lane == 0) base = atomicAdd(&tc->ntask, __popc(m));
   base = __shfl_sync(0xffffffffu, base, 0);
   if (want) f.tasks[base + __popc(m & ((1u << lane) - 1u))] = make_int2(s, c | (b << 3));
   const unsigned peers = __match_any_sync(0xffffffffu, want ? b : -1);
-  if (want && lane == __ffs(peers) - 1) atomicAdd(&ctr->hist[b], __popc(peers));
+  if (want && lane == __ffs(peers) - 1) atomicAdd(&tc->hist[b], __popc(peers));
 }
 
 // Groups the task list by bucket into f.tsorted (order within a bucket
 // follows the warps' arrival, roughly the served points' grid order).
 template <int D>
-__global__ void k_task_sort(FtleDev f, DevCounters* ctr) {
+__global__ void k_task_sort(FtleDev f, TaskCounters* tc) {
   __shared__ int off[8];
   if (threadIdx.x == 0) {
     int a = 0;
     for (int b = 0; b < 8; b++) {
       off[b] = a;
-      a += ((volatile int*)ctr->hist)[b];
+      a += ((volatile int*)tc->hist)[b];
     }
   }
   __syncthreads();
-  const long ntask = *(volatile int*)&ctr->ntask;
+  const long ntask = *(volatile int*)&tc->ntask;
   const int lane = threadIdx.x & 31;
   const long stride = (long)gridDim.x * blockDim.x;
   for (long base = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < ntask; base += stride) {
@@ -253,7 +253,7 @@ __global__ void k_task_sort(FtleDev f, DevCounters* ctr) {
     if (ok) {
       const int leader = __ffs(peers) - 1;
       int pos = 0;
-      if (lane == leader) pos = atomicAdd(&ctr->scat[b], __popc(peers));
+      if (lane == leader) pos = atomicAdd(&tc->scat[b], __popc(peers));
       pos = __shfl_sync(peers, pos, leader);
       f.tsorted[off[b] + pos + __popc(peers & ((1u << lane) - 1u))] = t;
     }
@@ -362,7 +362,7 @@ __global__ void k_ftle_queue_nb(FtleDev f, DevWindow w, int mixed, DevCounters* 
       // an advection checked after its first step mostly ends there
       b = r == 2 ? 1 : length_bucket(t1, te, inv_h);
     }
-    append_task(f, ctr, want, (int)s, c, b);
+    append_task(f, &ctr->tq[0], want, (int)s, c, b);
   }
   flush_rec(ctr, rsteps);
 }
@@ -402,7 +402,7 @@ __global__ void k_ftle_queue_self(FtleDev f, DevWindow w, int mixed, DevCounters
       if (r == 2) b = 1;
     }
   }
-  append_task(f, ctr, want, (int)s, c, b);
+  append_task(f, &ctr->tq[1], want, (int)s, c, b);
   }
   flush_rec(ctr, rsteps);
 }
@@ -412,7 +412,7 @@ __global__ void k_ftle_queue_self(FtleDev f, DevWindow w, int mixed, DevCounters
 template <int D, int M>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_tasks(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
                                                                    double t1, int phase, DevCounters* ctr) {
-  const long ntask = *(volatile int*)&ctr->ntask;
+  const long ntask = *(volatile int*)&ctr->tq[phase].ntask;
   int* cursor = &ctr->cur[1 + phase];
   unsigned steps = 0, rsteps = 0;
   int err = 0;
@@ -615,13 +615,12 @@ struct Variant {
     static const unsigned res_jacobi = resident_blocks(k_ftle_early_jacobi<D>, 64);
     static const unsigned res_sort = resident_blocks(k_task_sort<D>, 256);
     const double inv_h = 1.0 / fabs(in.h);
-    cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
+    // the task counters were cleared with the served count (ftle_triggers)
     k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, w, 0, ctr, t1, inv_h);
-    k_task_sort<D><<<capped(6L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
+    k_task_sort<D><<<capped(6L * f.n, 256, res_sort), 256, 0, s>>>(f, &ctr->tq[0]);
     k_ftle_tasks<D, M><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 0, ctr);
-    cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
     k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, w, 0, ctr, t1, inv_h);
-    k_task_sort<D><<<capped(7L * f.n, 256, res_sort), 256, 0, s>>>(f, ctr);
+    k_task_sort<D><<<capped(7L * f.n, 256, res_sort), 256, 0, s>>>(f, &ctr->tq[1]);
     k_ftle_tasks<D, M><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
     k_ftle_early_jacobi<D><<<capped(f.n, 64, res_jacobi), 64, 0, s>>>(f, ctr);

@@ -771,7 +771,7 @@ __global__ void k_ftle_triggers(FtleDev f, DevCounters* ctr) {
 }
 
 void ftle_triggers(const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
-  cudaMemsetAsync(&ctr->count, 0, sizeof(int), s);
+  cudaMemsetAsync(&ctr->count, 0, FVC_EARLY_COUNTERS_BYTES, s);
   k_ftle_triggers<<<nblk(f.n, 256), 256, 0, s>>>(f, ctr);
 }
 

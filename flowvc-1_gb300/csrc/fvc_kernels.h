@@ -3,11 +3,19 @@
 // pointers are device pointers.
 #pragma once
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "fvc_state.h"
 
 namespace fvc {
+
+// One early-FTLE task list's counters.
+struct TaskCounters {
+  int ntask;    // advections queued
+  int hist[8];  // queued advections per length bucket (steps, capped at 7)
+  int scat[8];  // fill cursors of the buckets in the sorted list
+};
 
 // Scratch counters shared by the launches of one call.
 struct DevCounters {
@@ -15,17 +23,15 @@ struct DevCounters {
   unsigned long long steps_early;  // accepted steps of the early-FTLE advections
   int status;
   int changed;
-  int count;   // points served an early FTLE this interval
   int nlive;   // live points of the current advection call
-  int ntask;    // early-FTLE advections queued
-  int hist[8];  // queued advections per length bucket (steps, capped at 7)
-  int scat[8];  // fill cursors of the buckets in the sorted list
-  int nfall;    // served points whose eigenvalue falls back to the Jacobi solver
-  int cur[4];   // work cursors of the persistent launches: 0 live list, 1-2 task lists
+  int cur[4];  // work cursors of the persistent launches: 0 live list, 1-2 task lists
+  // count .. nfall are cleared together before an interval's early-FTLE passes
+  int count;   // points served an early FTLE this interval
+  TaskCounters tq[2];  // the task lists: 0 neighbours to the exit time, 1 to MinExitTime
+  int nfall;   // served points whose eigenvalue falls back to the Jacobi solver
   unsigned long long steps_rec;  // early-FTLE steps read from the main pass's record
 };
-// ntask, hist, scat and nfall are cleared together before each task list
-#define FVC_TASK_COUNTERS_BYTES (18 * sizeof(int))
+#define FVC_EARLY_COUNTERS_BYTES (offsetof(DevCounters, nfall) + sizeof(int) - offsetof(DevCounters, count))
 
 // ---- mesh preprocessing
 void launch_geometry(const DevMesh& m, double* geom, float* geo32, cudaStream_t s);

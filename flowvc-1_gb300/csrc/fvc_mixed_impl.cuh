@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(128, FVC_MX_MINBLOCKS) k_ftle_pass1_mx(DevMesh
 template <int D>
 __global__ void __launch_bounds__(128, FVC_MX_MINBLOCKS) k_ftle_tasks_mx(DevMesh m, DevWindow w, int type, FtleDev f, int phase,
                                                        DevCounters* ctr) {
-  const long ntask = *(volatile int*)&ctr->ntask;
+  const long ntask = *(volatile int*)&ctr->tq[phase].ntask;
   int* cursor = &ctr->cur[1 + phase];
   unsigned steps = 0;
   int err = 0;
@@ -221,10 +221,9 @@ struct VariantMx {
     const double inv_h = 1.0 / fabs(in.h);
     FtleDev g = f;
     g.tsorted = g.tasks;
-    cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
+    // the task counters were cleared with the served count (ftle_triggers)
     k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, w, 1, ctr, t1, inv_h);
     k_ftle_tasks_mx<D><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, g, 0, ctr);
-    cudaMemsetAsync(&ctr->ntask, 0, FVC_TASK_COUNTERS_BYTES, s);
     k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, w, 1, ctr, t1, inv_h);
     k_ftle_tasks_mx<D><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, g, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
