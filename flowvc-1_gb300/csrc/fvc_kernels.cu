@@ -304,20 +304,22 @@ void outside_domain_flags(const DevMesh& m, int n, const double* X, int* left0, 
 
 // (1 - tloc) * U0 + tloc * U1 at every node for every stage time of the call
 // (the expression of ompVC/velocity.c:547-571), so stage evaluations read it.
+// One thread per node: both frames' values are read once and every slot's
+// field written from them.
 __global__ void k_time_fields(DevWindow w, long nnodes, double4_32a* vt) {
-  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  int sl = blockIdx.y;
-  if (i >= nnodes || sl >= w.nslots) return;
-  double tloc = w.tl[sl];
-  double4_32a a = w.f0[i], b = w.f1[i];
-  vt[(long)sl * nnodes + i] = make_double4_32a((1 - tloc) * a.x + tloc * b.x, (1 - tloc) * a.y + tloc * b.y,
-                                               (1 - tloc) * a.z + tloc * b.z, 0.0);
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnodes) return;
+  const double4_32a a = w.f0[i], b = w.f1[i];
+  for (int sl = 0; sl < w.nslots; sl++) {
+    const double tloc = w.tl[sl];
+    vt[(long)sl * nnodes + i] = make_double4_32a((1 - tloc) * a.x + tloc * b.x, (1 - tloc) * a.y + tloc * b.y,
+                                                 (1 - tloc) * a.z + tloc * b.z, 0.0);
+  }
 }
 
 void time_fields(const DevMesh& m, const DevWindow& w, double4_32a* vt, cudaStream_t s) {
   if (w.nslots <= 0 || m.nnodes <= 0) return;
-  dim3 grid(nblk(m.nnodes, 256), w.nslots);
-  k_time_fields<<<grid, 256, 0, s>>>(w, m.nnodes, vt);
+  k_time_fields<<<nblk(m.nnodes, 256), 256, 0, s>>>(w, m.nnodes, vt);
 }
 
 __global__ void k_pack_frame(const double* uvw, double4_32a* out, long n) {
