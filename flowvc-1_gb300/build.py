@@ -33,6 +33,7 @@ CU_SOURCES = ["fvc_kernels.cu", "fvc_api.cu", "fvc_variant_c2.cu", "fvc_variant_
 # (register budget 65536 / (128 * n)); FVC_MINBLOCKS overrides it for sweeps
 MINBLOCKS = os.environ.get("FVC_MINBLOCKS", "4")
 MX_MINBLOCKS = os.environ.get("FVC_MX_MINBLOCKS", "4")
+TASK_MINBLOCKS = os.environ.get("FVC_TASK_MINBLOCKS", "3")
 
 
 def _run(cmd):
@@ -67,7 +68,8 @@ def build_lib(force=False, verbose=False):
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(obj)
         if force or _newer(obj, deps):
-            jobs.append([NVCC, *ARCH, *NVFLAGS, "-DFVC_MINBLOCKS=" + MINBLOCKS, "-DFVC_MX_MINBLOCKS=" + MX_MINBLOCKS, "-c", os.path.join(CSRC, src),
+            jobs.append([NVCC, *ARCH, *NVFLAGS, "-DFVC_MINBLOCKS=" + MINBLOCKS, "-DFVC_MX_MINBLOCKS=" + MX_MINBLOCKS,
+                         "-DFVC_TASK_MINBLOCKS=" + TASK_MINBLOCKS, "-c", os.path.join(CSRC, src),
                          "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for r in ex.map(_run, jobs):

@@ -14,6 +14,11 @@ namespace fvc {
 #ifndef FVC_MINBLOCKS
 #define FVC_MINBLOCKS 4
 #endif
+// the early-FTLE task kernel: divergent short advections, which run better
+// with more registers a thread than the main pass (a sweep kept 3)
+#ifndef FVC_TASK_MINBLOCKS
+#define FVC_TASK_MINBLOCKS 3
+#endif
 
 static inline unsigned vblk(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
@@ -410,7 +415,7 @@ __global__ void k_ftle_queue_self(FtleDev f, DevWindow w, int mixed, DevCounters
 // The advections of A (phase 0: to te, recording exit times) and C (phase 1:
 // to MinExitTime).
 template <int D, int M>
-__global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_tasks(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
+__global__ void __launch_bounds__(128, FVC_TASK_MINBLOCKS) k_ftle_tasks(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
                                                                    double t1, int phase, DevCounters* ctr) {
   const long ntask = *(volatile int*)&ctr->tq[phase].ntask;
   int* cursor = &ctr->cur[1 + phase];
