@@ -256,7 +256,7 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
   const int gstride = c->mesh.dims == 3 ? 16 : 12;
   if (cudaMalloc(&c->d_elem, sizeof(int4) * he.size()) != cudaSuccess ||
       cudaMalloc(&c->d_geom, sizeof(double) * gstride * (size_t)nelem) != cudaSuccess ||
-      cudaMalloc(&c->d_geo32, sizeof(float) * 16 * (size_t)nelem) != cudaSuccess ||
+      cudaMalloc(&c->d_geo32, sizeof(float) * 20 * (size_t)nelem) != cudaSuccess ||
       cudaMalloc(&c->d_nodes, sizeof(double4_32a) * hn.size()) != cudaSuccess)
     return fail(c, FVC_ERR_OOM, "mesh allocation failed");
   FVC_CUDA(c, cudaMemcpyAsync(c->d_elem, he.data(), sizeof(int4) * he.size(), cudaMemcpyHostToDevice, c->stream));
@@ -265,6 +265,7 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
   m.elem = c->d_elem;
   m.geom = c->d_geom;
   m.geo32 = c->d_geo32;
+  m.geo32lo = reinterpret_cast<const float4*>(c->d_geo32 + 16L * nelem);
   m.nodes = c->d_nodes;
   m.nelem = nelem;
   m.nnodes = nnodes;

@@ -29,7 +29,7 @@ static inline unsigned nblk(long n, int bs) { return (unsigned)((n + bs - 1) / b
 // in the same record so one gather serves the containment test and the
 // interpolation (layout in fvc_device.cuh, struct Geo).
 template <int DIMS>
-__global__ void k_geometry(DevMesh m, double* geom, float* geo32) {
+__global__ void k_geometry(DevMesh m, double* geom, float* geo32, float4* geo32lo) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m.nelem) return;
   int4 nd = m.elem[2 * (long)e];
@@ -68,6 +68,7 @@ __global__ void k_geometry(DevMesh m, double* geom, float* geo32) {
     for (int c = 0; c < 9; c++) sa += fabs(g[c]);
     q[13] = (float)(sa / fabs(g[9]) * (1.0 + 1e-6));
     q[14] = q[15] = 0.f;
+    geo32lo[e] = make_float4((float)(x0 - (double)q[10]), (float)(y0 - (double)q[11]), (float)(z0 - (double)q[12]), 0.f);
   } else {
     double* g = geom + (long)e * 12;
     g[0] = y2 - y0;  // a11
@@ -88,12 +89,14 @@ __global__ void k_geometry(DevMesh m, double* geom, float* geo32) {
     double sa = fabs(g[0]) + fabs(g[1]) + fabs(g[2]) + fabs(g[3]);
     q[7] = (float)(sa / fabs(g[4]) * (1.0 + 1e-6));
     for (int c = 8; c < 16; c++) q[c] = 0.f;
+    geo32lo[e] = make_float4((float)(x0 - (double)q[5]), (float)(y0 - (double)q[6]), 0.f, 0.f);
   }
 }
 
 void launch_geometry(const DevMesh& m, double* geom, float* geo32, cudaStream_t s) {
-  if (m.dims == 3) k_geometry<3><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom, geo32);
-  else k_geometry<2><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom, geo32);
+  float4* lo = reinterpret_cast<float4*>(geo32 + 16L * m.nelem);
+  if (m.dims == 3) k_geometry<3><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom, geo32, lo);
+  else k_geometry<2><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom, geo32, lo);
 }
 
 // =============================================================== scans

@@ -34,6 +34,7 @@ struct DevCounters {
 #define FVC_EARLY_COUNTERS_BYTES (offsetof(DevCounters, nfall) + sizeof(int) - offsetof(DevCounters, count))
 
 // ---- mesh preprocessing
+// geo32 holds 16 floats per element followed by the float4 low parts (geo32lo)
 void launch_geometry(const DevMesh& m, double* geom, float* geo32, cudaStream_t s);
 
 // Builds the grid into caller-owned buffers; returns the number of entries

@@ -125,24 +125,34 @@ __device__ __forceinline__ float nat32(const DevMesh& m, int e, const float X[3]
   }
 }
 
-// The same coordinates with exact offsets: (X - C) - x0 formed in FP64 from
-// the element's FP64 node (6 FP64 adds, no FP64 solve) and rounded once to
-// FP32, then the FP32 map.  The offsets then err by 2^-24 |dx| instead of by
-// the FP32 positions' rounding, so tol shrinks to the map's own rounding,
+// (X - C) - x0 for a position X with compensation C (|C| within an ulp of X)
+// and a node x0 = xh + xl held as two floats: X - xh exactly by Knuth's
+// TwoSum, the small terms added to its error, one rounding at the end.  The
+// result errs by 2^-24 of itself plus about 2^-44 |X| (the small terms'
+// roundings), all in FP32.
+__device__ __forceinline__ float exact_offset(float X, float C, float xh, float xl) {
+  const float s = X - xh;
+  const float bb = s - X;
+  const float e = (X - (s - bb)) + (-xh - bb);
+  return s + ((e - C) - xl);
+}
+
+// The same coordinates with exact offsets: (X - C) - x0 formed from the
+// element's node in two floats (exact_offset) and rounded once, then the
+// FP32 map.  The offsets then err by 2^-24 |dx| instead of by the FP32
+// positions' rounding, so tol shrinks to the map's own rounding,
 // 1e-6 (1 + S) + 6e-8 A max |dx|, about 1e-5 for a well-shaped element.
 template <int D>
 __device__ __forceinline__ float nat32_fine(const DevMesh& m, int e, const float X[3], const float C[3], float& r,
                                             float& s, float& t, float& wv, float& tol) {
   const float* q = m.geo32 + (long)e * 16;
   if (D == 3) {
-    const double* g = m.geom + (long)e * 16;
-    const double2 gxy = __ldg(reinterpret_cast<const double2*>(g + 10));
-    const double gz = __ldg(g + 12);
-    const float dx = (float)(((double)X[0] - (double)C[0]) - gxy.x);
-    const float dy = (float)(((double)X[1] - (double)C[1]) - gxy.y);
-    const float dz = (float)(((double)X[2] - (double)C[2]) - gz);
     float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
     float4 q2 = __ldg(reinterpret_cast<const float4*>(q + 8));
+    const float4 lo = __ldg(m.geo32lo + e);
+    const float dx = exact_offset(X[0], C[0], q2.z, lo.x);
+    const float dy = exact_offset(X[1], C[1], q2.w, lo.y);
+    const float dz = exact_offset(X[2], C[2], __ldg(q + 12), lo.z);
     const float A = __ldg(q + 13);
     r = fmaf(q0.x, dx, fmaf(q0.y, dy, q0.z * dz)) * q2.y;
     s = fmaf(q0.w, dx, fmaf(q1.x, dy, q1.y * dz)) * q2.y;
@@ -152,11 +162,10 @@ __device__ __forceinline__ float nat32_fine(const DevMesh& m, int e, const float
     tol = fmaf(A, 1.06e-6f * dm, 1e-6f);
     return fminf(fminf(r, s), fminf(t, wv));
   } else {
-    const double* g = m.geom + (long)e * 12;
-    const double gx = __ldg(g + 5), gy = __ldg(g + 6);
-    const float dx = (float)(((double)X[0] - (double)C[0]) - gx);
-    const float dy = (float)(((double)X[1] - (double)C[1]) - gy);
     float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
+    const float4 lo = __ldg(m.geo32lo + e);
+    const float dx = exact_offset(X[0], C[0], q1.y, lo.x);
+    const float dy = exact_offset(X[1], C[1], q1.z, lo.y);
     r = fmaf(q0.x, dx, q0.y * dy) * q1.x;
     s = fmaf(q0.z, dx, q0.w * dy) * q1.x;
     t = 0.0f;

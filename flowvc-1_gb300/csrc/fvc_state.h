@@ -23,6 +23,7 @@ struct DevMesh {
   const int4* elem;     // 2 x nelem: {Nodes[4]}, {NeighborIndex[4]}
   const double* geom;   // natural-coordinate map + node ids, 16 (3D) or 12 (2D) doubles per element
   const float* geo32;   // FP32 copy of the map, node-0 coordinates and error scale, 64 B per element
+  const float4* geo32lo;  // node 0's coordinates minus their FP32 copies in geo32 (x, y, z, 0)
   const double4_32a* nodes; // x, y, z, 0 per node
   int nelem, nnodes;
   // Data_MeshBounds
