@@ -474,6 +474,20 @@ __global__ void __launch_bounds__(128, FVC_TASK_MINBLOCKS) k_ftle_tasks(DevMesh 
   flush_rec(ctr, rsteps);
 }
 
+// (u.x - u.y) - (v.x - v.y) for two (X, c) float pairs, as a double: the
+// difference of the X parts exactly by TwoSum, the compensations added to
+// its error, the float sum split exactly into two floats (TwoSum again).
+__device__ __forceinline__ double pair_diff(float2 u, float2 v) {
+  const float s = u.x - v.x;
+  const float b1 = s - u.x;
+  const float e = (u.x - (s - b1)) + (-v.x - b1);
+  const float t = (e - u.y) + v.y;
+  const float h = s + t;
+  const float b2 = h - s;
+  const float l = (s - (h - b2)) + (t - b2);
+  return (double)h + (double)l;
+}
+
 // GetFTLEForPointEarly's reduction (ompVC/ftle.c:900-1047) for served point
 // s.  The eigenvalue comes from the closed form; where that is not accurate
 // enough (jacobi false) the point is left for the Jacobi pass and false
@@ -485,34 +499,36 @@ __device__ __forceinline__ bool early_final_one(const FtleDev& f, long s, bool j
   long nb[6];
   int i, j, k;
   served_geometry(f, q, nb, i, j, k);
-  double P[21];
+  // the stencil's positions among the seven (neighbours -x +x -y +y -z +z,
+  // then q itself): lo / hi per direction, one-sided at the grid's faces
+  int lo[3], hi[3];
+  double fs[3];
+  const int ext[3] = {i == 0 ? 0 : i == f.xr - 1 ? 2 : 1, j == 0 ? 0 : j == f.yr - 1 ? 2 : 1,
+                      D != 3 ? 3 : k == 0 ? 0 : k == f.zr - 1 ? 2 : 1};
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    lo[a] = ext[a] == 0 || ext[a] == 3 ? 6 : 2 * a;
+    hi[a] = ext[a] == 2 || ext[a] == 3 ? 6 : 2 * a + 1;
+    fs[a] = ext[a] == 1 ? 2.0 : 1.0;
+  }
+  double d[3][3];  // d[component][direction] = hi - lo
   const double* E = f.epos + s * 21;
   if (f.mixed) {
-    // (X, c) float pairs: the position is X - c
+    // (X, c) float pairs, the position X - c: each difference formed in
+    // FP32 without error (TwoSum) and carried as two floats
     const float2* E2 = reinterpret_cast<const float2*>(E);
 #pragma unroll
-    for (int a = 0; a < 21; a++) P[a] = (double)E2[a].x - (double)E2[a].y;
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) d[c][a] = pair_diff(E2[3 * hi[a] + c], E2[3 * lo[a] + c]);
   } else {
 #pragma unroll
-    for (int a = 0; a < 21; a++) P[a] = E[a];
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) d[c][a] = E[3 * hi[a] + c] - E[3 * lo[a] + c];
   }
-  const double* pos = P;
-  const double* self = pos + 18;
-  const double *L, *R, *B, *T, *Bk, *F;
-  double fx, fy, fz;
-  if (i == 0) { L = self; R = pos + 3; fx = 1.0; }
-  else if (i == f.xr - 1) { L = pos; R = self; fx = 1.0; }
-  else { L = pos; R = pos + 3; fx = 2.0; }
-  if (j == 0) { B = self; T = pos + 9; fy = 1.0; }
-  else if (j == f.yr - 1) { B = pos + 6; T = self; fy = 1.0; }
-  else { B = pos + 6; T = pos + 9; fy = 2.0; }
-  if (D == 3) {
-    if (k == 0) { Bk = self; F = pos + 15; fz = 1.0; }
-    else if (k == f.zr - 1) { Bk = pos + 12; F = self; fz = 1.0; }
-    else { Bk = pos + 12; F = pos + 15; fz = 2.0; }
-  } else { Bk = F = self; fz = 1.0; }
   double C[3][3], lm1;  // C - I and lambda - 1
-  stencil_tensor(D, L, R, B, T, Bk, F, fx, fy, fz, f.dx, f.dy, f.dz, C);
+  tensor_from_diffs(D, d, fs[0], fs[1], fs[2], f.dx, f.dy, f.dz, C);
   if (jacobi) lm1 = max_eig(C);
   else if (!max_eig_closed(C, lm1)) return false;
   double wT = 0.0, wN = 0.0;

@@ -68,41 +68,43 @@ __device__ __forceinline__ bool max_eig_closed(const double a[3][3], double& lam
 }
 
 // Cauchy-Green tensor of the central / one-sided flow-map gradient
-// (ompVC/ftle.c:1000-1027, 1159-1187), returned minus the identity: its
-// largest eigenvalue is then lambda - 1 with an error relative to itself,
-// also where the flow map is close to a rigid motion.  The differences are
-// scaled by the reciprocal of each spacing (ompVC divides; the products
-// differ from the quotients by at most an ulp).
-__device__ __forceinline__ void stencil_tensor(int dims, const double* L, const double* R, const double* B,
-                                               const double* T, const double* Bk, const double* F, double fx,
-                                               double fy, double fz, double dx, double dy, double dz,
-                                               double C[3][3]) {
+// (ompVC/ftle.c:1000-1027, 1159-1187) from the stencil's differences
+// d[component][direction] (R - L, T - B, F - Bk), returned minus the
+// identity: its largest eigenvalue is then lambda - 1 with an error relative
+// to itself, also where the flow map is close to a rigid motion.  The
+// differences are scaled by the reciprocal of each spacing (ompVC divides;
+// the products differ from the quotients by at most an ulp).
+__device__ __forceinline__ void tensor_from_diffs(int dims, const double d[3][3], double fx, double fy, double fz,
+                                                  double dx, double dy, double dz, double C[3][3]) {
   double Dp[3][3];
-  const double ix = 1.0 / (fx * dx), iy = 1.0 / (fy * dy);
-  if (dims == 3) {
-    const double iz = 1.0 / (fz * dz);
-    Dp[0][2] = (F[0] - Bk[0]) * iz;
-    Dp[1][2] = (F[1] - Bk[1]) * iz;
-    Dp[2][0] = (R[2] - L[2]) * ix;
-    Dp[2][1] = (T[2] - B[2]) * iy;
-    Dp[2][2] = (F[2] - Bk[2]) * iz;
-  } else {
-    Dp[0][2] = 0;
-    Dp[1][2] = 0;
-    Dp[2][0] = 0;
-    Dp[2][1] = 0;
-    Dp[2][2] = 0;
+  const double ix = 1.0 / (fx * dx), iy = 1.0 / (fy * dy), iz = dims == 3 ? 1.0 / (fz * dz) : 0.0;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    Dp[q][0] = (dims == 3 || q < 2) ? d[q][0] * ix : 0.0;
+    Dp[q][1] = (dims == 3 || q < 2) ? d[q][1] * iy : 0.0;
+    Dp[q][2] = dims == 3 ? d[q][2] * iz : 0.0;
   }
-  Dp[0][0] = (R[0] - L[0]) * ix;
-  Dp[0][1] = (T[0] - B[0]) * iy;
-  Dp[1][0] = (R[1] - L[1]) * ix;
-  Dp[1][1] = (T[1] - B[1]) * iy;
   for (int a = 0; a < 3; a++)
     for (int b = 0; b < 3; b++) {
       double acc = 0;
       for (int q = 0; q < 3; q++) acc += Dp[q][a] * Dp[q][b];
       C[a][b] = a == b ? acc - 1.0 : acc;
     }
+}
+
+// The same from the six stencil positions.
+__device__ __forceinline__ void stencil_tensor(int dims, const double* L, const double* R, const double* B,
+                                               const double* T, const double* Bk, const double* F, double fx,
+                                               double fy, double fz, double dx, double dy, double dz,
+                                               double C[3][3]) {
+  double d[3][3];
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    d[q][0] = R[q] - L[q];
+    d[q][1] = T[q] - B[q];
+    d[q][2] = F[q] - Bk[q];
+  }
+  tensor_from_diffs(dims, d, fx, fy, fz, dx, dy, dz, C);
 }
 
 // lambda - 1 for the tensor's largest eigenvalue lambda (GetMaxEigenvalue,
