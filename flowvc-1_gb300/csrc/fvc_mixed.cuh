@@ -140,8 +140,15 @@ __device__ __forceinline__ float exact_offset(float X, float C, float xh, float 
 // The same coordinates with exact offsets: (X - C) - x0 formed from the
 // element's node in two floats (exact_offset) and rounded once, then the
 // FP32 map.  The offsets then err by 2^-24 |dx| instead of by the FP32
-// positions' rounding, so tol shrinks to the map's own rounding,
-// 1e-6 (1 + S) + 6e-8 A max |dx|, about 1e-5 for a well-shaped element.
+// positions' rounding, so tol shrinks to the map's own rounding.  Per
+// coordinate, r = fl(fl(fmaf(a11, dx, fmaf(a12, dy, a13 dz))) / V) carries
+// seven relative roundings of at most 2^-24 on sums bounded by
+// sum_j |a1j dxj| / |V| (the FP32 a1j and 1/V, the offsets, the product and
+// two partial sums, the scaling); w = ((1 - r) - s) - t adds three roundings
+// of at most 2^-24 (1 + |r| + |s| + |t|) <= 2^-23; exact_offset's absolute
+// error, 2^-44 max(|X|, |x0|), adds A times that.  The minimum coordinate
+// therefore errs by at most 4.2e-7 A max|dx| + 5.7e-14 A (|X| + max|dx|)
+// + 3.6e-7, and tol is set a little above that.
 template <int D>
 __device__ __forceinline__ float nat32_fine(const DevMesh& m, int e, const float X[3], const float C[3], float& r,
                                             float& s, float& t, float& wv, float& tol) {
@@ -159,7 +166,8 @@ __device__ __forceinline__ float nat32_fine(const DevMesh& m, int e, const float
     t = fmaf(q1.z, dx, fmaf(q1.w, dy, q2.x * dz)) * q2.y;
     wv = 1.0f - r - s - t;
     const float dm = fmaxf(fabsf(dx), fmaxf(fabsf(dy), fabsf(dz)));
-    tol = fmaf(A, 1.06e-6f * dm, 1e-6f);
+    const float xm = fmaxf(fabsf(X[0]), fmaxf(fabsf(X[1]), fabsf(X[2])));
+    tol = fmaf(A, fmaf(4.5e-7f, dm, 6e-14f * (xm + dm)), 4e-7f);
     return fminf(fminf(r, s), fminf(t, wv));
   } else {
     float4 q0 = __ldg(reinterpret_cast<const float4*>(q)), q1 = __ldg(reinterpret_cast<const float4*>(q + 4));
@@ -171,7 +179,8 @@ __device__ __forceinline__ float nat32_fine(const DevMesh& m, int e, const float
     t = 0.0f;
     wv = 1.0f - r - s;
     const float dm = fmaxf(fabsf(dx), fabsf(dy));
-    tol = fmaf(q1.w, 1.06e-6f * dm, 1e-6f);
+    const float xm = fmaxf(fabsf(X[0]), fabsf(X[1]));
+    tol = fmaf(q1.w, fmaf(4.5e-7f, dm, 6e-14f * (xm + dm)), 4e-7f);
     return fminf(fminf(r, s), wv);
   }
 }
