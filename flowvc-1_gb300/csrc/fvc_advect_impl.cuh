@@ -41,6 +41,14 @@ static inline unsigned capped(long n, int bs, unsigned resident) {
   return need < resident ? (need > 0 ? need : 1) : resident;
 }
 
+// count .. nfall of the counters (the triggers and early-FTLE passes that
+// follow the main pass), cleared by the main pass's first block.
+__device__ __forceinline__ void clear_early_counters(DevCounters* ctr) {
+  constexpr int n = (int)(FVC_EARLY_COUNTERS_BYTES / sizeof(int));
+  static_assert(n <= 128, "one store per thread of a 128-thread block");
+  if (blockIdx.x == 0 && threadIdx.x < n) (&ctr->count)[threadIdx.x] = 0;
+}
+
 // The first of the 32 items the calling warp takes next (all lanes call it).
 __device__ __forceinline__ long warp_grab(int* cursor) {
   int base = 0;
@@ -138,6 +146,7 @@ __global__ void k_ftle_launch(DevMesh m, DevWindow w, FtleDev f, double t, DevCo
 template <int D, int M>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_pass1(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
                                                     double t1, double t2, DevCounters* ctr) {
+  clear_early_counters(ctr);
   const long nlive = *(volatile int*)&ctr->nlive;
   const int lane = threadIdx.x & 31;
   unsigned steps = 0;

@@ -1131,8 +1131,9 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
     }
     j->pend.push_back(ev[k]);
   }
-  // the persistent launches' work cursors start at 0 every interval
-  FVC_CUDA(c, cudaMemsetAsync(ctr->cur, 0, sizeof(ctr->cur), s));
+  // the persistent launches' work cursors start at 0 every interval: the
+  // live-list kernels (ftle_live, or the previous interval's update) clear
+  // them, and the main pass clears the early-FTLE counters
   if (launch) ftle_launch(c->mesh, c->window, j->f, j->f.start, ctr, s);
   // the previous interval's update built the live list, unless the state
   // was set from the host since
@@ -1142,7 +1143,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   ftle_pass1(c->mesh, c->window, c->integ, j->f, t1, t2, ctr, s);
   cudaEventRecord(ev[1], s);
   if (!c->integ.extrapolate) {
-    ftle_triggers(j->f, ctr, s);
+    ftle_triggers(j->f, ctr, true, s);
     ftle_early(c->mesh, c->window, c->integ, j->f, t1, ctr, s);
   }
   cudaEventRecord(ev[2], s);

@@ -775,8 +775,8 @@ __global__ void k_ftle_triggers(FtleDev f, DevCounters* ctr) {
   f.trig[slot] = (int)trig;
 }
 
-void ftle_triggers(const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
-  cudaMemsetAsync(&ctr->count, 0, FVC_EARLY_COUNTERS_BYTES, s);
+void ftle_triggers(const FtleDev& f, DevCounters* ctr, bool cleared, cudaStream_t s) {
+  if (!cleared) cudaMemsetAsync(&ctr->count, 0, FVC_EARLY_COUNTERS_BYTES, s);
   k_ftle_triggers<<<nblk(f.n, 256), 256, 0, s>>>(f, ctr);
 }
 
@@ -865,14 +865,15 @@ __global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, Bricks br, int u
 
 void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
   const Bricks br = bricks_of(f);
-  if (ctr) cudaMemsetAsync(&ctr->nlive, 0, sizeof(int), s);
+  // the live count and the next interval's work cursors (adjacent)
+  if (ctr) cudaMemsetAsync(&ctr->nlive, 0, sizeof(int) + sizeof(ctr->cur), s);
   k_ftle_update<<<nblk(ctr ? br.count : f.n, 256), 256, 0, s>>>(f, br, 1, in.extrapolate, m.mesh_type == 1,
                                                                  ctr ? &ctr->nlive : nullptr);
 }
 
 void ftle_live(const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
   const Bricks br = bricks_of(f);
-  cudaMemsetAsync(&ctr->nlive, 0, sizeof(int), s);
+  cudaMemsetAsync(&ctr->nlive, 0, sizeof(int) + sizeof(ctr->cur), s);
   k_ftle_update<<<nblk(br.count, 256), 256, 0, s>>>(f, br, 0, in.extrapolate, 0, &ctr->nlive);
 }
 

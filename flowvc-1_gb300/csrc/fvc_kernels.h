@@ -24,7 +24,7 @@ struct DevCounters {
   int status;
   int changed;
   int nlive;   // live points of the current advection call
-  int cur[4];  // work cursors of the persistent launches: 0 live list, 1-2 task lists
+  int cur[4];  // work cursors of the persistent launches: 0 live list, 1-2 task lists (after nlive: cleared with it)
   // count .. nfall are cleared together before an interval's early-FTLE passes
   int count;   // points served an early FTLE this interval
   TaskCounters tq[2];  // the task lists: 0 neighbours to the exit time, 1 to MinExitTime
@@ -121,13 +121,17 @@ void ftle_launch(const DevMesh& m, const DevWindow& w, const FtleDev& f, double 
                  cudaStream_t s);
 void ftle_pass1(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
                 double t1, double t2, DevCounters* ctr, cudaStream_t s);
-void ftle_triggers(const FtleDev& f, DevCounters* ctr, cudaStream_t s);
+// cleared: the early-FTLE counters (count .. nfall) were cleared by the
+// interval's main pass; else they are cleared here
+void ftle_triggers(const FtleDev& f, DevCounters* ctr, bool cleared, cudaStream_t s);
 // the number of served points is read on the device from ctr->count
 void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
                 double t1, DevCounters* ctr, cudaStream_t s);
-// ctr: also build the next interval's live list (f.live, ctr->nlive)
+// ctr: also build the next interval's live list (f.live, ctr->nlive) and
+// clear the work cursors for it
 void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s);
-// the live list of the current state (and every flag cleared)
+// the live list of the current state (every flag and the work cursors
+// cleared)
 void ftle_live(const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s);
 void ftle_final(const FtleDev& f, int dims, double int_t, cudaStream_t s);
 

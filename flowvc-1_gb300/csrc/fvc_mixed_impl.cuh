@@ -81,6 +81,7 @@ __global__ void k_ftle_launch_mx(DevMesh m, DevWindow w, FtleDev f, float tl, De
 template <int D>
 __global__ void __launch_bounds__(128, FVC_MX_MINBLOCKS) k_ftle_pass1_mx(DevMesh m, DevWindow w, int type, FtleDev f,
                                                        DevCounters* ctr) {
+  clear_early_counters(ctr);
   const long nlive = *(volatile int*)&ctr->nlive;
   unsigned steps = 0;
   int err = 0;
