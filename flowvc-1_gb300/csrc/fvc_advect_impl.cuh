@@ -637,7 +637,7 @@ struct Variant {
     k_ftle_pass1<D, M><<<capped(f.n, 128, res), 128, 0, s>>>(m, w, in, f, t1, t2, ctr);
   }
   static void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
-                         double t1, DevCounters* ctr, cudaStream_t s) {
+                         double t1, DevCounters* ctr, bool jacobi, cudaStream_t s) {
     static const unsigned res_nb = resident_blocks(k_ftle_queue_nb<D>, 256);
     static const unsigned res_self = resident_blocks(k_ftle_queue_self<D>, 256);
     static const unsigned res_tasks = resident_blocks(k_ftle_tasks<D, M>, 128);
@@ -653,7 +653,7 @@ struct Variant {
     k_task_sort<D><<<capped(7L * f.n, 256, res_sort), 256, 0, s>>>(f, &ctr->tq[1]);
     k_ftle_tasks<D, M><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
-    k_ftle_early_jacobi<D><<<capped(f.n, 64, res_jacobi), 64, 0, s>>>(f, ctr);
+    if (jacobi) k_ftle_early_jacobi<D><<<capped(f.n, 64, res_jacobi), 64, 0, s>>>(f, ctr);
   }
   static void tracer_launch(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq,
                             DevCounters* ctr, cudaStream_t s) {

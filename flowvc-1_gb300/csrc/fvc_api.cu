@@ -1144,7 +1144,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   cudaEventRecord(ev[1], s);
   if (!c->integ.extrapolate) {
     ftle_triggers(j->f, ctr, true, s);
-    ftle_early(c->mesh, c->window, c->integ, j->f, t1, ctr, s);
+    ftle_early(c->mesh, c->window, c->integ, j->f, t1, ctr, false, s);
   }
   cudaEventRecord(ev[2], s);
   ftle_update(c->mesh, c->integ, j->f, ctr, s);
@@ -1154,7 +1154,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
   // launch, the live list, the main pass,
   // triggers and the early-FTLE kernels, the update
   j->stats.launches += (launch ? 1 : 0) + (compact ? 1 : 0) + 1 +
-                       (c->integ.extrapolate ? 0 : 1 + (j->prec ? 6 : 8)) + 1 + c->aux_launches;
+                       (c->integ.extrapolate ? 0 : 1 + (j->prec ? 5 : 7)) + 1 + c->aux_launches;
   c->aux_launches = 0;
   if (!steps) return FVC_OK;  // asynchronous: accounted by the next call that waits
   const long long before = j->stats.steps_main + j->stats.steps_early;

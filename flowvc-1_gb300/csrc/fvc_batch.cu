@@ -845,7 +845,7 @@ static fvc_status enqueue_tick(fvc_batch* b, const TickPlan& P, const BJob* d_jo
     // the task lists' work cursors start at 0 every interval
     FVC_CUDA(c, cudaMemsetAsync(ctr->cur, 0, sizeof(ctr->cur), s));
     ftle_triggers(f, ctr, false, s);
-    ftle_early(c->mesh, P.win[k], c->integ, f, P.iv[k].t1, ctr, s);
+    ftle_early(c->mesh, P.win[k], c->integ, f, P.iv[k].t1, ctr, true, s);
     ftle_update(c->mesh, c->integ, f, nullptr, s);
     b->stats.launches += 2 + (H.job->prec ? 6 : 8);
     if (P.iv[k].last) {

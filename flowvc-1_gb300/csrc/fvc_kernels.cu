@@ -814,11 +814,22 @@ __device__ __forceinline__ long brick_point(const FtleDev& f, const Bricks& b, l
 
 // update 0: only the live list (and the cleared flags) for the state as it
 // stands, the interval's first step after a launch or a host state change.
+// With nfall, the first threads first solve the early-FTLE points the
+// closed-form eigenvalue left (k_ftle_early_jacobi's work, a few hundred
+// points; the other blocks' updates run meanwhile).
 __global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, Bricks br, int update, int extrapolate,
-                                                     int unstructured, int* nlive) {
+                                                     int unstructured, int* nlive, const int* nfall, int dims) {
   __shared__ int warp_off[8];
   __shared__ int block_base;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (nfall) {
+    const long nf = *(volatile const int*)nfall;
+    const int* fall = reinterpret_cast<const int*>(f.tasks);
+    for (long i = t; i < nf; i += (long)gridDim.x * blockDim.x) {
+      if (dims == 3) early_final_one<3>(f, fall[i], true);
+      else early_final_one<2>(f, fall[i], true);
+    }
+  }
   const long p = nlive ? (t < br.count ? brick_point(f, br, t) : -1) : t;
   bool live = false;
   if (p >= 0 && p < f.n) {
@@ -868,13 +879,14 @@ void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCoun
   // the live count and the next interval's work cursors (adjacent)
   if (ctr) cudaMemsetAsync(&ctr->nlive, 0, sizeof(int) + sizeof(ctr->cur), s);
   k_ftle_update<<<nblk(ctr ? br.count : f.n, 256), 256, 0, s>>>(f, br, 1, in.extrapolate, m.mesh_type == 1,
-                                                                 ctr ? &ctr->nlive : nullptr);
+                                                                 ctr ? &ctr->nlive : nullptr,
+                                                                 ctr ? &ctr->nfall : nullptr, m.dims);
 }
 
 void ftle_live(const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
   const Bricks br = bricks_of(f);
   cudaMemsetAsync(&ctr->nlive, 0, sizeof(int) + sizeof(ctr->cur), s);
-  k_ftle_update<<<nblk(br.count, 256), 256, 0, s>>>(f, br, 0, in.extrapolate, 0, &ctr->nlive);
+  k_ftle_update<<<nblk(br.count, 256), 256, 0, s>>>(f, br, 0, in.extrapolate, 0, &ctr->nlive, nullptr, 0);
 }
 
 // GetFTLEForPoint (ompVC/ftle.c:1050-1203) for points without a value, and
@@ -1110,8 +1122,8 @@ void ftle_pass1(const DevMesh& m, const DevWindow& w, const DevInteg& in, const 
   FVC_VARIANT(m, ftle_pass1(m, w, in, f, t1, t2, ctr, s));
 }
 void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
-                double t1, DevCounters* ctr, cudaStream_t s) {
-  FVC_VARIANT(m, ftle_early(m, w, in, f, t1, ctr, s));
+                double t1, DevCounters* ctr, bool jacobi, cudaStream_t s) {
+  FVC_VARIANT(m, ftle_early(m, w, in, f, t1, ctr, jacobi, s));
 }
 void tracer_launch_vel(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq,
                        DevCounters* ctr, cudaStream_t s) {

@@ -125,10 +125,13 @@ void ftle_pass1(const DevMesh& m, const DevWindow& w, const DevInteg& in, const 
 // interval's main pass; else they are cleared here
 void ftle_triggers(const FtleDev& f, DevCounters* ctr, bool cleared, cudaStream_t s);
 // the number of served points is read on the device from ctr->count
+// jacobi false: the points the closed-form eigenvalue leaves are solved by
+// the update kernel that follows (ftle_update with ctr)
 void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
-                double t1, DevCounters* ctr, cudaStream_t s);
-// ctr: also build the next interval's live list (f.live, ctr->nlive) and
-// clear the work cursors for it
+                double t1, DevCounters* ctr, bool jacobi, cudaStream_t s);
+// ctr: also build the next interval's live list (f.live, ctr->nlive), clear
+// the work cursors for it and solve the early-FTLE points the closed-form
+// eigenvalue left (ctr->nfall; the list is in f.tasks)
 void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s);
 // the live list of the current state (every flag and the work cursors
 // cleared)

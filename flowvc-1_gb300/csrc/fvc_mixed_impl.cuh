@@ -213,7 +213,7 @@ struct VariantMx {
   // bound by gather latency, and grid order keeps a warp's points close
   // together, which pays more here than grouping them by length.
   static void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f, double t1,
-                         DevCounters* ctr, cudaStream_t s) {
+                         DevCounters* ctr, bool jacobi, cudaStream_t s) {
     static const unsigned res_nb = resident_blocks(k_ftle_queue_nb<D>, 256);
     static const unsigned res_self = resident_blocks(k_ftle_queue_self<D>, 256);
     static const unsigned res_tasks = resident_blocks(k_ftle_tasks_mx<D>, 128);
@@ -228,7 +228,7 @@ struct VariantMx {
     k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, w, 1, ctr, t1, inv_h);
     k_ftle_tasks_mx<D><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in.type, g, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
-    k_ftle_early_jacobi<D><<<capped(f.n, 64, res_jacobi), 64, 0, s>>>(f, ctr);
+    if (jacobi) k_ftle_early_jacobi<D><<<capped(f.n, 64, res_jacobi), 64, 0, s>>>(f, ctr);
   }
   static void tracer_launch(const DevMesh& m, const DevWindow& w, const TracerDev& t, double tq, DevCounters* ctr,
                             cudaStream_t s) {
