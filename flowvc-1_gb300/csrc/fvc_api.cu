@@ -213,31 +213,6 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
   if ((st = use_device(c))) return st;
   if (c->cet_sub) fvc_cet_enable(c, 0);  // the accumulators belong to the old mesh
   const int nv = c->mesh.dims == 3 ? 4 : 3;
-  // host-side validation keeps every device gather in bounds
-  for (long e = 0; e < nelem; e++) {
-    for (int k = 0; k < nv; k++) {
-      int nd = conn[4 * e + k], nb = adj[4 * e + k];
-      if (nd < 0 || nd >= nnodes) return fail(c, FVC_ERR_ARG, "element %ld: node %d out of range", e, nd);
-      if (nb < -1 || nb >= nelem) return fail(c, FVC_ERR_ARG, "element %ld: neighbour %d out of range", e, nb);
-    }
-  }
-  for (int a = 0; a < 3; a++) {
-    c->node_lo[a] = 1e300;
-    c->node_hi[a] = -1e300;
-  }
-  for (long k = 0; k < nnodes; k++)
-    for (int a = 0; a < 3; a++) {
-      const double v = xyz[3 * k + a];
-      c->node_lo[a] = v < c->node_lo[a] ? v : c->node_lo[a];
-      c->node_hi[a] = v > c->node_hi[a] ? v : c->node_hi[a];
-    }
-  std::vector<int4> he(2 * (size_t)nelem);
-  for (long e = 0; e < nelem; e++) {
-    const int* n = conn + 4 * e;
-    const int* a = adj + 4 * e;
-    he[2 * e] = make_int4(n[0], n[1], n[2], nv == 4 ? n[3] : n[2]);
-    he[2 * e + 1] = make_int4(a[0], a[1], a[2], nv == 4 ? a[3] : -1);
-  }
   std::vector<double4_32a> hn((size_t)nnodes);
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
   for (long i = 0; i < nnodes; i++) {
@@ -247,19 +222,63 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
       hi[a] = fmax(hi[a], xyz[3 * i + a]);
     }
   }
-  cudaFree(c->d_elem); c->d_elem = nullptr;
-  cudaFree(c->d_geom); c->d_geom = nullptr;
-  cudaFree(c->d_geo32); c->d_geo32 = nullptr;
-  cudaFree(c->d_nodes); c->d_nodes = nullptr;
+  // the new mesh's buffers; the old ones stay until the new mesh is valid
+  const int gstride = c->mesh.dims == 3 ? 16 : 12;
+  int4* n_elem = nullptr;
+  double* n_geom = nullptr;
+  float* n_geo32 = nullptr;
+  double4_32a* n_nodes = nullptr;
+  auto drop_new = [&]() {
+    cudaFree(n_elem);
+    cudaFree(n_geom);
+    cudaFree(n_geo32);
+    cudaFree(n_nodes);
+  };
+  if (cudaMalloc(&n_elem, sizeof(int4) * 2 * (size_t)nelem) != cudaSuccess ||
+      cudaMalloc(&n_geom, sizeof(double) * gstride * (size_t)nelem) != cudaSuccess ||
+      cudaMalloc(&n_geo32, sizeof(float) * 20 * (size_t)nelem) != cudaSuccess ||
+      cudaMalloc(&n_nodes, sizeof(double4_32a) * hn.size()) != cudaSuccess) {
+    drop_new();
+    return fail(c, FVC_ERR_OOM, "mesh allocation failed");
+  }
+  // node ids and neighbours go up as given (into the geometry buffer, free
+  // until the geometry kernel fills it) and are interleaved and range-checked
+  // on the device, which keeps every later gather in bounds
+  int4* raw = reinterpret_cast<int4*>(n_geom);
+  int* d_bad = reinterpret_cast<int*>(n_geo32);
+  int bad = -1;
+  if (cudaMemcpyAsync(raw, conn, sizeof(int4) * (size_t)nelem, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+      cudaMemcpyAsync(raw + nelem, adj, sizeof(int4) * (size_t)nelem, cudaMemcpyHostToDevice, c->stream) !=
+          cudaSuccess ||
+      cudaMemsetAsync(d_bad, 0x7f, sizeof(int), c->stream) != cudaSuccess) {
+    drop_new();
+    return fail(c, FVC_ERR_CUDA, "mesh upload failed");
+  }
+  pack_elements(raw, raw + nelem, nelem, nnodes, nv, n_elem, d_bad, c->stream);
+  if (cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    drop_new();
+    return fail(c, FVC_ERR_CUDA, "mesh check failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  if (bad < nelem) {
+    drop_new();
+    for (int k = 0; k < nv; k++) {
+      const int nd = conn[4L * bad + k], nb = adj[4L * bad + k];
+      if (nd < 0 || nd >= nnodes) return fail(c, FVC_ERR_ARG, "element %d: node %d out of range", bad, nd);
+      if (nb < -1 || nb >= nelem) return fail(c, FVC_ERR_ARG, "element %d: neighbour %d out of range", bad, nb);
+    }
+    return fail(c, FVC_ERR_ARG, "element %d out of range", bad);
+  }
+  for (int a = 0; a < 3; a++) {
+    c->node_lo[a] = lo[a];
+    c->node_hi[a] = hi[a];
+  }
+  cudaFree(c->d_elem); c->d_elem = n_elem;
+  cudaFree(c->d_geom); c->d_geom = n_geom;
+  cudaFree(c->d_geo32); c->d_geo32 = n_geo32;
+  cudaFree(c->d_nodes); c->d_nodes = n_nodes;
   cudaFree(c->d_cell_start); c->d_cell_start = nullptr;
   cudaFree(c->d_cell_ids); c->d_cell_ids = nullptr;
-  const int gstride = c->mesh.dims == 3 ? 16 : 12;
-  if (cudaMalloc(&c->d_elem, sizeof(int4) * he.size()) != cudaSuccess ||
-      cudaMalloc(&c->d_geom, sizeof(double) * gstride * (size_t)nelem) != cudaSuccess ||
-      cudaMalloc(&c->d_geo32, sizeof(float) * 20 * (size_t)nelem) != cudaSuccess ||
-      cudaMalloc(&c->d_nodes, sizeof(double4_32a) * hn.size()) != cudaSuccess)
-    return fail(c, FVC_ERR_OOM, "mesh allocation failed");
-  FVC_CUDA(c, cudaMemcpyAsync(c->d_elem, he.data(), sizeof(int4) * he.size(), cudaMemcpyHostToDevice, c->stream));
   FVC_CUDA(c, cudaMemcpyAsync(c->d_nodes, hn.data(), sizeof(double4_32a) * hn.size(), cudaMemcpyHostToDevice, c->stream));
   DevMesh& m = c->mesh;
   m.elem = c->d_elem;

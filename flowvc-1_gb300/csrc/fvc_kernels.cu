@@ -93,6 +93,28 @@ __global__ void k_geometry(DevMesh m, double* geom, float* geo32, float4* geo32l
   }
 }
 
+// Element e's node ids and neighbours as given (4 + 4 ints) interleaved into
+// the walk's layout (elem[2e] nodes, elem[2e + 1] neighbours; triangles
+// repeat their third node and have no fourth neighbour), with the ranges
+// checked: the lowest element with an id out of range goes to *bad.
+__global__ void k_pack_elements(const int4* conn, const int4* adj, int nelem, int nnodes, int nv, int4* elem,
+                                int* bad) {
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nelem) return;
+  const int4 n = conn[e], a = adj[e];
+  const bool ok = n.x >= 0 && n.x < nnodes && n.y >= 0 && n.y < nnodes && n.z >= 0 && n.z < nnodes &&
+                  (nv < 4 || (n.w >= 0 && n.w < nnodes)) && a.x >= -1 && a.x < nelem && a.y >= -1 &&
+                  a.y < nelem && a.z >= -1 && a.z < nelem && (nv < 4 || (a.w >= -1 && a.w < nelem));
+  if (!ok) atomicMin(bad, (int)e);
+  elem[2 * e] = make_int4(n.x, n.y, n.z, nv == 4 ? n.w : n.z);
+  elem[2 * e + 1] = make_int4(a.x, a.y, a.z, nv == 4 ? a.w : -1);
+}
+
+void pack_elements(const int4* conn, const int4* adj, int nelem, int nnodes, int nv, int4* elem, int* bad,
+                   cudaStream_t s) {
+  k_pack_elements<<<nblk(nelem, 256), 256, 0, s>>>(conn, adj, nelem, nnodes, nv, elem, bad);
+}
+
 void launch_geometry(const DevMesh& m, double* geom, float* geo32, cudaStream_t s) {
   float4* lo = reinterpret_cast<float4*>(geo32 + 16L * m.nelem);
   if (m.dims == 3) k_geometry<3><<<nblk(m.nelem, 256), 256, 0, s>>>(m, geom, geo32, lo);

@@ -34,6 +34,11 @@ struct DevCounters {
 #define FVC_EARLY_COUNTERS_BYTES (offsetof(DevCounters, nfall) + sizeof(int) - offsetof(DevCounters, count))
 
 // ---- mesh preprocessing
+// the mesh's element records from the caller's connectivity and adjacency
+// (4 ints each per element) with the ids range-checked (*bad: the lowest
+// element out of range, untouched if none)
+void pack_elements(const int4* conn, const int4* adj, int nelem, int nnodes, int nv, int4* elem, int* bad,
+                   cudaStream_t s);
 // geo32 holds 16 floats per element followed by the float4 low parts (geo32lo)
 void launch_geometry(const DevMesh& m, double* geom, float* geo32, cudaStream_t s);
 
