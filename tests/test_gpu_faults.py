@@ -91,3 +91,28 @@ def test_batch_reports_failed_jobs_and_keeps_the_rest():
     assert (r["left"] == 1).all()
     b.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("which", ["node", "neighbour"])
+def test_bad_mesh_is_refused_and_the_old_mesh_stays(which):
+    """An id out of range in the connectivity or adjacency is found on the
+    device before the old mesh is released: FVC_ERR_ARG naming the lowest
+    bad element, and the context keeps working on its old mesh."""
+    ctx, ax = cube_ctx()
+    xyz, conn, adj = synth.kuhn_cube_mesh(4, jitter=0.2, seed=1)
+    conn, adj = conn.copy(), adj.copy()
+    if which == "node":
+        conn[9, 2] = len(xyz) + 7
+        conn[30, 0] = -3
+    else:
+        adj[9, 1] = len(conn) + 1
+    with pytest.raises(fvc.FvcError) as e:
+        ctx.set_unstruct_mesh(xyz, conn, adj)
+    assert e.value.status == fvc.FVC_ERR_ARG
+    assert "element 9" in str(e.value)
+    ctx.set_window(0, 1, 0.0, 0.02)
+    P = synth.uniform_seeds(64, 3, seed=1)
+    eid = ctx.global_search(P)
+    assert (eid >= 0).all()
+    assert ctx.advect(*advect_args(P, eid), 0.0, 0.02) > 0
+    ctx.close()
