@@ -71,7 +71,10 @@ fvc_status fvc_set_cart_mesh(fvc_ctx *ctx, double xmin, double xmax, int xres, d
 
 /* Unstructured mesh; replaces LoadUnstructMeshData (ompVC/mesh.c:124-213).
  * xyz: nnodes x 3; conn, adj: nelem x 4 in ompVC's layout (triangles: 4th
- * connectivity slot -1).  Also builds the bucket grid used by global search. */
+ * connectivity slot -1).  Also builds the bucket grid used by global search.
+ * Every node id must lie in [0, nnodes) and every neighbour id in
+ * [-1, nelem): otherwise FVC_ERR_ARG names the lowest bad element and the
+ * context keeps its previous mesh. */
 fvc_status fvc_set_unstruct_mesh(fvc_ctx *ctx, int nnodes, const double *xyz, int nelem,
                                  const int *conn, const int *adj);
 
