@@ -18,7 +18,9 @@
  *
  * Options after the .in file:  --device N   --stats (print a JSON line of
  * step counts and timings on stdout)   --dump-state DIR (write the final FTLE
- * grid state of every output: n, X, element ids, left flags, have flags).
+ * grid state of every output: n, X, element ids, left flags, have flags)
+ * --precision fp64|bf16|fp16 (the arithmetic form, fvc_set_precision; fp64,
+ * ompVC's, by default).
  */
 #include <math.h>
 #include <pthread.h>
@@ -762,16 +764,27 @@ static int run_tracers(run_t *R)
 int main(int argc, char **argv)
 {
     if (argc < 2) {
-        fprintf(stderr, "usage: %s inputfile [--device N] [--stats] [--dump-state DIR]\n", argv[0]);
+        fprintf(stderr, "usage: %s inputfile [--device N] [--stats] [--dump-state DIR] [--precision fp64|bf16|fp16]\n",
+                argv[0]);
         return 1;
     }
-    int device = 0, stats = 0;
+    int device = 0, stats = 0, prec = FVC_PREC_FP64;
     run_t R;
     memset(&R, 0, sizeof(R));
     for (int i = 2; i < argc; i++) {
         if (!strcmp(argv[i], "--device") && i + 1 < argc) device = atoi(argv[++i]);
         else if (!strcmp(argv[i], "--stats")) stats = 1;
         else if (!strcmp(argv[i], "--dump-state") && i + 1 < argc) R.dump_dir = argv[++i];
+        else if (!strcmp(argv[i], "--precision") && i + 1 < argc) {
+            const char *p = argv[++i];
+            if (!strcmp(p, "fp64")) prec = FVC_PREC_FP64;
+            else if (!strcmp(p, "bf16")) prec = FVC_PREC_BF16;
+            else if (!strcmp(p, "fp16")) prec = FVC_PREC_FP16;
+            else {
+                fprintf(stderr, "unknown precision '%s' (fp64, bf16 or fp16)\n", p);
+                return 1;
+            }
+        }
     }
     char err[1024];
     double t_start = wall();
@@ -792,6 +805,8 @@ int main(int argc, char **argv)
         return die("settings", R.ctx, rc);
     if (R.P.int_type == 2 && (rc = fvc_set_rkf(R.ctx, R.P.int_acc, R.P.int_hmin, R.P.int_hmax)))
         return die("RKF settings", R.ctx, rc);
+    if (prec != FVC_PREC_FP64 && (rc = fvc_set_precision(R.ctx, prec)))
+        return die("precision", R.ctx, rc);
     int bad = load_mesh(&R);
     if (!bad) bad = pipe_start(&R);
     if (!bad) bad = R.P.ftle_compute ? run_ftle(&R) : run_tracers(&R);

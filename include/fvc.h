@@ -128,8 +128,9 @@ fvc_status fvc_set_window(fvc_ctx *ctx, int frame_lo, int frame_hi, double tmin,
  *                  scale per frame and component; point location,
  *                  interpolation and the integrator's stages in FP32;
  *                  positions accumulated in FP32 with Kahan compensation.
- *                  Within 1e-5 of an element face the containment test is
- *                  the FP64 one; the FTLE eigenvalue step stays FP64.
+ *                  Near an element face (within the element's own FP32
+ *                  error bound, at least 1e-5) the containment test is the
+ *                  FP64 one; the FTLE stencil and eigenvalue stay FP64.
  * Results differ from the FP64 form by the quantisation of the frames and
  * FP32 rounding.  Set it before creating jobs; jobs keep the form they were
  * created with. */

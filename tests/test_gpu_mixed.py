@@ -172,3 +172,22 @@ def test_state_roundtrip_in_mixed_form(engine):
     assert np.abs(back - X).max() <= 2.0 ** -48
     job.close()
     g.close()
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+def test_fvcflow_precision_option(engine, tmp_path, prec):
+    """fvcflow --precision runs the golden cube FTLE case in a mixed form:
+    the same output files as the FP64 form, finite, within the mixed form's
+    error of the reference's FTLE (short window, smooth flow)."""
+    import os
+    from conftest import GOLDEN, run_golden
+    got, _ = run_golden(engine.FVCFLOW, "cube", "ftle_fwd", tmp_path, extra_args=("--precision", prec))
+    exp = os.path.join(GOLDEN, "cube", "expected", "ftle_fwd")
+    assert sorted(os.listdir(got)) == sorted(os.listdir(exp))
+    for f in sorted(os.listdir(exp)):
+        if not f.endswith(".bin") or "Cartesian" in f:
+            continue
+        A = np.fromfile(os.path.join(exp, f), np.float64)[1:]
+        B = np.fromfile(os.path.join(got, f), np.float64)[1:]
+        assert A.shape == B.shape and np.isfinite(B).all(), f
+        assert np.abs(B - A).max() <= 0.05 * max(np.abs(A).max(), 1e-12), f
