@@ -44,3 +44,8 @@ def test_truncated_in_file(engine, tmp_path):
 def test_missing_in_file(engine, tmp_path):
     r = _run(engine, str(tmp_path / "nope.in"))
     assert r.returncode != 0 and "Could not open input file" in r.stderr
+
+
+def test_unknown_precision_refused(engine, tmp_path):
+    r = subprocess.run([engine.FVCFLOW, str(tmp_path / "x.in"), "--precision", "fp8"], capture_output=True, text=True)
+    assert r.returncode != 0 and "unknown precision 'fp8'" in r.stderr
