@@ -19,13 +19,28 @@ value      accepted RK4 steps / s with mesh and frames resident in HBM; each
            (steps_early_recorded).  ftle_points_per_s counts no steps.
 e2e        the same through the C ABI from pinned host buffers: mesh and all
            frames copied host->device inside each step, FTLE fields copied back.
-roofline   the main advection kernel (k_ftle_pass1) against the measured HBM
-           copy bandwidth, 1,384 algorithmic bytes per unstructured FP64 RK4
-           step (4 stages x (connectivity 16 + node coordinates 96 + 4 nodes x
-           2 frames x 3 x 8) + final containment 112 + state 56).
+roofline   the main advection kernel (k_ftle_pass1) against the bound that
+           applies to it, the FP64 pipe: FP64-pipe instructions per step (the
+           committed instruction-mix profile) x steps / CUDA-event time,
+           against the FP64 FMA rate measured on the same device in the same
+           run (tests/cuda/fp64_rate.cu).  roofline.hbm gives the same kernel
+           against the measured HBM copy bandwidth, 1,384 algorithmic bytes per
+           unstructured FP64 RK4 step (4 stages x (connectivity 16 + node
+           coordinates 96 + 4 nodes x 2 frames x 3 x 8) + final containment
+           112 + state 56), with the DRAM traffic ncu measured.
+steps_computed  the steps the GPU actually advanced (value also counts the
+           early-FTLE steps read from the main pass's record).
+parity     one more FP64 window against the CPU oracle's run of the same
+           window on the same inputs (final grid state bit for bit, FTLE
+           fields within 1e-12) and against ompVC's own outputs for this
+           workload (the committed summaries of tests/golden/scale/).
 cpu_baseline  the CPU oracle (the reference's algorithm restated in C,
-           OpenMP over all host cores) on a bounded sample: the same grid and
-           mesh over the first 5 frame intervals (T = 0.1).
+           OpenMP over all host cores) on the same workload: the whole
+           T = 1 window, advection phase timed.
+double_gyre   the 2D Cartesian workload: double gyre on 257 x 129 nodes,
+           101 frames dt = 0.1, FTLE on 512 x 256 seeds over T = 10, RK4
+           h = 0.01, FP64: steps/s, FTLE points/s, the 816 B/step roofline,
+           parity and the CPU oracle on the same window.
 
 tracers    the cube's second workload: 1M tracers released at t = 0, outputs
            every 10 steps, FP64 and BF16 forms.
@@ -34,8 +49,8 @@ batched    the bent-tube batch of 64 tracer releases (uneven seed counts and
 served     a Poisson request stream over the tube and the cube, served in the
            BF16 and FP64 forms: p50 / p95 / p99 latency and steps/s.
 
---impl reference runs that CPU implementation alone, every step one bounded
-sample, on the same metric.  Multi-GPU (torchrun, N > 1): every rank runs the
+--impl reference runs that CPU implementation alone on the same workload
+(every step one whole T = 1 window), on the same metric.  Multi-GPU (torchrun, N > 1): every rank runs the
 whole workload on its own GPU (replicas; the window has no exchange step),
 value = all ranks' steps / the slowest rank's time.
 """
@@ -65,7 +80,11 @@ CUBE_N = 64
 NFRAMES, DT = 51, 0.02
 H = 0.005
 T_WINDOW = 1.0
-SAMPLE_T = 0.1               # CPU sample: first 5 frame intervals
+# config 1: the double gyre on a Cartesian grid
+DG_NX, DG_NY, DG_FRAMES, DG_DT = 257, 129, 101, 0.1
+DG_GRID = (0.0, 2.0, 0.0, 1.0, 0.0, 0.0, 512, 256, 1)
+DG_H, DG_T = 0.01, 10.0
+DG_BYTES_PER_STEP = 816      # Cartesian 2D FP64 RK4 step, algorithmic
 
 
 def parse():
@@ -84,6 +103,8 @@ def parse():
     ap.add_argument("--tracers", type=int, default=1_000_000)
     ap.add_argument("--no-batched", action="store_true", help="skip the bent-tube batch")
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
+    ap.add_argument("--no-dg", action="store_true", help="skip the double-gyre (Cartesian 2D) workload")
+    ap.add_argument("--no-parity", action="store_true", help="skip the parity window")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--served-rate", type=float, default=200.0, help="requests / s")
     ap.add_argument("--served-seconds", type=float, default=10.0, help="arrival window, s")
@@ -181,37 +202,70 @@ def profiled_traffic():
         return None, None
 
 
+# ------------------------------------------------------------------ FP64 rate
+
+def probe_fp64(device):
+    """(FP64 FMAs / s, IEEE divisions / s) of the device, from the rate probe
+    tests/cuda/fp64_rate.cu (built here with nvcc); None if it cannot run."""
+    src = os.path.join(ROOT, "tests", "cuda", "fp64_rate.cu")
+    nvcc = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+    with tempfile.TemporaryDirectory() as td:
+        exe = os.path.join(td, "fp64_rate")
+        try:
+            subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", exe, src],
+                           check=True, capture_output=True, timeout=300)
+            r = subprocess.run([exe, str(device)], check=True, capture_output=True, text=True, timeout=120)
+            d = json.loads(r.stdout.strip().splitlines()[-1])
+            return {"fma_per_s": float(d["fma_per_s"]), "div_per_s": float(d["div_per_s"])}
+        except (OSError, subprocess.SubprocessError, ValueError, KeyError, IndexError):
+            return None
+
+
 # ------------------------------------------------------------------ CPU side
 
-def cpu_sample(inputs, grid, threads, tmpdir):
-    """The oracle on the bounded sample; returns (steps/s, steps, seconds, threads)."""
-    import oracle_lib
+def write_cube_files(inputs, d, nframes=NFRAMES):
     import synth
     xyz, conn, adj, frames = inputs
-    d = os.path.join(tmpdir, "c2")
-    if not os.path.exists(os.path.join(d, "cube_coordinates.bin")):
+    if not os.path.exists(os.path.join(d, f"cube_vel.{nframes - 1}.bin")):
         os.makedirs(d, exist_ok=True)
         synth.write_unstructured_mesh(os.path.join(d, "cube"), xyz, conn, adj)
-        nfr = int(round(SAMPLE_T / DT)) + 2
-        for f in range(min(nfr, NFRAMES)):
+        for f in range(nframes):
             synth.write_frame(os.path.join(d, f"cube_vel.{f}.bin"), f * DT, frames[f])
+    return d
+
+
+def cpu_window(inputs, grid, threads, tmpdir, dump=None):
+    """The oracle on the whole FTLE window (T = 1) of the benchmark, with all
+    host threads: returns (steps/s of the advection phase, steps, seconds,
+    threads, output directory).  dump: directory for its final grid state."""
+    import oracle_lib
+    import synth
+    d = write_cube_files(inputs, os.path.join(tmpdir, "c2"))
     out = os.path.join(tmpdir, "c2out")
     os.makedirs(out, exist_ok=True)
     inp = os.path.join(tmpdir, "c2.in")
     g = grid
     synth.write_in_file(
         inp, Path_Data=d + "/", Path_Output=out + "/", Dimensions=3, Data_MeshType=1, Data_InFilePrefix="cube",
-        Data_TRes=NFRAMES, Data_TDelta=DT, FTLE_Compute=1, FTLE_IntTLength=SAMPLE_T, Int_TimeStep=H,
+        Data_TRes=NFRAMES, Data_TDelta=DT, FTLE_Compute=1, FTLE_IntTLength=T_WINDOW, Int_TimeStep=H,
         LocalSearchChecking=1, **{"Data_MeshBounds.XMin": 0.0, "Data_MeshBounds.XMax": 1.0,
                                   "Data_MeshBounds.YMin": 0.0, "Data_MeshBounds.YMax": 1.0,
                                   "Data_MeshBounds.ZMin": 0.0, "Data_MeshBounds.ZMax": 1.0,
                                   "FTLE_MeshBounds.ZMax": 1.0, "FTLE_MeshBounds.XRes": g,
                                   "FTLE_MeshBounds.YRes": g, "FTLE_MeshBounds.ZRes": g})
     nthr = threads if threads > 0 else (os.cpu_count() or 1)
-    rc, secs, steps, err = oracle_lib.run(inp, nthr)
+    old = os.environ.get("ORC_DUMP_STATE")
+    os.environ["ORC_DUMP_STATE"] = dump or ""
+    try:
+        rc, secs, steps, err = oracle_lib.run(inp, nthr)
+    finally:
+        if old is None:
+            del os.environ["ORC_DUMP_STATE"]
+        else:
+            os.environ["ORC_DUMP_STATE"] = old
     if rc:
         raise RuntimeError(f"oracle failed: {err}")
-    return steps / secs, steps, secs, nthr
+    return steps / secs, steps, secs, nthr, out
 
 
 def run_reference(args, rank, world):
@@ -220,12 +274,11 @@ def run_reference(args, rank, world):
     inputs = make_inputs(args.cube)
     with tempfile.TemporaryDirectory() as td:
         for _ in range(args.warmup):
-            cpu_sample(inputs, args.grid, args.cpu_threads, td)
-        vals, steps_tot, secs_tot = [], 0, 0.0
+            cpu_window(inputs, args.grid, args.cpu_threads, td)
+        steps_tot, secs_tot = 0, 0.0
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            v, st, secs, nthr = cpu_sample(inputs, args.grid, args.cpu_threads, td)
-            vals.append(v)
+            v, st, secs, nthr, _ = cpu_window(inputs, args.grid, args.cpu_threads, td)
             steps_tot += st
             secs_tot += secs
         wall = time.perf_counter() - t0
@@ -235,14 +288,170 @@ def run_reference(args, rank, world):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"FTLE {args.grid}^3 seeds, {args.cube}^3x6 jittered Kuhn tets, ABC flow, "
-                               f"RK4 h={H}; sample: first {int(round(SAMPLE_T / DT))} frame intervals (T={SAMPLE_T})",
-                   "l2": "inputs larger than L2"},
+        "config": {"workload": f"FTLE {args.grid}^3 seeds over T={T_WINDOW}, {args.cube}^3x6 jittered Kuhn tets "
+                               f"({6 * args.cube ** 3} tets), ABC flow {NFRAMES} frames, RK4 h={H}",
+                   "l2": "inputs larger than L2 (frames 51 x 8.8 MB + 420 MB of grid state)",
+                   "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": nthr, "kind": "port",
-                         "sample": f"FTLE {args.grid}^3 over T={SAMPLE_T} (5 of 50 intervals), advection phase timed"},
+                         "sample": f"the whole window: FTLE {args.grid}^3 over T={T_WINDOW} (50 intervals), "
+                                   "advection phase timed"},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ parity
+
+def parity_against_oracle(state, wT, wN, orc_dump, orc_out):
+    """A GPU window's final grid state and FTLE fields against the oracle's
+    run of the same window (its ORC_DUMP_STATE file and output fields)."""
+    f = os.path.join(orc_dump, "state.0.bin")
+    a = np.fromfile(f, np.uint8)
+    n = int(a[:4].view(np.int32)[0])
+    X = a[4:4 + 24 * n].view(np.float64).reshape(n, 3)
+    ia = a[4 + 24 * n:].view(np.int32).reshape(3, n)
+    live = ia[1] == 0
+    res = {"points": n,
+           "positions_differing": int((X != state["X"]).any(1).sum()),
+           "left_differing": int((ia[1] != state["left"]).sum()),
+           "have_differing": int(((ia[2] != 0) != (state["have"] != 0)).sum()),
+           "eid_differing": int((ia[0][live] != state["eid"][live]).sum())}
+    worst = 0.0
+    for name, got in (("ftle.0.bin", wT), ("ftle_noT.0.bin", wN)):
+        ref = np.fromfile(os.path.join(orc_out, name), "<f8")[1:]
+        worst = max(worst, float((np.abs(got - ref) / np.maximum(np.abs(ref), 1e-13)).max()))
+    res["ftle_max_rel"] = worst
+    res["bitexact"] = not any(res[k] for k in ("positions_differing", "left_differing", "have_differing",
+                                                "eid_differing"))
+    return res
+
+
+def parity_against_ompvc(case, wT, wN, time_stamp):
+    """FTLE fields of a GPU window against ompVC's outputs for the same
+    inputs, through the committed summaries (every 509th value, block sums);
+    None when the fixture is missing."""
+    try:
+        import scale_cases as sc
+        meta, arrays = sc.load_fixture()
+    except (OSError, KeyError, ValueError):
+        return None
+    if case not in meta.get("cases", {}):
+        return None
+    worst, blocks_bad = 0.0, 0
+    for name, v in (("ftle.0.bin", wT), ("ftle_noT.0.bin", wN)):
+        ref = arrays[f"{case}:{name}:sub"]
+        sub = v[::sc.STRIDE]
+        if len(sub) != len(ref):
+            return {"error": "size differs from ompVC's output"}
+        worst = max(worst, float((np.abs(sub - ref) / np.maximum(np.abs(ref), 1e-13)).max()))
+        nb = len(v) // sc.BLOCK
+        blk = v[:nb * sc.BLOCK].reshape(nb, sc.BLOCK).sum(1)
+        tol = 1e-12 * arrays[f"{case}:{name}:absblk"] + sc.BLOCK * 1e-13
+        blocks_bad += int((np.abs(blk - arrays[f"{case}:{name}:blk"]) > tol).sum())
+    return {"ftle_max_rel_strided": worst, "block_sums_outside_1e-12": blocks_bad,
+            "time_stamp_matches": meta["cases"][case]["files"]["ftle.0.bin"]["time"] == time_stamp,
+            "within_1e-12": worst <= 1e-12 and blocks_bad == 0}
+
+
+# ------------------------------------------------------------------ double gyre
+
+def dg_frames():
+    """Config 1's frames in memory, exactly as synth.make_double_gyre_case
+    writes them: nodes in (j, i) order with i fastest, w = 0."""
+    import synth
+    xs, ys = np.linspace(0.0, 2.0, DG_NX), np.linspace(0.0, 1.0, DG_NY)
+    Y, X = np.meshgrid(ys, xs, indexing="ij")
+    out = []
+    for n in range(DG_FRAMES):
+        u, v = synth.double_gyre(X, Y, n * DG_DT)
+        out.append(np.ascontiguousarray(np.stack([u, v, np.zeros_like(u)], -1).reshape(-1, 3)))
+    return out
+
+
+def bench_double_gyre(args, stream_of, barrier, fp64, rank):
+    """Config 1 on the GPU: the double gyre's FTLE window (Cartesian 2D,
+    FP64) timed with CUDA events over args.steps windows after one warm-up;
+    one more window checked against the oracle and ompVC; the oracle on the
+    same window on the host cores (rank 0)."""
+    import torch
+
+    import flow
+    import fvc
+    import synth
+    frames = dg_frames()
+    ax = flow.TimeAxis(0.0, DG_DT, DG_FRAMES, 0)
+    ctx = fvc.Context(2, 0)
+    ctx.set_cart_mesh(0.0, 2.0, DG_NX, 0.0, 1.0, DG_NY, 0.0, 0.0, 1)
+    ctx.set_bounds([0.0, 2.0, 0.0, 1.0, 0.0, 0.0])
+    ctx.set_integrator(1, DG_H, 0)
+    flow.upload_frames(ctx, ax, frames)
+    stream = stream_of(ctx)
+    npts = DG_GRID[6] * DG_GRID[7]
+    for _ in range(max(1, min(args.warmup, 3))):
+        flow.run_ftle(ctx, ax, DG_GRID, DG_T)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps, stats = 0, []
+    e0.record(stream)
+    for _ in range(args.steps):
+        wT, wN, st, js = flow.run_ftle(ctx, ax, DG_GRID, DG_T)
+        steps += st
+        stats.append(js)
+    e1.record(stream)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    ms_main = sum(x["ms_main"] for x in stats)
+    steps_main = sum(x["steps_main"] for x in stats)
+    achieved = steps_main * DG_BYTES_PER_STEP / (ms_main / 1e3) / 1e9 if ms_main > 0 else 0.0
+    peak, peak_kind = measured_peak()
+    out = {"workload": f"double gyre, {DG_NX}x{DG_NY} nodes, {DG_FRAMES} frames dt={DG_DT}; FTLE "
+                       f"{DG_GRID[6]}x{DG_GRID[7]} seeds over [0,2]x[0,1], T={DG_T}, RK4 h={DG_H}, f64",
+           "value": steps / (ms / 1e3), "unit": "steps/s", "ms_per_step": ms / args.steps,
+           "ftle_points_per_s": npts * args.steps / (ms / 1e3),
+           "steps_per_window": steps / args.steps,
+           "phases_ms_per_step": {k: sum(x[k] for x in stats) / args.steps
+                                  for k in ("ms_setup", "ms_main", "ms_early", "ms_reduce")},
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_source": peak_kind, "kernel": "k_ftle_pass1 (Cartesian 2D)",
+                        "bytes_per_step": DG_BYTES_PER_STEP}}
+    _, prof = profiled_traffic()
+    ops = (prof or {}).get("cart2_fp64_pipe_ops_per_step")
+    if ops and fp64 and ms_main > 0:
+        r = ops * steps_main / (ms_main / 1e3)
+        out["fp64_pipe"] = {"ops_per_step": ops, "achieved": r / 1e9, "peak": fp64["fma_per_s"] / 1e9,
+                            "unit": "G FP64-pipe ops/s", "frac": r / fp64["fma_per_s"]}
+    if rank == 0 and not args.no_cpu:
+        state = {}
+        wT, wN, _, _ = flow.run_ftle(ctx, ax, DG_GRID, DG_T, state=state)
+        with tempfile.TemporaryDirectory() as td:
+            d = os.path.join(td, "dg")
+            c = synth.make_double_gyre_case(d, nx=DG_NX, ny=DG_NY, nframes=DG_FRAMES, dt=DG_DT, prefix="dg")
+            o, dump = os.path.join(td, "out"), os.path.join(td, "dump")
+            os.makedirs(o)
+            os.makedirs(dump)
+            inp = os.path.join(td, "dg.in")
+            synth.write_in_file(inp, **dict(c.params, Path_Output=o + "/", FTLE_Compute=1, FTLE_IntTLength=DG_T,
+                                            Int_TimeStep=DG_H, **{
+                                                "FTLE_MeshBounds.XMin": DG_GRID[0], "FTLE_MeshBounds.XMax": DG_GRID[1],
+                                                "FTLE_MeshBounds.YMin": DG_GRID[2], "FTLE_MeshBounds.YMax": DG_GRID[3],
+                                                "FTLE_MeshBounds.ZMin": 0.0, "FTLE_MeshBounds.ZMax": 0.0,
+                                                "FTLE_MeshBounds.XRes": DG_GRID[6], "FTLE_MeshBounds.YRes": DG_GRID[7],
+                                                "FTLE_MeshBounds.ZRes": 1}))
+            import oracle_lib
+            nthr = args.cpu_threads if args.cpu_threads > 0 else (os.cpu_count() or 1)
+            os.environ["ORC_DUMP_STATE"] = dump
+            try:
+                rc, secs, csteps, err = oracle_lib.run(inp, nthr)
+            finally:
+                del os.environ["ORC_DUMP_STATE"]
+            if rc:
+                raise RuntimeError(f"oracle failed on the double gyre: {err}")
+            out["cpu_baseline"] = {"value": csteps / secs, "unit": "steps/s", "cores": nthr, "kind": "port",
+                                   "sample": f"the same window, {csteps} steps in {secs:.2f} s of advection"}
+            out["parity"] = {"vs_oracle": parity_against_oracle(state, wT, wN, dump, o),
+                             "vs_ompvc": parity_against_ompvc("dg_ftle", wT, wN, 0.0)}
+    ctx.close()
+    return out
 
 
 # ------------------------------------------------------------------ tracers
@@ -385,15 +594,44 @@ def form_errors(ref, got):
             "points_left": float((rs["left"] == 1).mean())}
 
 
-def precision_forms(ctx, ax, grid, stream, barrier, args, fp64_value):
+def ftle_error_by_time(ref_T, ref_N, got_T):
+    """FTLE error (relative to the largest FP64 value) binned by each
+    point's FTLE integration time |MinExitTime - StartTime| = FTLEwoT /
+    FTLEwT of the FP64 window: early FTLE divides by that time, so short
+    times amplify any change of the stretching."""
+    scale = float(np.abs(ref_T).max()) or 1.0
+    e = np.abs(got_T - ref_T) / scale
+    with np.errstate(divide="ignore", invalid="ignore"):
+        teff = np.where(ref_T != 0, np.abs(ref_N / ref_T), np.nan)
+    out = []
+    for lo, hi in ((0.0, 0.05), (0.05, 0.1), (0.1, 0.25), (0.25, 0.5), (0.5, 1.0 + 1e-9)):
+        m = (teff >= lo) & (teff < hi)
+        if m.any():
+            out.append({"T_from": lo, "T_to": min(hi, 1.0), "points": int(m.sum()), "max": float(e[m].max()),
+                        "rms": float(np.sqrt((e[m] ** 2).mean())), "p99": float(np.quantile(e[m], 0.99))})
+    m = np.isnan(teff)
+    if m.any():
+        out.append({"T_from": None, "T_to": None, "points": int(m.sum()), "note": "FP64 FTLE is 0 (lambda <= 1)",
+                    "max": float(e[m].max())})
+    return out
+
+
+def precision_forms(ctx, ax, grid, stream, barrier, args, fp64_value, ref, inputs):
     """BF16 and FP16 frames with FP32 stages (fvc_set_precision) on the same
     context and workload: one warm-up window, then args.steps timed windows
-    with CUDA events; errors against one more FP64 window."""
+    with CUDA events; errors against ref = (FTLE field, FTLE-without-time
+    field, final state) of an FP64 window.  The error is split by source:
+    the FP64 form run on frames quantised and dequantised on the host
+    (tests/quantise.py) carries the storage error alone; the mixed form
+    against that run carries the FP32 arithmetic (and the mixed form's reuse
+    of the main pass's record)."""
     import torch
 
     import flow
-    ref_state = {}
-    ref_T = flow.run_ftle(ctx, ax, grid, T_WINDOW, state=ref_state)[0]
+    import fvc
+    import quantise
+    ref_T, ref_N, ref_state = ref
+    xyz, conn, adj, frames = inputs
     out = {}
     for name in ("bf16", "fp16"):
         ctx.set_precision(name)
@@ -412,13 +650,30 @@ def precision_forms(ctx, ax, grid, stream, barrier, args, fp64_value):
         got_state = {}
         T_last = flow.run_ftle(ctx, ax, grid, T_WINDOW, state=got_state)[0]
         value = steps / (ms / 1000.0)
+        # the storage error alone: the FP64 form on the 16-bit frames
+        cq = fvc.Context(3, 1)
+        cq.set_unstruct_mesh(xyz, conn, adj)
+        cq.set_bounds([0, 1, 0, 1, 0, 1])
+        cq.set_integrator(1, H, 0)
+        flow.upload_frames(cq, ax, [quantise.dequantised(f, name) for f in frames])
+        q_state = {}
+        q_T = flow.run_ftle(cq, ax, grid, T_WINDOW, state=q_state)[0]
+        cq.close()
+        total = form_errors((ref_T, ref_state), (T_last, got_state))
         out[name] = {"value": value, "unit": "steps/s", "ms_per_step": ms / args.steps,
                      "ftle_points_per_s": args.grid ** 3 * args.steps / (ms / 1000.0),
                      "speedup_vs_fp64": value / fp64_value,
                      "steps_early_recorded_per_step": sum(x["steps_early_recorded"] for x in stats) / args.steps,
                      "phases_ms_per_step": {k: sum(s[k] for s in stats) / args.steps
                                             for k in ("ms_setup", "ms_main", "ms_early", "ms_reduce")},
-                     "errors": form_errors((ref_T, ref_state), (T_last, got_state))}
+                     "errors": total,
+                     "ftle_max_rel_target": 1e-3,
+                     "ftle_max_rel_to_max_achieved": total["ftle_max_rel_to_max"],
+                     "errors_by_source": {
+                         "storage": form_errors((ref_T, ref_state), (q_T, q_state)),
+                         "arithmetic": form_errors((q_T, q_state), (T_last, got_state)),
+                         "ftle_by_time_total": ftle_error_by_time(ref_T, ref_N, T_last),
+                         "ftle_by_time_storage": ftle_error_by_time(ref_T, ref_N, q_T)}}
     ctx.set_precision("fp64")
     return out
 
@@ -456,11 +711,7 @@ def run_engine(args, rank, world, local_rank):
     grid = grid_tuple(args.grid)
     npts = args.grid ** 3
 
-    try:
-        fma_s, div_s = fvc.probe_fp64(local_rank)
-        fp64 = {"fma_per_s": fma_s, "div_per_s": div_s}
-    except fvc.FvcError:
-        fp64 = None
+    fp64 = probe_fp64(local_rank)
     ctx = fvc.Context(3, 1, device=local_rank)
     ctx.set_unstruct_mesh(xyz, conn, adj)
     ctx.set_bounds([0, 1, 0, 1, 0, 1])
@@ -492,8 +743,12 @@ def run_engine(args, rank, world, local_rank):
     clocks = clk.summary()
     secs = ms / 1000.0
     secs_max, steps_all = reduce_over_ranks(secs, steps_total, world)
+    steps_recorded = sum(s["steps_early_recorded"] for s in stats)
+    steps_computed = steps_total - steps_recorded
+    secs_c, steps_computed_all = reduce_over_ranks(secs, steps_computed, world)
 
-    # roofline of the main advection kernel from its CUDA-event times
+    # roofline of the main advection kernel from its CUDA-event times: the
+    # FP64 pipe (the bound that applies), and the HBM figure beside it
     ms_main = sum(s["ms_main"] for s in stats)
     steps_main = sum(s["steps_main"] for s in stats)
     launches_main = sum(s["intervals"] for s in stats)
@@ -501,20 +756,29 @@ def run_engine(args, rank, world, local_rank):
     achieved = (steps_main * BYTES_PER_STEP) / (ms_main / 1000.0) / 1e9 if ms_main > 0 else 0.0
     traffic_per_step, prof = profiled_traffic()
     traffic = traffic_per_step * steps_main / launches_main if traffic_per_step else None
-    # the bound that applies: FP64 issue (ops per step from the committed
-    # instruction-mix profile) against the FMA rate the probe measured
-    fp64_pipe = None
-    if prof and prof.get("fp64_pipe_ops_per_step") and fp64 and ms_main > 0:
-        ops = prof["fp64_pipe_ops_per_step"] * steps_main / (ms_main / 1000.0)
-        fp64_pipe = {"ops_per_step": prof["fp64_pipe_ops_per_step"], "achieved": ops / 1e9,
-                     "peak": fp64["fma_per_s"] / 1e9, "unit": "G FP64-pipe ops/s",
-                     "frac": ops / fp64["fma_per_s"], "kernel": "k_ftle_pass1"}
+    hbm = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+           "traffic": traffic, "peak_source": peak_kind, "bytes_per_step": BYTES_PER_STEP}
+    ops_per_step = (prof or {}).get("fp64_pipe_ops_per_step")
+    if ops_per_step and fp64 and ms_main > 0:
+        ops = ops_per_step * steps_main / (ms_main / 1000.0)
+        roofline = {"bound": "fp64", "achieved": ops / 1e9, "peak": fp64["fma_per_s"] / 1e9,
+                    "unit": "G FP64-pipe instructions/s", "frac": ops / fp64["fma_per_s"], "traffic": traffic,
+                    "peak_source": "measured in this run (tests/cuda/fp64_rate.cu, FP64 FMA rate)",
+                    "ops_per_step": ops_per_step, "kernel": "k_ftle_pass1", "hbm": hbm}
+    else:
+        roofline = dict(hbm, kernel="k_ftle_pass1")
     gpu_launches = int(sum(s["launches"] for s in stats))
 
-    # the mixed-precision forms on the same workload, against this FP64 run
+    # one more FP64 window, kept for the parity check and as the mixed forms'
+    # reference
+    ref_state = {}
+    ref_T, ref_N, _, _ = flow.run_ftle(ctx, ax, grid, T_WINDOW, state=ref_state)
+
+    # the mixed-precision forms on the same workload, against this FP64 window
     forms = None
     if not args.no_precision:
-        forms = precision_forms(ctx, ax, grid, stream, barrier, args, steps_all / secs_max)
+        forms = precision_forms(ctx, ax, grid, stream, barrier, args, steps_all / secs_max,
+                                (ref_T, ref_N, ref_state), inputs)
 
     # end to end through the C ABI from pinned host buffers
     e2e = None
@@ -544,6 +808,10 @@ def run_engine(args, rank, world, local_rank):
     else:
         ctx.close()
 
+    dg = None
+    if not args.no_dg:
+        dg = bench_double_gyre(args, lambda c: torch.cuda.ExternalStream(c.stream()), barrier, fp64, rank)
+
     tracers = None if args.no_tracers else bench_tracers(args, inputs)
     batched = served = None
     if not (args.no_batched and args.no_served):
@@ -557,13 +825,20 @@ def run_engine(args, rank, world, local_rank):
             served = bench_served(args, tube, tframes, inputs)
         del tube, tframes
 
-    cpu = None
+    # the CPU oracle on the same window, and the parity of the FP64 window
+    cpu = parity = None
     if rank == 0 and not args.no_cpu:
         with tempfile.TemporaryDirectory() as td:
-            v, st, s2, nthr = cpu_sample(inputs, args.grid, args.cpu_threads, td)
+            dump = os.path.join(td, "state")
+            os.makedirs(dump)
+            v, st, s2, nthr, out_dir = cpu_window(inputs, args.grid, args.cpu_threads, td, dump=dump)
+            parity = {"vs_oracle": parity_against_oracle(ref_state, ref_T, ref_N, dump, out_dir)}
         cpu = {"value": v, "unit": "steps/s", "cores": nthr, "kind": "port",
-               "sample": f"FTLE {args.grid}^3 over T={SAMPLE_T} (5 of 50 intervals), {st} steps in {s2:.2f} s "
-                         f"of advection"}
+               "sample": f"the whole window: FTLE {args.grid}^3 over T={T_WINDOW} (50 intervals), {st} steps in "
+                         f"{s2:.2f} s of advection"}
+    if rank == 0 and args.grid == 128 and args.cube == CUBE_N:
+        parity = parity or {}
+        parity["vs_ompvc"] = parity_against_ompvc("cube_ftle", ref_T, ref_N, 0.0)
 
     if rank == 0:
         value = steps_all / secs_max
@@ -577,14 +852,14 @@ def run_engine(args, rank, world, local_rank):
                        "l2": "inputs larger than L2 (frames 51 x 8.8 MB + 420 MB of grid state)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "ftle_points_per_s": npts * args.steps * world / secs_max,
+            "steps_computed": int(steps_computed), "steps_computed_per_s": steps_computed_all / secs_c,
             "steps_main": int(steps_main), "steps_early": int(sum(s["steps_early"] for s in stats)),
-            "steps_early_recorded": int(sum(s["steps_early_recorded"] for s in stats)),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "k_ftle_pass1", "bytes_per_step": BYTES_PER_STEP},
+            "steps_early_recorded": int(steps_recorded),
+            "roofline": roofline,
             "gpu_launches": gpu_launches,
-            "fp64_pipe": fp64_pipe,
+            "parity": parity,
             "precision_forms": forms,
+            "double_gyre": dg,
             "tracers": tracers,
             "batched": batched,
             "served": served,
@@ -595,6 +870,8 @@ def run_engine(args, rank, world, local_rank):
             "e2e": e2e,
             "cpu_baseline": cpu,
         }
+        if parity and parity.get("vs_oracle"):
+            line["parity"]["summary"] = "bitexact" if parity["vs_oracle"]["bitexact"] else "MISMATCH"
         print(json.dumps(line), flush=True)
 
 

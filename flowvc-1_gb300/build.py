@@ -28,7 +28,7 @@ NVFLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPI
 
 CU_SOURCES = ["fvc_kernels.cu", "fvc_api.cu", "fvc_variant_c2.cu", "fvc_variant_c3.cu",
               "fvc_variant_u2.cu", "fvc_variant_u3.cu", "fvc_variant_u2m.cu", "fvc_variant_u3m.cu",
-              "fvc_mixed_kernels.cu", "fvc_probe.cu", "fvc_cet.cu", "fvc_batch.cu"]
+              "fvc_mixed_kernels.cu", "fvc_cet.cu", "fvc_batch.cu"]
 # resident 128-thread blocks per SM the integrator kernels are compiled for
 # (register budget 65536 / (128 * n)); FVC_MINBLOCKS overrides it for sweeps
 MINBLOCKS = os.environ.get("FVC_MINBLOCKS", "4")

@@ -4,6 +4,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <mutex>
@@ -204,6 +205,17 @@ extern "C" fvc_status fvc_set_cart_mesh(fvc_ctx* c, double xmin, double xmax, in
   return FVC_OK;
 }
 
+// Cells of the global-search bucket grid at most (about two elements a cell;
+// FVC_BUCKET_MAX_CELLS lowers the cap, e.g. to bound the grid's memory).
+static long bucket_cell_cap() {
+  const long dflt = 1L << 26;
+  const char* e = getenv("FVC_BUCKET_MAX_CELLS");
+  if (!e || !*e) return dflt;
+  char* end = nullptr;
+  long v = strtol(e, &end, 10);
+  return (end && *end == 0 && v > 0 && v < dflt) ? v : dflt;
+}
+
 extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double* xyz, int nelem,
                                             const int* conn, const int* adj) {
   if (!c) return FVC_ERR_ARG;
@@ -211,7 +223,6 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
   if (nnodes <= 0 || nelem <= 0 || !xyz || !conn || !adj) return fail(c, FVC_ERR_ARG, "empty mesh");
   fvc_status st;
   if ((st = use_device(c))) return st;
-  if (c->cet_sub) fvc_cet_enable(c, 0);  // the accumulators belong to the old mesh
   const int nv = c->mesh.dims == 3 ? 4 : 3;
   std::vector<double4_32a> hn((size_t)nnodes);
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
@@ -222,17 +233,29 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
       hi[a] = fmax(hi[a], xyz[3 * i + a]);
     }
   }
-  // the new mesh's buffers; the old ones stay until the new mesh is valid
+  // Everything of the new mesh -- records, nodes and bucket grid -- is built
+  // in buffers of its own; the context's mesh, grid and exposure-time sums
+  // change only once the last step has succeeded, so every failure below
+  // leaves the previous mesh in use.
   const int gstride = c->mesh.dims == 3 ? 16 : 12;
   int4* n_elem = nullptr;
   double* n_geom = nullptr;
   float* n_geo32 = nullptr;
   double4_32a* n_nodes = nullptr;
+  int* n_start = nullptr;
+  int* n_ids = nullptr;
+  int* d_count = nullptr;
+  long long* d_tmp = nullptr;
   auto drop_new = [&]() {
+    cudaStreamSynchronize(c->stream);  // nothing queued may still write them
     cudaFree(n_elem);
     cudaFree(n_geom);
     cudaFree(n_geo32);
     cudaFree(n_nodes);
+    cudaFree(n_start);
+    cudaFree(n_ids);
+    cudaFree(d_count);
+    cudaFree(d_tmp);
   };
   if (cudaMalloc(&n_elem, sizeof(int4) * 2 * (size_t)nelem) != cudaSuccess ||
       cudaMalloc(&n_geom, sizeof(double) * gstride * (size_t)nelem) != cudaSuccess ||
@@ -269,31 +292,28 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
     }
     return fail(c, FVC_ERR_ARG, "element %d out of range", bad);
   }
-  for (int a = 0; a < 3; a++) {
-    c->node_lo[a] = lo[a];
-    c->node_hi[a] = hi[a];
+  if (cudaMemcpyAsync(n_nodes, hn.data(), sizeof(double4_32a) * hn.size(), cudaMemcpyHostToDevice, c->stream) !=
+      cudaSuccess) {
+    drop_new();
+    return fail(c, FVC_ERR_CUDA, "mesh node upload failed");
   }
-  cudaFree(c->d_elem); c->d_elem = n_elem;
-  cudaFree(c->d_geom); c->d_geom = n_geom;
-  cudaFree(c->d_geo32); c->d_geo32 = n_geo32;
-  cudaFree(c->d_nodes); c->d_nodes = n_nodes;
-  cudaFree(c->d_cell_start); c->d_cell_start = nullptr;
-  cudaFree(c->d_cell_ids); c->d_cell_ids = nullptr;
-  FVC_CUDA(c, cudaMemcpyAsync(c->d_nodes, hn.data(), sizeof(double4_32a) * hn.size(), cudaMemcpyHostToDevice, c->stream));
-  DevMesh& m = c->mesh;
-  m.elem = c->d_elem;
-  m.geom = c->d_geom;
-  m.geo32 = c->d_geo32;
-  m.geo32lo = reinterpret_cast<const float4*>(c->d_geo32 + 16L * nelem);
-  m.nodes = c->d_nodes;
+  DevMesh m = c->mesh;
+  m.elem = n_elem;
+  m.geom = n_geom;
+  m.geo32 = n_geo32;
+  m.geo32lo = reinterpret_cast<const float4*>(n_geo32 + 16L * nelem);
+  m.nodes = n_nodes;
   m.nelem = nelem;
   m.nnodes = nnodes;
-  launch_geometry(m, c->d_geom, c->d_geo32, c->stream);
-  if ((st = check_launch(c, "geometry"))) return st;
+  launch_geometry(m, n_geom, n_geo32, c->stream);
+  if (cudaGetLastError() != cudaSuccess) {
+    drop_new();
+    return fail(c, FVC_ERR_CUDA, "geometry launch failed");
+  }
 
   // Uniform bucket grid over the mesh's bounding box, about two elements per
   // cell, for the lowest-id global search.
-  BucketGrid& g = c->grid;
+  BucketGrid g = c->grid;
   int dims = m.dims;
   double ext[3], vol = 1.0;
   for (int a = 0; a < 3; a++) {
@@ -316,33 +336,53 @@ extern "C" fvc_status fvc_set_unstruct_mesh(fvc_ctx* c, int nnodes, const double
     g.inv[a] = (double)na / ext[a];
     ncells *= na;
   }
-  if (ncells > (1L << 26)) return fail(c, FVC_ERR_ARG, "bucket grid too large");
-  int* d_count = nullptr;
-  long long* d_tmp = nullptr;
-  if (cudaMalloc(&c->d_cell_start, sizeof(int) * (ncells + 1)) != cudaSuccess ||
+  const long cap = bucket_cell_cap();
+  if (ncells > cap) {
+    drop_new();
+    return fail(c, FVC_ERR_ARG, "bucket grid too large (%ld cells, at most %ld)", ncells, cap);
+  }
+  if (cudaMalloc(&n_start, sizeof(int) * (ncells + 1)) != cudaSuccess ||
       cudaMalloc(&d_count, sizeof(int) * ncells) != cudaSuccess ||
       cudaMalloc(&d_tmp, sizeof(long long) * (ncells / 1024 + 8)) != cudaSuccess) {
-    cudaFree(d_count);
-    cudaFree(d_tmp);
+    drop_new();
     return fail(c, FVC_ERR_OOM, "bucket grid allocation failed");
   }
   bucket_count(m, g, d_count, (int)ncells, nullptr, c->stream);
-  scan_counts(d_count, c->d_cell_start, (int)ncells, d_tmp, c->stream);
+  scan_counts(d_count, n_start, (int)ncells, d_tmp, c->stream);
   int total = 0;
-  FVC_CUDA(c, cudaMemcpyAsync(&total, c->d_cell_start + ncells, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
-  if (total < 0 || cudaMalloc(&c->d_cell_ids, sizeof(int) * ((size_t)total + 1)) != cudaSuccess) {
-    cudaFree(d_count);
-    cudaFree(d_tmp);
+  if (cudaMemcpyAsync(&total, n_start + ncells, sizeof(int), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    drop_new();
+    return fail(c, FVC_ERR_CUDA, "bucket grid count failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  if (total < 0 || cudaMalloc(&n_ids, sizeof(int) * ((size_t)total + 1)) != cudaSuccess) {
+    drop_new();
     return fail(c, FVC_ERR_OOM, "bucket list allocation failed (%d entries)", total);
   }
-  g.start = c->d_cell_start;
-  g.ids = c->d_cell_ids;
-  bucket_fill(m, g, c->d_cell_start, d_count, c->d_cell_ids, (int)ncells, nullptr, c->stream);
-  if ((st = check_launch(c, "bucket grid"))) return st;
-  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
+  g.start = n_start;
+  g.ids = n_ids;
+  bucket_fill(m, g, n_start, d_count, n_ids, (int)ncells, nullptr, c->stream);
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    drop_new();
+    return fail(c, FVC_ERR_CUDA, "bucket grid build failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
   cudaFree(d_count);
   cudaFree(d_tmp);
+
+  // the new mesh is valid: it replaces the old one
+  if (c->cet_sub) fvc_cet_enable(c, 0);  // the accumulators belong to the old mesh
+  cudaFree(c->d_elem); c->d_elem = n_elem;
+  cudaFree(c->d_geom); c->d_geom = n_geom;
+  cudaFree(c->d_geo32); c->d_geo32 = n_geo32;
+  cudaFree(c->d_nodes); c->d_nodes = n_nodes;
+  cudaFree(c->d_cell_start); c->d_cell_start = n_start;
+  cudaFree(c->d_cell_ids); c->d_cell_ids = n_ids;
+  c->mesh = m;
+  c->grid = g;
+  for (int a = 0; a < 3; a++) {
+    c->node_lo[a] = lo[a];
+    c->node_hi[a] = hi[a];
+  }
   if (c->frame_nodes && c->frame_nodes != nnodes) {
     for (auto& kv : c->frames) cudaFree(kv.second);
     c->frames.clear();
@@ -1461,7 +1501,8 @@ static unsigned char* g_noalloc_base[FVC_NOALLOC_MAX_DEVICES];
 // The array's device address on the context's device (current when this is
 // called).  In host code g_noalloc_scratch only names the array; the address
 // the kernels get is the one cudaGetSymbolAddress returns, looked up on a
-// device's first call and kept.
+// device's first call and kept for the process's life (a cudaDeviceReset
+// would make it stale; the header tells callers not to reset).
 static fvc_status noalloc_base(fvc_ctx* c, unsigned char** base) {
   if (c->device >= FVC_NOALLOC_MAX_DEVICES)
     return fail(c, FVC_ERR_ARG, "fvc_advect_noalloc supports devices 0..%d", FVC_NOALLOC_MAX_DEVICES - 1);

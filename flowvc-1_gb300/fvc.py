@@ -102,7 +102,6 @@ SIGNATURES = {
     "fvc_job_get_stats": (C.c_int, [_vp, C.POINTER(JobStats)]),
     "fvc_stream": (_vp, [_vp]),
     "fvc_job_destroy": (None, [_vp]),
-    "fvc_probe_fp64": (C.c_int, [C.c_int, _dp]),
     "fvc_cet_enable": (C.c_int, [_vp, C.c_int]),
     "fvc_cet_results": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip]),
     "fvc_tracer_residence": (C.c_int, [_vp, C.c_double, C.c_double, _dp]),
@@ -144,16 +143,6 @@ def load(path: str = LIB_PATH):
     if path == LIB_PATH:
         _lib = lib
     return lib
-
-
-def probe_fp64(device=0):
-    """(FP64 fused multiply-adds / s, IEEE divisions / s) measured on the device."""
-    lib = load()
-    r = np.zeros(2)
-    st = lib.fvc_probe_fp64(device, _d(r))
-    if st:
-        raise FvcError(st, "fvc_probe_fp64 failed")
-    return float(r[0]), float(r[1])
 
 
 class PinnedArray:

@@ -221,21 +221,71 @@ def tri_square_mesh(n, jitter=0.2, seed=0, lo=0.0, hi=1.0, ny=None, yhi=None):
 # ---------------------------------------------------------------- flows
 
 
+# ---------------------------------------------------------------- portable sine / cosine
+#
+# Frames are generated on more than one machine (an x86-64 host makes the
+# fixtures, an aarch64 host runs the same tests), and libm's sin / cos may
+# differ between them in the last bit, which a chaotic flow amplifies.  The
+# analytic flows below therefore use this sine and cosine, built from
+# IEEE additions and multiplications only (each a separate numpy ufunc, so
+# nothing is fused): Cody-Waite reduction by pi/2 split in two parts (the
+# first with 33 significant bits, so k * part exactly for the |k| < 2^20 used
+# here), then the Taylor series of sin and cos on [-pi/4, pi/4] to degree
+# 21 / 20 (truncation below 1e-24).  Same bytes on every IEEE machine.
+
+_PIO2_HI = 1.57079632673412561417e+00   # pi/2 to 33 bits
+_PIO2_LO = 6.07710050650619224932e-11   # pi/2 - _PIO2_HI
+_SIN_C = [(-1.0) ** k / math.factorial(2 * k + 1) for k in range(11)]   # r^(2k+1)
+_COS_C = [(-1.0) ** k / math.factorial(2 * k) for k in range(11)]       # r^(2k)
+
+
+def _sincos(x):
+    x = np.asarray(x, np.float64)
+    k = np.rint(x * (2.0 / math.pi))
+    r = (x - k * _PIO2_HI) - k * _PIO2_LO
+    r2 = r * r
+    ps = np.full_like(r, _SIN_C[-1])
+    pc = np.full_like(r, _COS_C[-1])
+    for cs, cc in zip(_SIN_C[-2::-1], _COS_C[-2::-1]):
+        ps = ps * r2 + cs
+        pc = pc * r2 + cc
+    sr, cr = ps * r, pc
+    q = np.mod(k, 4.0)
+    sin = np.where(q == 0, sr, np.where(q == 1, cr, np.where(q == 2, -sr, -cr)))
+    cos = np.where(q == 0, cr, np.where(q == 1, -sr, np.where(q == 2, -cr, sr)))
+    return sin, cos
+
+
+def psin(x):
+    """sin(x), identical bytes on every IEEE-754 machine (|x| < 1e6)."""
+    s = _sincos(x)[0]
+    return float(s) if np.ndim(s) == 0 else s
+
+
+def pcos(x):
+    """cos(x), identical bytes on every IEEE-754 machine (|x| < 1e6)."""
+    c = _sincos(x)[1]
+    return float(c) if np.ndim(c) == 0 else c
+
+
 def double_gyre(x, y, t, A=0.1, eps=0.25, omega=2 * math.pi / 10):
-    s = eps * np.sin(omega * t)
+    s = eps * psin(omega * t)
     f = s * x * x + (1 - 2 * s) * x
     dfdx = 2 * s * x + (1 - 2 * s)
-    u = -math.pi * A * np.sin(math.pi * f) * np.cos(math.pi * y)
-    v = math.pi * A * np.cos(math.pi * f) * np.sin(math.pi * y) * dfdx
+    u = -math.pi * A * psin(math.pi * f) * pcos(math.pi * y)
+    v = math.pi * A * pcos(math.pi * f) * psin(math.pi * y) * dfdx
     return u, v
 
 
 def abc_flow(xyz, t, A=math.sqrt(3), B=math.sqrt(2), C=1.0, amp=0.1):
     x, y, z = xyz[:, 0], xyz[:, 1], xyz[:, 2]
-    g = 1.0 + amp * math.sin(2 * math.pi * t)
-    u = (A * np.sin(z) + C * np.cos(y)) * g
-    v = (B * np.sin(x) + A * np.cos(z)) * g
-    w = (C * np.sin(y) + B * np.cos(x)) * g
+    g = 1.0 + amp * psin(2 * math.pi * t)
+    sx, cx = _sincos(x)
+    sy, cy = _sincos(y)
+    sz, cz = _sincos(z)
+    u = (A * sz + C * cy) * g
+    v = (B * sx + A * cz) * g
+    w = (C * sy + B * cx) * g
     return np.stack([u, v, w], axis=-1)
 
 

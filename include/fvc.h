@@ -170,6 +170,10 @@ fvc_status fvc_advect_device(fvc_ctx *ctx, int n, double *dX, double *dV, int *d
  *   - The first call on a device looks the array's device address up (one
  *     cudaGetSymbolAddress, which loads the library's device code if it is
  *     not loaded yet); make that first call before any stream capture.
+ *   - That address is kept until the process exits.  It does not survive a
+ *     cudaDeviceReset (or any other teardown of the device's primary
+ *     context): the array may then load elsewhere, so a process that resets
+ *     a device must not call this function on that device again.
  *   - All calls, from every context on a device, share the one array and
  *     it keeps the last call's contents.  Calls whose GPU work overlaps
  *     (from several threads, or several contexts on other streams) race and
@@ -399,11 +403,6 @@ fvc_status fvc_batch_get_stats(fvc_batch *batch, fvc_batch_stats *out);
 void *fvc_stream(fvc_ctx *ctx);
 
 void fvc_job_destroy(fvc_job *job);
-
-/* Measured FP64 rates of a device, the denominators of the exact path's
- * FP64 roofline: rates[0] fused multiply-adds / s (one operation each),
- * rates[1] IEEE divisions / s.  No reference counterpart (measurement aid). */
-fvc_status fvc_probe_fp64(int device, double rates[2]);
 
 #ifdef __cplusplus
 }

@@ -121,3 +121,27 @@ def compare_outputs(expected_dir, got_dir, ftle_rtol=FTLE_RTOL, ftle_atol=FTLE_A
         B = np.frombuffer(b, "<f8")
         assert A[0] == B[0], f"{f}: time stamp"
         np.testing.assert_allclose(B[1:], A[1:], rtol=ftle_rtol, atol=ftle_atol, err_msg=f)
+
+
+def compare_state_dumps(dump_expected, dump_got):
+    """FTLE grid states written by `--dump-state` (fvcflow) and ORC_DUMP_STATE
+    (the oracle): int32 n, n x 3 positions, then element ids, left flags and
+    have-FTLE flags (n int32 each).  Positions, left flags and have flags
+    must be identical, element ids wherever the point is still inside."""
+    files = sorted(os.listdir(dump_expected))
+    assert files == sorted(os.listdir(dump_got)), "state dumps differ in number"
+    for f in files:
+        a = np.fromfile(os.path.join(dump_expected, f), np.uint8)
+        b = np.fromfile(os.path.join(dump_got, f), np.uint8)
+        assert a.size == b.size, f"{f}: sizes differ"
+        n = int(a[:4].view(np.int32)[0])
+        Xa = a[4:4 + 24 * n].view(np.float64)
+        Xb = b[4:4 + 24 * n].view(np.float64)
+        ia = a[4 + 24 * n:].view(np.int32).reshape(3, n)
+        ib = b[4 + 24 * n:].view(np.int32).reshape(3, n)
+        live = ia[1] == 0
+        assert np.array_equal(Xa, Xb), f"{f}: positions differ at {int((Xa != Xb).sum())} coordinates"
+        assert np.array_equal(ia[1], ib[1]), f"{f}: left flags differ"
+        assert np.array_equal(ia[2] != 0, ib[2] != 0), f"{f}: have flags differ"
+        assert np.array_equal(ia[0][live], ib[0][live]), f"{f}: element ids differ"
+    return len(files)

@@ -1,9 +1,15 @@
-// fvc_probe.cu -- FP64 issue-rate probes: the denominators of the FP64
-// roofline the exact advection path is measured against (GB300's FP64 rate
-// is a small fraction of its FP32 rate, and no vendor figure is assumed).
-#include <cuda_runtime.h>
+// fp64_rate.cu -- FP64 issue-rate probe of a device: the denominators of the
+// FP64 roofline the exact advection path is measured against (GB300's FP64
+// rate is a small fraction of its FP32 rate, and no vendor figure is
+// assumed).  A measurement aid of the benchmark, not part of the engine.
+//
+//   fp64_rate [device]   prints {"fma_per_s": F, "div_per_s": D}
+//
+// F counts fused multiply-adds (one operation each), D IEEE divisions.
+#include <cstdio>
+#include <cstdlib>
 
-#include "fvc.h"
+#include <cuda_runtime.h>
 
 namespace {
 
@@ -38,18 +44,21 @@ __global__ void k_fp64_div(double* out, int iters, double a) {
   if (s == 12345.678) out[0] = s;
 }
 
+int fail(const char* what, cudaError_t e) {
+  fprintf(stderr, "fp64_rate: %s: %s\n", what, cudaGetErrorString(e));
+  return 1;
+}
+
 }  // namespace
 
-// Measured FP64 rates of this device: rates[0] = fused multiply-adds per
-// second (each counted as one operation), rates[1] = IEEE divisions per
-// second.  Runs on the calling thread's current device, a few milliseconds.
-extern "C" fvc_status fvc_probe_fp64(int device, double rates[2]) {
-  if (!rates) return FVC_ERR_ARG;
-  if (cudaSetDevice(device) != cudaSuccess) return FVC_ERR_CUDA;
+int main(int argc, char** argv) {
+  const int device = argc > 1 ? atoi(argv[1]) : 0;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return fail("cudaSetDevice", e);
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   double* d = nullptr;
-  if (cudaMalloc(&d, sizeof(double)) != cudaSuccess) return FVC_ERR_OOM;
+  if ((e = cudaMalloc(&d, sizeof(double))) != cudaSuccess) return fail("cudaMalloc", e);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -62,16 +71,17 @@ extern "C" fvc_status fvc_probe_fp64(int device, double rates[2]) {
   cudaEventRecord(e1);
   cudaEventSynchronize(e1);
   cudaEventElapsedTime(&ms, e0, e1);
-  rates[0] = (double)blocks * threads * it_fma * 8 / (ms * 1e-3);
+  const double fma_s = (double)blocks * threads * it_fma * 8 / (ms * 1e-3);
   cudaEventRecord(e0);
   k_fp64_div<<<blocks, threads>>>(d, it_div, 1.0000001);
   cudaEventRecord(e1);
   cudaEventSynchronize(e1);
   cudaEventElapsedTime(&ms, e0, e1);
-  rates[1] = (double)blocks * threads * it_div * 8 / (ms * 1e-3);
-  cudaError_t err = cudaGetLastError();
+  const double div_s = (double)blocks * threads * it_div * 8 / (ms * 1e-3);
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail("probe kernels", e);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(d);
-  return err == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+  printf("{\"fma_per_s\": %.6e, \"div_per_s\": %.6e}\n", fma_s, div_s);
+  return 0;
 }

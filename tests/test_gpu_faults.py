@@ -99,6 +99,7 @@ def test_bad_mesh_is_refused_and_the_old_mesh_stays(which):
     device before the old mesh is released: FVC_ERR_ARG naming the lowest
     bad element, and the context keeps working on its old mesh."""
     ctx, ax = cube_ctx()
+    ctx.cet_enable(3)  # exposure-time sums on the old mesh must survive the refusal
     xyz, conn, adj = synth.kuhn_cube_mesh(4, jitter=0.2, seed=1)
     conn, adj = conn.copy(), adj.copy()
     if which == "node":
@@ -110,9 +111,41 @@ def test_bad_mesh_is_refused_and_the_old_mesh_stays(which):
         ctx.set_unstruct_mesh(xyz, conn, adj)
     assert e.value.status == fvc.FVC_ERR_ARG
     assert "element 9" in str(e.value)
+    old_mesh_still_works(ctx)
+    ctx.close()
+
+
+def old_mesh_still_works(ctx):
+    """The 6^3 cube of cube_ctx is still the context's mesh: global search,
+    advection and the exposure-time sums (enabled by the caller) on it."""
+    nelem = 6 * 6 ** 3
+    cet, met, enc = ctx.cet_results(1, nelem)  # still enabled, still sized for the old mesh
+    assert len(enc) == nelem and (enc == 0).all()
     ctx.set_window(0, 1, 0.0, 0.02)
     P = synth.uniform_seeds(64, 3, seed=1)
     eid = ctx.global_search(P)
     assert (eid >= 0).all()
     assert ctx.advect(*advect_args(P, eid), 0.0, 0.02) > 0
+
+
+def test_bucket_grid_failure_keeps_the_old_mesh(monkeypatch):
+    """A valid mesh whose bucket grid cannot be built (here: a cell cap far
+    below what the mesh needs) is refused after its records were made; the
+    context keeps its old mesh, grid and exposure-time sums, and a later mesh
+    within the cap is accepted."""
+    ctx, ax = cube_ctx()
+    ctx.cet_enable(2)
+    xyz, conn, adj = synth.kuhn_cube_mesh(8, jitter=0.2, seed=1)
+    monkeypatch.setenv("FVC_BUCKET_MAX_CELLS", "16")
+    with pytest.raises(fvc.FvcError) as e:
+        ctx.set_unstruct_mesh(xyz, conn, adj)
+    assert e.value.status == fvc.FVC_ERR_ARG and "bucket grid" in str(e.value)
+    old_mesh_still_works(ctx)
+    monkeypatch.delenv("FVC_BUCKET_MAX_CELLS")
+    ctx.set_unstruct_mesh(xyz, conn, adj)  # within the default cap: replaces the mesh
+    with pytest.raises(fvc.FvcError) as e:
+        ctx.cet_results(1, len(conn))  # the old mesh's sums went with it
+    assert e.value.status == fvc.FVC_ERR_STATE
+    P = synth.uniform_seeds(64, 3, seed=2)
+    assert (ctx.global_search(P) >= 0).all()
     ctx.close()

@@ -8,7 +8,8 @@ import os
 import numpy as np
 import pytest
 
-from conftest import CET_RTOL, GOLDEN, compare_outputs, golden_cases, run_golden, undefined_files
+from conftest import (CET_RTOL, GOLDEN, compare_outputs, compare_state_dumps, golden_cases, run_golden,
+                      undefined_files)
 
 pytestmark = pytest.mark.gpu
 
@@ -62,16 +63,4 @@ def test_engine_matches_reference(engine, oracle_bin, tmp_path, case, run):
         del os.environ["ORC_DUMP_STATE"]
     # against the oracle: FTLE to a few ulps (CUDA's log vs glibc's), the rest exact
     compare_outputs(orc, got, ftle_rtol=1e-14, ftle_atol=1e-15, cet_rtol=CET_RTOL)
-    for f in sorted(os.listdir(dump_o)):
-        a = np.fromfile(dump_o / f, np.uint8)
-        b = np.fromfile(dump_g / f, np.uint8)
-        n = int(a[:4].view(np.int32)[0])
-        Xa = a[4:4 + 24 * n].view(np.float64)
-        Xb = b[4:4 + 24 * n].view(np.float64)
-        ia = a[4 + 24 * n:].view(np.int32).reshape(3, n)
-        ib = b[4 + 24 * n:].view(np.int32).reshape(3, n)
-        live = ia[1] == 0
-        assert np.array_equal(Xa, Xb), f"{f}: positions differ"
-        assert np.array_equal(ia[1], ib[1]), f"{f}: left flags differ"
-        assert np.array_equal(ia[2] != 0, ib[2] != 0), f"{f}: have flags differ"
-        assert np.array_equal(ia[0][live], ib[0][live]), f"{f}: element ids differ"
+    compare_state_dumps(str(dump_o), str(dump_g))

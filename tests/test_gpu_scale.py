@@ -1,0 +1,72 @@
+"""The GPU engine at the benchmark configurations' full sizes, against the
+oracle on the same inputs and against ompVC's own outputs.
+
+Each case (tests/scale_cases.py) runs through fvcflow, the drop-in program
+over libfvc, in the FP64 form:
+  - against ompVC (committed digests and FTLE summaries): tracer files and
+    FTLE .info / _Cartesian files byte-identical, FTLE fields within the
+    tolerance of conftest through every 509th value and block sums;
+  - against the oracle run here on the same inputs: final FTLE grid states
+    bit-identical (positions, element ids of points inside, left and
+    have-FTLE flags), FTLE fields within a few ulps (CUDA's log against
+    glibc's).
+These are the sizes where the engine's shortcuts are exercised: the
+per-step record the early-FTLE tasks read, the step-1 element-state check,
+the three-level seed chain and hint ties on shared faces."""
+import os
+import subprocess
+
+import pytest
+
+import scale_cases as sc
+from conftest import FTLE_ATOL, FTLE_RTOL, compare_outputs, compare_state_dumps
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scale_data(tmp_path_factory):
+    meta, arrays = sc.load_fixture()
+    return str(tmp_path_factory.mktemp("scale")), meta, arrays
+
+
+def run_both(engine, oracle_bin, case, root, meta):
+    kind, _ = sc.CASES[case]
+    data = sc.make_inputs(kind, root)
+    assert sc.input_digests(data) == meta["inputs"][kind], "generated inputs differ from ompVC's"
+    out = {}
+    for name, exe, extra in (("gpu", engine.FVCFLOW, ["--dump-state"]), ("orc", oracle_bin, [])):
+        o = os.path.join(root, f"{name}_{case}")
+        dump = os.path.join(root, f"{name}_{case}_state")
+        os.makedirs(dump, exist_ok=True)
+        inp = sc.write_in(case, data, o, os.path.join(root, f"{name}_{case}.in"))
+        env = dict(os.environ)
+        args = [exe, inp]
+        if name == "gpu":
+            args += [extra[0], dump]
+        else:
+            env["ORC_DUMP_STATE"] = dump
+            args += [str(os.cpu_count() or 1)]
+        r = subprocess.run(args, capture_output=True, text=True, env=env, timeout=900)
+        assert r.returncode == 0, f"{name} failed on {case}:\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}"
+        out[name] = (o, dump)
+    return out
+
+
+@pytest.mark.parametrize("case", ["cube_ftle_5", "cube_ftle", "dg_ftle"])
+def test_engine_ftle_at_scale(engine, oracle_bin, scale_data, case):
+    root, meta, arrays = scale_data
+    out = run_both(engine, oracle_bin, case, root, meta)
+    (g, gdump), (o, odump) = out["gpu"], out["orc"]
+    sc.check_exact_files(case, g, meta)
+    worst = sc.check_ftle_against_fixture(case, g, meta, arrays, rtol=FTLE_RTOL, atol=FTLE_ATOL)
+    compare_outputs(o, g, ftle_rtol=1e-14, ftle_atol=1e-15)
+    assert compare_state_dumps(odump, gdump) == 1
+    print(case, "largest relative FTLE difference from ompVC (strided values):", worst)
+
+
+def test_engine_tracers_at_scale(engine, oracle_bin, scale_data):
+    root, meta, arrays = scale_data
+    out = run_both(engine, oracle_bin, "cube_tracers", root, meta)
+    sc.check_exact_files("cube_tracers", out["gpu"][0], meta)
+    compare_outputs(out["orc"][0], out["gpu"][0])

@@ -100,6 +100,26 @@ def test_noalloc_cart2_matches_advect_twice(engine):
     g.close()
 
 
+def test_noalloc_allocates_no_device_memory(engine):
+    """The entry point's own claim: calls of different sizes leave the
+    device's free memory unchanged, on a context that has never run
+    fvc_advect (so no pool or scratch of the context exists to reuse).  One
+    warm-up call comes first: the driver may load the kernels' code on their
+    first launch, which is not an allocation of this library."""
+    torch = pytest.importorskip("torch")
+    g = tet_context(1, 0)
+    rng = np.random.default_rng(11)
+    calls = [points(g, n, rng, 3) for n in (64, 17, 5000, header_limit())]
+    g.advect_noalloc(*[x.copy() for x in calls[0]], 0.3, 0.33)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    for st in calls[1:]:
+        assert g.advect_noalloc(*[x.copy() for x in st], 0.3, 0.35) > 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(0)[0] == free0, "fvc_advect_noalloc changed the device's free memory"
+    g.close()
+
+
 def test_noalloc_at_its_limit_and_beyond(engine):
     limit = header_limit()
     g = tet_context(1, 0)
