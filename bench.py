@@ -46,8 +46,10 @@ tracers    the cube's second workload: 1M tracers released at t = 0, outputs
            every 10 steps, FP64 and BF16 forms.
 batched    the bent-tube batch of 64 tracer releases (uneven seed counts and
            windows) in the BF16 form and the FP64 form, one CUDA graph each.
-served     a Poisson request stream over the tube and the cube, served in the
-           BF16 and FP64 forms: p50 / p95 / p99 latency and steps/s.
+served     a Poisson request stream over the tube and the cube (200 requests/s
+           for 60 s at the served workload's sizes), served in the BF16 and
+           FP64 forms: p50 / p95 / p99 latency and steps/s; a form that cannot
+           keep up is stopped and reported with its backlog.
 
 --impl reference runs that CPU implementation alone on the same workload
 (every step one whole T = 1 window), on the same metric.  Multi-GPU (torchrun, N > 1): every rank runs the
@@ -107,7 +109,9 @@ def parse():
     ap.add_argument("--no-parity", action="store_true", help="skip the parity window")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--served-rate", type=float, default=200.0, help="requests / s")
-    ap.add_argument("--served-seconds", type=float, default=10.0, help="arrival window, s")
+    ap.add_argument("--served-seconds", type=float, default=60.0, help="arrival window, s")
+    ap.add_argument("--served-sweep", action="store_true", help="add a rate sweep of the served form")
+    ap.add_argument("--sweep-seconds", type=float, default=15.0, help="arrival window of each sweep point, s")
     return ap.parse_args()
 
 
@@ -469,7 +473,8 @@ def bench_tracers(args, inputs):
     ax = flow.TimeAxis(0.0, DT, NFRAMES, 0)
     seeds = synth.uniform_seeds(args.tracers, 3, seed=0)
     out = {"workload": f"{args.tracers} tracers uniform in the cube at t=0, T={T_WINDOW}, RK4 h={H}, "
-                       "positions output every 10 steps (21 outputs copied to the host)"}
+                       "positions output every 10 steps (21 outputs, each copied to host memory by a writer "
+                       "thread)"}
     finals = {}
     for prec in ("fp64", "bf16"):
         ctx = fvc.Context(3, 1)
@@ -479,13 +484,26 @@ def bench_tracers(args, inputs):
         ctx.set_precision(prec)
         flow.upload_frames(ctx, ax, frames)
         flow.run_tracers(ctx, ax, seeds[:4096], 0.0, 0.05, 21)          # warm-up
+        flow.run_tracers(ctx, ax, seeds[:4096], 0.0, 0.05, 21, asynchronous=False)
+        # the blocking loop (each advance waits, each output is a blocking
+        # compact-and-copy), for comparison
+        t0 = time.perf_counter()
+        outs_b, steps_b, _ = flow.run_tracers(ctx, ax, seeds, 0.0, 0.05, 21, asynchronous=False)
+        wall_b = time.perf_counter() - t0
+        # the release loop as it runs: advances queued, outputs through the
+        # output ring to a writer thread that copies each into host memory
         t0 = time.perf_counter()
         fin = {}
         outs, steps, st = flow.run_tracers(ctx, ax, seeds, 0.0, 0.05, 21, state=fin)
         wall = time.perf_counter() - t0
         finals[prec] = fin
+        same = len(outs) == len(outs_b) and all(np.array_equal(x, y) for x, y in zip(outs, outs_b))
         out[prec] = {"value": steps / wall, "unit": "steps/s", "steps": int(steps), "wall_s": wall,
+                     "kernel_s": st["ms_main"] / 1e3,
                      "kernel_value": st["steps_main"] / (st["ms_main"] / 1e3) if st["ms_main"] > 0 else None,
+                     "wall_over_kernel": wall / (st["ms_main"] / 1e3) if st["ms_main"] > 0 else None,
+                     "blocking_wall_s": wall_b, "blocking_value": steps_b / wall_b,
+                     "outputs_identical_to_blocking": bool(same and steps == steps_b),
                      "outputs": len(outs), "written": int(sum(len(o) for o in outs))}
         ctx.close()
     # final tracer states: endpoints (the last position inside for tracers that
@@ -539,32 +557,54 @@ def bench_batched(args, tube, frames):
 
 
 def bench_served(args, tube, frames, cube_inputs):
-    """A request stream over both resident data sets: Poisson arrivals for
-    args.served_seconds, 50% tracer releases on the tube, 40% FTLE grids on
-    the cube, 10% residence-time releases on the tube; admission by an HBM
-    budget; latency from arrival to results on the host.  The same stream is
-    served in the BF16 form and in the FP64 form."""
+    """The served workload: a Poisson request stream over both resident data
+    sets for args.served_seconds at args.served_rate requests/s, 50% tracer
+    releases on the tube (1e3-1e6 seeds, log-uniform), 40% FTLE grids on the
+    cube (32^3-128^3), 10% residence-time releases on the tube (1e5 seeds, 3
+    periods); admission by an HBM budget; latency from arrival to results on
+    the host.  The same stream is served in the BF16 form and in the FP64
+    form; a form that cannot keep up is stopped after the arrival window plus
+    a grace period and reported as such (finished requests' latencies, the
+    backlog).  args.served_sweep adds, per form, shorter streams at a range of
+    rates and the highest rate that was sustained."""
     import serve
     xyz, conn, adj, cframes = cube_inputs
-    kw = dict(rate=args.served_rate, duration=args.served_seconds, seed=7)
-    out = {"workload": f"Poisson {args.served_rate:g} requests/s for {args.served_seconds:g} s: 50% tracer releases "
-                       "(tube, 1e3-1e5 seeds log-uniform, 0.2-2 periods), 40% FTLE grids (cube, 16^3-48^3, T=1), "
-                       "10% residence time (tube, 1e4 seeds, 3 periods)",
-           "hbm_budget_bytes": SERVED_BUDGET}
-    for prec in ("bf16", "fp64"):
-        reqs = serve.poisson_requests(tube, **kw)
-        frame_bytes = 32 * (len(tube.xyz) * serve.TUBE_FRAMES + len(xyz) * len(cframes))
-        budget = max((SERVED_BUDGET - frame_bytes) // 2, 1)
+    frame_bytes = 32 * (len(tube.xyz) * serve.TUBE_FRAMES + len(xyz) * len(cframes))
+    budget = max((SERVED_BUDGET - frame_bytes) // 2, 1)
+
+    def run(prec, rate, duration, limit, seed=7):
+        reqs = serve.poisson_requests(tube, rate=rate, duration=duration, seed=seed)
         sites = {"tube": serve.tube_site(prec, tube=tube, frames=frames, hbm_budget=budget),
                  "cube": serve.cube_site(prec, mesh=(xyz, conn, adj), frames=cframes, hbm_budget=budget)}
         serve.warm_pairs(sites["tube"])
         serve.run_batched(sites["cube"], [("ftle", (0, 1, 0, 1, 0, 1, 8, 8, 8), 0.0, 1.0)], graph=False, tune=False)
-        r = serve.serve(sites, reqs)
-        out[prec] = r
-        out["requests"] = r["requests"]
+        r = serve.serve(sites, reqs, time_limit=limit, censor=True)
+        r["offered_rate"] = rate
+        r["sustained"] = serve.sustained(r, reqs, duration)
         for st in sites.values():
             st.close()
+        return r
+
+    out = {"workload": f"Poisson {args.served_rate:g} requests/s for {args.served_seconds:g} s: 50% tracer releases "
+                       "(tube, 1e3-1e6 seeds log-uniform, 0.2-2 periods, +-direction), 40% FTLE grids (cube, "
+                       "32^3-128^3, T=1), 10% residence time (tube, 1e5 seeds, 3 periods)",
+           "hbm_budget_bytes": SERVED_BUDGET}
+    limits = {"bf16": args.served_seconds + 240.0, "fp64": args.served_seconds + 30.0}
+    for prec in ("bf16", "fp64"):
+        out[prec] = run(prec, args.served_rate, args.served_seconds, limits[prec])
+        out["requests"] = out[prec].get("requests_total", out[prec]["requests"])
     out["speedup_vs_fp64"] = out["bf16"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    if args.served_sweep:
+        sweep = {}
+        for prec, rates in (("bf16", (25, 50, 100, 150, 200, 300)), ("fp64", (1, 2, 5, 10, 20))):
+            rows = []
+            for rate in rates:
+                r = run(prec, rate, args.sweep_seconds, args.sweep_seconds + 20.0, seed=11)
+                rows.append({k: r.get(k) for k in ("offered_rate", "requests", "requests_unfinished", "steps_per_s",
+                                                  "p50_ms", "p95_ms", "p99_ms", "sustained")})
+            ok = [x["offered_rate"] for x in rows if x["sustained"]]
+            sweep[prec] = {"rows": rows, "max_sustained_rate": max(ok) if ok else None}
+        out["rate_sweep"] = sweep
     return out
 
 

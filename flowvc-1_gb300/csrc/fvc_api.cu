@@ -105,6 +105,8 @@ void unpack_host(double* A, size_t n) {
 
 // ------------------------------------------------------------------ context
 
+static void out_free(fvc_ctx* c);
+
 extern "C" int fvc_abi_version(void) { return FVC_ABI_VERSION; }
 
 extern "C" fvc_status fvc_create(fvc_ctx** out, const fvc_opts* o) {
@@ -159,6 +161,7 @@ extern "C" void fvc_destroy(fvc_ctx* c) {
   cudaFree(c->d_vt);
   cudaFree(c->d_cet_sum);
   cudaFree(c->d_cet_enc);
+  out_free(c);
   if (c->up_stream) {
     cudaStreamSynchronize(c->up_stream);
     cudaStreamDestroy(c->up_stream);
@@ -945,13 +948,15 @@ static fvc_status job_sync(fvc_job* j, const char* what) {
     return fail(c, FVC_ERR_TLOC, "%s: query time outside the loaded frame interval", what);
   if (h.status & PT_ERR_WALK)
     return fail(c, FVC_ERR_WALK, "%s: neighbour walk failed (indeterminate neighbour or hop cap)", what);
+  if (h.status & PT_ERR_CET)
+    return fail(c, FVC_ERR_WALK, "%s: exposure time: a step started outside the velocity domain", what);
   return FVC_OK;
 }
 
 extern "C" fvc_status fvc_job_get_stats(fvc_job* j, fvc_job_stats* out) {
   if (!j || !out) return FVC_ERR_ARG;
   fvc_status st = FVC_OK;
-  if (j->d_ctr && use_device(j->ctx) == FVC_OK) st = job_sync(j, "ftle interval");
+  if (j->d_ctr && use_device(j->ctx) == FVC_OK) st = job_sync(j, j->kind == 1 ? "tracer advance" : "ftle interval");
   *out = j->stats;
   return st;
 }
@@ -1322,6 +1327,7 @@ extern "C" fvc_status fvc_tracer_residence(fvc_job* j, double launch_time, doubl
   fvc_ctx* c = j->ctx;
   fvc_status st;
   if ((st = use_device(c))) return st;
+  if ((st = job_sync(j, "tracer advance"))) return st;
   size_t n = (size_t)j->t.n;
   if (n == 0) return FVC_OK;
   if ((st = ensure_scratch(c, 8 * n))) return st;
@@ -1409,6 +1415,31 @@ extern "C" fvc_status fvc_tracer_launch(fvc_job* j, double t_start) {
   return finish(c, "tracer launch", nullptr);
 }
 
+// The job's own counters (FTLE intervals and tracer advances run on them
+// asynchronously; job_sync reads and clears them).
+static fvc_status job_counters(fvc_job* j) {
+  if (j->d_ctr) return FVC_OK;
+  fvc_ctx* c = j->ctx;
+  if (cudaMalloc(&j->d_ctr, sizeof(DevCounters)) != cudaSuccess) return fail(c, FVC_ERR_OOM, "job counters");
+  FVC_CUDA(c, cudaMemsetAsync(j->d_ctr, 0, sizeof(DevCounters), c->stream));
+  return FVC_OK;
+}
+
+// Three events of an asynchronous call, accounted by job_sync as (main
+// start, main end, early end).
+static fvc_status job_event_triple(fvc_job* j, cudaEvent_t ev[3]) {
+  for (int k = 0; k < 3; k++) {
+    if (!j->spare.empty()) {
+      ev[k] = j->spare.back();
+      j->spare.pop_back();
+    } else if (cudaEventCreate(&ev[k]) != cudaSuccess) {
+      return fail(j->ctx, FVC_ERR_CUDA, "event creation failed");
+    }
+    j->pend.push_back(ev[k]);
+  }
+  return FVC_OK;
+}
+
 extern "C" fvc_status fvc_tracer_advance(fvc_job* j, double t1, double t2, long long* steps) {
   if (!j || j->kind != 1) return FVC_ERR_ARG;
   fvc_ctx* c = j->ctx;
@@ -1419,20 +1450,193 @@ extern "C" fvc_status fvc_tracer_advance(fvc_job* j, double t1, double t2, long 
   if ((st = mixed_ok(c))) return st;
   if ((st = cet_ok(c, j))) return st;
   if ((st = prepare_slots(c, t1, t2))) return st;
-  compact_live(j->t.n, j->t.ldt, j->t.left, c->integ.extrapolate, j->t.live, nullptr, j->t.block_cnt, c->d_ctr,
+  if ((st = job_counters(j))) return st;
+  cudaEvent_t ev[3];
+  if ((st = job_event_triple(j, ev))) return st;
+  compact_live(j->t.n, j->t.ldt, j->t.left, c->integ.extrapolate, j->t.live, nullptr, j->t.block_cnt, j->d_ctr,
                c->stream);
-  cudaEventRecord(j->ev[0], c->stream);
-  if (c->cet_sub) tracer_advance_cet(c->mesh, c->window, c->integ, j->t, t1, t2, cet_dev(c), c->d_ctr, c->stream);
-  else tracer_advance(c->mesh, c->window, c->integ, j->t, t1, t2, c->d_ctr, c->stream);
-  cudaEventRecord(j->ev[1], c->stream);
+  cudaEventRecord(ev[0], c->stream);
+  if (c->cet_sub) tracer_advance_cet(c->mesh, c->window, c->integ, j->t, t1, t2, cet_dev(c), j->d_ctr, c->stream);
+  else tracer_advance(c->mesh, c->window, c->integ, j->t, t1, t2, j->d_ctr, c->stream);
+  cudaEventRecord(ev[1], c->stream);
+  cudaEventRecord(ev[2], c->stream);
   if ((st = check_launch(c, "tracer advance"))) return st;
-  DevCounters h{};
-  st = finish(c, "tracer advance", steps, &h);
   j->stats.intervals++;
-  j->stats.launches += 5;
-  j->stats.steps_main += (long long)h.steps;
-  j->stats.ms_main += ev_ms(j->ev[0], j->ev[1]);
+  j->stats.launches += 5 + c->aux_launches;
+  c->aux_launches = 0;
+  if (!steps) return FVC_OK;  // asynchronous: accounted by the next call that waits
+  const long long before = j->stats.steps_main;
+  st = job_sync(j, "tracer advance");
+  *steps = j->stats.steps_main - before;
   return st;
+}
+
+// ------------------------------------------------------ asynchronous outputs
+
+// Frees the output ring (its device and page-locked blocks start at slot 0).
+static void out_free(fvc_ctx* c) {
+  if (c->out_stream) cudaStreamSynchronize(c->out_stream);
+  cudaFree(c->out[0].d);
+  cudaFreeHost(c->out[0].h);
+  for (auto& o : c->out) {
+    o.d = nullptr;
+    o.h = nullptr;
+    o.hc = nullptr;
+    if (o.copied) cudaEventDestroy(o.copied);
+    if (o.compacted) cudaEventDestroy(o.compacted);
+    o.copied = o.compacted = nullptr;
+    o.ticket = -1;
+    o.busy = false;
+  }
+  c->out_rows_cap = 0;
+  if (c->out_stream) cudaStreamDestroy(c->out_stream);
+  c->out_stream = nullptr;
+}
+
+// The ring's buffers with room for `rows` rows a slot: one device block and
+// one page-locked block (positions, then the slots' counts and statuses).
+static fvc_status out_reserve(fvc_ctx* c, size_t rows) {
+  if (rows <= c->out_rows_cap && c->out[0].d) return FVC_OK;
+  {
+    std::lock_guard<std::mutex> lock(c->out_mu);
+    for (auto& o : c->out)
+      if (o.busy) return fail(c, FVC_ERR_STATE, "tracer outputs of a smaller job are still held: release them first");
+  }
+  if (!c->out_stream && cudaStreamCreateWithFlags(&c->out_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(c, FVC_ERR_CUDA, "output stream");
+  cudaStreamSynchronize(c->out_stream);
+  void* hold = c->out[0].h;
+  cudaFree(c->out[0].d);
+  cudaFreeHost(hold);
+  for (auto& o : c->out) {
+    o.d = nullptr;
+    o.h = nullptr;
+    o.hc = nullptr;
+  }
+  const size_t slot = al256(24 * rows);
+  const int ns = FVC_TRACER_OUTPUT_SLOTS;
+  unsigned char *d = nullptr, *h = nullptr;
+  if (cudaMalloc(&d, slot * ns) != cudaSuccess) return fail(c, FVC_ERR_OOM, "tracer output ring (device)");
+  if (cudaMallocHost(&h, slot * ns + 256) != cudaSuccess) {
+    cudaFree(d);
+    return fail(c, FVC_ERR_OOM, "tracer output ring (page-locked host)");
+  }
+  for (int k = 0; k < ns; k++) {
+    auto& o = c->out[k];
+    o.d = (double*)(d + k * slot);
+    o.h = (double*)(h + k * slot);
+    o.hc = (int*)(h + ns * slot) + 2 * k;
+    o.ticket = -1;
+    o.busy = false;
+    if ((!o.copied && cudaEventCreateWithFlags(&o.copied, cudaEventDisableTiming) != cudaSuccess) ||
+        (!o.compacted && cudaEventCreateWithFlags(&o.compacted, cudaEventDisableTiming) != cudaSuccess))
+      return fail(c, FVC_ERR_CUDA, "output event");
+  }
+  c->out_rows_cap = rows;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_tracer_output_begin(fvc_job* j, int always, long long* ticket) {
+  if (!j || j->kind != 1 || !ticket) return FVC_ERR_ARG;
+  fvc_ctx* c = j->ctx;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  if ((st = job_counters(j))) return st;
+  const size_t n = (size_t)j->t.n;
+  if ((st = out_reserve(c, n > 0 ? n : 1))) return st;
+  int k;
+  {
+    std::lock_guard<std::mutex> lock(c->out_mu);
+    k = (int)(c->out_next % FVC_TRACER_OUTPUT_SLOTS);
+    if (c->out[k].busy)
+      return fail(c, FVC_ERR_STATE, "all %d tracer output slots are held: release output %lld first",
+                  FVC_TRACER_OUTPUT_SLOTS, c->out[k].ticket);
+    // completed outputs of this job bound the next one's count
+    for (auto& o : c->out)
+      if (o.n == (long long)n && o.ticket >= 0 && o.hc && cudaEventQuery(o.copied) == cudaSuccess &&
+          o.tag == (const void*)j && (j->out_bound < 0 || o.hc[0] < j->out_bound))
+        j->out_bound = o.hc[0];
+    cudaGetLastError();  // cudaEventQuery's cudaErrorNotReady is not an error
+  }
+  auto& o = c->out[k];
+  cudaStream_t s = c->stream;
+  // the slot's previous copy must be done before its buffer is rewritten
+  FVC_CUDA(c, cudaStreamWaitEvent(s, o.copied, 0));
+  TracerDev t = j->t;
+  t.outX = o.d;
+  tracer_compact(t, always, j->d_ctr, s);
+  if (j->packed) unpack_pairs_counted(o.d, (long)n, &j->d_ctr->count, s);
+  if ((st = check_launch(c, "tracer output"))) return st;
+  j->stats.launches += 5 + (j->packed ? 1 : 0);
+  FVC_CUDA(c, cudaMemcpyAsync(o.hc, &j->d_ctr->count, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FVC_CUDA(c, cudaMemcpyAsync(o.hc + 1, &j->d_ctr->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  // the copy runs on the side stream after the compaction; its length is a
+  // bound on the count (the last completed output's count, else every
+  // tracer), and wait() copies the rest in the rare case the bound was short
+  const long long rows = j->out_bound >= 0 ? j->out_bound : (long long)n;
+  FVC_CUDA(c, cudaEventRecord(o.compacted, s));
+  FVC_CUDA(c, cudaStreamWaitEvent(c->out_stream, o.compacted, 0));
+  if (rows > 0)
+    FVC_CUDA(c, cudaMemcpyAsync(o.h, o.d, 24 * (size_t)rows, cudaMemcpyDeviceToHost, c->out_stream));
+  FVC_CUDA(c, cudaEventRecord(o.copied, c->out_stream));
+  {
+    std::lock_guard<std::mutex> lock(c->out_mu);
+    o.rows = rows;
+    o.n = (long long)n;
+    o.tag = (const void*)j;
+    o.ticket = c->out_next++;
+    o.busy = true;
+    *ticket = o.ticket;
+  }
+  return FVC_OK;
+}
+
+static fvc_ctx::OutSlot* out_find(fvc_ctx* c, long long ticket) {
+  for (auto& o : c->out)
+    if (o.busy && o.ticket == ticket) return &o;
+  return nullptr;
+}
+
+extern "C" fvc_status fvc_tracer_output_wait(fvc_ctx* c, long long ticket, const double** X, long long* count) {
+  if (!c || !X || !count) return FVC_ERR_ARG;
+  fvc_ctx::OutSlot* o;
+  {
+    std::lock_guard<std::mutex> lock(c->out_mu);
+    o = out_find(c, ticket);
+  }
+  if (!o) return FVC_ERR_STATE;
+  if (cudaSetDevice(c->device) != cudaSuccess || cudaEventSynchronize(o->copied) != cudaSuccess)
+    return FVC_ERR_CUDA;
+  const int status = o->hc[1];
+  if (status & PT_ERR_STATE) return FVC_ERR_STATE;
+  if (status & PT_ERR_TLOC) return FVC_ERR_TLOC;
+  if (status & (PT_ERR_WALK | PT_ERR_CET)) return FVC_ERR_WALK;
+  const long long cnt = o->hc[0];
+  if (cnt > o->rows) {
+    // the bound was short: the rest of the rows, from the slot (intact
+    // until released), on a stream of this call's own
+    cudaStream_t s2 = nullptr;
+    if (cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) != cudaSuccess) return FVC_ERR_CUDA;
+    cudaError_t e = cudaMemcpyAsync(o->h + 3 * o->rows, o->d + 3 * o->rows, 24 * (size_t)(cnt - o->rows),
+                                    cudaMemcpyDeviceToHost, s2);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s2);
+    cudaStreamDestroy(s2);
+    if (e != cudaSuccess) return FVC_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(c->out_mu);
+    o->rows = cnt;
+  }
+  *X = o->h;
+  *count = cnt;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_tracer_output_release(fvc_ctx* c, long long ticket) {
+  if (!c) return FVC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(c->out_mu);
+  fvc_ctx::OutSlot* o = out_find(c, ticket);
+  if (!o) return FVC_ERR_STATE;
+  o->busy = false;
+  return FVC_OK;
 }
 
 extern "C" fvc_status fvc_tracer_snapshot(fvc_job* j, int always, double* X_out, long long* count) {
@@ -1440,6 +1644,7 @@ extern "C" fvc_status fvc_tracer_snapshot(fvc_job* j, int always, double* X_out,
   fvc_ctx* c = j->ctx;
   fvc_status st;
   if ((st = use_device(c))) return st;
+  if ((st = job_sync(j, "tracer advance"))) return st;  // faults of queued advances
   tracer_compact(j->t, always, c->d_ctr, c->stream);
   if ((st = check_launch(c, "tracer snapshot"))) return st;
   j->stats.launches += 5;
@@ -1459,6 +1664,7 @@ extern "C" fvc_status fvc_tracer_get_state(fvc_job* j, double* X, int* eid, int*
   fvc_ctx* c = j->ctx;
   fvc_status st;
   if ((st = use_device(c))) return st;
+  if ((st = job_sync(j, "tracer advance"))) return st;
   size_t n = (size_t)j->t.n;
   cudaStream_t s = c->stream;
   if (n == 0) return FVC_OK;

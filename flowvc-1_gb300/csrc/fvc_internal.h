@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <map>
+#include <mutex>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -77,6 +78,26 @@ struct fvc_ctx {
   // sizes again and again; reuse is ordered by the context's stream
   std::multimap<size_t, void*> pool;
   size_t pool_bytes = 0;
+  // asynchronous tracer outputs: a ring of FVC_TRACER_OUTPUT_SLOTS slots,
+  // each a device buffer for one compacted output and a page-locked host
+  // copy, filled on a side stream; tickets number the outputs of the context
+  struct OutSlot {
+    double* d = nullptr;        // compacted positions (device)
+    double* h = nullptr;        // page-locked copy
+    int* hc = nullptr;          // page-locked [count, status]
+    cudaEvent_t compacted = nullptr;  // the compaction into d finished (context stream)
+    cudaEvent_t copied = nullptr;     // the copy to h finished (side stream)
+    const void* tag = nullptr;  // the job the output came from (compared, never dereferenced)
+    long long ticket = -1;      // output in the slot, -1 none
+    long long rows = 0;         // rows the side-stream copy moved
+    long long n = 0;            // tracers of the output's job (its largest count)
+    bool busy = false;          // begun and not released
+  };
+  OutSlot out[FVC_TRACER_OUTPUT_SLOTS];
+  size_t out_rows_cap = 0;      // rows each slot has room for
+  long long out_next = 0;       // the next ticket
+  cudaStream_t out_stream = nullptr;
+  std::mutex out_mu;            // the slots' ticket / busy state (waits may come from another thread)
   // exposure time (Trace_CETCompute): per-element sums shared by all releases
   double* d_cet_sum = nullptr;
   int* d_cet_enc = nullptr;
@@ -105,6 +126,9 @@ struct fvc_job {
   DevCounters* d_ctr = nullptr;
   std::vector<cudaEvent_t> pend;
   std::vector<cudaEvent_t> spare;
+  // tracers: the largest output count a completed output of this job had
+  // (outputs only shrink: a tracer that left stays left), -1 unknown
+  long long out_bound = -1;
 };
 
 // ---- helpers defined in fvc_api.cu

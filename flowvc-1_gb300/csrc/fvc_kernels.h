@@ -201,6 +201,9 @@ void pair_frames(const ushort4* a, const ushort4* b, long n, uint4* out, cudaStr
 // FP64 values <-> (X, c) float pairs in place (X = RN(v), c = RN(X - v)).
 void pack_pairs(double* A, long n, cudaStream_t s);
 void unpack_pairs(double* A, long n, cudaStream_t s);
+// unpack_pairs over the first *count rows of 3 slots (count on the device,
+// at most max_rows)
+void unpack_pairs_counted(double* A, long max_rows, const int* count, cudaStream_t s);
 
 // ---- utilities
 void outside_domain_flags(const DevMesh& m, int n, const double* X, int* left0, cudaStream_t s);

@@ -92,6 +92,15 @@ __global__ void k_unpack_pairs(double* A, long n) {
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     A[i] = join_pos(reinterpret_cast<const float2*>(A)[i]);
 }
+// unpack the first 3 * (*count) slots (a count on the device)
+__global__ void k_unpack_pairs_counted(double* A, const int* count) {
+  const long n = 3L * *count;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    A[i] = join_pos(reinterpret_cast<const float2*>(A)[i]);
+}
+void unpack_pairs_counted(double* A, long max_rows, const int* count, cudaStream_t s) {
+  if (max_rows > 0) k_unpack_pairs_counted<<<nblk_q(3 * max_rows, 256), 256, 0, s>>>(A, count);
+}
 void pack_pairs(double* A, long n, cudaStream_t s) {
   if (n > 0) k_pack_pairs<<<nblk_q(n, 256), 256, 0, s>>>(A, n);
 }

@@ -105,44 +105,120 @@ def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, 
     return out[0], out[1], steps, st
 
 
+class OutputWriter:
+    """Takes a release's asynchronous outputs (fvc_tracer_output_wait) on a
+    thread of its own, in ticket order, hands each to consume(index, array)
+    and frees its slot, so the loop that advances the tracers never waits for
+    the GPU.  consume runs on the writer thread and must copy what it keeps
+    (the array is the library's page-locked slot).  At most `slots` outputs
+    are outstanding: submit() blocks until one is freed."""
+
+    def __init__(self, ctx: fvc.Context, consume, slots=fvc.TRACER_OUTPUT_SLOTS):
+        import queue
+        import threading
+        self.ctx, self.consume = ctx, consume
+        self.free = threading.Semaphore(slots)
+        self.q = queue.Queue()
+        self.err = None
+        self.th = threading.Thread(target=self._run, daemon=True)
+        self.th.start()
+
+    def _run(self):
+        while True:
+            item = self.q.get()
+            if item is None:
+                return
+            idx, ticket = item
+            try:
+                if self.err is None:
+                    self.consume(idx, self.ctx.output_wait(ticket))
+            except BaseException as e:  # reported by close()
+                self.err = e
+            finally:
+                try:
+                    self.ctx.output_release(ticket)
+                except fvc.FvcError as e:
+                    self.err = self.err or e
+                self.free.release()
+
+    def submit(self, idx, job: fvc.TracerJob, always=0):
+        self.free.acquire()
+        try:
+            self.q.put((idx, job.output_begin(always)))
+        except BaseException:
+            self.free.release()
+            raise
+
+    def close(self):
+        self.q.put(None)
+        self.th.join()
+        if self.err is not None:
+            raise self.err
+
+
 def run_tracers(ctx: fvc.Context, ax: TimeAxis, seeds, t_start, out_delta, out_res, direction=1, lsc=1,
-                always=0, snapshots=True, state=None):
+                always=0, snapshots=True, state=None, asynchronous=True, consume=None):
     """One tracer release from t_start with outputs every out_delta (ompVC's
     Compute_Tracer loop, ompVC/tracers.c:25-289).  Returns (list of output
     arrays, steps, job stats); a dict passed as state receives the release's
-    final tracer state (fvc_tracer_get_state)."""
+    final tracer state (fvc_tracer_get_state).
+
+    asynchronous (default): advances are queued without waiting and every
+    output goes through the output ring to an OutputWriter thread, which
+    passes it to consume(index, array) (default: keep a copy in the list
+    returned); otherwise each advance waits and each output is a blocking
+    fvc_tracer_snapshot."""
     t_end = t_start + (out_res - 1) * direction * out_delta
     first = int(math.floor((t_start - ax.tmin) / ax.tdelta)) if direction > 0 else int(math.ceil((t_start - ax.tmin) / ax.tdelta))
     last = int(math.ceil((t_end - ax.tmin) / ax.tdelta)) if direction > 0 else int(math.floor((t_end - ax.tmin) / ax.tdelta))
     job = fvc.TracerJob(ctx, seeds, lsc=lsc, chain=0)
     stop = t_end
     outs = []
+    writer = None
+    if asynchronous and snapshots:
+        def keep(idx, a):
+            outs.append(np.array(a))
+        writer = OutputWriter(ctx, consume or keep)
     nxt, frame_out, status, steps = t_start, 0, 0, 0
     df = first
-    while df != last:
-        lo, tmin, tmax = ax.window(df, direction)
-        ctx.set_window(ax.frame_mod(lo), ax.frame_mod(lo + 1), tmin, tmax)
-        t1 = tmin if direction > 0 else tmax
-        while ((t1 - tmax) if direction > 0 else (tmin - t1)) < 0:
-            t2 = min(nxt, tmax) if direction > 0 else max(tmin, nxt)
-            if status != 2 and (status == 1 or (min(t1, t2) <= t_start <= max(t1, t2))):
-                if status == 0:
-                    status = 1
-                    t1 = t_start
-                    job.launch(t_start)
-                steps += job.advance(t1, t2)
-                if abs(nxt - t2) < TINY and frame_out < out_res:
-                    outs.append(job.snapshot(always) if snapshots else None)
-            if ((stop - t2) if direction > 0 else (t2 - stop)) < TINY:
-                status = 2
-            if abs(t2 - nxt) < TINY:
-                nxt += direction * out_delta
-                frame_out += 1
-                if frame_out >= out_res:
-                    break
-            t1 = t2
-        df += direction
+    try:
+        while df != last:
+            lo, tmin, tmax = ax.window(df, direction)
+            ctx.set_window(ax.frame_mod(lo), ax.frame_mod(lo + 1), tmin, tmax)
+            t1 = tmin if direction > 0 else tmax
+            while ((t1 - tmax) if direction > 0 else (tmin - t1)) < 0:
+                t2 = min(nxt, tmax) if direction > 0 else max(tmin, nxt)
+                if status != 2 and (status == 1 or (min(t1, t2) <= t_start <= max(t1, t2))):
+                    if status == 0:
+                        status = 1
+                        t1 = t_start
+                        job.launch(t_start)
+                    if asynchronous:
+                        job.advance(t1, t2, wait=False)
+                    else:
+                        steps += job.advance(t1, t2)
+                    if abs(nxt - t2) < TINY and frame_out < out_res and snapshots:
+                        if writer is not None:
+                            writer.submit(frame_out, job, always)
+                        else:
+                            outs.append(job.snapshot(always))
+                    elif abs(nxt - t2) < TINY and frame_out < out_res:
+                        outs.append(None)
+                if ((stop - t2) if direction > 0 else (t2 - stop)) < TINY:
+                    status = 2
+                if abs(t2 - nxt) < TINY:
+                    nxt += direction * out_delta
+                    frame_out += 1
+                    if frame_out >= out_res:
+                        break
+                t1 = t2
+            df += direction
+    finally:
+        if writer is not None:
+            writer.close()
     st = job.stats()
+    if asynchronous:
+        steps = st["steps_main"]
     if state is not None:
         state.update(job.get_state())
     job.close()

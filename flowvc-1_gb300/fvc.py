@@ -99,6 +99,9 @@ SIGNATURES = {
     "fvc_tracer_advance": (C.c_int, [_vp, C.c_double, C.c_double, _llp]),
     "fvc_tracer_snapshot": (C.c_int, [_vp, C.c_int, _dp, _llp]),
     "fvc_tracer_get_state": (C.c_int, [_vp, _dp, _ip, _ip, _dp]),
+    "fvc_tracer_output_begin": (C.c_int, [_vp, C.c_int, _llp]),
+    "fvc_tracer_output_wait": (C.c_int, [_vp, C.c_longlong, C.POINTER(_dp), _llp]),
+    "fvc_tracer_output_release": (C.c_int, [_vp, C.c_longlong]),
     "fvc_job_get_stats": (C.c_int, [_vp, C.POINTER(JobStats)]),
     "fvc_stream": (_vp, [_vp]),
     "fvc_job_destroy": (None, [_vp]),
@@ -167,6 +170,9 @@ class PinnedArray:
                 self.p = _vp()
         except Exception:
             pass
+
+
+TRACER_OUTPUT_SLOTS = 4  # FVC_TRACER_OUTPUT_SLOTS of fvc.h
 
 
 class FvcError(RuntimeError):
@@ -284,6 +290,25 @@ class Context:
                                       C.byref(steps)))
         return steps.value
 
+    def output_wait(self, ticket):
+        """The positions of a queued tracer output as a read-only view of the
+        library's page-locked slot (count x 3), valid until output_release.
+        Safe to call from another thread than the context's."""
+        p, cnt = _dp(), C.c_longlong(0)
+        st = self.lib.fvc_tracer_output_wait(self.h, ticket, C.byref(p), C.byref(cnt))
+        if st:
+            raise FvcError(st, f"fvc_tracer_output_wait: status {st}")
+        if cnt.value == 0:
+            return np.empty((0, 3))
+        a = np.ctypeslib.as_array(p, shape=(cnt.value, 3))
+        a.flags.writeable = False
+        return a
+
+    def output_release(self, ticket):
+        st = self.lib.fvc_tracer_output_release(self.h, ticket)
+        if st:
+            raise FvcError(st, f"fvc_tracer_output_release: status {st}")
+
     def advect_noalloc(self, X, V, eid, left, ldt, t0, t1):
         """advect() through fvc_advect_noalloc: same results, no device
         allocation (at most NOALLOC_MAX_POINTS points a call)."""
@@ -382,10 +407,21 @@ class TracerJob:
     def launch(self, t):
         self.ctx._chk(self.lib.fvc_tracer_launch(self.h, t))
 
-    def advance(self, t1, t2):
+    def advance(self, t1, t2, wait=True):
+        """Accepted steps of the advance; wait=False queues it and returns
+        None (its steps appear in stats())."""
+        if not wait:
+            self.ctx._chk(self.lib.fvc_tracer_advance(self.h, t1, t2, None))
+            return None
         steps = C.c_longlong(0)
         self.ctx._chk(self.lib.fvc_tracer_advance(self.h, t1, t2, C.byref(steps)))
         return steps.value
+
+    def output_begin(self, always=0):
+        """Queues an asynchronous output (fvc_tracer_output_begin); returns its ticket."""
+        t = C.c_longlong(0)
+        self.ctx._chk(self.lib.fvc_tracer_output_begin(self.h, always, C.byref(t)))
+        return t.value
 
     def snapshot(self, always=0):
         out = np.empty((max(self.n, 1), 3))

@@ -657,6 +657,136 @@ static int output_cet(run_t *R, int ntracers)
     return 0;
 }
 
+/* Tracer outputs are written by a thread of their own (OutputTracers,
+ * ompVC/tracers.c:1763-1816): the release loop queues each output with
+ * fvc_tracer_output_begin and goes on advancing; the writer waits for the
+ * outputs in ticket order, appends each to its output file (created when
+ * the first release with tracers to write reaches it, as ompVC creates it)
+ * and frees the slot.  At most FVC_TRACER_OUTPUT_SLOTS outputs are
+ * outstanding. */
+typedef struct {
+    long long ticket;
+    int frame;
+    double time;
+} wr_item;
+
+typedef struct {
+    fvc_ctx *ctx;
+    const char *dir, *prefix;
+    wr_item q[FVC_TRACER_OUTPUT_SLOTS];
+    int head, count, inflight, stop, err;
+    pthread_mutex_t mu;
+    pthread_cond_t cv;
+    pthread_t th;
+    FILE *fo;
+    int fo_frame;
+    char msg[256];
+} writer_t;
+
+static void *writer_main(void *arg)
+{
+    writer_t *W = (writer_t *)arg;
+    for (;;) {
+        pthread_mutex_lock(&W->mu);
+        while (W->count == 0 && !W->stop) pthread_cond_wait(&W->cv, &W->mu);
+        if (W->count == 0) {
+            pthread_mutex_unlock(&W->mu);
+            break;
+        }
+        wr_item it = W->q[W->head];
+        W->head = (W->head + 1) % FVC_TRACER_OUTPUT_SLOTS;
+        W->count--;
+        int err = W->err;
+        pthread_mutex_unlock(&W->mu);
+        const double *X = NULL;
+        long long cnt = 0;
+        int rc = err ? 0 : fvc_tracer_output_wait(W->ctx, it.ticket, &X, &cnt);
+        if (!err && rc) {
+            err = rc;
+            snprintf(W->msg, sizeof(W->msg), "tracer output %d: status %d", it.frame, rc);
+        }
+        if (!err && W->fo && W->fo_frame != it.frame) {
+            fclose(W->fo);
+            W->fo = NULL;
+        }
+        if (!err && cnt > 0) {
+            if (!W->fo) {
+                char path[2 * FVCP_STR];
+                snprintf(path, sizeof(path), "%s%s.%d.bin", W->dir, W->prefix, it.frame);
+                W->fo = fopen(path, "wb");
+                W->fo_frame = it.frame;
+                if (!W->fo || fwrite(&it.time, 8, 1, W->fo) != 1) {
+                    err = FVC_ERR_IO;
+                    snprintf(W->msg, sizeof(W->msg), "Could not open file %s", path);
+                }
+            }
+            if (!err && fwrite(X, 24, (size_t)cnt, W->fo) != (size_t)cnt) {
+                err = FVC_ERR_IO;
+                snprintf(W->msg, sizeof(W->msg), "Could not write output %d", it.frame);
+            }
+        }
+        fvc_tracer_output_release(W->ctx, it.ticket);
+        pthread_mutex_lock(&W->mu);
+        W->inflight--;
+        if (err && !W->err) W->err = err;
+        pthread_cond_broadcast(&W->cv);
+        pthread_mutex_unlock(&W->mu);
+    }
+    if (W->fo) fclose(W->fo);
+    W->fo = NULL;
+    return NULL;
+}
+
+static int writer_start(writer_t *W, fvc_ctx *ctx, const char *dir, const char *prefix)
+{
+    memset(W, 0, sizeof(*W));
+    W->ctx = ctx;
+    W->dir = dir;
+    W->prefix = prefix;
+    W->fo_frame = -1;
+    pthread_mutex_init(&W->mu, NULL);
+    pthread_cond_init(&W->cv, NULL);
+    return pthread_create(&W->th, NULL, writer_main, W) ? 1 : 0;
+}
+
+/* queues output `frame` of job (waits while every slot is taken) */
+static int writer_submit(writer_t *W, fvc_job *job, int always, int frame, double time)
+{
+    pthread_mutex_lock(&W->mu);
+    while (W->inflight >= FVC_TRACER_OUTPUT_SLOTS && !W->err) pthread_cond_wait(&W->cv, &W->mu);
+    int err = W->err;
+    if (!err) W->inflight++;
+    pthread_mutex_unlock(&W->mu);
+    if (err) return err;
+    long long ticket = 0;
+    int rc = fvc_tracer_output_begin(job, always, &ticket);
+    pthread_mutex_lock(&W->mu);
+    if (rc) {
+        W->inflight--;
+    } else {
+        wr_item it = {ticket, frame, time};
+        W->q[(W->head + W->count) % FVC_TRACER_OUTPUT_SLOTS] = it;
+        W->count++;
+        pthread_cond_broadcast(&W->cv);
+    }
+    pthread_mutex_unlock(&W->mu);
+    return rc;
+}
+
+/* drains the queue and joins the thread; returns the first failure */
+static int writer_stop(writer_t *W)
+{
+    pthread_mutex_lock(&W->mu);
+    W->stop = 1;
+    pthread_cond_broadcast(&W->cv);
+    pthread_mutex_unlock(&W->mu);
+    pthread_join(W->th, NULL);
+    pthread_mutex_destroy(&W->mu);
+    pthread_cond_destroy(&W->cv);
+    if (W->err) fprintf(stderr, "%s\n", W->msg[0] ? W->msg : "tracer output failed");
+    return W->err;
+}
+
 static int run_tracers(run_t *R)
 {
     fvcp_params *P = &R->P;
@@ -671,8 +801,7 @@ static int run_tracers(run_t *R)
     fvc_job **rel = (fvc_job **)calloc((size_t)nl, sizeof(fvc_job *));
     double *start = (double *)calloc((size_t)nl, 8), *stop = (double *)calloc((size_t)nl, 8);
     int *status = (int *)calloc((size_t)nl, sizeof(int));
-    double *snap = (double *)malloc(24 * (size_t)(n ? n : 1));
-    if (!rel || !start || !stop || !status || !snap) { fprintf(stderr, "out of memory\n"); return 1; }
+    if (!rel || !start || !stop || !status) { fprintf(stderr, "out of memory\n"); return 1; }
     double t0 = wall();
     for (int ss = 0; ss < nl; ss++) {
         if ((rc = fvc_tracer_create(R->ctx, &sp, n, seeds, &rel[ss]))) return die("tracer seeds", R->ctx, rc);
@@ -705,7 +834,8 @@ static int run_tracers(run_t *R)
     }
     int outputframe = 0;
     double next = P->out_tstart;
-    char path[2 * FVCP_STR];
+    writer_t W;
+    if (writer_start(&W, R->ctx, P->path_output, P->tr_prefix)) { fprintf(stderr, "writer thread\n"); return 1; }
     for (int df = P->first_frame; df != P->last_frame; df = df + P->int_dir) {
         double tmin, tmax;
         if (set_window(R, df, &tmin, &tmax)) return 1;
@@ -714,38 +844,26 @@ static int run_tracers(run_t *R)
         while (((P->int_dir > 0) ? (t1 - tmax) : (tmin - t1)) < 0) {
             t2 = P->int_dir > 0 ? MIN(next, tmax) : MAX(tmin, next);
             int out_now = fabs(next - t2) < TINY && outputframe < P->out_tres;
-            FILE *fo = NULL;
-            long long written = 0;
             for (int ss = 0; ss < nl; ss++) {
                 if (status[ss] != 2 && (status[ss] == 1 || (start[ss] <= MAX(t1, t2) && start[ss] >= MIN(t1, t2)))) {
                     t0 = wall();
                     if (status[ss] == 0) {
                         status[ss] = 1;
                         t1 = start[ss];
-                        if ((rc = fvc_tracer_launch(rel[ss], start[ss]))) return die("tracer release", R->ctx, rc);
+                        if ((rc = fvc_tracer_launch(rel[ss], start[ss]))) { writer_stop(&W); return die("tracer release", R->ctx, rc); }
                     }
-                    long long st = 0, cnt = 0;
-                    if ((rc = fvc_tracer_advance(rel[ss], t1, t2, &st))) return die("tracer advection", R->ctx, rc);
-                    R->steps += st;
-                    if (out_now && (rc = fvc_tracer_snapshot(rel[ss], P->tr_always, snap, &cnt)))
+                    /* queued, not waited for: its steps are counted from the job's statistics */
+                    if ((rc = fvc_tracer_advance(rel[ss], t1, t2, NULL))) { writer_stop(&W); return die("tracer advection", R->ctx, rc); }
+                    /* OutputTracers, ompVC/tracers.c:1777-1804, on the writer thread */
+                    double time = P->out_tstart + outputframe * P->int_dir * P->out_tdelta;
+                    if (out_now && (rc = writer_submit(&W, rel[ss], P->tr_always, outputframe, time))) {
+                        writer_stop(&W);
                         return die("tracer output", R->ctx, rc);
-                    R->t_compute += wall() - t0;
-                    if (out_now && cnt > 0) {
-                        if (!fo) {
-                            /* OutputTracers, ompVC/tracers.c:1777-1804 */
-                            snprintf(path, sizeof(path), "%s%s.%d.bin", P->path_output, P->tr_prefix, outputframe);
-                            fo = fopen(path, "wb");
-                            if (!fo) { fprintf(stderr, "Could not open file %s\n", path); return 1; }
-                            double time = P->out_tstart + outputframe * P->int_dir * P->out_tdelta;
-                            fwrite(&time, 8, 1, fo);
-                        }
-                        if (fwrite(snap, 24, (size_t)cnt, fo) != (size_t)cnt) { fprintf(stderr, "Could not write %s\n", path); return 1; }
-                        written += cnt;
                     }
+                    R->t_compute += wall() - t0;
                 }
                 if (((P->int_dir > 0) ? (stop[ss] - t2) : (t2 - stop[ss])) < TINY) status[ss] = 2;
             }
-            if (fo) fclose(fo);
             if (fabs(t2 - next) < TINY) {
                 next += P->int_dir * P->out_tdelta;
                 outputframe++;
@@ -754,10 +872,16 @@ static int run_tracers(run_t *R)
             t1 = t2;
         }
     }
+    if (writer_stop(&W)) return 1;
+    for (int ss = 0; ss < nl; ss++) {
+        fvc_job_stats js;
+        if ((rc = fvc_job_get_stats(rel[ss], &js))) return die("tracer advection", R->ctx, rc);
+        R->steps += js.steps_main;
+    }
     if (P->tr_rt && output_rt(R, n, icX, rel, stop)) return 1;
     if (P->tr_cet && output_cet(R, n)) return 1;
     for (int ss = 0; ss < nl; ss++) fvc_job_destroy(rel[ss]);
-    free(rel); free(start); free(stop); free(status); free(snap); free(seeds); free(icX);
+    free(rel); free(start); free(stop); free(status); free(seeds); free(icX);
     return 0;
 }
 

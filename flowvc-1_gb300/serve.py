@@ -110,11 +110,41 @@ def tube_batch_jobs(tube, njobs=64, nmin=1e3, nmax=1e6, seed=0):
     return jobs
 
 
+class SectionSeeds:
+    """n seeds on the tube's cross-section at axial position s, made when the
+    request is submitted: a slice of one shared pool of points uniform in the
+    disc of radius 1 - margin (tube_cross_section_seeds' distribution), mapped
+    onto the section.  Keeps a stream of thousands of requests with up to a
+    million seeds each from holding all their seeds in host memory at once."""
+    _pool = None
+
+    def __init__(self, tube, n, s, offset):
+        self.tube, self.n, self.s, self.offset = tube, int(n), float(s), int(offset)
+
+    @classmethod
+    def pool(cls, size=1 << 20, margin=0.02, seed=12345):
+        if cls._pool is None or len(cls._pool) < size:
+            rng = np.random.default_rng(seed)
+            rr = np.sqrt(rng.uniform(0.0, (1.0 - margin) ** 2, size))
+            th = rng.uniform(0.0, 2 * math.pi, size)
+            cls._pool = np.stack([rr * np.cos(th), rr * np.sin(th)], -1)
+        return cls._pool
+
+    def __call__(self):
+        P = self.pool()
+        idx = (self.offset + np.arange(self.n)) % len(P)
+        C, T, N = synth.tube_centreline(np.array([self.s]), self.tube.length, self.tube.bend_radius)
+        B = np.array([0.0, 1.0, 0.0])
+        R = self.tube.radius
+        return C[0] + R * (P[idx, 0:1] * N[0] + P[idx, 1:2] * B)
+
+
 def submit(batch, job):
     kind, arg, t0, t1 = job
     if kind == "ftle":
         return batch.submit_ftle(arg, t0, t1)
-    return batch.submit_tracers(arg, t0, t1, residence=kind == "residence")
+    seeds = arg() if callable(arg) else arg
+    return batch.submit_tracers(seeds, t0, t1, residence=kind == "residence")
 
 
 def run_batched(site, jobs, graph=True, tune=True, results=False):
@@ -172,13 +202,16 @@ class Request:
     result: object = None
 
 
-def poisson_requests(tube, rate=200.0, duration=10.0, mix=(0.5, 0.4, 0.1), seed=0, tracer_range=(1e3, 1e5),
-                     ftle_edges=(16, 48), rt_seeds=10_000, rt_periods=3.0, ftle_T=1.0):
+def poisson_requests(tube, rate=200.0, duration=60.0, mix=(0.5, 0.4, 0.1), seed=0, tracer_range=(1e3, 1e6),
+                     ftle_edges=(32, 128), rt_seeds=100_000, rt_periods=3.0, ftle_T=1.0):
     """Arrivals at Poisson times over `duration` seconds: tracer releases on the
     tube (seed counts log-uniform in tracer_range, windows as the batch's),
     FTLE grids on the cube (edge uniform in ftle_edges, forward over ftle_T)
     and residence-time releases on the tube (rt_seeds seeds, rt_periods
-    periods), in the proportions of mix."""
+    periods), in the proportions of mix.  The defaults are the served
+    workload's: 200 requests/s for 60 s, 1e3-1e6 tracer seeds, 32^3-128^3
+    FTLE grids, 1e5-seed three-period residence-time releases.  Seeds are
+    made at submission (SectionSeeds)."""
     rng = np.random.default_rng(seed)
     t, reqs = 0.0, []
     while True:
@@ -192,7 +225,7 @@ def poisson_requests(tube, rate=200.0, duration=10.0, mix=(0.5, 0.4, 0.1), seed=
             t0 = float(rng.uniform(0.0, TUBE_PERIOD))
             T = float(rng.uniform(0.2, 2.0)) * TUBE_PERIOD
             d = 1 if rng.uniform() < 0.5 else -1
-            seeds = synth.tube_cross_section_seeds(tube, n, s, seed=int(rng.integers(1 << 30)))
+            seeds = SectionSeeds(tube, n, s, int(rng.integers(1 << 30)))
             reqs.append(Request(t, "tube", ("tracers", seeds, t0, t0 + d * T), "tracers", n))
         elif u < mix[0] + mix[1]:
             e = int(rng.integers(ftle_edges[0], ftle_edges[1] + 1))
@@ -200,29 +233,38 @@ def poisson_requests(tube, rate=200.0, duration=10.0, mix=(0.5, 0.4, 0.1), seed=
         else:
             s = rng.uniform(0.05 * tube.length, 0.5 * tube.length)
             t0 = float(rng.uniform(0.0, TUBE_PERIOD))
-            seeds = synth.tube_cross_section_seeds(tube, rt_seeds, s, seed=int(rng.integers(1 << 30)))
+            seeds = SectionSeeds(tube, rt_seeds, s, int(rng.integers(1 << 30)))
             reqs.append(Request(t, "tube", ("residence", seeds, t0, t0 + rt_periods * TUBE_PERIOD), "residence",
                                 rt_seeds))
     return reqs
 
 
-def serve(sites, requests, keep_results=False, time_limit=600.0):
+def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
     """Serves the requests in arrival order against the sites' batches.
 
     The loop submits every request whose arrival time has passed, ticks each
     site's batch (a tick enqueues one frame interval of every admitted job
     and returns; at most two are in flight per site, and the sites' streams
     run concurrently), and collects finished jobs: results copied to the
-    host, the job released, its latency recorded.  Returns a summary dict."""
+    host, the job released, its latency recorded.  Returns a summary dict.
+
+    time_limit: wall seconds.  Past it serving raises, or with censor=True
+    stops: the summary then covers the requests that finished, counts the
+    rest (arrived or not) and gives the unfinished requests' waiting time so
+    far as a lower bound of their latency."""
     pending = sorted(requests, key=lambda r: r.t_arrive)
     nxt = 0
     running = {name: {} for name in sites}
     done = []
     t0 = time.perf_counter()
+    stopped = False
     while len(done) < len(pending):
         now = time.perf_counter() - t0
         if now > time_limit:
-            raise RuntimeError(f"serving did not finish within {time_limit} s")
+            if not censor:
+                raise RuntimeError(f"serving did not finish within {time_limit} s")
+            stopped = True
+            break
         while nxt < len(pending) and pending[nxt].t_arrive <= now:
             r = pending[nxt]
             r.jid = submit(sites[r.site].batch, r.job)
@@ -256,15 +298,47 @@ def serve(sites, requests, keep_results=False, time_limit=600.0):
             if wait > 0:
                 time.sleep(min(wait, 0.001))
     wall = time.perf_counter() - t0
-    lat = np.array([r.t_done - r.t_arrive for r in done])
+    lat = np.array([r.t_done - r.t_arrive for r in done]) if done else np.zeros(1)
     steps = sum(r.steps for r in done)
+    if stopped:
+        # the jobs still running have advanced too: count their steps so far
+        for name, site in sites.items():
+            for jid in running[name]:
+                try:
+                    js = site.batch.job_stats(jid)
+                    steps += js["steps_main"] + js["steps_early"]
+                except fvc.FvcError:
+                    pass
     by_kind = {}
     for k in ("tracers", "ftle", "residence"):
         lk = np.array([r.t_done - r.t_arrive for r in done if r.kind == k])
         if len(lk):
             by_kind[k] = {"n": int(len(lk)), "p50_ms": 1e3 * float(np.percentile(lk, 50)),
                           "p99_ms": 1e3 * float(np.percentile(lk, 99))}
-    return {"requests": len(done), "wall_s": wall, "steps": int(steps), "steps_per_s": steps / wall,
-            "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p95_ms": 1e3 * float(np.percentile(lat, 95)),
-            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "max_ms": 1e3 * float(lat.max()),
-            "by_kind": by_kind}
+    out = {"requests": len(done), "wall_s": wall, "steps": int(steps), "steps_per_s": steps / wall,
+           "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p95_ms": 1e3 * float(np.percentile(lat, 95)),
+           "p99_ms": 1e3 * float(np.percentile(lat, 99)), "max_ms": 1e3 * float(lat.max()),
+           "by_kind": by_kind}
+    if stopped:
+        waiting = np.array([wall - r.t_arrive for r in pending[:nxt] if r.t_done is None])
+        out.update({"stopped_at_s": wall, "requests_total": len(pending), "requests_unfinished": len(pending) - len(done),
+                    "requests_not_yet_arrived": len(pending) - nxt,
+                    "unfinished_waited_p50_ms": 1e3 * float(np.percentile(waiting, 50)) if len(waiting) else None,
+                    "note": "stopped at the time limit: latencies cover the finished requests only"})
+    return out
+
+
+def sustained(summary, reqs, duration):
+    """Whether a served run kept up with its arrivals: every request finished
+    within 5 s after the last arrival, and the requests arriving in the last
+    third of the window waited (p99) no more than twice those of the first
+    third (a queue that grows fails both)."""
+    if summary.get("requests_unfinished"):
+        return False
+    if summary["wall_s"] > duration + 5.0:
+        return False
+    early = [r.t_done - r.t_arrive for r in reqs if r.t_done is not None and r.t_arrive < duration / 3]
+    late = [r.t_done - r.t_arrive for r in reqs if r.t_done is not None and r.t_arrive > 2 * duration / 3]
+    if not early or not late:
+        return True
+    return float(np.percentile(late, 99)) <= 2.0 * float(np.percentile(early, 99))

@@ -252,13 +252,41 @@ fvc_status fvc_tracer_create(fvc_ctx *ctx, const fvc_tracer_spec *spec, int n, c
                              fvc_job **job);
 /* Release velocity at t_start (ompVC/tracers.c:190-207). */
 fvc_status fvc_tracer_launch(fvc_job *job, double t_start);
-/* Advect live tracers over [t1, t2] (ompVC/tracers.c:217-240). */
+/* Advect live tracers over [t1, t2] (ompVC/tracers.c:217-240).  With
+ * steps != NULL the call waits and returns the accepted steps; with NULL it
+ * returns once the work is queued, and device faults are returned by the
+ * job's next call that waits (fvc_tracer_output_wait, fvc_tracer_snapshot,
+ * fvc_tracer_get_state, fvc_tracer_residence, fvc_job_get_stats). */
 fvc_status fvc_tracer_advance(fvc_job *job, double t1, double t2, long long *steps);
 /* Positions of the tracers ompVC writes at an output time, in seed order
  * (ompVC/tracers.c:243-256): LeftDomainTime > -TINY and (not left or
  * always_output).  X_out must hold n x 3; *count receives the number. */
 fvc_status fvc_tracer_snapshot(fvc_job *job, int always_output, double *X_out, long long *count);
 fvc_status fvc_tracer_get_state(fvc_job *job, double *X, int *eid, int *left, double *ldt);
+
+/* Asynchronous tracer outputs: the output step of Compute_Tracer
+ * (ompVC/tracers.c:243-256, written by OutputTracers,
+ * ompVC/tracers.c:1763-1816) without a wait on the GPU.
+ * fvc_tracer_output_begin queues, behind the job's queued advances, the
+ * compaction of the tracers fvc_tracer_snapshot would return into a slot
+ * of the context's output ring and their copy to page-locked host memory on
+ * a side stream, and returns at once with a ticket.
+ * fvc_tracer_output_wait waits for that output only and gives its
+ * positions (count x 3, seed order) in library-owned page-locked memory,
+ * valid until fvc_tracer_output_release frees the slot.  A context has
+ * FVC_TRACER_OUTPUT_SLOTS slots: begin returns FVC_ERR_STATE while all
+ * are held (release one first).  wait and release touch only the ring and
+ * may be called from another thread (a file writer) while the context's
+ * thread makes other calls; their failures return a status without
+ * setting fvc_last_error.  A device fault of the advances before the
+ * output is returned by wait.  fvc_tracer_advance with steps == NULL
+ * queues its work without waiting (its steps are counted in the job's
+ * statistics), so a release loop of advances and outputs never waits for
+ * the GPU. */
+#define FVC_TRACER_OUTPUT_SLOTS 4
+fvc_status fvc_tracer_output_begin(fvc_job *job, int always_output, long long *ticket);
+fvc_status fvc_tracer_output_wait(fvc_ctx *ctx, long long ticket, const double **X, long long *count);
+fvc_status fvc_tracer_output_release(fvc_ctx *ctx, long long ticket);
 
 /* ---- tracer side analyses (unstructured meshes, FP64 form) ------------- */
 

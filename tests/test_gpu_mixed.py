@@ -110,12 +110,18 @@ def test_kahan_keeps_fp64_accuracy(engine):
     g.close()
 
 
-@pytest.mark.parametrize("prec,tol_max,tol_rms", [("bf16", 0.2, 0.02), ("fp16", 0.05, 0.004)])
+# Measured on a GB300 (error / largest FP64 FTLE value): BF16 total max
+# 0.0852 rms 0.0116, FP16 max 0.0101 rms 0.00135, all but ~4e-6 of it the
+# 16-bit storage; the FP32 arithmetic against the FP64 form on the same
+# 16-bit frames: max 4.2e-6 / 3.8e-6, rms 4.8e-7 / 4.9e-7.  The bounds sit
+# 1.4-2.5x above those figures.
+@pytest.mark.parametrize("prec,tol_max,tol_rms", [("bf16", 0.12, 0.016), ("fp16", 0.015, 0.002)])
 def test_ftle_errors_bounded(engine, prec, tol_max, tol_rms):
     """FTLE on a 24^3 grid over T = 0.4 (20 frame intervals): max and RMS
     error relative to the largest FP64 FTLE value.  The error is also split
     by source: the FP64 form on the frames quantised and dequantised on the
-    host carries the 16-bit storage error alone."""
+    host carries the 16-bit storage error alone, and the mixed form against
+    that run carries the FP32 arithmetic, bounded on its own."""
     import quantise
     xyz, conn, adj = synth.kuhn_cube_mesh(8, jitter=0.2, seed=0)
     frames = [synth.abc_flow(xyz, t) for t in np.arange(21) * 0.02]
@@ -143,6 +149,8 @@ def test_ftle_errors_bounded(engine, prec, tol_max, tol_rms):
                                             np.sqrt((arith ** 2).mean())))
     assert err.max() < tol_max, err.max()
     assert np.sqrt((err ** 2).mean()) < tol_rms
+    assert arith.max() < 1e-5, arith.max()
+    assert np.sqrt((arith ** 2).mean()) < 1.2e-6
 
 
 def test_mixed_refusals(engine):

@@ -73,3 +73,19 @@ def test_tube_batch_and_requests_are_seeded_and_shaped():
             assert r.site == "tube"
         if r.kind == "residence":
             assert r.job[3] > r.job[2]
+
+
+def test_section_seeds_lie_on_their_cross_section():
+    """Seeds made at submission (serve.SectionSeeds): deterministic, inside
+    the disc of radius (1 - margin) R around the centreline point, in the
+    plane normal to the axis there."""
+    import serve
+    t = synth.bent_tube_mesh(nc=6, nax=12)
+    for s in (0.3, 0.5 * t.length, 0.97 * t.length):
+        a = serve.SectionSeeds(t, 5000, s, 123)()
+        b = serve.SectionSeeds(t, 5000, s, 123)()
+        assert a.shape == (5000, 3) and np.array_equal(a, b)
+        C, T, N = synth.tube_centreline(np.array([s]), t.length, t.bend_radius)
+        d = a - C[0]
+        assert np.abs(d @ T[0]).max() < 1e-12
+        assert np.linalg.norm(d, axis=1).max() <= 0.98 * t.radius + 1e-12
