@@ -518,7 +518,7 @@ def bench_tracers(args, inputs):
         "left_mismatch_rate": float((~same).mean()),
         "exit_time_mismatch_rate": float((np.abs(a["ldt"][both] - b["ldt"][both]) > 1e-9).mean()) if both.any() else 0.0,
         "left_fraction": float((a["left"] == 1).mean())}
-    out["speedup_vs_fp64"] = out["bf16"]["value"] / out["fp64"]["value"]
+    out["speedup_vs_fp64"] = out["bf16"]["value"] / out["fp64"]["value"] if out["fp64"]["value"] else None
     return out
 
 
@@ -550,7 +550,7 @@ def bench_batched(args, tube, frames):
                      "tuned": {"threads": st["tuned_threads"], "blocks": st["tuned_blocks"],
                                "resort_every": st["tuned_resort"]}}
         site.close()
-    out["speedup_vs_fp64"] = out["bf16"]["value"] / out["fp64"]["value"]
+    out["speedup_vs_fp64"] = out["bf16"]["value"] / out["fp64"]["value"] if out["fp64"]["value"] else None
     import serve as _s
     out["bf16"]["errors_vs_fp64"] = _s.endpoint_errors(res["fp64"], res["bf16"])
     return out
@@ -593,7 +593,8 @@ def bench_served(args, tube, frames, cube_inputs):
     for prec in ("bf16", "fp64"):
         out[prec] = run(prec, args.served_rate, args.served_seconds, limits[prec])
         out["requests"] = out[prec].get("requests_total", out[prec]["requests"])
-    out["speedup_vs_fp64"] = out["bf16"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    out["speedup_vs_fp64"] = (out["bf16"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+                              if out["fp64"]["steps_per_s"] else None)
     if args.served_sweep:
         sweep = {}
         for prec, rates in (("bf16", (25, 50, 100, 150, 200, 300)), ("fp64", (1, 2, 5, 10, 20))):

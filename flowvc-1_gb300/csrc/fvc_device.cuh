@@ -79,8 +79,13 @@ __device__ __forceinline__ double4_32a ldf(const double4_32a* p) {
 // partial sum unchanged; the 2D branch skips them.
 // tloc of a query time (ompVC/velocity.c:275-277): from the slot table when
 // the query is a tabulated stage time, else computed and range-checked.
+// The times are compared with integer instructions, off the FP64 pipe: equal
+// bit patterns, or both zero (+0 == -0, as the FP64 comparison has it).
 __device__ __forceinline__ bool slot_hit(const DevWindow& w, int slot, double tq) {
-  return slot >= 0 && slot < w.nslots && w.tq[slot] == tq;
+  if (slot < 0 || slot >= w.nslots) return false;
+  const unsigned long long a = (unsigned long long)__double_as_longlong(w.tq[slot]);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(tq);
+  return a == b || ((a | b) << 1) == 0ull;
 }
 __device__ __forceinline__ int get_tloc(const DevWindow& w, int slot, double tq, double& tloc) {
   if (slot_hit(w, slot, tq)) {
@@ -378,9 +383,18 @@ __device__ __forceinline__ int neighbour(const DevMesh& m, int e, int slot) { re
 // with its records, so a hop costs one memory round trip.  Returns 0 with
 // the element's coordinates, or 1 when the walk stops: eid = -1 when it left
 // through a boundary face, EID_FAULT when it failed.
+//
+// nc (velocity walks only): the last locate's element and coordinates at
+// this same position.  When the walk reaches that element, the FP64 solve
+// there would recompute the cached doubles and pass (the locate's d > -TINY
+// implies (d + TINY) >= 0), so the cache stands in for it.  An RK4 step's
+// first stage walks from its own hint, which lags the located element
+// whenever the previous step crossed a face: without this those walks
+// repeated the locate's solve, lane by lane.
 template <int DIMS>
 __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& eid, bool vel_rule, double& r,
-                                    double& s, double& t, double& wv, double& d, int4& nd) {
+                                    double& s, double& t, double& wv, double& d, int4& nd,
+                                    const NatCache* nc = nullptr) {
   const PosF P = pos_f32(X);
   int4 nb = neighbours(m, eid);
   for (int hop = 0; hop < m.max_hops;) {
@@ -392,6 +406,15 @@ __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& ei
       nb = neighbours(m, eid);
     }
     if (hop >= m.max_hops) break;
+    if (nc && eid == nc->e) {
+      r = nc->r;
+      s = nc->s;
+      t = nc->t;
+      wv = nc->w;
+      d = nc->d;
+      nd = nc->nd;
+      return 0;
+    }
     Geo<DIMS> g;
     load_geo<DIMS>(m, eid, g);
     d = natural_from<DIMS>(g, X, r, s, t, wv);
@@ -438,7 +461,7 @@ __device__ __forceinline__ int vel_unstruct(const DevMesh& m, const DevWindow& w
     t = nc->t;
     wv = nc->w;
   } else {
-    if (walk<DIMS>(m, X, eid, true, r, s, t, wv, d, nd)) {
+    if (walk<DIMS>(m, X, eid, true, r, s, t, wv, d, nd, nc)) {
       // out of the domain, or a failed walk (eid = EID_FAULT): the point stops
       left = 1;
       out[0] = out[1] = out[2] = 0.0;

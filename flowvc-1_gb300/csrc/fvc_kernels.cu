@@ -1061,7 +1061,7 @@ __global__ void k_live_count(int n, const double* ldt, const int* left, int extr
 }
 
 __global__ void k_live_scatter(int n, const double* ldt, const int* left, int extrap, const int* block_off,
-                               int* live, unsigned char* flag, int* nlive) {
+                               int* live, unsigned char* flag, DevCounters* ctr) {
   __shared__ int warp_off[32];
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   bool sel = is_live(i, n, ldt, left, extrap);
@@ -1080,13 +1080,19 @@ __global__ void k_live_scatter(int n, const double* ldt, const int* left, int ex
   __syncthreads();
   if (i < n && flag) flag[i] = 0;
   if (sel) live[block_off[blockIdx.x] + warp_off[wid] + __popc(b & ((1u << lane) - 1u))] = (int)i;
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *nlive = block_off[gridDim.x];
+  // the live count, and the work cursors of the persistent launch that
+  // takes the list next start at 0 (calls may be queued back to back on
+  // the same counters)
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x < 5) {
+    if (threadIdx.x == 0) ctr->nlive = block_off[gridDim.x];
+    else ctr->cur[threadIdx.x - 1] = 0;
+  }
 }
 
 void compact_live(int n, const double* ldt, const int* left, int extrapolate, int* live,
                   unsigned char* flag, int* block_cnt, DevCounters* ctr, cudaStream_t s) {
   if (n <= 0) {
-    cudaMemsetAsync(&ctr->nlive, 0, sizeof(int), s);
+    cudaMemsetAsync(&ctr->nlive, 0, sizeof(int) * 5, s);  // nlive and the cursors
     return;
   }
   unsigned nb = nblk(n, 1024);
@@ -1094,7 +1100,7 @@ void compact_live(int n, const double* ldt, const int* left, int extrapolate, in
   long long* tmp = reinterpret_cast<long long*>(block_cnt + ((2 * nb + 4) & ~1u));
   k_live_count<<<nb, 1024, 0, s>>>(n, ldt, left, extrapolate, block_cnt);
   exclusive_scan(block_cnt, off, (int)nb, tmp, s);
-  k_live_scatter<<<nb, 1024, 0, s>>>(n, ldt, left, extrapolate, off, live, flag, &ctr->nlive);
+  k_live_scatter<<<nb, 1024, 0, s>>>(n, ldt, left, extrapolate, off, live, flag, ctr);
 }
 
 void tracer_compact(const TracerDev& t, int always, DevCounters* ctr, cudaStream_t s) {

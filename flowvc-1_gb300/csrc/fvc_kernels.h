@@ -32,6 +32,8 @@ struct DevCounters {
   unsigned long long steps_rec;  // early-FTLE steps read from the main pass's record
 };
 #define FVC_EARLY_COUNTERS_BYTES (offsetof(DevCounters, nfall) + sizeof(int) - offsetof(DevCounters, count))
+static_assert(offsetof(DevCounters, cur) == offsetof(DevCounters, nlive) + sizeof(int),
+              "the live-list kernels clear nlive and the cursors as one run of ints");
 
 // ---- mesh preprocessing
 // the mesh's element records from the caller's connectivity and adjacency

@@ -214,10 +214,30 @@ __device__ __noinline__ int near_face_fp64(const DevMesh& m, int e, const float*
   return -1;
 }
 
+// The last locate's element and coordinates at the current position.
+struct NatM {
+  int e;
+  int4 nd;
+  float r, s, t;
+};
+
+// nc (velocity walks only): as in the FP64 walk, reaching the element the
+// last locate found at this position gives that locate's coordinates, which
+// the tests below would reproduce there (the locate passed, so the velocity
+// rule passes too).
 template <int D>
 __device__ __forceinline__ int walk_mx(const DevMesh& m, const float X[3], const float C[3], int& eid, bool vel_rule,
-                                       float& r, float& s, float& t, float& wv, int4& nd) {
+                                       float& r, float& s, float& t, float& wv, int4& nd,
+                                       const NatM* nc = nullptr) {
   for (int hop = 0; hop < m.max_hops; hop++) {
+    if (nc && eid == nc->e) {
+      nd = nc->nd;
+      r = nc->r;
+      s = nc->s;
+      t = nc->t;
+      wv = 1.0f - r - s - t;
+      return 0;
+    }
     // the element's node ids and neighbours (one 32-byte sector), loaded
     // beside its record
     nd = __ldg(m.elem + 2 * (long)eid);
@@ -256,13 +276,6 @@ __device__ __forceinline__ int walk_mx(const DevMesh& m, const float X[3], const
   return 1;
 }
 
-// The last locate's element and coordinates at the current position.
-struct NatM {
-  int e;
-  int4 nd;
-  float r, s, t;
-};
-
 // Velocity at X (compensation C) and tloc tl: P1 in space, linear in time.
 template <int D, class W>
 __device__ __forceinline__ int vel_mx(const DevMesh& m, const W& w, float tl, const float X[3],
@@ -276,7 +289,7 @@ __device__ __forceinline__ int vel_mx(const DevMesh& m, const W& w, float tl, co
     s = nc->s;
     t = nc->t;
   } else {
-    if (walk_mx<D>(m, X, C, eid, true, r, s, t, wv, nd)) {
+    if (walk_mx<D>(m, X, C, eid, true, r, s, t, wv, nd, nc)) {
       // out of the domain, or a failed walk (eid = EID_FAULT): the point stops
       left = 1;
       out[0] = out[1] = out[2] = 0.0f;
