@@ -107,6 +107,10 @@ def parse():
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
     ap.add_argument("--no-dg", action="store_true", help="skip the double-gyre (Cartesian 2D) workload")
     ap.add_argument("--no-parity", action="store_true", help="skip the parity window")
+    ap.add_argument("--probe-advect", type=int, default=0, metavar="NPTS",
+                    help="instead of the benchmark: a fixed step-level workload for instruction-mix profiles "
+                         "(fvc_advect, RK4 h=0.005 over one frame interval, NPTS points on the 32^3 cube, "
+                         "two calls; per-step figures = the second k_advect launch's counters / its steps)")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--served-rate", type=float, default=200.0, help="requests / s")
     ap.add_argument("--served-seconds", type=float, default=60.0, help="arrival window, s")
@@ -485,6 +489,9 @@ def bench_tracers(args, inputs):
         flow.upload_frames(ctx, ax, frames)
         flow.run_tracers(ctx, ax, seeds[:4096], 0.0, 0.05, 21)          # warm-up
         flow.run_tracers(ctx, ax, seeds[:4096], 0.0, 0.05, 21, asynchronous=False)
+        # one short release of the full size: the context's output ring is
+        # sized to the largest release it has seen (allocated once)
+        flow.run_tracers(ctx, ax, seeds, 0.0, 0.05, 2)
         # the blocking loop (each advance waits, each output is a blocking
         # compact-and-copy), for comparison
         t0 = time.perf_counter()
@@ -916,8 +923,35 @@ def run_engine(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def probe_advect(npts):
+    """The step-level workload of --probe-advect; prints each call's steps."""
+    import fvc
+    import synth
+    import build as fvc_build
+    fvc_build.build()
+    xyz, conn, adj = synth.kuhn_cube_mesh(32, jitter=0.2, seed=0)
+    g = fvc.Context(3, 1)
+    g.set_unstruct_mesh(xyz, conn, adj)
+    g.set_bounds([0, 1, 0, 1, 0, 1])
+    g.upload_frame(0, synth.abc_flow(xyz, 0.0))
+    g.upload_frame(1, synth.abc_flow(xyz, 0.02))
+    g.set_window(0, 1, 0.0, 0.02)
+    g.set_integrator(1, H, 0)
+    P = np.random.default_rng(0).uniform(0.05, 0.95, size=(npts, 3))
+    eid = g.global_search(P)
+    left = (eid < 0).astype(np.int32)
+    for call in range(2):
+        a = [P.copy(), np.zeros_like(P), eid.copy(), left.copy(), np.zeros(npts)]
+        steps = g.advect(*a, 0.0, 0.02)
+        print(json.dumps({"probe_advect_call": call, "steps": int(steps), "left": int(a[3].sum())}), flush=True)
+    g.close()
+
+
 def main():
     args = parse()
+    if args.probe_advect:
+        probe_advect(args.probe_advect)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

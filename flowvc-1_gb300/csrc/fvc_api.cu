@@ -426,6 +426,24 @@ extern "C" fvc_status fvc_set_integrator(fvc_ctx* c, int int_type, double h, int
 
 // ---------------------------------------------------------------- frames
 
+// Cartesian 2D frames whose w components are all +0.0: GetVelocity_Cartesian's
+// w sum over them is exactly +0.0, so the kernels skip it.  Each of its eight
+// products of +0.0 with a weight is a zero, and at least one is +0.0: a
+// weight t x y, t x (1-y), ..., (1-t)(1-x)(1-y) is negative (or -0) only if
+// an odd number of its factors is, and t and 1-t (x and 1-x, y and 1-y)
+// cannot both be, so not all eight are; a sum of zeros holding a +0.0 is
+// +0.0.  Other meshes use no flag.
+static void note_wzero(fvc_ctx* c, int frame_id, const double* uvw) {
+  if (c->mesh.dims != 2 || c->mesh.mesh_type != 0) return;
+  bool z = true;
+  for (long i = 0; i < c->frame_nodes && z; i++) {
+    unsigned long long b;
+    memcpy(&b, uvw + 3 * i + 2, sizeof(b));
+    z = b == 0ull;
+  }
+  c->frame_wzero[frame_id] = z;
+}
+
 extern "C" fvc_status fvc_upload_frame(fvc_ctx* c, int frame_id, const double* uvw) {
   if (!c || !uvw) return FVC_ERR_ARG;
   if (!c->mesh_set) return fail(c, FVC_ERR_STATE, "set the mesh before uploading frames");
@@ -444,6 +462,7 @@ extern "C" fvc_status fvc_upload_frame(fvc_ctx* c, int frame_id, const double* u
   FVC_CUDA(c, cudaMemcpyAsync(c->d_stage, uvw, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
   auto qf = c->qframes.find(frame_id);
   if (qf != c->qframes.end()) qf->second.fmt = 0;  // stale: quantised again when next used
+  note_wzero(c, frame_id, uvw);
   pack_frame(c->d_stage, dst, n, c->stream);
   if ((st = check_launch(c, "pack_frame"))) return st;
   FVC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -539,6 +558,7 @@ extern "C" fvc_status fvc_upload_frame_async(fvc_ctx* c, int frame_id, const dou
   if ((st = check_launch(c, "pack_frame"))) return st;
   auto qf = c->qframes.find(frame_id);
   if (qf != c->qframes.end()) qf->second.fmt = 0;
+  note_wzero(c, frame_id, uvw);
   FVC_CUDA(c, cudaEventRecord(ev, c->up_stream));
   return FVC_OK;
 }
@@ -648,6 +668,10 @@ extern "C" fvc_status fvc_set_window(fvc_ctx* c, int lo, int hi, double tmin, do
   c->window.rspan = rcp_for_div(tmax - tmin);
   c->window.nslots = 0;
   c->window.nsteps = 0;
+  {
+    auto za = c->frame_wzero.find(lo), zb = c->frame_wzero.find(hi);
+    c->window.wz = za != c->frame_wzero.end() && zb != c->frame_wzero.end() && za->second && zb->second;
+  }
   c->window_set = true;
   c->window_lo = lo;
   c->window_hi = hi;

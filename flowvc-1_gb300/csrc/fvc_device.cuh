@@ -180,7 +180,7 @@ __device__ __forceinline__ int vel_cart(const DevMesh& m, const DevWindow& w, do
    b100.c * V4 + b110.c * V2)
     out[0] = FVC_CSUM2(x);
     out[1] = FVC_CSUM2(y);
-    out[2] = FVC_CSUM2(z);
+    out[2] = w.wz ? 0.0 : FVC_CSUM2(z);  // the w sum of all-zero frames is +0.0
 #undef FVC_CSUM2
   }
   return 0;

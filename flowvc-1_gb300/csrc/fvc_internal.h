@@ -38,6 +38,8 @@ struct fvc_ctx {
   int* d_cell_ids = nullptr;
   BucketGrid grid{};
   std::unordered_map<int, double4_32a*> frames;
+  // Cartesian 2D: frames whose w components are all +0.0 (bit pattern 0)
+  std::unordered_map<int, bool> frame_wzero;
   double* d_stage = nullptr;  // frame upload staging, 3 doubles a node
   DevCounters* d_ctr = nullptr;
   double4_32a* d_vt = nullptr;  // stage-time node velocities

@@ -72,6 +72,9 @@ struct DevWindow {
   int qfmt;  // FVC_PREC_BF16 or FVC_PREC_FP16
   const StepM* steps;
   int nsteps;
+  // Cartesian 2D: both frames' w components are all +0.0, so the w sum of
+  // GetVelocity_Cartesian is +0.0 and is not computed
+  int wz;
 };
 
 // Uniform bucket grid over the mesh for Get_Element_Global_Search.

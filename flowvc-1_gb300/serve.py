@@ -256,6 +256,8 @@ def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
     nxt = 0
     running = {name: {} for name in sites}
     done = []
+    host = {"submit": 0.0, "tick": 0.0, "poll": 0.0, "results": 0.0, "idle": 0.0}
+    clock = time.perf_counter
     t0 = time.perf_counter()
     stopped = False
     while len(done) < len(pending):
@@ -265,38 +267,49 @@ def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
                 raise RuntimeError(f"serving did not finish within {time_limit} s")
             stopped = True
             break
+        c0 = clock()
         while nxt < len(pending) and pending[nxt].t_arrive <= now:
             r = pending[nxt]
             r.jid = submit(sites[r.site].batch, r.job)
             running[r.site][r.jid] = r
             nxt += 1
+        c1 = clock()
+        host["submit"] += c1 - c0
         busy = False
         for name, site in sites.items():
             if not running[name]:
                 continue
             busy = True
             b = site.batch
+            c0 = clock()
             b.tick()
-            for jid in list(running[name]):
-                if b.poll(jid) == fvc.BATCH_DONE:
-                    r = running[name].pop(jid)
-                    if r.kind == "ftle":
-                        res = b.ftle_result(jid)
-                    elif r.kind == "residence":
-                        res = b.residence_result(jid)
-                    else:
-                        res = b.tracer_result(jid)
-                    js = b.job_stats(jid)
-                    r.steps = js["steps_main"] + js["steps_early"]
-                    r.t_done = time.perf_counter() - t0
-                    if keep_results:
-                        r.result = res
-                    b.release(jid)
-                    done.append(r)
+            c1 = clock()
+            host["tick"] += c1 - c0
+            finished = [jid for jid in running[name] if b.poll(jid) == fvc.BATCH_DONE]
+            c2 = clock()
+            host["poll"] += c2 - c1
+            for jid in finished:
+                r = running[name].pop(jid)
+                if r.kind == "ftle":
+                    res = b.ftle_result(jid)
+                elif r.kind == "residence":
+                    res = b.residence_result(jid)
+                else:
+                    res = b.tracer_result(jid)
+                js = b.job_stats(jid)
+                r.steps = js["steps_main"] + js["steps_early"]
+                r.t_done = time.perf_counter() - t0
+                if keep_results:
+                    r.result = res
+                b.release(jid)
+                done.append(r)
+            host["results"] += clock() - c2
         if not busy and nxt < len(pending):
             wait = pending[nxt].t_arrive - (time.perf_counter() - t0)
             if wait > 0:
+                c0 = clock()
                 time.sleep(min(wait, 0.001))
+                host["idle"] += clock() - c0
     wall = time.perf_counter() - t0
     lat = np.array([r.t_done - r.t_arrive for r in done]) if done else np.zeros(1)
     steps = sum(r.steps for r in done)
@@ -318,7 +331,7 @@ def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
     out = {"requests": len(done), "wall_s": wall, "steps": int(steps), "steps_per_s": steps / wall,
            "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p95_ms": 1e3 * float(np.percentile(lat, 95)),
            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "max_ms": 1e3 * float(lat.max()),
-           "by_kind": by_kind}
+           "by_kind": by_kind, "host_s": {k: round(v, 3) for k, v in host.items()}}
     if stopped:
         waiting = np.array([wall - r.t_arrive for r in pending[:nxt] if r.t_done is None])
         out.update({"stopped_at_s": wall, "requests_total": len(pending), "requests_unfinished": len(pending) - len(done),
