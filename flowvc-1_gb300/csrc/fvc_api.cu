@@ -927,6 +927,27 @@ extern "C" fvc_status fvc_global_search(fvc_ctx* c, int n, const double* X, int*
 
 // ---------------------------------------------------------------- jobs
 
+// Frees a job that no queued GPU work uses any more (its last kernels have
+// completed and nothing reads it on another stream): as fvc_job_destroy,
+// without waiting for the context's stream.
+void job_destroy_idle(fvc_job* j) {
+  if (!j) return;
+  if (j->ctx) {
+    cudaSetDevice(j->ctx->device);
+    pool_put(j->ctx, j->mem, j->mem_bytes);
+    pool_put(j->ctx, j->rec_mem, j->rec_bytes);
+  } else {
+    cudaFree(j->mem);
+    cudaFree(j->rec_mem);
+  }
+  if (j->d_ctr) cudaFree(j->d_ctr);
+  for (int k = 0; k < 4; k++)
+    if (j->ev[k]) cudaEventDestroy(j->ev[k]);
+  for (cudaEvent_t e : j->pend) cudaEventDestroy(e);
+  for (cudaEvent_t e : j->spare) cudaEventDestroy(e);
+  delete j;
+}
+
 extern "C" void fvc_job_destroy(fvc_job* j) {
   if (!j) return;
   if (j->ctx) {

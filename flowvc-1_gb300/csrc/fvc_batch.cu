@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <deque>
+#include <initializer_list>
 #include <map>
 #include <memory>
 #include <vector>
@@ -400,6 +401,12 @@ struct fvc_batch {
   size_t qsort_cap = 0;  // entries
   int* d_qhist = nullptr;  // hist, off (+1), cur
   long long* d_qtmp = nullptr;
+  // results of finished jobs are read on a stream of their own, after the
+  // job's last tick (its done event), so reading them never waits for the
+  // ticks still in flight; d_res is that stream's scratch
+  cudaStream_t res_stream = nullptr;
+  double* d_res = nullptr;
+  size_t res_cap = 0;  // doubles
 };
 
 static constexpr int QSORT_KEYS = 1 << 22;
@@ -1125,6 +1132,10 @@ extern "C" fvc_status fvc_batch_create(fvc_ctx* c, const fvc_batch_opts* o, fvc_
   b->launch.blocks = (int)batch_resident(c->mesh.dims, c->prec, 128);
   b->resort = o->resort_every > 0 ? o->resort_every : 0;
   b->stats.tuned_resort = b->resort;
+  if (cudaStreamCreateWithFlags(&b->res_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    fvc_batch_destroy(b);
+    return fail(c, FVC_ERR_CUDA, "batch result stream");
+  }
   *out = b;
   return check_launch(c, "batch create");
 }
@@ -1155,6 +1166,11 @@ extern "C" void fvc_batch_destroy(fvc_batch* b) {
   for (auto& e : b->tick_ev) cudaEventDestroy(e);
   if (b->t_start) cudaEventDestroy(b->t_start);
   if (b->t_end) cudaEventDestroy(b->t_end);
+  if (b->res_stream) {
+    cudaStreamSynchronize(b->res_stream);
+    cudaStreamDestroy(b->res_stream);
+  }
+  cudaFree(b->d_res);
   delete b;
 }
 
@@ -1357,11 +1373,31 @@ static void unpermute(const std::vector<int>& perm, T* v, size_t w) {
     for (size_t a = 0; a < w; a++) v[(size_t)perm[j] * w + a] = tmp[j * w + a];
 }
 
+// Device-to-host copies of a finished job's arrays on the result stream,
+// ordered after the job's last tick; waits for this stream only.
+static fvc_status res_copy(fvc_batch* b, HostJob* J, std::initializer_list<std::pair<void*, const void*>> dst_src,
+                           std::initializer_list<size_t> bytes) {
+  fvc_ctx* c = b->c;
+  FVC_CUDA(c, cudaStreamWaitEvent(b->res_stream, J->done, 0));
+  auto bs = bytes.begin();
+  for (auto& ds : dst_src) {
+    const size_t n = *bs++;
+    if (ds.first && n) FVC_CUDA(c, cudaMemcpyAsync(ds.first, ds.second, n, cudaMemcpyDeviceToHost, b->res_stream));
+  }
+  FVC_CUDA(c, cudaStreamSynchronize(b->res_stream));
+  return FVC_OK;
+}
+
 extern "C" fvc_status fvc_batch_tracer_result(fvc_batch* b, int id, double* X, int* eid, int* left, double* ldt) {
   HostJob* J = job_of(b, id);
   fvc_status st = job_ready(b, J, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE));
   if (st) return st;
-  if ((st = fvc_tracer_get_state(J->job, X, eid, left, ldt))) return st;
+  if ((st = use_device(b->c))) return st;
+  const TracerDev& t = J->job->t;
+  const size_t n = (size_t)t.n;
+  if ((st = res_copy(b, J, {{X, t.X}, {eid, t.eid}, {left, t.left}, {ldt, t.ldt}}, {24 * n, 4 * n, 4 * n, 8 * n})))
+    return st;
+  if (X && J->job->packed) unpack_host(X, 3 * n);
   unpermute(J->perm, X, 3);
   unpermute(J->perm, eid, 1);
   unpermute(J->perm, left, 1);
@@ -1373,7 +1409,23 @@ extern "C" fvc_status fvc_batch_residence_result(fvc_batch* b, int id, double* r
   HostJob* J = job_of(b, id);
   fvc_status st = job_ready(b, J, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE));
   if (st) return st;
-  if ((st = fvc_tracer_residence(J->job, J->spec.t_start, J->stop, rt))) return st;
+  if (!rt) return FVC_ERR_ARG;
+  fvc_ctx* c = b->c;
+  if ((st = use_device(c))) return st;
+  const size_t n = (size_t)J->job->t.n;
+  if (n == 0) return FVC_OK;
+  if (n > b->res_cap) {
+    FVC_CUDA(c, cudaStreamSynchronize(b->res_stream));
+    cudaFree(b->d_res);
+    b->d_res = nullptr;
+    b->res_cap = 0;
+    if (cudaMalloc(&b->d_res, 8 * n) != cudaSuccess) return fail(c, FVC_ERR_OOM, "batch result scratch");
+    b->res_cap = n;
+  }
+  FVC_CUDA(c, cudaStreamWaitEvent(b->res_stream, J->done, 0));
+  tracer_residence(J->job->t, J->spec.t_start, J->stop, b->d_res, b->res_stream);
+  if ((st = check_launch(c, "residence time"))) return st;
+  if ((st = res_copy(b, J, {{rt, b->d_res}}, {8 * n}))) return st;
   unpermute(J->perm, rt, 1);
   return FVC_OK;
 }
@@ -1382,13 +1434,9 @@ extern "C" fvc_status fvc_batch_ftle_result(fvc_batch* b, int id, double* wT, do
   HostJob* J = job_of(b, id);
   fvc_status st = job_ready(b, J, 1 << FVC_JOB_FTLE);
   if (st) return st;
-  fvc_ctx* c = b->c;
-  if ((st = use_device(c))) return st;
-  size_t n = (size_t)J->job->f.n;
-  if (wT) FVC_CUDA(c, cudaMemcpyAsync(wT, J->job->f.out, 8 * n, cudaMemcpyDeviceToHost, c->stream));
-  if (wN) FVC_CUDA(c, cudaMemcpyAsync(wN, J->job->f.out + n, 8 * n, cudaMemcpyDeviceToHost, c->stream));
-  FVC_CUDA(c, cudaStreamSynchronize(c->stream));
-  return FVC_OK;
+  if ((st = use_device(b->c))) return st;
+  const size_t n = (size_t)J->job->f.n;
+  return res_copy(b, J, {{wT, J->job->f.out}, {wN, J->job->f.out + n}}, {8 * n, 8 * n});
 }
 
 extern "C" fvc_status fvc_batch_job_stats(fvc_batch* b, int id, fvc_job_stats* out) {
@@ -1407,7 +1455,10 @@ extern "C" fvc_status fvc_batch_release(fvc_batch* b, int id) {
     return fail(b->c, FVC_ERR_STATE, "batch job %d is still running", id);
   if (J->state == JQ_FINISHING) retire(b, true);
   if (J->job) {
-    fvc_job_destroy(J->job);
+    // the job's last tick has completed (done or failed) and result reads
+    // waited for their own stream: nothing queued uses its memory, so it
+    // goes back to the pool without draining the ticks in flight
+    job_destroy_idle(J->job);
     J->job = nullptr;
     b->used -= J->bytes;
   }

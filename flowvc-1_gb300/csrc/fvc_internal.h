@@ -143,6 +143,10 @@ fvc_status quantised(fvc_ctx* c, int id, fvc_ctx::QFrame** out);
 // the integrator / precision combination is one the form supports
 fvc_status mixed_ok(fvc_ctx* c);
 void job_events(fvc_job* j);
+// frees a job whose GPU work has all completed, without a stream wait
+void job_destroy_idle(fvc_job* j);
+// (X, c) float pairs copied to the host back to FP64 positions X - c
+void unpack_host(double* A, size_t n);
 // device memory from / back to the context's pool of freed blocks (a block
 // of at least `bytes` and at most twice that, else cudaMalloc)
 void* pool_get(fvc_ctx* c, size_t bytes);
@@ -150,8 +154,6 @@ void pool_put(fvc_ctx* c, void* p, size_t bytes);
 // orders the context's stream after a pending asynchronous upload of frame id
 void frame_dep(fvc_ctx* c, int id);
 float ev_ms(cudaEvent_t a, cudaEvent_t b);
-// (X, c) float pairs copied to the host back to FP64 positions X - c
-void unpack_host(double* A, size_t n);
 
 #define FVC_CUDA(c, x)                                                                   \
   do {                                                                                   \

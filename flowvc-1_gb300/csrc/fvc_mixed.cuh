@@ -347,48 +347,84 @@ __device__ __forceinline__ void kahan_add(float X[3], float c[3], const float in
 }
 
 // Euler or RK4 over table steps [0, kend) (Advect, ompVC/integration.c:
-// 22-45, with RK4's stage hints and exit rules, integration.c:317-462).  A
-// particle that leaves keeps its position before the step and records the
-// step's start time as LeftDomainTime.
+// 22-45, with RK4's exit rules, integration.c:317-462).  A particle that
+// leaves keeps its position before the step and records the step's start
+// time as LeftDomainTime.
+//
+// Walk hints.  ompVC starts each RK4 stage's walk from the element that
+// stage ended in on the previous step, and the step's locate from the
+// point's element; the FP64 form keeps that (its element ids are compared
+// bit for bit).  Here each walk starts where the previous one ended: stage
+// 1 at the located element (its coordinates are the locate's), stage k + 1
+// at stage k's element, the locate at stage 4's.  Consecutive stage points
+// lie half a step apart instead of a whole step, so walks hop about half as
+// often, and one running hint replaces four.  Only a point within the walk's
+// tolerance of a shared face can end in another element, where the P1
+// velocity is continuous: the results differ by rounding.  A stage whose
+// walk leaves the domain leaves the hint where it was.
 template <int D, class W>
 __device__ __forceinline__ void advect_mx(const DevMesh& m, const W& w, int type, PtM& p, int kend,
                                           unsigned& steps, int& err, const RecOut* rec = nullptr) {
   if (p.left) return;
   const float zero[3] = {0.0f, 0.0f, 0.0f};
-  int e[4] = {p.eid, p.eid, p.eid, p.eid};
-  int l[4] = {0, 0, 0, 0};
   NatM nc;
   nc.e = -1;
   for (int k = 0; k < kend; k++) {
     const StepM st = w.steps[k];
     const float h = st.h;
     float inc[3];
+    int hint = p.eid, out = 0;
+    // one stage: velocity at Y (compensation C) from the running hint
+    auto stage = [&](float tl, const float* Y, const float* C, const NatM* cache, float v[3]) {
+      int e = hint, l = 0;
+      err |= vel_mx<D>(m, w, tl, Y, C, e, l, v, cache);
+      if (l) {
+        err |= walk_fault(e);
+        out = 1;
+      } else {
+        hint = e;
+      }
+    };
     if (type == 0) {
       float v[3];
-      if ((err |= vel_mx<D>(m, w, st.tl0, p.X, p.c, e[0], l[0], v, &nc))) return;
+      stage(st.tl0, p.X, p.c, &nc, v);
+      if (err) return;
 #pragma unroll
       for (int q = 0; q < 3; q++) inc[q] = h * v[q];
     } else {
-      float k1[3], k2[3], k3[3], k4[3], M[3];
-      if ((err |= vel_mx<D>(m, w, st.tl0, p.X, p.c, e[0], l[0], k1, &nc))) return;
+      float kq[3], acc[3], M[3];
+      stage(st.tl0, p.X, p.c, &nc, kq);
+      if (err) return;
 #pragma unroll
-      for (int q = 0; q < 3; q++) M[q] = fmaf(0.5f * h, k1[q], p.X[q]);
-      if ((err |= vel_mx<D>(m, w, st.tlh, M, zero, e[1], l[1], k2, nullptr))) return;
+      for (int q = 0; q < 3; q++) {
+        acc[q] = kq[q];
+        M[q] = fmaf(0.5f * h, kq[q], p.X[q]);
+      }
+      stage(st.tlh, M, zero, nullptr, kq);
+      if (err) return;
 #pragma unroll
-      for (int q = 0; q < 3; q++) M[q] = fmaf(0.5f * h, k2[q], p.X[q]);
-      if ((err |= vel_mx<D>(m, w, st.tlh, M, zero, e[2], l[2], k3, nullptr))) return;
+      for (int q = 0; q < 3; q++) {
+        acc[q] = acc[q] + 2.0f * kq[q];
+        M[q] = fmaf(0.5f * h, kq[q], p.X[q]);
+      }
+      stage(st.tlh, M, zero, nullptr, kq);
+      if (err) return;
 #pragma unroll
-      for (int q = 0; q < 3; q++) M[q] = fmaf(h, k3[q], p.X[q]);
-      if ((err |= vel_mx<D>(m, w, st.tl1, M, zero, e[3], l[3], k4, nullptr))) return;
+      for (int q = 0; q < 3; q++) {
+        acc[q] = acc[q] + 2.0f * kq[q];
+        M[q] = fmaf(h, kq[q], p.X[q]);
+      }
+      stage(st.tl1, M, zero, nullptr, kq);
+      if (err) return;
 #pragma unroll
-      for (int q = 0; q < 3; q++) inc[q] = h * ((k1[q] + 2.0f * k2[q] + 2.0f * k3[q] + k4[q]) * (1.0f / 6.0f));
+      for (int q = 0; q < 3; q++) inc[q] = h * ((acc[q] + kq[q]) * (1.0f / 6.0f));
     }
     float X0[3] = {p.X[0], p.X[1], p.X[2]}, c0[3] = {p.c[0], p.c[1], p.c[2]};
     kahan_add(p.X, p.c, inc);
-    p.eid = locate_mx<D>(m, p.X, p.c, p.eid, err, &nc);
+    p.eid = locate_mx<D>(m, p.X, p.c, hint, err, &nc);
     if (err) return;
-    if (p.eid < 0 || l[0] || l[1] || l[2] || l[3]) {
-      err |= walk_fault(p.eid) | walk_fault(e[0]) | walk_fault(e[1]) | walk_fault(e[2]) | walk_fault(e[3]);
+    if (p.eid < 0 || out) {
+      err |= walk_fault(p.eid);
       p.left = 1;
       p.ldt = st.tc;
 #pragma unroll

@@ -239,6 +239,48 @@ def poisson_requests(tube, rate=200.0, duration=60.0, mix=(0.5, 0.4, 0.1), seed=
     return reqs
 
 
+class SeedPrefetch:
+    """Makes the requests' seed arrays (SectionSeeds) on a thread of its own,
+    in arrival order and at most `ahead` requests before the submission
+    cursor, so that a request arrives with its seeds ready, as it would from
+    a client, and their making does not hold up the serving loop."""
+
+    def __init__(self, reqs, ahead=64):
+        import threading
+        self.reqs, self.ahead = reqs, ahead
+        self.pos = 0
+        self.cv = threading.Condition()
+        self.ready = [threading.Event() for _ in reqs]
+        self.stop = False
+        self.th = threading.Thread(target=self._run, daemon=True)
+        self.th.start()
+
+    def _run(self):
+        for i, r in enumerate(self.reqs):
+            with self.cv:
+                while i >= self.pos + self.ahead and not self.stop:
+                    self.cv.wait()
+                if self.stop:
+                    return
+            kind, arg, t0, t1 = r.job
+            if callable(arg):
+                r.job = (kind, arg(), t0, t1)
+            self.ready[i].set()
+
+    def take(self, i):
+        with self.cv:
+            self.pos = i + 1
+            self.cv.notify()
+        self.ready[i].wait()
+        return self.reqs[i].job
+
+    def close(self):
+        with self.cv:
+            self.stop = True
+            self.cv.notify()
+        self.th.join()
+
+
 def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
     """Serves the requests in arrival order against the sites' batches.
 
@@ -258,19 +300,21 @@ def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
     done = []
     host = {"submit": 0.0, "tick": 0.0, "poll": 0.0, "results": 0.0, "idle": 0.0}
     clock = time.perf_counter
+    seeds = SeedPrefetch(pending)
     t0 = time.perf_counter()
     stopped = False
     while len(done) < len(pending):
         now = time.perf_counter() - t0
         if now > time_limit:
             if not censor:
+                seeds.close()
                 raise RuntimeError(f"serving did not finish within {time_limit} s")
             stopped = True
             break
         c0 = clock()
         while nxt < len(pending) and pending[nxt].t_arrive <= now:
             r = pending[nxt]
-            r.jid = submit(sites[r.site].batch, r.job)
+            r.jid = submit(sites[r.site].batch, seeds.take(nxt))
             running[r.site][r.jid] = r
             nxt += 1
         c1 = clock()
@@ -311,6 +355,7 @@ def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
                 time.sleep(min(wait, 0.001))
                 host["idle"] += clock() - c0
     wall = time.perf_counter() - t0
+    seeds.close()
     lat = np.array([r.t_done - r.t_arrive for r in done]) if done else np.zeros(1)
     steps = sum(r.steps for r in done)
     if stopped:
