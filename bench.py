@@ -18,7 +18,9 @@ value      accepted RK4 steps / s with mesh and frames resident in HBM; each
            are counted (ompVC performs them) and also reported on their own
            (steps_early_recorded).  ftle_points_per_s counts no steps.
 e2e        the same through the C ABI from pinned host buffers: mesh and all
-           frames copied host->device inside each step, FTLE fields copied back.
+           frames copied host->device inside each step (the mesh validated and
+           its records and bucket grid rebuilt), FTLE fields copied back; one
+           context for all steps.
 roofline   the main advection kernel (k_ftle_pass1) against the bound that
            applies to it, the FP64 pipe: FP64-pipe instructions per step (the
            committed instruction-mix profile) x steps / CUDA-event time,
@@ -500,8 +502,8 @@ def bench_tracers(args, inputs):
         # the release loop as it runs: advances queued, outputs through the
         # output ring to a writer thread that copies each into host memory
         t0 = time.perf_counter()
-        fin = {}
-        outs, steps, st = flow.run_tracers(ctx, ax, seeds, 0.0, 0.05, 21, state=fin)
+        fin, phases = {}, {}
+        outs, steps, st = flow.run_tracers(ctx, ax, seeds, 0.0, 0.05, 21, state=fin, timings=phases)
         wall = time.perf_counter() - t0
         finals[prec] = fin
         same = len(outs) == len(outs_b) and all(np.array_equal(x, y) for x, y in zip(outs, outs_b))
@@ -511,6 +513,7 @@ def bench_tracers(args, inputs):
                      "wall_over_kernel": wall / (st["ms_main"] / 1e3) if st["ms_main"] > 0 else None,
                      "blocking_wall_s": wall_b, "blocking_value": steps_b / wall_b,
                      "outputs_identical_to_blocking": bool(same and steps == steps_b),
+                     "host_phases_s": phases, "seeding_ms_device": st["ms_setup"],
                      "outputs": len(outs), "written": int(sum(len(o) for o in outs))}
         ctx.close()
     # final tracer states: endpoints (the last position inside for tracers that
@@ -836,20 +839,19 @@ def run_engine(args, rank, world, local_rank):
         pframes = [pin(f) for f in frames]
         h2d = pxyz.nbytes + pconn.nbytes + padj.nbytes + sum(f.nbytes for f in pframes)
         d2h = 2 * 8 * npts
-        ctx.close()
+        # the context stays (as an application keeps it); every step sends
+        # the mesh (validated, its records and bucket grid rebuilt on the
+        # device) and all frames up again and reads both FTLE fields back
         barrier()
         t0 = time.perf_counter()
         e2e_steps = 0
         for _ in range(args.steps):
-            c2 = fvc.Context(3, 1, device=local_rank)
-            c2.set_unstruct_mesh(pxyz, pconn, padj)
-            c2.set_bounds([0, 1, 0, 1, 0, 1])
-            c2.set_integrator(1, H, 0)
-            flow.upload_frames(c2, ax, pframes, asynchronous=True)
-            wT, wN, st, _ = flow.run_ftle(c2, ax, grid, T_WINDOW)
+            ctx.set_unstruct_mesh(pxyz, pconn, padj)
+            flow.upload_frames(ctx, ax, pframes, asynchronous=True)
+            wT, wN, st, _ = flow.run_ftle(ctx, ax, grid, T_WINDOW)
             e2e_steps += st
-            c2.close()
         barrier()
+        ctx.close()
         e2e_secs, e2e_all = reduce_over_ranks(time.perf_counter() - t0, e2e_steps, world)
         e2e = {"value": e2e_all / e2e_secs, "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}

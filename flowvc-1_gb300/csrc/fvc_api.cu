@@ -1416,6 +1416,8 @@ extern "C" fvc_status fvc_tracer_create(fvc_ctx* c, const fvc_tracer_spec* sp, i
   }
   cudaStream_t s = c->stream;
   if (n > 0) {
+    job_events(j);
+    cudaEventRecord(j->ev[3], s);
     FVC_CUDA(c, cudaMemcpyAsync(t.X, seeds, 24 * (size_t)n, cudaMemcpyHostToDevice, s));
     outside_domain_flags(c->mesh, n, t.X, left0, s);
     FVC_CUDA(c, cudaMemsetAsync(t.eid, 0xff, 4 * (size_t)n, s));
@@ -1436,7 +1438,9 @@ extern "C" fvc_status fvc_tracer_create(fvc_ctx* c, const fvc_tracer_spec* sp, i
       pack_pairs(t.X, 3L * n, s);
       j->packed = true;
     }
+    cudaEventRecord(j->ev[0], s);
     FVC_CUDA(c, cudaStreamSynchronize(s));
+    j->stats.ms_setup += ev_ms(j->ev[3], j->ev[0]);  // seeds up, located, marked
   }
   *out = j;
   return FVC_OK;

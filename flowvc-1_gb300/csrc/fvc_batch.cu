@@ -407,6 +407,9 @@ struct fvc_batch {
   cudaStream_t res_stream = nullptr;
   double* d_res = nullptr;
   size_t res_cap = 0;  // doubles
+  // admission (seed upload and location, Z-ordering) runs on a stream of
+  // its own, so its waits do not drain the ticks in flight
+  cudaStream_t setup_stream = nullptr;
 };
 
 static constexpr int QSORT_KEYS = 1 << 22;
@@ -616,21 +619,40 @@ static fvc_status zorder_tracers(fvc_batch* b, HostJob& J) {
   return FVC_OK;
 }
 
+// The job's device state is made on the batch's setup stream: the creation
+// calls wait for their own work (seed location is host-driven), and on the
+// context's stream that wait would take the ticks in flight with it.  Every
+// creation call returns after its work has completed, so the ticks that use
+// the job, issued later on the context's stream, see it.  The blocks the
+// creation takes from the context's pool were returned by jobs whose last
+// kernels have completed.
+struct SetupStream {
+  fvc_ctx* c;
+  cudaStream_t main;
+  SetupStream(fvc_batch* b) : c(b->c), main(b->c->stream) {
+    if (b->setup_stream) c->stream = b->setup_stream;
+  }
+  ~SetupStream() { c->stream = main; }
+};
+
 static fvc_status admit_one(fvc_batch* b, HostJob& J) {
   fvc_ctx* c = b->c;
   fvc_status st;
-  if (J.kind == FVC_JOB_FTLE) {
-    fvc_ftle_spec sp = J.spec.grid;
-    sp.start_time = J.spec.t_start;
-    sp.stop_time = J.stop;
-    sp.generate = 1;
-    st = fvc_ftle_create(c, &sp, &J.job);
-  } else {
-    fvc_tracer_spec sp{};
-    sp.local_search_checking = J.spec.local_search_checking;
-    sp.seed_chain = 0;
-    st = fvc_tracer_create(c, &sp, J.spec.n, J.seeds.data(), &J.job);
-    if (!st) st = zorder_tracers(b, J);
+  {
+    SetupStream on_setup(b);
+    if (J.kind == FVC_JOB_FTLE) {
+      fvc_ftle_spec sp = J.spec.grid;
+      sp.start_time = J.spec.t_start;
+      sp.stop_time = J.stop;
+      sp.generate = 1;
+      st = fvc_ftle_create(c, &sp, &J.job);
+    } else {
+      fvc_tracer_spec sp{};
+      sp.local_search_checking = J.spec.local_search_checking;
+      sp.seed_chain = 0;
+      st = fvc_tracer_create(c, &sp, J.spec.n, J.seeds.data(), &J.job);
+      if (!st) st = zorder_tracers(b, J);
+    }
   }
   if (st) return st;
   J.slot = b->free_slots.back();
@@ -1132,9 +1154,10 @@ extern "C" fvc_status fvc_batch_create(fvc_ctx* c, const fvc_batch_opts* o, fvc_
   b->launch.blocks = (int)batch_resident(c->mesh.dims, c->prec, 128);
   b->resort = o->resort_every > 0 ? o->resort_every : 0;
   b->stats.tuned_resort = b->resort;
-  if (cudaStreamCreateWithFlags(&b->res_stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&b->res_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->setup_stream, cudaStreamNonBlocking) != cudaSuccess) {
     fvc_batch_destroy(b);
-    return fail(c, FVC_ERR_CUDA, "batch result stream");
+    return fail(c, FVC_ERR_CUDA, "batch result / setup stream");
   }
   *out = b;
   return check_launch(c, "batch create");
@@ -1169,6 +1192,10 @@ extern "C" void fvc_batch_destroy(fvc_batch* b) {
   if (b->res_stream) {
     cudaStreamSynchronize(b->res_stream);
     cudaStreamDestroy(b->res_stream);
+  }
+  if (b->setup_stream) {
+    cudaStreamSynchronize(b->setup_stream);
+    cudaStreamDestroy(b->setup_stream);
   }
   cudaFree(b->d_res);
   delete b;

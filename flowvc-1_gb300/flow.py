@@ -157,7 +157,7 @@ class OutputWriter:
 
 
 def run_tracers(ctx: fvc.Context, ax: TimeAxis, seeds, t_start, out_delta, out_res, direction=1, lsc=1,
-                always=0, snapshots=True, state=None, asynchronous=True, consume=None):
+                always=0, snapshots=True, state=None, asynchronous=True, consume=None, timings=None):
     """One tracer release from t_start with outputs every out_delta (ompVC's
     Compute_Tracer loop, ompVC/tracers.c:25-289).  Returns (list of output
     arrays, steps, job stats); a dict passed as state receives the release's
@@ -167,11 +167,17 @@ def run_tracers(ctx: fvc.Context, ax: TimeAxis, seeds, t_start, out_delta, out_r
     output goes through the output ring to an OutputWriter thread, which
     passes it to consume(index, array) (default: keep a copy in the list
     returned); otherwise each advance waits and each output is a blocking
-    fvc_tracer_snapshot."""
+    fvc_tracer_snapshot.  A dict passed as timings receives the host
+    seconds of the release's phases (seeding, loop, draining the outputs,
+    reading the final state)."""
+    import time
+    clock = time.perf_counter
+    c0 = clock()
     t_end = t_start + (out_res - 1) * direction * out_delta
     first = int(math.floor((t_start - ax.tmin) / ax.tdelta)) if direction > 0 else int(math.ceil((t_start - ax.tmin) / ax.tdelta))
     last = int(math.ceil((t_end - ax.tmin) / ax.tdelta)) if direction > 0 else int(math.floor((t_end - ax.tmin) / ax.tdelta))
     job = fvc.TracerJob(ctx, seeds, lsc=lsc, chain=0)
+    c1 = clock()
     stop = t_end
     outs = []
     writer = None
@@ -214,12 +220,16 @@ def run_tracers(ctx: fvc.Context, ax: TimeAxis, seeds, t_start, out_delta, out_r
                 t1 = t2
             df += direction
     finally:
+        c2 = clock()
         if writer is not None:
             writer.close()
+    c3 = clock()
     st = job.stats()
     if asynchronous:
         steps = st["steps_main"]
     if state is not None:
         state.update(job.get_state())
     job.close()
+    if timings is not None:
+        timings.update({"seeding_s": c1 - c0, "loop_s": c2 - c1, "drain_s": c3 - c2, "finish_s": clock() - c3})
     return outs, steps, st
