@@ -221,25 +221,49 @@ __device__ __forceinline__ void load_geo(const DevMesh& m, int e, Geo<DIMS>& g) 
 }
 
 // Natural coordinates of X (ompVC/velocity.c:512-517 and 537-542, the same in
-// ompVC/mesh.c:542-547 and 587-591); returns d, their minimum.
+// ompVC/mesh.c:542-547 and 587-591).
 template <int DIMS>
-__device__ __forceinline__ double natural_from(const Geo<DIMS>& g, const double X[3], double& r,
-                                               double& s, double& t, double& wv) {
+__device__ __forceinline__ void natural_coords(const Geo<DIMS>& g, const double X[3], double& r, double& s,
+                                               double& t, double& wv) {
   if (DIMS == 3) {
     double dx = X[0] - g.x0, dy = X[1] - g.y0, dz = X[2] - g.z0;
     r = div_rn(g.a[0] * dx + g.a[1] * dy + g.a[2] * dz, g.V, g.rV);
     s = div_rn(g.a[3] * dx + g.a[4] * dy + g.a[5] * dz, g.V, g.rV);
     t = div_rn(g.a[6] * dx + g.a[7] * dy + g.a[8] * dz, g.V, g.rV);
     wv = 1 - r - s - t;
-    return dmin(r, dmin(s, dmin(t, wv)));
   } else {
     double dx = X[0] - g.x0, dy = X[1] - g.y0;
     r = div_rn(g.a[0] * dx + g.a[1] * dy, g.V, g.rV);
     s = div_rn(g.a[2] * dx + g.a[3] * dy, g.V, g.rV);
     t = 0;
     wv = 1 - r - s;
-    return dmin(r, dmin(s, wv));
   }
+}
+
+// d, the coordinates' minimum, as the reference forms it
+template <int DIMS>
+__device__ __forceinline__ double natural_min(double r, double s, double t, double wv) {
+  return DIMS == 3 ? dmin(r, dmin(s, dmin(t, wv))) : dmin(r, dmin(s, wv));
+}
+
+// Natural coordinates of X; returns d, their minimum.
+template <int DIMS>
+__device__ __forceinline__ double natural_from(const Geo<DIMS>& g, const double X[3], double& r,
+                                               double& s, double& t, double& wv) {
+  natural_coords<DIMS>(g, X, r, s, t, wv);
+  return natural_min<DIMS>(r, s, t, wv);
+}
+
+// The containment tests of the walk on the coordinates themselves: the
+// reference's (d + TINY) >= 0 (vel_rule) or d > -TINY, with d the minimum.
+// For a finite d, d + TINY rounds to a negative number exactly when
+// d < -TINY (within a factor two of TINY the sum is exact), so the first
+// test is d >= -TINY; a NaN coordinate makes wv, and so d, NaN, and fails
+// both forms.  Hence: every coordinate >= -TINY (> -TINY).
+template <int DIMS>
+__device__ __forceinline__ bool inside_tiny(double r, double s, double t, double wv, bool vel_rule) {
+  return above_neg_tiny(r, vel_rule) & above_neg_tiny(s, vel_rule) & (DIMS == 2 || above_neg_tiny(t, vel_rule)) &
+         above_neg_tiny(wv, vel_rule);
 }
 
 template <int DIMS>
@@ -256,7 +280,7 @@ __device__ __forceinline__ double natural(const DevMesh& m, int e, const double 
 struct NatCache {
   int e;
   int4 nd;
-  double r, s, t, w, d;
+  double r, s, t, w;
 };
 
 // The node velocities a tabulated stage evaluation interpolates, gathered
@@ -393,8 +417,7 @@ __device__ __forceinline__ int neighbour(const DevMesh& m, int e, int slot) { re
 // repeated the locate's solve, lane by lane.
 template <int DIMS>
 __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& eid, bool vel_rule, double& r,
-                                    double& s, double& t, double& wv, double& d, int4& nd,
-                                    const NatCache* nc = nullptr) {
+                                    double& s, double& t, double& wv, int4& nd, const NatCache* nc = nullptr) {
   const PosF P = pos_f32(X);
   int4 nb = neighbours(m, eid);
   for (int hop = 0; hop < m.max_hops;) {
@@ -411,15 +434,16 @@ __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& ei
       s = nc->s;
       t = nc->t;
       wv = nc->w;
-      d = nc->d;
       nd = nc->nd;
       return 0;
     }
     Geo<DIMS> g;
     load_geo<DIMS>(m, eid, g);
-    d = natural_from<DIMS>(g, X, r, s, t, wv);
+    natural_coords<DIMS>(g, X, r, s, t, wv);
     nd = g.nd;
-    if (vel_rule ? ((d + FVC_TINY) >= 0) : (d > -FVC_TINY)) return 0;
+    if (inside_tiny<DIMS>(r, s, t, wv, vel_rule)) return 0;
+    // the point is outside: the reference's face choice on d
+    const double d = natural_min<DIMS>(r, s, t, wv);
     int slot;
     if (fabs(r - d) < FVC_TINY) slot = 0;
     else if (fabs(s - d) < FVC_TINY) slot = 1;
@@ -451,7 +475,7 @@ __device__ __forceinline__ int vel_unstruct(const DevMesh& m, const DevWindow& w
     tloc = div_rn(tq - w.tmin, w.tmax - w.tmin, w.rspan);
     if ((tloc > 1 + FVC_TINY) || (tloc < 0 - FVC_TINY)) return PT_ERR_TLOC;
   }
-  double r, s, t, wv, d;
+  double r, s, t, wv;
   int4 nd;
   if (nc && nc->e == eid) {
     // the last locate tested this element at this position (d > -TINY)
@@ -461,7 +485,7 @@ __device__ __forceinline__ int vel_unstruct(const DevMesh& m, const DevWindow& w
     t = nc->t;
     wv = nc->w;
   } else {
-    if (walk<DIMS>(m, X, eid, true, r, s, t, wv, d, nd, nc)) {
+    if (walk<DIMS>(m, X, eid, true, r, s, t, wv, nd, nc)) {
       // out of the domain, or a failed walk (eid = EID_FAULT): the point stops
       left = 1;
       out[0] = out[1] = out[2] = 0.0;
@@ -506,9 +530,9 @@ __device__ __forceinline__ int locate_walk(const DevMesh& m, const double X[3], 
     err |= PT_ERR_WALK;
     return -1;
   }
-  double r, s, t, wv, d;
+  double r, s, t, wv;
   int4 nd;
-  if (walk<DIMS>(m, X, guess, false, r, s, t, wv, d, nd)) return guess == EID_FAULT ? EID_FAULT : -1;
+  if (walk<DIMS>(m, X, guess, false, r, s, t, wv, nd)) return guess == EID_FAULT ? EID_FAULT : -1;
   if (nc) {
     nc->e = guess;
     nc->nd = nd;
@@ -516,7 +540,6 @@ __device__ __forceinline__ int locate_walk(const DevMesh& m, const double X[3], 
     nc->s = s;
     nc->t = t;
     nc->w = wv;
-    nc->d = d;
   }
   return guess;
 }

@@ -72,4 +72,16 @@ __device__ __forceinline__ float f32_trunc(double x) {
   return __uint_as_float(bits);
 }
 
+// x >= -1e-10 (ge) or x > -1e-10 -- the walk's TINY -- decided on the bit
+// pattern with integer instructions (off the FP64 pipe), with the FP64
+// comparison's outcome for every x: +0 .. +inf pass; a negative x passes when
+// its magnitude is at most (below) 1e-10's; NaNs fail.
+__device__ __forceinline__ bool above_neg_tiny(double x, bool ge) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long a = u & 0x7fffffffffffffffull;
+  const unsigned long long tiny = 0x3ddb7cdfd9d7bdbbull;  // bits of 1.0e-10
+  if (!(u >> 63)) return a <= 0x7ff0000000000000ull;
+  return ge ? a <= tiny : a < tiny;
+}
+
 }  // namespace fvc

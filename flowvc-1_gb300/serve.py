@@ -386,14 +386,14 @@ def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
     return out
 
 
-def sustained(summary, reqs, duration):
+def sustained(summary, reqs, duration, p99_limit_ms=1000.0):
     """Whether a served run kept up with its arrivals: every request finished
-    within 5 s after the last arrival, and the requests arriving in the last
-    third of the window waited (p99) no more than twice those of the first
-    third (a queue that grows fails both)."""
+    within 5 s after the last arrival, p99 stayed under p99_limit_ms, and the
+    requests arriving in the last third of the window waited (p99) no more
+    than twice those of the first third (a queue that grows fails these)."""
     if summary.get("requests_unfinished"):
         return False
-    if summary["wall_s"] > duration + 5.0:
+    if summary["wall_s"] > duration + 5.0 or summary["p99_ms"] > p99_limit_ms:
         return False
     early = [r.t_done - r.t_arrive for r in reqs if r.t_done is not None and r.t_arrive < duration / 3]
     late = [r.t_done - r.t_arrive for r in reqs if r.t_done is not None and r.t_arrive > 2 * duration / 3]

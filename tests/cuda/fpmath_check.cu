@@ -1,7 +1,8 @@
 // Checks the helpers of fvc_fpmath.cuh on the GPU: div_rn(a, b,
 // rcp_for_div(b)) must equal CUDA's IEEE a / b bit for bit, and f32_trunc(x)
 // must equal __double2float_rz(x), on many seeded operands from several
-// distributions (one line of counts on stdout).  With a file argument it
+// distributions, and above_neg_tiny(x) must agree with the FP64 comparisons
+// against -1e-10 it stands for (one line of counts on stdout).  With a file argument it
 // also writes seeded (x, rn_root4(x)) pairs there for the host to check.
 #include <cstdio>
 #include <cstdint>
@@ -62,6 +63,29 @@ __global__ void k_div(uint64_t seed, long n, Out* o) {
   if (__float_as_uint(fw) != __float_as_uint(fg)) atomicAdd(&o->bad_cvt, 1ull);
 }
 
+// above_neg_tiny against the FP64 comparisons it replaces, x >= -TINY,
+// x > -TINY and the reference's own form (x + TINY) >= 0, on values around
+// -TINY, random magnitudes and the special values
+__global__ void k_tiny(uint64_t seed, long n, unsigned long long* bad) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double TINY = 1.0e-10;
+  uint64_t h = mix(seed ^ (uint64_t)i);
+  double x;
+  const int kind = (int)(i % 8);
+  if (kind == 0) x = rnd(h, -40, -28);                                     // around TINY's exponent
+  else if (kind == 1) x = __longlong_as_double(__double_as_longlong(-TINY) + (long long)(h % 65) - 32);
+  else if (kind == 2) x = __longlong_as_double(__double_as_longlong(TINY) + (long long)(h % 65) - 32);
+  else if (kind == 3) x = rnd(h, -1022, 1023);
+  else if (kind == 4) x = __longlong_as_double((long long)h);               // any bit pattern (NaNs, subnormals)
+  else {
+    const double sp[8] = {0.0, -0.0, INFINITY, -INFINITY, NAN, -NAN, -TINY, TINY};
+    x = sp[h % 8];
+  }
+  const bool ge = above_neg_tiny(x, true), gt = above_neg_tiny(x, false);
+  if (ge != (x >= -TINY) || ge != ((x + TINY) >= 0) || gt != (x > -TINY)) atomicAdd(bad, 1ull);
+}
+
 __global__ void k_root4(uint64_t seed, long n, double* out) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -82,8 +106,15 @@ int main(int argc, char** argv) {
   Out h;
   if (cudaMemcpy(&h, d, sizeof(Out), cudaMemcpyDeviceToHost) != cudaSuccess) return 3;
   h.n_div = h.n_cvt = (unsigned long long)n * reps;
-  printf("{\"n_div\": %llu, \"bad_div\": %llu, \"n_cvt\": %llu, \"bad_cvt\": %llu, \"first_bad\": [%.17g, %.17g, %d]}\n",
-         h.n_div, h.bad_div, h.n_cvt, h.bad_cvt, h.a, h.b, h.kind);
+  unsigned long long* dt = nullptr, bad_tiny = 0;
+  if (cudaMalloc(&dt, sizeof(unsigned long long)) != cudaSuccess) return 2;
+  cudaMemset(dt, 0, sizeof(unsigned long long));
+  k_tiny<<<(unsigned)((n + 255) / 256), 256>>>(0x5151ull, n, dt);
+  if (cudaMemcpy(&bad_tiny, dt, sizeof(bad_tiny), cudaMemcpyDeviceToHost) != cudaSuccess) return 3;
+  cudaFree(dt);
+  printf("{\"n_div\": %llu, \"bad_div\": %llu, \"n_cvt\": %llu, \"bad_cvt\": %llu, \"n_tiny\": %ld, "
+         "\"bad_tiny\": %llu, \"first_bad\": [%.17g, %.17g, %d]}\n",
+         h.n_div, h.bad_div, h.n_cvt, h.bad_cvt, n, bad_tiny, h.a, h.b, h.kind);
   cudaFree(d);
   if (argc > 3) {
     const long nr = 1L << 18;

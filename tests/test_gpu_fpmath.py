@@ -29,6 +29,7 @@ def test_div_rn_and_f32_trunc_match_ieee(tmp_path):
     assert out["n_div"] == 1 << 28
     assert out["bad_div"] == 0, out
     assert out["bad_cvt"] == 0, out
+    assert out["n_tiny"] == 1 << 26 and out["bad_tiny"] == 0, out
     # rn_root4: correctly rounded, checked exactly on the host with rationals
     # ((c -/+ half an ulp)^4 must bracket x).  The host libm's pow(x, 0.25),
     # which the reference's RKF calls, is not always correctly rounded: how
