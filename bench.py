@@ -117,6 +117,7 @@ def parse():
     ap.add_argument("--served-rate", type=float, default=200.0, help="requests / s")
     ap.add_argument("--served-seconds", type=float, default=60.0, help="arrival window, s")
     ap.add_argument("--served-sweep", action="store_true", help="add a rate sweep of the served form")
+    ap.add_argument("--served-forms", default="bf16,fp64", help="arithmetic forms of the served stream")
     ap.add_argument("--sweep-seconds", type=float, default=15.0, help="arrival window of each sweep point, s")
     return ap.parse_args()
 
@@ -600,11 +601,13 @@ def bench_served(args, tube, frames, cube_inputs):
                        "32^3-128^3, T=1), 10% residence time (tube, 1e5 seeds, 3 periods)",
            "hbm_budget_bytes": SERVED_BUDGET}
     limits = {"bf16": args.served_seconds + 240.0, "fp64": args.served_seconds + 30.0}
-    for prec in ("bf16", "fp64"):
+    forms = [f for f in ("bf16", "fp64") if f in args.served_forms.split(",")]
+    for prec in forms:
         out[prec] = run(prec, args.served_rate, args.served_seconds, limits[prec])
         out["requests"] = out[prec].get("requests_total", out[prec]["requests"])
-    out["speedup_vs_fp64"] = (out["bf16"]["steps_per_s"] / out["fp64"]["steps_per_s"]
-                              if out["fp64"]["steps_per_s"] else None)
+    if "bf16" in out and "fp64" in out:
+        out["speedup_vs_fp64"] = (out["bf16"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+                                  if out["fp64"]["steps_per_s"] else None)
     if args.served_sweep:
         sweep = {}
         for prec, rates in (("bf16", (25, 50, 100, 150, 200, 300)), ("fp64", (1, 2, 5, 10, 20))):

@@ -77,7 +77,10 @@ __device__ __forceinline__ float f32_trunc(double x) {
 // comparison's outcome for every x: +0 .. +inf pass; a negative x passes when
 // its magnitude is at most (below) 1e-10's; NaNs fail.
 __device__ __forceinline__ bool above_neg_tiny(double x, bool ge) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  // the move through inline PTX keeps the compiler from turning the integer
+  // tests back into FP64 comparisons (it recognises the sign-mask idiom)
+  unsigned long long u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
   const unsigned long long a = u & 0x7fffffffffffffffull;
   const unsigned long long tiny = 0x3ddb7cdfd9d7bdbbull;  // bits of 1.0e-10
   if (!(u >> 63)) return a <= 0x7ff0000000000000ull;
