@@ -288,6 +288,46 @@ __global__ void k_global(DevMesh m, BucketGrid g, int n, const double* X, const 
   out[i] = global_find<DIMS>(m, g, x);
 }
 
+// The global search's answer and whether it is the only element that
+// passes the containment test d > -TINY at the point.  Every element that can
+// pass it is a candidate of the point's bucket (their padded boxes hold the
+// point), so scanning the whole list decides it.  When it is the only one, a
+// neighbour walk from any start can stop nowhere else: it ends there, or
+// leaves the mesh (and with LocalSearchChecking the global search answers).
+template <int DIMS>
+__global__ void k_global_unique(DevMesh m, BucketGrid g, int n, const double* X, const int* skip, int* out,
+                                int* unique) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int first = -1, hits = 0;
+  if (!(skip && skip[i])) {
+    const double x[3] = {X[3 * (long)i], X[3 * (long)i + 1], X[3 * (long)i + 2]};
+    int c[3];
+    bool in = true;
+    for (int a = 0; a < 3; a++) {
+      if (a == 2 && DIMS == 2) { c[a] = 0; continue; }
+      double f = (x[a] - g.lo[a]) * g.inv[a];
+      if (!(f >= 0.0) || f >= (double)g.n[a]) { in = false; break; }
+      c[a] = min(g.n[a] - 1, (int)f);
+    }
+    if (in) {
+      const long cell = ((long)c[2] * g.n[1] + c[1]) * g.n[0] + c[0];
+      const int b = __ldg(g.start + cell), e = __ldg(g.start + cell + 1);
+      const PosF P = pos_f32(x);
+      for (int k = b; k < e && hits < 2; k++) {
+        const int el = __ldg(g.ids + k);
+        if (quick_hop<DIMS>(m, el, P) >= 0) continue;
+        if (contains<DIMS>(m, el, x)) {
+          if (!hits) first = el;
+          hits++;
+        }
+      }
+    }
+  }
+  out[i] = first;
+  unique[i] = hits == 1;
+}
+
 void launch_global_search(const DevMesh& m, const BucketGrid& g, int n, const double* X,
                           const int* skip, int* out, cudaStream_t s) {
   if (n <= 0) return;
@@ -374,6 +414,7 @@ struct ChainDev {
   const double* X;
   const int* left0;
   const int* R0;   // global-search answer of every seed
+  const int* U;    // 1: R0 is the only element holding the seed (see k_global_unique)
   int* R;          // current answers
   int* Rn;         // next answers
   int* g;          // guess of every seed
@@ -500,6 +541,7 @@ __global__ void k_chain_eval(DevMesh m, ChainDev c, DevCounters* ctr) {
     int r;
     if (c.left0[p]) r = -1;
     else if (p <= c.pstar) r = c.R0[p];
+    else if (c.lsc && c.U[p]) r = c.R0[p];  // every walk ends there (k_global_unique)
     else if (c.gprev && c.gprev[p] == c.g[p]) r = c.R[p];  // same guess, same walk
     else {
       double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
@@ -537,6 +579,7 @@ template <int DIMS>
 __device__ __forceinline__ int chain_one(const DevMesh& m, const BucketGrid& g, const ChainDev& c, long p,
                                          int guess, int& err) {
   if (c.left0[p]) return -1;
+  if (c.lsc && c.U[p]) return c.R0[p];  // every walk ends there (k_global_unique)
   const double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
   int r = locate_once<DIMS>(m, x, guess, err);
   if (r < 0) r = locate_once<DIMS>(m, x, c.seed, err);
@@ -618,6 +661,7 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
   c.nchunks = nblk(n, 1024);
   int* w = work;
   int* R0 = w; w += n;
+  int* U = w; w += n;
   c.R = w; w += n;
   c.Rn = w; w += n;
   c.g = w; w += n;
@@ -631,6 +675,13 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
   c.chunk_carry = w; w += c.nchunks + 1;
   int* d_first = w; w += 1;
   c.R0 = R0;
+  c.U = U;
+  // every seed's global-search answer and whether it is the only element
+  // holding it: such seeds' answers do not depend on their guesses (with
+  // LocalSearchChecking), which leaves the chain's walks to the few seeds
+  // on shared faces
+  if (m.dims == 3) k_global_unique<3><<<nblk(n, 128), 128, 0, s>>>(m, g, n, X, left0, R0, U);
+  else k_global_unique<2><<<nblk(n, 128), 128, 0, s>>>(m, g, n, X, left0, R0, U);
   if (a.kind == 0 && a.center_eid >= 0) {
     c.seed = a.center_eid;
     c.pstar = -1;
@@ -649,7 +700,6 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
     if (cudaStreamSynchronize(s) != cudaSuccess || status) return -1;
     return 0;
   }
-  launch_global_search(m, g, n, X, left0, R0, s);
   // first seed found by the global search: the chain's start when no centre
   // element is known (and always for a tracer list)
   int big = 0x7fffffff, first = big;
