@@ -34,6 +34,8 @@ CU_SOURCES = ["fvc_kernels.cu", "fvc_api.cu", "fvc_variant_c2.cu", "fvc_variant_
 MINBLOCKS = os.environ.get("FVC_MINBLOCKS", "4")
 MX_MINBLOCKS = os.environ.get("FVC_MX_MINBLOCKS", "4")
 TASK_MINBLOCKS = os.environ.get("FVC_TASK_MINBLOCKS", "3")
+# batch ticks queued on the GPU at once (FVC_BATCH_INFLIGHT overrides it)
+BATCH_INFLIGHT = os.environ.get("FVC_BATCH_INFLIGHT", "2")
 
 
 def _run(cmd):
@@ -69,7 +71,8 @@ def build_lib(force=False, verbose=False):
         objs.append(obj)
         if force or _newer(obj, deps):
             jobs.append([NVCC, *ARCH, *NVFLAGS, "-DFVC_MINBLOCKS=" + MINBLOCKS, "-DFVC_MX_MINBLOCKS=" + MX_MINBLOCKS,
-                         "-DFVC_TASK_MINBLOCKS=" + TASK_MINBLOCKS, "-c", os.path.join(CSRC, src),
+                         "-DFVC_TASK_MINBLOCKS=" + TASK_MINBLOCKS, "-DFVC_BATCH_INFLIGHT=" + BATCH_INFLIGHT,
+                         "-c", os.path.join(CSRC, src),
                          "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for r in ex.map(_run, jobs):

@@ -414,6 +414,12 @@ struct fvc_batch {
 
 static constexpr int QSORT_KEYS = 1 << 22;
 
+// ticks a batch may have queued on the GPU before fvc_batch_tick waits for
+// the oldest (build knob)
+#ifndef FVC_BATCH_INFLIGHT
+#define FVC_BATCH_INFLIGHT 2
+#endif
+
 using namespace fvc;
 
 static int frame_mod(const fvc_batch* b, long long frame) {
@@ -1146,7 +1152,7 @@ extern "C" fvc_status fvc_batch_create(fvc_ctx* c, const fvc_batch_opts* o, fvc_
   }
   for (int k = b->max_jobs - 1; k >= 0; k--) b->free_slots.push_back(k);
   for (int k = 0; k < 2; k++) cudaEventCreateWithFlags(&b->h_ev[k], cudaEventDisableTiming);
-  b->tick_ev.resize(2);
+  b->tick_ev.resize(FVC_BATCH_INFLIGHT);
   for (auto& e : b->tick_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   cudaEventCreate(&b->t_start);
   cudaEventCreate(&b->t_end);

@@ -541,7 +541,7 @@ __global__ void k_chain_eval(DevMesh m, ChainDev c, DevCounters* ctr) {
     int r;
     if (c.left0[p]) r = -1;
     else if (p <= c.pstar) r = c.R0[p];
-    else if (c.lsc && c.U[p]) r = c.R0[p];  // every walk ends there (k_global_unique)
+    else if (c.U && c.lsc && c.U[p]) r = c.R0[p];  // every walk ends there (k_global_unique)
     else if (c.gprev && c.gprev[p] == c.g[p]) r = c.R[p];  // same guess, same walk
     else {
       double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
@@ -579,7 +579,7 @@ template <int DIMS>
 __device__ __forceinline__ int chain_one(const DevMesh& m, const BucketGrid& g, const ChainDev& c, long p,
                                          int guess, int& err) {
   if (c.left0[p]) return -1;
-  if (c.lsc && c.U[p]) return c.R0[p];  // every walk ends there (k_global_unique)
+  if (c.U && c.lsc && c.U[p]) return c.R0[p];  // every walk ends there (k_global_unique)
   const double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
   int r = locate_once<DIMS>(m, x, guess, err);
   if (r < 0) r = locate_once<DIMS>(m, x, c.seed, err);
@@ -675,14 +675,10 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
   c.chunk_carry = w; w += c.nchunks + 1;
   int* d_first = w; w += 1;
   c.R0 = R0;
-  c.U = U;
-  // every seed's global-search answer and whether it is the only element
-  // holding it: such seeds' answers do not depend on their guesses (with
-  // LocalSearchChecking), which leaves the chain's walks to the few seeds
-  // on shared faces
-  if (m.dims == 3) k_global_unique<3><<<nblk(n, 128), 128, 0, s>>>(m, g, n, X, left0, R0, U);
-  else k_global_unique<2><<<nblk(n, 128), 128, 0, s>>>(m, g, n, X, left0, R0, U);
+  c.U = nullptr;
   if (a.kind == 0 && a.center_eid >= 0) {
+    // an FTLE grid: consecutive seeds are neighbours, so the serial walks
+    // are short and cheaper than the global search the shortcut needs
     c.seed = a.center_eid;
     c.pstar = -1;
     c.init_guess = a.center_eid;
@@ -700,6 +696,13 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
     if (cudaStreamSynchronize(s) != cudaSuccess || status) return -1;
     return 0;
   }
+  // every seed's global-search answer and whether it is the only element
+  // holding it: such seeds' answers do not depend on their guesses (with
+  // LocalSearchChecking), which leaves the rounds' walks to the few seeds on
+  // shared faces (a seed list's consecutive seeds can lie far apart)
+  c.U = U;
+  if (m.dims == 3) k_global_unique<3><<<nblk(n, 128), 128, 0, s>>>(m, g, n, X, left0, R0, U);
+  else k_global_unique<2><<<nblk(n, 128), 128, 0, s>>>(m, g, n, X, left0, R0, U);
   // first seed found by the global search: the chain's start when no centre
   // element is known (and always for a tracer list)
   int big = 0x7fffffff, first = big;
