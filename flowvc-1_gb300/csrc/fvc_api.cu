@@ -1027,8 +1027,7 @@ static fvc_status carve(fvc_ctx* c, void** mem, std::vector<std::pair<void**, si
 
 static fvc_status run_chain(fvc_ctx* c, const ChainArgs& a, const double* dX, const int* dleft0, int* deid,
                             long long* launches) {
-  size_t words = 6 * (size_t)a.n + 2 * ((size_t)a.res[0] * a.res[1] + 1) + 2 * ((size_t)a.res[0] + 1) +
-                 2 * ((size_t)a.n / 1024 + 2) + 16;
+  const size_t words = chain_words(a);
   int* work = (int*)pool_get(c, sizeof(int) * words);
   if (!work) return fail(c, FVC_ERR_OOM, "seed-chain scratch");
   int rounds = locate_chain(c->mesh, c->grid, a, dX, dleft0, deid, work, c->d_ctr, c->stream);

@@ -413,77 +413,50 @@ void pack_frame(const double* uvw, double4_32a* out, long n, cudaStream_t s) {
 struct ChainDev {
   const double* X;
   const int* left0;
-  const int* R0;   // global-search answer of every seed
+  const int* R0;   // global-search answer of every seed (FTLE chunks: of the marked seeds)
   const int* U;    // 1: R0 is the only element holding the seed (see k_global_unique)
   int* R;          // current answers
   int* Rn;         // next answers
   int* g;          // guess of every seed
   int* gprev;      // guesses of the previous round (null in the first round)
-  int* rowfirst;   // kind 0: first answer in each (i, j) row
-  int* rowstart;   // kind 0: guess at the start of each row
-  int* planefirst; // kind 0
-  int* planestart; // kind 0
-  int* chunk_last; // kinds 1, 2
+  int* planeexit;  // kind 0: the guess a plane leaves to the next, -1 none found
+  int* planestart; // kind 0: the guess at the start of each plane
+  int* planetarget;// kind 0 chunks: the seed whose answer is the plane's exit
+  int* chunk_last; // rounds: last found seed of each block of 1024
   int* chunk_carry;
-  int n, nrows, nplanes, nchunks;
+  int n, nplanes, plane, nchunks;
   int res[3];
   int kind, lsc, seed, pstar, init_guess;
 };
 
-// kind 0 (ompVC/ftle.c:467-601): a row restarts from the first element found
-// in the previous row (jguess), a plane from the first found in the previous
-// plane (iguess); within a row the guess is the last element found.
-__global__ void k_chain_rowfirst(ChainDev c) {
-  int row = blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= c.nrows) return;
-  int zr = c.res[2], first = -1;
-  for (int k = 0; k < zr; k++) {
-    int r = c.R[(long)row * zr + k];
-    if (r >= 0) { first = r; break; }
-  }
-  c.rowfirst[row] = first;
-}
-__global__ void k_chain_planefirst(ChainDev c) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+// The kind 0 guess (ompVC/ftle.c:467-601, as its braces nest): the running
+// guess is the last element found, across the rows of a plane as within
+// them (jguess is taken up only after the j loop); at the end of a plane it
+// becomes the first element found in the plane's last row (jguess), if any.
+// iguess is taken up after the i loop, when no seed is left.
+
+// Rounds: the guess each plane leaves, from the current answers.
+__global__ void k_chain_plane_exit(ChainDev c) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.nplanes) return;
-  int first = -1;
-  for (int j = 0; j < c.res[1]; j++) {
-    int r = c.rowfirst[(long)i * c.res[1] + j];
-    if (r >= 0) { first = r; break; }
-  }
-  c.planefirst[i] = first;
+  const long base = (long)i * c.plane, last_row = base + (long)(c.res[1] - 1) * c.res[2];
+  int e = -1;
+  for (int k = 0; k < c.res[2] && e < 0; k++) e = c.R[last_row + k];
+  for (long p = last_row - 1; p >= base && e < 0; p--) e = c.R[p];
+  c.planeexit[i] = e;
 }
 __global__ void k_chain_planes(ChainDev c) {
   if (threadIdx.x || blockIdx.x) return;
   int G = c.init_guess;
   for (int i = 0; i < c.nplanes; i++) {
     c.planestart[i] = G;
-    if (c.planefirst[i] >= 0) G = c.planefirst[i];
-  }
-}
-__global__ void k_chain_rows(ChainDev c) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.nplanes) return;
-  int G = c.planestart[i];
-  for (int j = 0; j < c.res[1]; j++) {
-    long row = (long)i * c.res[1] + j;
-    c.rowstart[row] = G;
-    if (c.rowfirst[row] >= 0) G = c.rowfirst[row];
-  }
-}
-__global__ void k_chain_row_guess(ChainDev c) {
-  int row = blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= c.nrows) return;
-  int zr = c.res[2], cur = c.rowstart[row];
-  for (int k = 0; k < zr; k++) {
-    long p = (long)row * zr + k;
-    c.g[p] = cur;
-    if (c.R[p] >= 0) cur = c.R[p];
+    if (c.planeexit[i] >= 0) G = c.planeexit[i];
   }
 }
 
 // kinds 1 and 2 (ompVC/tracers.c:1156-1243, 1379-1524): the guess is the
-// last element found before the seed in list order.
+// last element found before the seed in list order; kind 0 the same within
+// a plane, else the plane's start.
 __global__ void k_chain_chunk_last(ChainDev c) {
   __shared__ int best;
   if (threadIdx.x == 0) best = -1;
@@ -530,7 +503,13 @@ __global__ void k_chain_linear_guess(ChainDev c) {
   int excl_in_block = __shfl_up_sync(0xffffffffu, incl, 1);
   if (lane == 0) excl_in_block = before_warp;
   int last = max(excl_in_block, c.chunk_carry[blockIdx.x]);
-  if (p < c.n) c.g[p] = last >= 0 ? c.R[last] : c.init_guess;
+  if (p >= c.n) return;
+  if (c.kind == 0) {
+    const long i = p / c.plane;
+    c.g[p] = last >= i * c.plane ? c.R[last] : c.planestart[i];
+  } else {
+    c.g[p] = last >= 0 ? c.R[last] : c.init_guess;
+  }
 }
 
 template <int DIMS>
@@ -560,17 +539,25 @@ __global__ void k_chain_eval(DevMesh m, ChainDev c, DevCounters* ctr) {
   }
 }
 
-// The FTLE chain (kind 0) with a centre element, solved in its own order in
-// three sequential levels instead of by rounds: ompVC's answer for a seed
+// The FTLE chain (kind 0) with a centre element and LocalSearchChecking,
+// solved in its own order instead of by rounds: ompVC's answer for a seed
 // depends on its guess only when the seed lies within TINY of a shared face,
 // and on such seeds (grid points on the cube's edges, for example) the
-// rounds of the fixed point advance one seed at a time.  Level 1 (one
-// thread) follows the planes: each plane starts from the first element found
-// in the previous plane (iguess).  Level 2 (a thread per plane) follows the
-// rows of a plane from the first element found in the previous row
-// (jguess).  Level 3 (a thread per row) walks the row from the last element
-// found.  Each level evaluates the seeds it needs with the guess the serial
-// loop would hold, so the answers are the serial loop's.
+// rounds of the fixed point advance one seed at a time.  With
+// LocalSearchChecking a seed the global search finds in one element alone
+// has that element as its answer whatever its guess, and whether a seed is
+// found at all does not depend on its guess (the global search settles it).
+// Each plane's seeds are cut into chunks of CHAIN_CHUNK in loop order; the
+// seeds that end a chunk and the seeds of each plane's last row are tested
+// (k_chain_marks).  A chunk after a uniquely held seed starts from that
+// seed's element; one after any other seed is taken on by the thread of the
+// chunk before it, which goes on past its end.  The guess a plane leaves is
+// the answer of one seed (the first found in its last row, or the plane's
+// last found seed), worked out from the nearest uniquely held seed before
+// it; only when the plane holds none before it does the plane's start enter,
+// and the serial pass over the planes then walks that plane from its start.
+// Every seed is evaluated with exactly the guess the serial loop holds.
+constexpr int CHAIN_CHUNK = 16;
 
 // One seed with the given guess (ompVC/ftle.c:520-597): a walk from the
 // guess, then from the centre seed's element, then the global search when
@@ -579,59 +566,134 @@ template <int DIMS>
 __device__ __forceinline__ int chain_one(const DevMesh& m, const BucketGrid& g, const ChainDev& c, long p,
                                          int guess, int& err) {
   if (c.left0[p]) return -1;
-  if (c.U && c.lsc && c.U[p]) return c.R0[p];  // every walk ends there (k_global_unique)
+  if (c.U[p]) return c.R0[p];  // every walk ends there
   const double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
   int r = locate_once<DIMS>(m, x, guess, err);
   if (r < 0) r = locate_once<DIMS>(m, x, c.seed, err);
-  if (r < 0 && c.lsc) r = global_find<DIMS>(m, g, x);
+  if (r < 0) r = global_find<DIMS>(m, g, x);
   return r;
 }
 
+// first: lowest-id element holding x among the bucket's candidates; the
+// return value counts them up to 2
 template <int DIMS>
-__global__ void k_chain3_planes(DevMesh m, BucketGrid g, ChainDev c, DevCounters* ctr) {
-  if (threadIdx.x || blockIdx.x) return;
-  int err = 0, G = c.init_guess;
-  const long plane = (long)c.res[1] * c.res[2];
-  for (int i = 0; i < c.nplanes; i++) {
-    c.planestart[i] = G;
-    // before the plane's first find every seed's guess is the plane start
-    for (long q = 0; q < plane; q++) {
-      const int r = chain_one<DIMS>(m, g, c, i * plane + q, G, err);
-      if (r >= 0) {
-        G = r;
-        break;
-      }
+__device__ __forceinline__ int holders(const DevMesh& m, const BucketGrid& g, const double x[3], int& first) {
+  first = -1;
+  int cc[3];
+  for (int a = 0; a < 3; a++) {
+    if (a == 2 && DIMS == 2) { cc[a] = 0; continue; }
+    double f = (x[a] - g.lo[a]) * g.inv[a];
+    if (!(f >= 0.0) || f >= (double)g.n[a]) return 0;
+    cc[a] = min(g.n[a] - 1, (int)f);
+  }
+  const long cell = ((long)cc[2] * g.n[1] + cc[1]) * g.n[0] + cc[0];
+  const int b0 = __ldg(g.start + cell), e0 = __ldg(g.start + cell + 1);
+  const PosF P = pos_f32(x);
+  int hits = 0;
+  for (int q = b0; q < e0 && hits < 2; q++) {
+    const int el = __ldg(g.ids + q);
+    if (quick_hop<DIMS>(m, el, P) >= 0) continue;
+    if (contains<DIMS>(m, el, x)) {
+      if (!hits) first = el;
+      hits++;
     }
   }
-  if (err) atomicOr(&ctr->status, err);
+  return hits;
 }
 
+// R0 and U for the seeds that end a chunk of their plane and for the seeds
+// of each plane's last row; every other seed gets U = 0 and R0 = -1.
 template <int DIMS>
-__global__ void k_chain3_rows(DevMesh m, BucketGrid g, ChainDev c, DevCounters* ctr) {
+__global__ void k_chain_marks(DevMesh m, BucketGrid g, ChainDev c) {
+  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n) return;
+  const int q = (int)(p % c.plane);
+  const bool mark = (q + 1) % CHAIN_CHUNK == 0 || q + 1 == c.plane || q >= (c.res[1] - 1) * c.res[2];
+  int first = -1, hits = 0;
+  if (mark && !c.left0[p]) {
+    const double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
+    hits = holders<DIMS>(m, g, x, first);
+  }
+  const_cast<int*>(c.R0)[p] = first;
+  const_cast<int*>(c.U)[p] = hits == 1;
+}
+
+// The guess plane i leaves, where it does not depend on the plane's start:
+// planeexit = that element (-1: no seed of the plane is found, the guess
+// passes through), planetarget = the seed it is the answer of; planeexit =
+// -2 when the plane holds no uniquely held seed before the target.
+template <int DIMS>
+__global__ void k_chain_exits(DevMesh m, BucketGrid g, ChainDev c, DevCounters* ctr) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.nplanes) return;
-  int err = 0, G = c.planestart[i];
-  for (int j = 0; j < c.res[1]; j++) {
-    const long row = (long)i * c.res[1] + j;
-    c.rowstart[row] = G;
-    for (int k = 0; k < c.res[2]; k++) {
-      const int r = chain_one<DIMS>(m, g, c, row * c.res[2] + k, G, err);
-      if (r >= 0) {
-        G = r;
-        break;
+  const long base = (long)i * c.plane, last_row = base + (long)(c.res[1] - 1) * c.res[2];
+  long t = -1;
+  for (int k = 0; k < c.res[2] && t < 0; k++)
+    if (!c.left0[last_row + k] && c.R0[last_row + k] >= 0) t = last_row + k;
+  for (long p = last_row - 1; p >= base && t < 0; p--) {
+    if (c.left0[p]) continue;
+    int first = c.R0[p];
+    if (first < 0) {
+      const double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
+      holders<DIMS>(m, g, x, first);
+    }
+    if (first >= 0) t = p;
+  }
+  c.planetarget[i] = (int)t;
+  if (t < 0) { c.planeexit[i] = -1; return; }
+  long a = t - 1;
+  if (!c.U[t])
+    while (a >= base && !c.U[a]) a--;
+  if (!c.U[t] && a < base) { c.planeexit[i] = -2; return; }
+  int err = 0, G = c.U[t] ? c.R0[t] : c.R0[a];
+  if (!c.U[t])
+    for (long p = a + 1; p <= t; p++) {
+      const int r = chain_one<DIMS>(m, g, c, p, G, err);
+      if (r >= 0) G = r;
+    }
+  c.planeexit[i] = G;
+  if (err) atomicOr(&ctr->status, err);
+}
+
+// The planes in order: each plane's start, walking a plane from its start
+// where its exit depends on it.
+template <int DIMS>
+__global__ void k_chain_plane_starts(DevMesh m, BucketGrid g, ChainDev c, DevCounters* ctr) {
+  if (threadIdx.x || blockIdx.x) return;
+  int err = 0, G = c.init_guess;
+  for (int i = 0; i < c.nplanes; i++) {
+    c.planestart[i] = G;
+    int e = c.planeexit[i];
+    if (e == -2) {
+      for (long p = (long)i * c.plane; p <= c.planetarget[i]; p++) {
+        const int r = chain_one<DIMS>(m, g, c, p, G, err);
+        if (r >= 0) G = r;
       }
+    } else if (e >= 0) {
+      G = e;
     }
   }
   if (err) atomicOr(&ctr->status, err);
 }
 
+// One thread per (plane, chunk): the chunk's seeds from its starting guess,
+// on into the next chunks until one starts after a uniquely held seed.
 template <int DIMS>
-__global__ void k_chain3_points(DevMesh m, BucketGrid g, ChainDev c, int* eid, DevCounters* ctr) {
-  const long row = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= c.nrows) return;
-  int err = 0, cur = c.rowstart[row];
-  for (int k = 0; k < c.res[2]; k++) {
-    const long p = row * c.res[2] + k;
+__global__ void k_chain_points(DevMesh m, BucketGrid g, ChainDev c, int* eid, DevCounters* ctr) {
+  const int nch = (c.plane + CHAIN_CHUNK - 1) / CHAIN_CHUNK;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)c.nplanes * nch) return;
+  const long i = t / nch;
+  const int ch = (int)(t % nch), start = ch * CHAIN_CHUNK;
+  const long base = i * c.plane;
+  int cur;
+  if (ch == 0) cur = c.planestart[i];
+  else if (c.U[base + start - 1]) cur = c.R0[base + start - 1];
+  else return;  // the chunk before goes on into this one
+  int err = 0;
+  for (int q = start; q < c.plane; q++) {
+    if (q > start && q % CHAIN_CHUNK == 0 && c.U[base + q - 1]) break;  // that chunk's own thread
+    const long p = base + q;
     const int r = chain_one<DIMS>(m, g, c, p, cur, err);
     eid[p] = r;
     if (r >= 0) cur = r;
@@ -642,6 +704,11 @@ __global__ void k_chain3_points(DevMesh m, BucketGrid g, ChainDev c, int* eid, D
 __global__ void k_first_found(int n, const int* left0, const int* R0, int* out) {
   long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p < n && !left0[p] && R0[p] >= 0) atomicMin(out, (int)p);
+}
+
+size_t chain_words(const ChainArgs& a) {
+  const size_t planes = a.kind == 0 ? (size_t)a.res[0] : 0;
+  return 6 * (size_t)a.n + 3 * (planes + 1) + 2 * ((size_t)a.n / 1024 + 2) + 16;
 }
 
 int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, const double* X,
@@ -657,7 +724,7 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
   c.res[1] = a.res[1];
   c.res[2] = a.res[2];
   c.nplanes = a.kind == 0 ? a.res[0] : 0;
-  c.nrows = a.kind == 0 ? a.res[0] * a.res[1] : 0;
+  c.plane = a.kind == 0 ? a.res[1] * a.res[2] : 1;
   c.nchunks = nblk(n, 1024);
   int* w = work;
   int* R0 = w; w += n;
@@ -667,29 +734,29 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
   c.g = w; w += n;
   int* gother = w; w += n;
   c.gprev = nullptr;
-  c.rowfirst = w; w += c.nrows + 1;
-  c.rowstart = w; w += c.nrows + 1;
-  c.planefirst = w; w += c.nplanes + 1;
+  c.planeexit = w; w += c.nplanes + 1;
   c.planestart = w; w += c.nplanes + 1;
+  c.planetarget = w; w += c.nplanes + 1;
   c.chunk_last = w; w += c.nchunks + 1;
   c.chunk_carry = w; w += c.nchunks + 1;
   int* d_first = w; w += 1;
   c.R0 = R0;
-  c.U = nullptr;
-  if (a.kind == 0 && a.center_eid >= 0) {
-    // an FTLE grid: consecutive seeds are neighbours, so the serial walks
-    // are short and cheaper than the global search the shortcut needs
+  c.U = U;
+  if (a.kind == 0 && a.center_eid >= 0 && a.lsc) {
     c.seed = a.center_eid;
     c.pstar = -1;
     c.init_guess = a.center_eid;
+    const long nch = (long)c.nplanes * ((c.plane + CHAIN_CHUNK - 1) / CHAIN_CHUNK);
     if (m.dims == 3) {
-      k_chain3_planes<3><<<1, 32, 0, s>>>(m, g, c, ctr);
-      k_chain3_rows<3><<<nblk(c.nplanes, 32), 32, 0, s>>>(m, g, c, ctr);
-      k_chain3_points<3><<<nblk(c.nrows, 64), 64, 0, s>>>(m, g, c, eid, ctr);
+      k_chain_marks<3><<<nblk(n, 128), 128, 0, s>>>(m, g, c);
+      k_chain_exits<3><<<nblk(c.nplanes, 32), 32, 0, s>>>(m, g, c, ctr);
+      k_chain_plane_starts<3><<<1, 32, 0, s>>>(m, g, c, ctr);
+      k_chain_points<3><<<nblk(nch, 64), 64, 0, s>>>(m, g, c, eid, ctr);
     } else {
-      k_chain3_planes<2><<<1, 32, 0, s>>>(m, g, c, ctr);
-      k_chain3_rows<2><<<nblk(c.nplanes, 32), 32, 0, s>>>(m, g, c, ctr);
-      k_chain3_points<2><<<nblk(c.nrows, 64), 64, 0, s>>>(m, g, c, eid, ctr);
+      k_chain_marks<2><<<nblk(n, 128), 128, 0, s>>>(m, g, c);
+      k_chain_exits<2><<<nblk(c.nplanes, 32), 32, 0, s>>>(m, g, c, ctr);
+      k_chain_plane_starts<2><<<1, 32, 0, s>>>(m, g, c, ctr);
+      k_chain_points<2><<<nblk(nch, 64), 64, 0, s>>>(m, g, c, eid, ctr);
     }
     int status = 0;
     cudaMemcpyAsync(&status, &ctr->status, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -700,7 +767,6 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
   // holding it: such seeds' answers do not depend on their guesses (with
   // LocalSearchChecking), which leaves the rounds' walks to the few seeds on
   // shared faces (a seed list's consecutive seeds can lie far apart)
-  c.U = U;
   if (m.dims == 3) k_global_unique<3><<<nblk(n, 128), 128, 0, s>>>(m, g, n, X, left0, R0, U);
   else k_global_unique<2><<<nblk(n, 128), 128, 0, s>>>(m, g, n, X, left0, R0, U);
   // first seed found by the global search: the chain's start when no centre
@@ -730,16 +796,12 @@ int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, cons
   for (;;) {
     rounds++;
     if (a.kind == 0) {
-      k_chain_rowfirst<<<nblk(c.nrows, 128), 128, 0, s>>>(c);
-      k_chain_planefirst<<<nblk(c.nplanes, 128), 128, 0, s>>>(c);
+      k_chain_plane_exit<<<nblk(c.nplanes, 128), 128, 0, s>>>(c);
       k_chain_planes<<<1, 32, 0, s>>>(c);
-      k_chain_rows<<<nblk(c.nplanes, 128), 128, 0, s>>>(c);
-      k_chain_row_guess<<<nblk(c.nrows, 128), 128, 0, s>>>(c);
-    } else {
-      k_chain_chunk_last<<<c.nchunks, 1024, 0, s>>>(c);
-      k_chain_carry<<<1, 32, 0, s>>>(c);
-      k_chain_linear_guess<<<c.nchunks, 1024, 0, s>>>(c);
     }
+    k_chain_chunk_last<<<c.nchunks, 1024, 0, s>>>(c);
+    k_chain_carry<<<1, 32, 0, s>>>(c);
+    k_chain_linear_guess<<<c.nchunks, 1024, 0, s>>>(c);
     cudaMemsetAsync(&ctr->changed, 0, sizeof(int), s);
     if (m.dims == 3) k_chain_eval<3><<<nblk(n, 128), 128, 0, s>>>(m, c, ctr);
     else k_chain_eval<2><<<nblk(n, 128), 128, 0, s>>>(m, c, ctr);

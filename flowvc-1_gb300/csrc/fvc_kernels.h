@@ -78,6 +78,8 @@ struct ChainArgs {
 // fixed-point rounds, or -1 on a device fault.
 int locate_chain(const DevMesh& m, const BucketGrid& g, const ChainArgs& a, const double* X,
                  const int* left0, int* eid, int* work, DevCounters* ctr, cudaStream_t s);
+// ints of scratch locate_chain needs in `work`
+size_t chain_words(const ChainArgs& a);
 
 // ---- FTLE slide
 struct FtleDev {

@@ -251,10 +251,11 @@ static int ftle_seed(orc_run_state *S, ftle_slide *s, long long *ngs)
     Xs[2] = P->fb[4] + ((int)(zr / 2)) * P->fdelta[2];
     int seed = orc_global(c, Xs), guess = -1, err = 0;
     if (seed >= 0) guess = seed;
+    int iguess = -1, jguess = -1;
     for (int i = 0; i < xr; i++) {
-        int iguess = -1;
+        iguess = -1;
         for (int j = 0; j < yr; j++) {
-            int jguess = -1;
+            jguess = -1;
             for (int k = 0; k < zr; k++) {
                 int p = (i * yr + j) * zr + k;
                 if (s->left[p]) continue;
@@ -275,10 +276,14 @@ static int ftle_seed(orc_run_state *S, ftle_slide *s, long long *ngs)
                 if (jguess < 0) jguess = index;
                 if (iguess < 0) iguess = index;
             }
-            if (jguess >= 0) guess = jguess;
         }
-        if (iguess >= 0) guess = iguess;
+        /* ompVC/ftle.c:597-598 stand after the j loop (the indentation there
+         * suggests a restart per row): within a plane the guess runs on from
+         * row to row, and the next plane starts from the first element found
+         * in this plane's last row */
+        if (jguess >= 0) guess = jguess;
     }
+    if (iguess >= 0) guess = iguess; /* ompVC/ftle.c:600-601, after the i loop: no effect */
     return err ? ORC_ERR_WALK : ORC_OK;
 }
 

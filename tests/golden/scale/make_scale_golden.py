@@ -7,8 +7,10 @@ runs the unmodified ompVC program built from the reference sources
 outputs themselves (tens of MB each), their summaries:
 
   expected.json        SHA-256 and size of every output file, the FTLE time
-                       stamps, the SHA-256 of every input file, and the
-                       wall time and settings of each ompVC run
+                       stamps, the SHA-256 of every input file, of the
+                       located seed grid's element ids and left flags
+                       (ompVC's FTLE_ICFile), and the wall time and
+                       settings of each ompVC run
   ftle_summaries.npz   per FTLE field every 509th value and the sums of
                        blocks of 4096 values (with the sums of magnitudes)
 
@@ -61,6 +63,11 @@ def main(names):
                 sys.exit(f"ompVC failed on {case}:\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
             files, arr = sc.summarise(out)
             meta["cases"][case] = {"files": files, "ompvc_wall_s": round(wall, 2), "host_threads": nthreads}
+            ic = os.path.join(data, "ftle_ic.bin")
+            if sc.CASES[case][1].get("FTLE_Compute") and kind == "cube" and os.path.exists(ic):
+                # the located seed grid: element ids and left flags
+                meta["cases"][case]["ic"] = sc.ic_digests(ic)
+                os.remove(ic)
             for k in [k for k in arrays if k.startswith(case + ":")]:
                 del arrays[k]
             arrays.update({f"{case}:{k}": v for k, v in arr.items()})

@@ -133,6 +133,40 @@ def summarise(out_dir):
     return files, arrays
 
 
+def ic_arrays(path):
+    """Element ids and left flags of an FTLE_ICFile (the located seed grid
+    ompVC writes at initialisation, ompVC/ftle.c:383-628): three int32
+    resolutions, then one 104-byte FTLEPoint record a seed with the element
+    id at byte 48 and LeftDomain at byte 56 (ompVC/structs.h layout on
+    x86-64 and aarch64)."""
+    raw = np.fromfile(path, np.uint8)
+    res = raw[:12].view(np.int32)
+    n = int(res[0]) * int(res[1]) * int(res[2])
+    rec = raw[12:12 + 104 * n].reshape(n, 104)
+    eid = rec[:, 48:52].copy().view(np.int32).ravel()
+    left = rec[:, 56:60].copy().view(np.int32).ravel()
+    return eid, left
+
+
+def ic_digests(path):
+    eid, left = ic_arrays(path)
+    return {"n": int(len(eid)), "eid_sha256": hashlib.sha256(eid.tobytes()).hexdigest(),
+            "left_sha256": hashlib.sha256(left.tobytes()).hexdigest()}
+
+
+def check_ic_against_fixture(case, ic_path, meta):
+    """The located seed grid (element ids, left flags) of an FTLE run on the
+    cube against ompVC's; every cube FTLE case shares cube_ftle_5's grid."""
+    if not case.startswith("cube_ftle"):
+        return False
+    exp = meta["cases"]["cube_ftle_5"]["ic"]
+    got = ic_digests(ic_path)
+    assert got["n"] == exp["n"], f"{case}: {got['n']} seeds in the IC file, ompVC wrote {exp['n']}"
+    assert got["left_sha256"] == exp["left_sha256"], f"{case}: seed left flags differ from ompVC's"
+    assert got["eid_sha256"] == exp["eid_sha256"], f"{case}: seed element ids differ from ompVC's"
+    return True
+
+
 def load_fixture():
     with open(os.path.join(FIXTURE, "expected.json")) as f:
         meta = json.load(f)

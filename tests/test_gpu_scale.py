@@ -16,6 +16,7 @@ the three-level seed chain and hint ties on shared faces."""
 import os
 import subprocess
 
+import numpy as np
 import pytest
 
 import scale_cases as sc
@@ -49,6 +50,9 @@ def run_both(engine, oracle_bin, case, root, meta):
             args += [str(os.cpu_count() or 1)]
         r = subprocess.run(args, capture_output=True, text=True, env=env, timeout=900)
         assert r.returncode == 0, f"{name} failed on {case}:\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}"
+        ic = os.path.join(data, "ftle_ic.bin")
+        if os.path.exists(ic):  # the located seed grid, written into the data directory
+            os.replace(ic, os.path.join(root, f"{name}_{case}_ftle_ic.bin"))
         out[name] = (o, dump)
     return out
 
@@ -59,6 +63,12 @@ def test_engine_ftle_at_scale(engine, oracle_bin, scale_data, case):
     out = run_both(engine, oracle_bin, case, root, meta)
     (g, gdump), (o, odump) = out["gpu"], out["orc"]
     assert compare_state_dumps(odump, gdump) == 1
+    if case.startswith("cube_ftle"):
+        # the seed chain's answers against ompVC's and the oracle's
+        gic = os.path.join(root, f"gpu_{case}_ftle_ic.bin")
+        assert sc.check_ic_against_fixture(case, gic, meta)
+        for a, b in zip(sc.ic_arrays(gic), sc.ic_arrays(os.path.join(root, f"orc_{case}_ftle_ic.bin"))):
+            assert np.array_equal(a, b)
     sc.check_exact_files(case, g, meta)
     worst = sc.check_ftle_against_fixture(case, g, meta, arrays, rtol=FTLE_RTOL, atol=FTLE_ATOL)
     # the oracle's eigen-solver (Jacobi) is not the engine's (closed form),

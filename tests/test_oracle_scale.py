@@ -42,6 +42,7 @@ def test_oracle_ftle_matches_ompvc_at_scale(oracle_bin, scale_data, case):
     root, meta, arrays = scale_data
     out = run_oracle(oracle_bin, case, root, meta)
     sc.check_exact_files(case, out, meta)
+    sc.check_ic_against_fixture(case, os.path.join(root, sc.CASES[case][0], "ftle_ic.bin"), meta)
     worst = sc.check_ftle_against_fixture(case, out, meta, arrays, rtol=FTLE_RTOL, atol=FTLE_ATOL)
     print(case, "largest relative FTLE difference from ompVC (strided values):", worst)
 
