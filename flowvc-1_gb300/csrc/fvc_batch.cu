@@ -45,6 +45,14 @@ struct WinQ {
   int nsteps;
 };
 
+// One frame interval of a job in a tick: its integration range and window
+// (the FP64 form's frames, or the mixed form's pair records and step table).
+struct BWin {
+  double t1, t2;
+  const DevWindow* w;
+  WinQ q;
+};
+
 // One job's work in one tick, as the kernels see it.
 struct BJob {
   int kind;             // 0 tracers (state advanced in place), 1 FTLE pass 1
@@ -65,6 +73,8 @@ struct BJob {
   double tmin, tmax, rspan;
   WinQ q;
   const DevWindow* w;   // FP64 form: the job's window (two frames, no stage table)
+  int nwin;             // frame intervals of this tick (tracer jobs may run several)
+  const BWin* wins;     // their windows, in order (wins[0] is the one above)
 };
 
 struct BatchCtr {
@@ -132,8 +142,13 @@ __global__ void __launch_bounds__(256, (FVC_MX_MINBLOCKS + 1) / 2) k_batch_advan
       t.eid = J.eid[p];
       t.left = J.left[p];
       t.ldt = J.ldt[p];
-      const WinQ w = J.q;
-      advect_mx<D>(m, w, type, t, w.nsteps, steps, err);
+      // the job's intervals of this tick in order; a tracer that leaves is
+      // not advanced further (the live test of every later interval)
+      for (int k = 0; k < J.nwin; k++) {
+        const WinQ w = J.wins[k].q;
+        advect_mx<D>(m, w, type, t, w.nsteps, steps, err);
+        if (t.left || err) break;
+      }
       if (J.kind == 0) {
         store_pos_pair(J.X, p, t.X, t.c);
         J.eid[p] = t.eid;
@@ -169,7 +184,11 @@ __global__ void __launch_bounds__(256, FVC_MINBLOCKS / 2) k_batch_advance(DevMes
       const long p = e.y;
       Pt t;
       load_pt(t, p, J.X, nullptr, J.eid, J.left, J.ldt);
-      err = advect<D, 1>(m, *J.w, in, t, J.t1, J.t2, steps);
+      for (int k = 0; k < J.nwin; k++) {
+        const BWin& W = J.wins[k];
+        err |= advect<D, 1>(m, *W.w, in, t, W.t1, W.t2, steps);
+        if (t.left || err) break;
+      }
       if (J.kind == 0) {
         J.X[3 * p] = t.X[0];
         J.X[3 * p + 1] = t.X[1];
@@ -318,6 +337,32 @@ __global__ void k_zgather(TracerDev t, const int* perm, double* X2, double* V2, 
   d2[j] = t.ldt[i];
 }
 
+// inv[perm[j]] = j: the device position of each seed
+__global__ void k_zinverse(const int* perm, int n, int* inv) {
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) inv[perm[j]] = (int)j;
+}
+
+// A finished tracer job's state in seed order, written straight into the
+// result's page-locked block: positions (the mixed form's (X, c) pairs
+// joined to FP64, as the host-side unpacking does), exit data and the
+// residence times of OutputRT (ompVC/residencetime.c:160-178, as k_residence).
+__global__ void k_res_tracer(TracerDev t, const int* inv, int packed, double launch, double stop, double* X,
+                             double* ldt, double* rt, int* eid, int* left) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.n) return;
+  const long j = inv ? inv[i] : i;
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+    X[3 * i + a] = packed ? join_pos(reinterpret_cast<const float2*>(t.X)[3 * j + a]) : t.X[3 * j + a];
+  const double d = t.ldt[j];
+  const int l = t.left[j];
+  ldt[i] = d;
+  rt[i] = fabs(d + 1) < FVC_TINY ? -1.0 : (l ? d : stop) - launch;
+  eid[i] = t.eid[j];
+  left[i] = l;
+}
+
 }  // namespace fvc
 
 // ====================================================================== host
@@ -344,7 +389,9 @@ struct HostJob {
   cudaEvent_t done = nullptr;
   long long ticks = 0;
   long npts = 0;  // points (work-queue entries at most)
-  std::vector<int> perm;  // tracers: device position -> seed index (empty: seed order)
+  int* d_inv = nullptr;   // tracers: seed index -> device position (null: seed order)
+  int per_tick = 1;       // frame intervals a tick advances the job by
+  int res_held = 0;       // result tickets held on the job
   fvc_status err = FVC_OK;
   std::string msg;
 };
@@ -360,7 +407,7 @@ struct PairQ {
 // fvc_ftle_create, rounded up) and the seed-chain scratch.
 size_t job_bytes(int kind, long n) {
   if (kind == FVC_JOB_FTLE) return (size_t)n * 560 + (1u << 20);
-  return (size_t)n * 130 + (1u << 20);
+  return (size_t)n * 134 + (1u << 20);
 }
 
 }  // namespace
@@ -403,10 +450,21 @@ struct fvc_batch {
   long long* d_qtmp = nullptr;
   // results of finished jobs are read on a stream of their own, after the
   // job's last tick (its done event), so reading them never waits for the
-  // ticks still in flight; d_res is that stream's scratch
+  // ticks still in flight
   cudaStream_t res_stream = nullptr;
-  double* d_res = nullptr;
-  size_t res_cap = 0;  // doubles
+  // result tickets: FVC_BATCH_RESULT_SLOTS page-locked blocks for the
+  // caller, and one more for the blocking result calls
+  struct ResSlot {
+    unsigned char* h = nullptr;
+    size_t cap = 0;
+    cudaEvent_t ev = nullptr;
+    long long ticket = -1;
+    int job = -1;
+    bool busy = false;
+    fvc_batch_result r{};
+  };
+  ResSlot res[FVC_BATCH_RESULT_SLOTS + 1];
+  long long res_next = 0;
   // admission (seed upload and location, Z-ordering) runs on a stream of
   // its own, so its waits do not drain the ticks in flight
   cudaStream_t setup_stream = nullptr;
@@ -442,18 +500,20 @@ struct Interval {
   bool launch, last;
 };
 
-static Interval interval_of(const fvc_batch* b, const HostJob& J) {
+static Interval interval_at(const fvc_batch* b, const HostJob& J, long long df, bool launched) {
   Interval I{};
-  I.lo = J.dir > 0 ? J.df : J.df - 1;
+  I.lo = J.dir > 0 ? df : df - 1;
   I.tmin = b->o.tmin + (double)I.lo * b->o.tdelta;
   I.tmax = I.tmin + b->o.tdelta;
-  I.launch = !J.launched;
+  I.launch = !launched;
   const double t0 = J.spec.t_start;
   I.t1 = I.launch ? t0 : (J.dir > 0 ? I.tmin : I.tmax);
   I.t2 = J.dir > 0 ? std::min(I.tmax, J.stop) : std::max(I.tmin, J.stop);
   I.last = (J.dir > 0 ? (J.stop - I.tmax) : (I.tmin - J.stop)) < kTiny;
   return I;
 }
+
+static Interval interval_of(const fvc_batch* b, const HostJob& J) { return interval_at(b, J, J.df, J.launched); }
 
 // The first frame interval of a window starting at t0 (ompVC/parameters.c:
 // 322-333 for one slide).
@@ -567,12 +627,15 @@ static fvc_status job_window(fvc_batch* b, const Interval& I, const StepM* d_ste
 
 // Reorders a located release's tracers along the Z-order curve of 64^3 cells
 // over the seeds' bounding box (counting sort: key histogram, scan, scatter,
-// gather) and keeps the permutation for reading results in seed order.
+// gather) and keeps the inverse permutation on the device, for putting
+// results back in seed order.
 static fvc_status zorder_tracers(fvc_batch* b, HostJob& J) {
   fvc_ctx* c = b->c;
   TracerDev& t = J.job->t;
   const int n = t.n;
   if (n < 64) return FVC_OK;
+  int* d_inv = (int*)pool_get(c, 4 * (size_t)n);
+  if (!d_inv) return FVC_OK;  // no room: keep seed order
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
   for (long i = 0; i < n; i++)
     for (int a = 0; a < 3; a++) {
@@ -587,7 +650,10 @@ static fvc_status zorder_tracers(fvc_batch* b, HostJob& J) {
   char* mem = nullptr;
   const size_t bytes = 4 * nb * 2 + 4 * (3 * (size_t)K + 2) + 8 * ((size_t)K / 1024 + 2) + 64 * nb + 256 * 16;
   mem = (char*)pool_get(c, bytes);
-  if (!mem) return FVC_OK;  // no room: keep seed order
+  if (!mem) {
+    pool_put(c, d_inv, 4 * (size_t)n);
+    return FVC_OK;  // no room: keep seed order
+  }
   char* q = mem;
   auto take = [&](size_t sz) { char* r = q; q += (sz + 255) & ~(size_t)255; return r; };
   int* key = (int*)take(4 * nb);
@@ -614,14 +680,16 @@ static fvc_status zorder_tracers(fvc_batch* b, HostJob& J) {
   cudaMemcpyAsync(t.eid, e2, 4 * nb, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(t.left, l2, 4 * nb, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(t.ldt, d2, 8 * nb, cudaMemcpyDeviceToDevice, s);
-  J.perm.resize(nb);
-  cudaMemcpyAsync(J.perm.data(), perm, 4 * nb, cudaMemcpyDeviceToHost, s);
+  k_zinverse<<<g, 256, 0, s>>>(perm, n, d_inv);
   fvc_status st = check_launch(c, "z-order");
   cudaError_t e = cudaStreamSynchronize(s);
   pool_put(c, mem, bytes);
-  if (st) return st;
-  if (e != cudaSuccess) return fail(c, FVC_ERR_CUDA, "z-order: %s", cudaGetErrorString(e));
-  b->stats.launches += 6;
+  if (st || e != cudaSuccess) {
+    pool_put(c, d_inv, 4 * (size_t)n);
+    return st ? st : fail(c, FVC_ERR_CUDA, "z-order: %s", cudaGetErrorString(e));
+  }
+  J.d_inv = d_inv;
+  b->stats.launches += 7;
   return FVC_OK;
 }
 
@@ -717,7 +785,9 @@ static fvc_status admit(fvc_batch* b) {
 struct TickPlan {
   std::vector<char> blob;
   std::vector<int> ids;           // job ids in BJob order
-  std::vector<Interval> iv;
+  std::vector<Interval> iv;       // per job: its first interval of the tick
+  std::vector<int> nint;          // per job: intervals in the tick
+  std::vector<char> last;         // per job: the tick ends the job's window
   std::vector<DevWindow> win;     // per job (launch velocity, early FTLE)
   long long ngroups = 0;
   long long npts = 0;             // points of the tick's jobs (queue entries at most)
@@ -725,37 +795,89 @@ struct TickPlan {
 
 static size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 
+// The tick's layout: BJob[jobs] | BWin[intervals] | DevWindow[intervals]
+// (FP64 form) | step tables (mixed form), one window per interval.
 static fvc_status plan_tick(fvc_batch* b, const std::vector<int>& ids, char* dev_base, TickPlan& P) {
   fvc_ctx* c = b->c;
   P.ids = ids;
   const size_t nj = ids.size();
   P.iv.resize(nj);
+  P.nint.resize(nj);
+  P.last.resize(nj);
   P.win.resize(nj);
-  std::vector<BJob> J(nj);
-  std::vector<std::vector<StepM>> tabs(nj);
-  size_t off = al16(sizeof(BJob) * nj);
-  const size_t woff = off;  // FP64 form: the jobs' windows
-  if (!c->prec) off = al16(off + sizeof(DevWindow) * nj);
-  std::vector<size_t> toff(nj, 0);
+  // every job's intervals of this tick: one for FTLE jobs, up to per_tick
+  // for releases, never past the window's last
+  std::vector<std::vector<Interval>> ivs(nj);
+  size_t nw = 0;
   for (size_t k = 0; k < nj; k++) {
-    HostJob& H = *b->jobs[ids[k]];
-    P.iv[k] = interval_of(b, H);
-    if (c->prec) {
-      if (!build_steps_for(c->integ.h, P.iv[k].tmin, P.iv[k].tmax, P.iv[k].t1, P.iv[k].t2, tabs[k]))
-        return fail(c, FVC_ERR_TLOC, "batch job %d: query time outside the loaded frame interval", H.id);
-      toff[k] = off;
-      off = al16(off + sizeof(StepM) * tabs[k].size());
+    const HostJob& H = *b->jobs[ids[k]];
+    const int K = H.kind == FVC_JOB_FTLE ? 1 : H.per_tick;
+    long long df = H.df;
+    bool launched = H.launched;
+    for (int i = 0; i < K; i++) {
+      const Interval I = interval_at(b, H, df, launched);
+      ivs[k].push_back(I);
+      if (I.last) break;
+      df += H.dir;
+      launched = true;
     }
+    nw += ivs[k].size();
+    P.iv[k] = ivs[k].front();
+    P.nint[k] = (int)ivs[k].size();
+    P.last[k] = ivs[k].back().last;
+  }
+  size_t off = al16(sizeof(BJob) * nj);
+  const size_t bwoff = off;
+  off = al16(off + sizeof(BWin) * nw);
+  const size_t woff = off;  // FP64 form: the intervals' windows
+  if (!c->prec) off = al16(off + sizeof(DevWindow) * nw);
+  std::vector<std::vector<StepM>> tabs(nw);
+  std::vector<size_t> toff(nw, 0);
+  if (c->prec) {
+    size_t wi = 0;
+    for (size_t k = 0; k < nj; k++)
+      for (const Interval& I : ivs[k]) {
+        if (!build_steps_for(c->integ.h, I.tmin, I.tmax, I.t1, I.t2, tabs[wi]))
+          return fail(c, FVC_ERR_TLOC, "batch job %d: query time outside the loaded frame interval", ids[k]);
+        toff[wi] = off;
+        off = al16(off + sizeof(StepM) * tabs[wi].size());
+        wi++;
+      }
   }
   P.blob.assign(off, 0);
+  std::vector<BJob> J(nj);
+  std::vector<BWin> W(nw);
   long long groups = 0;
+  size_t wi = 0;
   for (size_t k = 0; k < nj; k++) {
     HostJob& H = *b->jobs[ids[k]];
     BJob& B = J[k];
     memset(&B, 0, sizeof(B));
-    const StepM* dsteps = c->prec ? (const StepM*)(dev_base + toff[k]) : nullptr;
-    fvc_status st = job_window(b, P.iv[k], dsteps, c->prec ? (int)tabs[k].size() - 1 : 0, P.win[k], B);
-    if (st) return st;
+    B.nwin = (int)ivs[k].size();
+    B.wins = (const BWin*)(dev_base + bwoff + sizeof(BWin) * wi);
+    for (size_t i = 0; i < ivs[k].size(); i++, wi++) {
+      const StepM* dsteps = c->prec ? (const StepM*)(dev_base + toff[wi]) : nullptr;
+      const int nsteps = c->prec ? (int)tabs[wi].size() - 1 : 0;
+      DevWindow w;
+      BJob tmp;
+      memset(&tmp, 0, sizeof(tmp));
+      fvc_status st = job_window(b, ivs[k][i], dsteps, nsteps, w, i == 0 ? B : tmp);
+      if (st) return st;
+      const BJob& src = i == 0 ? B : tmp;
+      W[wi].t1 = ivs[k][i].t1;
+      W[wi].t2 = ivs[k][i].t2;
+      W[wi].q = src.q;
+      if (c->prec) {
+        memcpy(P.blob.data() + toff[wi], tabs[wi].data(), sizeof(StepM) * tabs[wi].size());
+      } else {
+        memcpy(P.blob.data() + woff + sizeof(DevWindow) * wi, &w, sizeof(DevWindow));
+        W[wi].w = (const DevWindow*)(dev_base + woff + sizeof(DevWindow) * wi);
+      }
+      if (i == 0) {
+        P.win[k] = w;
+        B.w = W[wi].w;
+      }
+    }
     B.ctr = b->d_ctrs + H.slot;
     B.group0 = groups;
     if (H.kind == FVC_JOB_FTLE) {
@@ -781,14 +903,9 @@ static fvc_status plan_tick(fvc_batch* b, const std::vector<int>& ids, char* dev
     }
     groups += (B.n + 31) / 32;
     P.npts += B.n;
-    if (c->prec) {
-      memcpy(P.blob.data() + toff[k], tabs[k].data(), sizeof(StepM) * tabs[k].size());
-    } else {
-      memcpy(P.blob.data() + woff + sizeof(DevWindow) * k, &P.win[k], sizeof(DevWindow));
-      B.w = (const DevWindow*)(dev_base + woff + sizeof(DevWindow) * k);
-    }
   }
   memcpy(P.blob.data(), J.data(), sizeof(BJob) * nj);
+  if (nw) memcpy(P.blob.data() + bwoff, W.data(), sizeof(BWin) * nw);
   P.ngroups = groups;
   return FVC_OK;
 }
@@ -883,7 +1000,7 @@ static fvc_status enqueue_tick(fvc_batch* b, const TickPlan& P, const BJob* d_jo
     ftle_early(c->mesh, P.win[k], c->integ, f, P.iv[k].t1, ctr, true, s);
     ftle_update(c->mesh, c->integ, f, nullptr, s);
     b->stats.launches += 2 + (H.job->prec ? 6 : 8);
-    if (P.iv[k].last) {
+    if (P.last[k]) {
       if (H.job->packed) {
         unpack_pairs(H.job->f.X, 3L * f.n, s);
         H.job->packed = false;
@@ -903,9 +1020,9 @@ static void advance_cursors(fvc_batch* b, const TickPlan& P) {
   for (size_t k = 0; k < P.ids.size(); k++) {
     HostJob& H = *b->jobs[P.ids[k]];
     H.launched = true;
-    H.df += H.dir;
-    H.ticks++;
-    if (P.iv[k].last) {
+    H.df += (long long)H.dir * P.nint[k];
+    H.ticks += P.nint[k];
+    if (P.last[k]) {
       cudaMemcpyAsync(b->h_ctrs + H.slot, b->d_ctrs + H.slot, sizeof(DevCounters), cudaMemcpyDeviceToHost,
                       b->c->stream);
       cudaEventRecord(H.done, b->c->stream);
@@ -1174,8 +1291,12 @@ extern "C" void fvc_batch_destroy(fvc_batch* b) {
   fvc_ctx* c = b->c;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (b->res_stream) cudaStreamSynchronize(b->res_stream);
   for (auto& J : b->jobs) {
-    if (J->job) fvc_job_destroy(J->job);
+    if (J->job) {
+      if (J->d_inv) pool_put(c, J->d_inv, 4 * (size_t)J->job->t.n);
+      fvc_job_destroy(J->job);
+    }
     if (J->done) cudaEventDestroy(J->done);
   }
   for (auto& kv : b->pairs) cudaFree(kv.second.q);
@@ -1203,7 +1324,10 @@ extern "C" void fvc_batch_destroy(fvc_batch* b) {
     cudaStreamSynchronize(b->setup_stream);
     cudaStreamDestroy(b->setup_stream);
   }
-  cudaFree(b->d_res);
+  for (auto& r : b->res) {
+    cudaFreeHost(r.h);
+    if (r.ev) cudaEventDestroy(r.ev);
+  }
   delete b;
 }
 
@@ -1240,6 +1364,12 @@ extern "C" fvc_status fvc_batch_submit(fvc_batch* b, const fvc_batch_job_spec* s
   }
   J->spec.seeds = nullptr;
   J->bytes = job_bytes(sp->kind, n);
+  if (sp->kind != FVC_JOB_FTLE && b->o.tick_intervals > 0) {
+    // the frame intervals the window touches, at most; a long release runs
+    // several of them per tick
+    const double nint = ceil(fabs(J->stop - sp->t_start) / b->o.tdelta) + 1.0;
+    J->per_tick = (int)std::min(64.0, std::max(1.0, ceil(nint / (double)b->o.tick_intervals)));
+  }
   *id = J->id;
   b->queued.push_back(J->id);
   b->jobs.push_back(std::move(J));
@@ -1288,8 +1418,8 @@ extern "C" fvc_status fvc_batch_run(fvc_batch* b, int graph) {
       for (size_t k = 0; k < act.size(); k++) {
         HostJob& H = *b->jobs[act[k]];
         H.launched = true;
-        H.df += H.dir;
-        if (!plans.back().iv[k].last) still.push_back(act[k]);
+        H.df += (long long)H.dir * plans.back().nint[k];
+        if (!plans.back().last[k]) still.push_back(act[k]);
       }
       act.swap(still);
     }
@@ -1310,8 +1440,8 @@ extern "C" fvc_status fvc_batch_run(fvc_batch* b, int graph) {
       for (size_t k = 0; k < act.size(); k++) {
         HostJob& H = *b->jobs[act[k]];
         H.launched = true;
-        H.df += H.dir;
-        if (!plans[t].iv[k].last) still.push_back(act[k]);
+        H.df += (long long)H.dir * plans[t].nint[k];
+        if (!plans[t].last[k]) still.push_back(act[k]);
       }
       act.swap(still);
     }
@@ -1397,79 +1527,196 @@ static fvc_status job_ready(fvc_batch* b, HostJob* J, int kind_ok) {
   return FVC_OK;
 }
 
-// v (count items of w elements each, in device order) back to seed order
-template <class T>
-static void unpermute(const std::vector<int>& perm, T* v, size_t w) {
-  if (!v || perm.empty()) return;
-  std::vector<T> tmp(v, v + perm.size() * w);
-  for (size_t j = 0; j < perm.size(); j++)
-    for (size_t a = 0; a < w; a++) v[(size_t)perm[j] * w + a] = tmp[j * w + a];
+// ------------------------------------------------------------ results
+
+// Queues a finished job's results into a free result block (slot k) on the
+// result stream, after the job's last tick: the tracer state in seed order
+// with its residence times (k_res_tracer writes the page-locked block
+// directly), or the FTLE fields (copied).
+static fvc_status result_begin(fvc_batch* b, HostJob* J, int k, long long* ticket) {
+  fvc_ctx* c = b->c;
+  fvc_status st;
+  if ((st = use_device(c))) return st;
+  auto& S = b->res[k];
+  const bool ftle = J->kind == FVC_JOB_FTLE;
+  const size_t n = ftle ? (size_t)J->job->f.n : (size_t)J->job->t.n;
+  const size_t need = std::max<size_t>((ftle ? 16 : 48) * n, 256);
+  if (need > S.cap) {
+    if (S.h) {
+      cudaEventSynchronize(S.ev);  // a released ticket's copy may still run
+      cudaFreeHost(S.h);
+      S.h = nullptr;
+      S.cap = 0;
+    }
+    const size_t cap = need + need / 4;
+    if (cudaMallocHost(&S.h, cap) != cudaSuccess) {
+      S.h = nullptr;
+      return fail(c, FVC_ERR_OOM, "batch result block (page-locked, %zu bytes)", cap);
+    }
+    S.cap = cap;
+  }
+  if (!S.ev && cudaEventCreateWithFlags(&S.ev, cudaEventDisableTiming) != cudaSuccess)
+    return fail(c, FVC_ERR_CUDA, "batch result event");
+  cudaStream_t s = b->res_stream;
+  FVC_CUDA(c, cudaStreamWaitEvent(s, J->done, 0));
+  fvc_batch_result r{};
+  r.kind = J->kind;
+  r.n = (long long)n;
+  if (ftle) {
+    double* w = reinterpret_cast<double*>(S.h);
+    if (n) {
+      FVC_CUDA(c, cudaMemcpyAsync(w, J->job->f.out, 8 * n, cudaMemcpyDeviceToHost, s));
+      FVC_CUDA(c, cudaMemcpyAsync(w + n, J->job->f.out + n, 8 * n, cudaMemcpyDeviceToHost, s));
+    }
+    r.ftle_wT = w;
+    r.ftle_woT = w + n;
+  } else {
+    double* X = reinterpret_cast<double*>(S.h);
+    double* ldt = X + 3 * n;
+    double* rt = ldt + n;
+    int* eid = reinterpret_cast<int*>(rt + n);
+    int* left = eid + n;
+    if (n) {
+      const TracerDev& t = J->job->t;
+      k_res_tracer<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(t, J->d_inv, J->job->packed ? 1 : 0, J->spec.t_start,
+                                                      J->stop, X, ldt, rt, eid, left);
+      if ((st = check_launch(c, "batch result"))) return st;
+    }
+    r.X = X;
+    r.ldt = ldt;
+    r.rt = rt;
+    r.eid = eid;
+    r.left = left;
+  }
+  FVC_CUDA(c, cudaEventRecord(S.ev, s));
+  S.r = r;
+  S.job = J->id;
+  S.ticket = b->res_next++;
+  S.busy = true;
+  J->res_held++;
+  *ticket = S.ticket;
+  return FVC_OK;
 }
 
-// Device-to-host copies of a finished job's arrays on the result stream,
-// ordered after the job's last tick; waits for this stream only.
-static fvc_status res_copy(fvc_batch* b, HostJob* J, std::initializer_list<std::pair<void*, const void*>> dst_src,
-                           std::initializer_list<size_t> bytes) {
-  fvc_ctx* c = b->c;
-  FVC_CUDA(c, cudaStreamWaitEvent(b->res_stream, J->done, 0));
-  auto bs = bytes.begin();
-  for (auto& ds : dst_src) {
-    const size_t n = *bs++;
-    if (ds.first && n) FVC_CUDA(c, cudaMemcpyAsync(ds.first, ds.second, n, cudaMemcpyDeviceToHost, b->res_stream));
+static int res_slot(fvc_batch* b, long long ticket) {
+  for (int k = 0; k <= FVC_BATCH_RESULT_SLOTS; k++)
+    if (b->res[k].busy && b->res[k].ticket == ticket) return k;
+  return -1;
+}
+
+static fvc_status result_get(fvc_batch* b, int k, fvc_batch_result* out) {
+  auto& S = b->res[k];
+  if (cudaEventSynchronize(S.ev) != cudaSuccess) return fail(b->c, FVC_ERR_CUDA, "batch result copy failed");
+  *out = S.r;
+  return FVC_OK;
+}
+
+static void result_release(fvc_batch* b, int k) {
+  auto& S = b->res[k];
+  cudaEventSynchronize(S.ev);  // the job's memory stays read until the copy ends
+  HostJob* J = job_of(b, S.job);
+  if (J && J->res_held > 0) J->res_held--;
+  S.busy = false;
+  S.ticket = -1;
+  S.job = -1;
+}
+
+extern "C" fvc_status fvc_batch_result_begin(fvc_batch* b, int id, long long* ticket) {
+  if (!b || !ticket) return FVC_ERR_ARG;
+  HostJob* J = job_of(b, id);
+  fvc_status st = job_ready(b, J, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE) | (1 << FVC_JOB_FTLE));
+  if (st) return st;
+  for (int k = 0; k < FVC_BATCH_RESULT_SLOTS; k++)
+    if (!b->res[k].busy) return result_begin(b, J, k, ticket);
+  return fail(b->c, FVC_ERR_STATE, "all %d batch result blocks are held: release a ticket first",
+              FVC_BATCH_RESULT_SLOTS);
+}
+
+extern "C" fvc_status fvc_batch_result_ready(fvc_batch* b, long long ticket, int* ready) {
+  if (!b || !ready) return FVC_ERR_ARG;
+  const int k = res_slot(b, ticket);
+  if (k < 0) return fail(b->c, FVC_ERR_STATE, "no batch result with ticket %lld is held", ticket);
+  const cudaError_t e = cudaEventQuery(b->res[k].ev);
+  if (e == cudaErrorNotReady) {
+    cudaGetLastError();  // not an error
+    *ready = 0;
+    return FVC_OK;
   }
-  FVC_CUDA(c, cudaStreamSynchronize(b->res_stream));
+  if (e != cudaSuccess) return fail(b->c, FVC_ERR_CUDA, "batch result copy: %s", cudaGetErrorString(e));
+  *ready = 1;
+  return FVC_OK;
+}
+
+extern "C" fvc_status fvc_batch_result_get(fvc_batch* b, long long ticket, fvc_batch_result* out) {
+  if (!b || !out) return FVC_ERR_ARG;
+  const int k = res_slot(b, ticket);
+  if (k < 0) return fail(b->c, FVC_ERR_STATE, "no batch result with ticket %lld is held", ticket);
+  return result_get(b, k, out);
+}
+
+extern "C" fvc_status fvc_batch_result_release(fvc_batch* b, long long ticket) {
+  if (!b) return FVC_ERR_ARG;
+  const int k = res_slot(b, ticket);
+  if (k < 0) return fail(b->c, FVC_ERR_STATE, "no batch result with ticket %lld is held", ticket);
+  result_release(b, k);
+  return FVC_OK;
+}
+
+// The blocking result calls: the same path through the batch's own block,
+// then copied into the caller's arrays.
+static fvc_status result_now(fvc_batch* b, int id, int kinds, fvc_batch_result* r, int* slot) {
+  HostJob* J = job_of(b, id);
+  fvc_status st = job_ready(b, J, kinds);
+  if (st) return st;
+  const int k = FVC_BATCH_RESULT_SLOTS;
+  long long t;
+  if ((st = result_begin(b, J, k, &t))) return st;
+  if ((st = result_get(b, k, r))) {
+    result_release(b, k);
+    return st;
+  }
+  *slot = k;
   return FVC_OK;
 }
 
 extern "C" fvc_status fvc_batch_tracer_result(fvc_batch* b, int id, double* X, int* eid, int* left, double* ldt) {
-  HostJob* J = job_of(b, id);
-  fvc_status st = job_ready(b, J, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE));
+  if (!b) return FVC_ERR_ARG;
+  fvc_batch_result r;
+  int k;
+  fvc_status st = result_now(b, id, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE), &r, &k);
   if (st) return st;
-  if ((st = use_device(b->c))) return st;
-  const TracerDev& t = J->job->t;
-  const size_t n = (size_t)t.n;
-  if ((st = res_copy(b, J, {{X, t.X}, {eid, t.eid}, {left, t.left}, {ldt, t.ldt}}, {24 * n, 4 * n, 4 * n, 8 * n})))
-    return st;
-  if (X && J->job->packed) unpack_host(X, 3 * n);
-  unpermute(J->perm, X, 3);
-  unpermute(J->perm, eid, 1);
-  unpermute(J->perm, left, 1);
-  unpermute(J->perm, ldt, 1);
+  const size_t n = (size_t)r.n;
+  if (X) memcpy(X, r.X, 24 * n);
+  if (eid) memcpy(eid, r.eid, 4 * n);
+  if (left) memcpy(left, r.left, 4 * n);
+  if (ldt) memcpy(ldt, r.ldt, 8 * n);
+  result_release(b, k);
   return FVC_OK;
 }
 
 extern "C" fvc_status fvc_batch_residence_result(fvc_batch* b, int id, double* rt) {
-  HostJob* J = job_of(b, id);
-  fvc_status st = job_ready(b, J, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE));
-  if (st) return st;
+  if (!b) return FVC_ERR_ARG;
   if (!rt) return FVC_ERR_ARG;
-  fvc_ctx* c = b->c;
-  if ((st = use_device(c))) return st;
-  const size_t n = (size_t)J->job->t.n;
-  if (n == 0) return FVC_OK;
-  if (n > b->res_cap) {
-    FVC_CUDA(c, cudaStreamSynchronize(b->res_stream));
-    cudaFree(b->d_res);
-    b->d_res = nullptr;
-    b->res_cap = 0;
-    if (cudaMalloc(&b->d_res, 8 * n) != cudaSuccess) return fail(c, FVC_ERR_OOM, "batch result scratch");
-    b->res_cap = n;
-  }
-  FVC_CUDA(c, cudaStreamWaitEvent(b->res_stream, J->done, 0));
-  tracer_residence(J->job->t, J->spec.t_start, J->stop, b->d_res, b->res_stream);
-  if ((st = check_launch(c, "residence time"))) return st;
-  if ((st = res_copy(b, J, {{rt, b->d_res}}, {8 * n}))) return st;
-  unpermute(J->perm, rt, 1);
+  fvc_batch_result r;
+  int k;
+  fvc_status st = result_now(b, id, (1 << FVC_JOB_TRACERS) | (1 << FVC_JOB_RESIDENCE), &r, &k);
+  if (st) return st;
+  memcpy(rt, r.rt, 8 * (size_t)r.n);
+  result_release(b, k);
   return FVC_OK;
 }
 
 extern "C" fvc_status fvc_batch_ftle_result(fvc_batch* b, int id, double* wT, double* wN) {
-  HostJob* J = job_of(b, id);
-  fvc_status st = job_ready(b, J, 1 << FVC_JOB_FTLE);
+  if (!b) return FVC_ERR_ARG;
+  fvc_batch_result r;
+  int k;
+  fvc_status st = result_now(b, id, 1 << FVC_JOB_FTLE, &r, &k);
   if (st) return st;
-  if ((st = use_device(b->c))) return st;
-  const size_t n = (size_t)J->job->f.n;
-  return res_copy(b, J, {{wT, J->job->f.out}, {wN, J->job->f.out + n}}, {8 * n, 8 * n});
+  const size_t n = (size_t)r.n;
+  if (wT) memcpy(wT, r.ftle_wT, 8 * n);
+  if (wN) memcpy(wN, r.ftle_woT, 8 * n);
+  result_release(b, k);
+  return FVC_OK;
 }
 
 extern "C" fvc_status fvc_batch_job_stats(fvc_batch* b, int id, fvc_job_stats* out) {
@@ -1486,11 +1733,15 @@ extern "C" fvc_status fvc_batch_release(fvc_batch* b, int id) {
   if (!J) return FVC_ERR_ARG;
   if (J->state == JQ_QUEUED || J->state == JQ_ACTIVE)
     return fail(b->c, FVC_ERR_STATE, "batch job %d is still running", id);
+  if (J->res_held > 0)
+    return fail(b->c, FVC_ERR_STATE, "batch job %d still has %d result ticket(s) held", id, J->res_held);
   if (J->state == JQ_FINISHING) retire(b, true);
   if (J->job) {
     // the job's last tick has completed (done or failed) and result reads
     // waited for their own stream: nothing queued uses its memory, so it
     // goes back to the pool without draining the ticks in flight
+    if (J->d_inv) pool_put(b->c, J->d_inv, 4 * (size_t)J->job->t.n);
+    J->d_inv = nullptr;
     job_destroy_idle(J->job);
     J->job = nullptr;
     b->used -= J->bytes;
@@ -1501,8 +1752,6 @@ extern "C" fvc_status fvc_batch_release(fvc_batch* b, int id) {
   }
   J->seeds.clear();
   J->seeds.shrink_to_fit();
-  J->perm.clear();
-  J->perm.shrink_to_fit();
   if (J->state != JQ_FAILED) J->state = JQ_RELEASED;
   return FVC_OK;
 }

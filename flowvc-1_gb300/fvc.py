@@ -51,12 +51,18 @@ class JobStats(C.Structure):
 
 class BatchOpts(C.Structure):
     _fields_ = [("tmin", C.c_double), ("tdelta", C.c_double), ("tres", C.c_int), ("periodic", C.c_int),
-                ("hbm_budget", C.c_longlong), ("max_jobs", C.c_int), ("resort_every", C.c_int)]
+                ("hbm_budget", C.c_longlong), ("max_jobs", C.c_int), ("resort_every", C.c_int),
+                ("tick_intervals", C.c_int)]
 
 
 class BatchJobSpec(C.Structure):
     _fields_ = [("kind", C.c_int), ("t_start", C.c_double), ("t_stop", C.c_double), ("n", C.c_int),
                 ("seeds", C.POINTER(C.c_double)), ("local_search_checking", C.c_int), ("grid", FtleSpec)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("kind", C.c_int), ("n", C.c_longlong), ("X", _dp), ("eid", _ip), ("left", _ip), ("ldt", _dp),
+                ("rt", _dp), ("ftle_wT", _dp), ("ftle_woT", _dp)]
 
 
 class BatchStats(C.Structure):
@@ -124,6 +130,10 @@ SIGNATURES = {
     "fvc_batch_residence_result": (C.c_int, [_vp, C.c_int, _dp]),
     "fvc_batch_ftle_result": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "fvc_batch_job_stats": (C.c_int, [_vp, C.c_int, C.POINTER(JobStats)]),
+    "fvc_batch_result_begin": (C.c_int, [_vp, C.c_int, _llp]),
+    "fvc_batch_result_ready": (C.c_int, [_vp, C.c_longlong, _ip]),
+    "fvc_batch_result_get": (C.c_int, [_vp, C.c_longlong, C.POINTER(BatchResult)]),
+    "fvc_batch_result_release": (C.c_int, [_vp, C.c_longlong]),
     "fvc_batch_release": (C.c_int, [_vp, C.c_int]),
     "fvc_batch_get_stats": (C.c_int, [_vp, C.POINTER(BatchStats)]),
 }
@@ -173,6 +183,7 @@ class PinnedArray:
 
 
 TRACER_OUTPUT_SLOTS = 4  # FVC_TRACER_OUTPUT_SLOTS of fvc.h
+BATCH_RESULT_SLOTS = 8  # FVC_BATCH_RESULT_SLOTS of fvc.h
 
 
 class FvcError(RuntimeError):
@@ -462,11 +473,12 @@ class Batch:
     """Batched / served jobs on one context (fvc_batch_*): submit jobs, then
     run them all (run) or advance tick by tick (tick) while submitting more."""
 
-    def __init__(self, ctx: Context, tmin, tdelta, tres, periodic=0, hbm_budget=0, max_jobs=0, resort_every=0):
+    def __init__(self, ctx: Context, tmin, tdelta, tres, periodic=0, hbm_budget=0, max_jobs=0, resort_every=0,
+                 tick_intervals=0):
         self.ctx, self.lib = ctx, ctx.lib
         self.h = _vp()
         self.sizes = {}
-        o = BatchOpts(tmin, tdelta, tres, periodic, int(hbm_budget), max_jobs, resort_every)
+        o = BatchOpts(tmin, tdelta, tres, periodic, int(hbm_budget), max_jobs, resort_every, tick_intervals)
         ctx._chk(self.lib.fvc_batch_create(ctx.h, C.byref(o), C.byref(self.h)))
 
     def _submit(self, spec, keep=None):
@@ -523,6 +535,37 @@ class Batch:
         wT, wN = np.empty(n), np.empty(n)
         self.ctx._chk(self.lib.fvc_batch_ftle_result(self.h, jid, _d(wT), _d(wN)))
         return wT, wN
+
+    def result_begin(self, jid):
+        """Queues a finished job's results into a page-locked block
+        (fvc_batch_result_begin); returns the ticket."""
+        t = C.c_longlong(0)
+        self.ctx._chk(self.lib.fvc_batch_result_begin(self.h, jid, C.byref(t)))
+        return t.value
+
+    def result_ready(self, ticket):
+        r = C.c_int(0)
+        self.ctx._chk(self.lib.fvc_batch_result_ready(self.h, ticket, C.byref(r)))
+        return bool(r.value)
+
+    def result_get(self, ticket):
+        """Waits for the ticket's results and returns them as numpy views of
+        the library's block (valid until result_release): for tracer kinds
+        X, eid, left, ldt, rt; for FTLE wT, wN."""
+        r = BatchResult()
+        self.ctx._chk(self.lib.fvc_batch_result_get(self.h, ticket, C.byref(r)))
+        n = int(r.n)
+
+        def view(p, shape, dt):
+            return np.ctypeslib.as_array(p, shape=shape) if n else np.empty(shape, dt)
+        if r.kind == JOB_FTLE:
+            return {"wT": view(r.ftle_wT, (n,), np.float64), "wN": view(r.ftle_woT, (n,), np.float64)}
+        return {"X": view(r.X, (n, 3), np.float64), "eid": view(r.eid, (n,), np.int32),
+                "left": view(r.left, (n,), np.int32), "ldt": view(r.ldt, (n,), np.float64),
+                "rt": view(r.rt, (n,), np.float64)}
+
+    def result_release(self, ticket):
+        self.ctx._chk(self.lib.fvc_batch_result_release(self.h, ticket))
 
     def job_stats(self, jid):
         st = JobStats()

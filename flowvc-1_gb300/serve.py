@@ -42,7 +42,15 @@ class Site:
         self.ctx.close()
 
 
-def tube_site(prec="bf16", nc=40, nax=320, h=0.002, hbm_budget=0, tube=None, frames=None, resort_every=-1):
+# Releases advance ceil(intervals / TICK_INTERVALS) frame intervals per tick
+# (fvc_batch_opts.tick_intervals), so a long release finishes in about as
+# many ticks as a cube FTLE job of T = 1 (50 intervals) instead of holding
+# its latency to one interval a tick.
+TICK_INTERVALS = 48
+
+
+def tube_site(prec="bf16", nc=40, nax=320, h=0.002, hbm_budget=0, tube=None, frames=None, resort_every=-1,
+              tick_intervals=TICK_INTERVALS):
     """The bent tube (3,072,000 tets at nc = 40, nax = 320) with Womersley
     frames over one period, resident on a new context."""
     if tube is None:
@@ -58,11 +66,12 @@ def tube_site(prec="bf16", nc=40, nax=320, h=0.002, hbm_budget=0, tube=None, fra
     flow.upload_frames(ctx, ax, frames)
     site = Site("tube", ctx, ax, tube=tube)
     site.batch = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, ax.periodic, hbm_budget=hbm_budget,
-                           resort_every=resort_every)
+                           resort_every=resort_every, tick_intervals=tick_intervals)
     return site
 
 
-def cube_site(prec="bf16", n=64, h=0.005, nframes=51, dt=0.02, hbm_budget=0, mesh=None, frames=None):
+def cube_site(prec="bf16", n=64, h=0.005, nframes=51, dt=0.02, hbm_budget=0, mesh=None, frames=None,
+              tick_intervals=TICK_INTERVALS):
     """The jittered Kuhn cube with ABC frames (the FTLE workload's data)."""
     if mesh is None:
         mesh = synth.kuhn_cube_mesh(n, jitter=0.2, seed=0)
@@ -77,7 +86,8 @@ def cube_site(prec="bf16", n=64, h=0.005, nframes=51, dt=0.02, hbm_budget=0, mes
     ax = flow.TimeAxis(0.0, dt, nframes, 0)
     flow.upload_frames(ctx, ax, frames)
     site = Site("cube", ctx, ax)
-    site.batch = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, ax.periodic, hbm_budget=hbm_budget)
+    site.batch = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, ax.periodic, hbm_budget=hbm_budget,
+                           tick_intervals=tick_intervals)
     return site
 
 
@@ -281,14 +291,27 @@ class SeedPrefetch:
         self.th.join()
 
 
+def _result_copy(kind, res):
+    """A request's results copied out of the batch's result block, in the
+    blocking calls' shapes: (wT, wN), residence times, or the tracer state."""
+    if kind == "ftle":
+        return res["wT"].copy(), res["wN"].copy()
+    if kind == "residence":
+        return res["rt"].copy()
+    return {k: res[k].copy() for k in ("X", "eid", "left", "ldt")}
+
+
 def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
     """Serves the requests in arrival order against the sites' batches.
 
     The loop submits every request whose arrival time has passed, ticks each
     site's batch (a tick enqueues one frame interval of every admitted job
     and returns; at most two are in flight per site, and the sites' streams
-    run concurrently), and collects finished jobs: results copied to the
-    host, the job released, its latency recorded.  Returns a summary dict.
+    run concurrently), and collects finished jobs: each job's results are
+    queued to the host on the batch's result stream (fvc_batch_result_begin,
+    at most fvc.BATCH_RESULT_SLOTS at a time per site) and, once there, the
+    job is released and its latency recorded.  The loop never waits for a
+    result's copy.  Returns a summary dict.
 
     time_limit: wall seconds.  Past it serving raises, or with censor=True
     stops: the summary then covers the requests that finished, counts the
@@ -301,6 +324,8 @@ def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
     host = {"submit": 0.0, "tick": 0.0, "poll": 0.0, "results": 0.0, "idle": 0.0}
     clock = time.perf_counter
     seeds = SeedPrefetch(pending)
+    to_collect = {name: [] for name in sites}   # finished, results not yet queued
+    collecting = {name: [] for name in sites}   # (jid, request, ticket)
     t0 = time.perf_counter()
     stopped = False
     while len(done) < len(pending):
@@ -321,32 +346,37 @@ def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
         host["submit"] += c1 - c0
         busy = False
         for name, site in sites.items():
-            if not running[name]:
+            b = site.batch
+            if running[name]:
+                busy = True
+                c0 = clock()
+                b.tick()
+                c1 = clock()
+                host["tick"] += c1 - c0
+                finished = [jid for jid in running[name] if b.poll(jid) == fvc.BATCH_DONE]
+                host["poll"] += clock() - c1
+                to_collect[name].extend((jid, running[name].pop(jid)) for jid in finished)
+            if not (to_collect[name] or collecting[name]):
                 continue
             busy = True
-            b = site.batch
-            c0 = clock()
-            b.tick()
-            c1 = clock()
-            host["tick"] += c1 - c0
-            finished = [jid for jid in running[name] if b.poll(jid) == fvc.BATCH_DONE]
             c2 = clock()
-            host["poll"] += c2 - c1
-            for jid in finished:
-                r = running[name].pop(jid)
-                if r.kind == "ftle":
-                    res = b.ftle_result(jid)
-                elif r.kind == "residence":
-                    res = b.residence_result(jid)
-                else:
-                    res = b.tracer_result(jid)
-                js = b.job_stats(jid)
-                r.steps = js["steps_main"] + js["steps_early"]
+            while to_collect[name] and len(collecting[name]) < fvc.BATCH_RESULT_SLOTS:
+                jid, r = to_collect[name].pop(0)
+                collecting[name].append((jid, r, b.result_begin(jid)))
+            still = []
+            for jid, r, ticket in collecting[name]:
+                if not b.result_ready(ticket):
+                    still.append((jid, r, ticket))
+                    continue
                 r.t_done = time.perf_counter() - t0
                 if keep_results:
-                    r.result = res
+                    r.result = _result_copy(r.kind, b.result_get(ticket))
+                js = b.job_stats(jid)
+                r.steps = js["steps_main"] + js["steps_early"]
+                b.result_release(ticket)
                 b.release(jid)
                 done.append(r)
+            collecting[name] = still
             host["results"] += clock() - c2
         if not busy and nxt < len(pending):
             wait = pending[nxt].t_arrive - (time.perf_counter() - t0)
@@ -361,7 +391,8 @@ def serve(sites, requests, keep_results=False, time_limit=600.0, censor=False):
     if stopped:
         # the jobs still running have advanced too: count their steps so far
         for name, site in sites.items():
-            for jid in running[name]:
+            jids = list(running[name]) + [j for j, _ in to_collect[name]] + [j for j, _, _ in collecting[name]]
+            for jid in jids:
                 try:
                     js = site.batch.job_stats(jid)
                     steps += js["steps_main"] + js["steps_early"]

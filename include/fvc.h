@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define FVC_ABI_VERSION 2
+#define FVC_ABI_VERSION 3
 
 typedef int fvc_status;
 enum {
@@ -364,6 +364,12 @@ typedef struct {
                             ticks, so a warp's tracers walk neighbouring
                             elements after releases disperse; 0 = never,
                             -1 = chosen by fvc_batch_autotune (default 0) */
+  int tick_intervals;    /* tracer and residence-time jobs advance
+                            ceil(their frame intervals / tick_intervals)
+                            intervals per tick (in one launch, each interval
+                            exactly as alone), so that a long release takes
+                            about this many ticks, like an FTLE job of as many
+                            intervals; 0 = one interval per tick */
 } fvc_batch_opts;
 
 enum { FVC_JOB_TRACERS = 0, FVC_JOB_RESIDENCE = 1, FVC_JOB_FTLE = 2 };
@@ -421,6 +427,35 @@ fvc_status fvc_batch_tracer_result(fvc_batch *batch, int id, double *X, int *eid
 fvc_status fvc_batch_residence_result(fvc_batch *batch, int id, double *rt);
 fvc_status fvc_batch_ftle_result(fvc_batch *batch, int id, double *ftle_wT, double *ftle_woT);
 fvc_status fvc_batch_job_stats(fvc_batch *batch, int id, fvc_job_stats *out);
+
+/* Asynchronous results, for a request loop that must go on ticking while
+ * results travel.  fvc_batch_result_begin queues a finished job's results on
+ * the batch's result stream, after the job's last tick, into a page-locked
+ * block the batch owns (tracer state put back in seed order and residence
+ * times on the device, or the two FTLE fields) and returns a ticket at once.
+ * fvc_batch_result_ready polls it; fvc_batch_result_get waits for it and
+ * fills *out with pointers into the block, valid until the ticket is
+ * released; fvc_batch_result_release gives the block back.  At most
+ * FVC_BATCH_RESULT_SLOTS tickets are held at a time (begin refuses another
+ * with FVC_ERR_STATE), and a job holding a ticket cannot be released.  The
+ * blocking result calls above stay available beside these. */
+#define FVC_BATCH_RESULT_SLOTS 8
+typedef struct {
+  int kind;               /* FVC_JOB_* of the job */
+  long long n;            /* tracers, or FTLE points */
+  const double *X;        /* tracer kinds: n x 3 positions, seed order */
+  const int *eid;         /* tracer kinds */
+  const int *left;        /* tracer kinds */
+  const double *ldt;      /* tracer kinds: LeftDomainTime */
+  const double *rt;       /* tracer kinds: residence times over the job's window */
+  const double *ftle_wT;  /* FTLE: fields in output order */
+  const double *ftle_woT;
+} fvc_batch_result;
+fvc_status fvc_batch_result_begin(fvc_batch *batch, int id, long long *ticket);
+fvc_status fvc_batch_result_ready(fvc_batch *batch, long long ticket, int *ready);
+fvc_status fvc_batch_result_get(fvc_batch *batch, long long ticket, fvc_batch_result *out);
+fvc_status fvc_batch_result_release(fvc_batch *batch, long long ticket);
+
 /* Frees a finished job's device memory (its results become unavailable). */
 fvc_status fvc_batch_release(fvc_batch *batch, int id);
 fvc_status fvc_batch_get_stats(fvc_batch *batch, fvc_batch_stats *out);

@@ -31,7 +31,7 @@ def test_python_binding_covers_header(engine):
     import fvc
     assert sorted(fvc.SIGNATURES) == declared()
     lib = fvc.load()
-    assert lib.fvc_abi_version() == 2
+    assert lib.fvc_abi_version() == 3
 
 
 def test_create_without_gpu_fails_cleanly(engine):

@@ -116,15 +116,19 @@ def check(b, jid, spec, ref):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "bf16"])
-@pytest.mark.parametrize("mode", ["eager", "graph", "budget", "served", "tuned", "resort", "resort_graph"])
+@pytest.mark.parametrize("mode", ["eager", "graph", "budget", "served", "tuned", "resort", "resort_graph",
+                                  "multi", "multi_graph", "multi_served"])
 def test_batch_matches_single_jobs(case, prec, mode):
     ctx, ax = make_ctx(case, prec)
     specs = jobs_spec()
     ref = single_results(ctx, ax, specs)
     budget = 2_500_000 if mode == "budget" else 0
     resort = 1 if mode.startswith("resort") else (-1 if mode == "tuned" else 0)
-    b = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, 0, hbm_budget=budget, resort_every=resort)
-    if mode == "served":
+    # multi: releases run several frame intervals a tick (tick_intervals 3:
+    # 3 to 5 for these windows), FTLE jobs one
+    ticks = 3 if mode.startswith("multi") else 0
+    b = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, 0, hbm_budget=budget, resort_every=resort, tick_intervals=ticks)
+    if mode in ("served", "multi_served"):
         # half the jobs first, the rest arriving while those run
         ids = [submit(b, s) for s in specs[::2]]
         for _ in range(3):
@@ -139,13 +143,15 @@ def test_batch_matches_single_jobs(case, prec, mode):
         order = list(range(len(specs)))
         if mode == "tuned":
             b.autotune()
-        b.run(graph=mode in ("graph", "resort_graph"))
+        b.run(graph=mode in ("graph", "resort_graph", "multi_graph"))
     for jid, k in zip(ids, order):
         check(b, jid, specs[k], ref[k])
     st = b.stats()
     assert st["jobs_done"] == len(specs)
-    if mode in ("graph", "resort_graph"):
+    if mode in ("graph", "resort_graph", "multi_graph"):
         assert st["graphs"] == 1
+    if mode in ("multi", "multi_graph"):
+        assert st["ticks"] < 13  # the longest release alone spans 13 intervals
     if mode == "tuned":
         assert st["tuned_threads"] in (64, 128, 256)
         assert st["tuned_resort"] in (0, 1)
@@ -211,5 +217,46 @@ def test_batch_release_and_errors(case):
     assert b.poll(jid) == fvc.BATCH_RELEASED
     with pytest.raises(fvc.FvcError):
         b.tracer_result(jid)
+    b.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "bf16"])
+def test_batch_async_results(case, prec):
+    """fvc_batch_result_*: the results a ticket points at equal the blocking
+    calls' (tracer state in seed order through the device-side reordering,
+    residence times, FTLE fields); at most FVC_BATCH_RESULT_SLOTS tickets are
+    held; a job holding a ticket is not released; unknown tickets are refused."""
+    ctx, ax = make_ctx(case, prec)
+    specs = jobs_spec()
+    b = fvc.Batch(ctx, ax.tmin, ax.tdelta, ax.tres, 0)
+    ids = [submit(b, s) for s in specs]
+    b.run()
+    tickets = [b.result_begin(j) for j in ids]
+    assert len(tickets) == len(set(tickets)) == fvc.BATCH_RESULT_SLOTS
+    with pytest.raises(fvc.FvcError) as e:
+        b.result_begin(ids[0])  # every block is held
+    assert e.value.status == fvc.FVC_ERR_STATE
+    with pytest.raises(fvc.FvcError) as e:
+        b.release(ids[0])  # its ticket is held
+    assert e.value.status == fvc.FVC_ERR_STATE
+    for jid, s, t in zip(ids, specs, tickets):
+        got = b.result_get(t)
+        assert b.result_ready(t)
+        if s[0] == "ftle":
+            wT, wN = b.ftle_result(jid)
+            assert np.array_equal(got["wT"], wT) and np.array_equal(got["wN"], wN)
+        else:
+            ref = b.tracer_result(jid)
+            for k in ("X", "eid", "left", "ldt"):
+                assert np.array_equal(got[k], ref[k]), (s[0], k)
+            if s[0] == "residence":
+                assert np.array_equal(got["rt"], b.residence_result(jid))
+        b.result_release(t)
+        with pytest.raises(fvc.FvcError):
+            b.result_get(t)  # released
+        b.release(jid)
+    with pytest.raises(fvc.FvcError):
+        b.result_release(10 ** 6)
     b.close()
     ctx.close()
