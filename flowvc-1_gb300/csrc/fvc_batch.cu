@@ -412,6 +412,8 @@ size_t job_bytes(int kind, long n) {
 
 }  // namespace
 
+static constexpr int FTLE_SIDE_STREAMS = 4;
+
 struct fvc_batch {
   fvc_ctx* c = nullptr;
   fvc_batch_opts o{};
@@ -468,6 +470,12 @@ struct fvc_batch {
   // admission (seed upload and location, Z-ordering) runs on a stream of
   // its own, so its waits do not drain the ticks in flight
   cudaStream_t setup_stream = nullptr;
+  // the FTLE jobs' per-interval kernels (early FTLE, update) of a tick are
+  // spread over these streams, forked after the tick's advection and joined
+  // before its end: the jobs' small launches run side by side
+  cudaStream_t side[FTLE_SIDE_STREAMS] = {};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join[FTLE_SIDE_STREAMS] = {};
 };
 
 static constexpr int QSORT_KEYS = 1 << 22;
@@ -989,9 +997,19 @@ static fvc_status enqueue_tick(fvc_batch* b, const TickPlan& P, const BJob* d_jo
     batch_advance(c->mesh, c->integ, d_jobs, q, b->d_bc, b->launch, s);
     b->stats.launches += 2;
   }
+  // the FTLE jobs' per-interval work, spread over the side streams
+  int nftle = 0;
+  for (size_t k = 0; k < nj; k++) nftle += b->jobs[P.ids[k]]->kind == FVC_JOB_FTLE;
+  const int nside = std::min(nftle > 1 ? nftle : 0, FTLE_SIDE_STREAMS);
+  if (nside) {
+    FVC_CUDA(c, cudaEventRecord(b->fork, s));
+    for (int q = 0; q < nside; q++) FVC_CUDA(c, cudaStreamWaitEvent(b->side[q], b->fork, 0));
+  }
+  int fj = 0;
   for (size_t k = 0; k < nj; k++) {
     HostJob& H = *b->jobs[P.ids[k]];
     if (H.kind != FVC_JOB_FTLE) continue;
+    cudaStream_t s = nside ? b->side[fj++ % nside] : c->stream;
     DevCounters* ctr = b->d_ctrs + H.slot;
     const FtleDev& f = H.job->f;
     // the task lists' work cursors start at 0 every interval
@@ -1009,6 +1027,10 @@ static fvc_status enqueue_tick(fvc_batch* b, const TickPlan& P, const BJob* d_jo
       ftle_final(f, c->mesh.dims, H.T, s);
       b->stats.launches++;
     }
+  }
+  for (int q = 0; q < nside; q++) {
+    FVC_CUDA(c, cudaEventRecord(b->join[q], b->side[q]));
+    FVC_CUDA(c, cudaStreamWaitEvent(c->stream, b->join[q], 0));
   }
   return check_launch(c, "batch tick");
 }
@@ -1282,6 +1304,14 @@ extern "C" fvc_status fvc_batch_create(fvc_ctx* c, const fvc_batch_opts* o, fvc_
     fvc_batch_destroy(b);
     return fail(c, FVC_ERR_CUDA, "batch result / setup stream");
   }
+  bool side_ok = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int k = 0; k < FTLE_SIDE_STREAMS && side_ok; k++)
+    side_ok = cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming) == cudaSuccess;
+  if (!side_ok) {
+    fvc_batch_destroy(b);
+    return fail(c, FVC_ERR_CUDA, "batch side streams");
+  }
   *out = b;
   return check_launch(c, "batch create");
 }
@@ -1324,6 +1354,14 @@ extern "C" void fvc_batch_destroy(fvc_batch* b) {
     cudaStreamSynchronize(b->setup_stream);
     cudaStreamDestroy(b->setup_stream);
   }
+  for (int k = 0; k < FTLE_SIDE_STREAMS; k++) {
+    if (b->side[k]) {
+      cudaStreamSynchronize(b->side[k]);
+      cudaStreamDestroy(b->side[k]);
+    }
+    if (b->join[k]) cudaEventDestroy(b->join[k]);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   for (auto& r : b->res) {
     cudaFreeHost(r.h);
     if (r.ev) cudaEventDestroy(r.ev);
