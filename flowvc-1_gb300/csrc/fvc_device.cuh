@@ -40,29 +40,44 @@ __device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : 
 __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
 __device__ __forceinline__ double dsign(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
 
-// TestOutsideDomain, ompVC/velocity.c:654-669
+// TestOutsideDomain, ompVC/velocity.c:654-669 (the comparisons on the bit
+// patterns, off the FP64 pipe, with the FP64 comparisons' outcomes)
 __device__ __forceinline__ int outside_domain(const DevMesh& m, const double X[3]) {
-  if (X[0] < (m.bounds[0] - FVC_TINY) || X[0] > (m.bounds[1] + FVC_TINY)) return 1;
-  if (X[1] < (m.bounds[2] - FVC_TINY) || X[1] > (m.bounds[3] + FVC_TINY)) return 1;
-  if (X[2] < (m.bounds[4] - FVC_TINY) || X[2] > (m.bounds[5] + FVC_TINY)) return 1;
+  if (lt_bits(X[0], m.bounds[0] - FVC_TINY) || lt_bits(m.bounds[1] + FVC_TINY, X[0])) return 1;
+  if (lt_bits(X[1], m.bounds[2] - FVC_TINY) || lt_bits(m.bounds[3] + FVC_TINY, X[1])) return 1;
+  if (lt_bits(X[2], m.bounds[4] - FVC_TINY) || lt_bits(m.bounds[5] + FVC_TINY, X[2])) return 1;
   return 0;
 }
 
 // ------------------------------------------------------------------ Cartesian
 
-// TestOutsideCartVelDomain, ompVC/velocity.c:624-651
+// One axis of TestOutsideCartVelDomain: (int)floor(f) >= 0 and (int)ceil(f)
+// <= last hold exactly when 0 <= f <= last (last an integer); a NaN is
+// outside, as the x86-64 conversion (INT_MIN) makes it for ompVC.  Decided
+// on the bit patterns.
+__device__ __forceinline__ bool cell_index_ok(double f, int last) {
+  long long kf, kl;
+  if (!bits_of(f, kf)) return false;
+  bits_of(double_of_nonneg(last), kl);
+  return kf >= 0 && kf <= kl;
+}
+
+// TestOutsideCartVelDomain, ompVC/velocity.c:624-651: the point's grid
+// coordinates f = (X - min) / delta and whether the cell they index lies in
+// the grid.  GetVelocity_Cartesian (ompVC/velocity.c:257-457) divides the
+// same differences by the same deltas again; the engine keeps the quotients.
+template <int DIMS>
+__device__ __forceinline__ bool cart_coords(const DevMesh& m, const double X[3], double f[3]) {
+  f[0] = div_rn(X[0] - m.xmin, m.dx, m.rdx);
+  f[1] = div_rn(X[1] - m.ymin, m.dy, m.rdy);
+  f[2] = DIMS == 3 ? div_rn(X[2] - m.zmin, m.dz, m.rdz) : 0.0;
+  return cell_index_ok(f[0], m.xres - 1) && cell_index_ok(f[1], m.yres - 1) &&
+         (DIMS != 3 || cell_index_ok(f[2], m.zres - 1));
+}
 template <int DIMS>
 __device__ __forceinline__ int outside_cart_grid(const DevMesh& m, const double X[3]) {
-  const double fx = div_rn(X[0] - m.xmin, m.dx, m.rdx), fy = div_rn(X[1] - m.ymin, m.dy, m.rdy);
-  const double fz = DIMS == 3 ? div_rn(X[2] - m.zmin, m.dz, m.rdz) : 0.0;
-  int imin = (int)floor(fx);
-  int jmin = (int)floor(fy);
-  int kmin = DIMS == 3 ? (int)floor(fz) : 0;
-  int imax = (int)ceil(fx);
-  int jmax = (int)ceil(fy);
-  int kmax = DIMS == 3 ? (int)ceil(fz) : 0;
-  return imin < 0 || imax > (m.xres - 1) || jmin < 0 || jmax > (m.yres - 1) || kmin < 0 ||
-         kmax > (m.zres - 1);
+  double f[3];
+  return !cart_coords<DIMS>(m, X, f);
 }
 
 // one 32-byte node record as two read-only 16-byte loads
@@ -100,37 +115,40 @@ __device__ __forceinline__ int get_tloc(const DevWindow& w, int slot, double tq,
 template <int DIMS>
 __device__ __forceinline__ int vel_cart(const DevMesh& m, const DevWindow& w, double tq, int tslot,
                                         const double X[3], int& left, double out[3]) {
-  if (outside_cart_grid<DIMS>(m, X)) {
+  double f[3];
+  if (!cart_coords<DIMS>(m, X, f)) {
     out[0] = out[1] = out[2] = 0.0;
     left = 1;
     return 0;
   }
   double tloc;
   if (get_tloc(w, tslot, tq, tloc)) return PT_ERR_TLOC;
+  // cell indices (int)floor(f) of a point inside the grid, and the offsets
+  // X - min - i delta with i converted exactly, on integer instructions
   double xloc, yloc;
-  int i = (int)floor(div_rn(X[0] - m.xmin, m.dx, m.rdx));
+  int i = floor_nonneg_bits(f[0]);
   if (i == (m.xres - 1)) {
     i = m.xres - 2;
     xloc = 1.0;
   } else
-    xloc = div_rn(X[0] - m.xmin - i * m.dx, m.dx, m.rdx);
-  int j = (int)floor(div_rn(X[1] - m.ymin, m.dy, m.rdy));
+    xloc = div_rn(X[0] - m.xmin - double_of_nonneg(i) * m.dx, m.dx, m.rdx);
+  int j = floor_nonneg_bits(f[1]);
   if (j == (m.yres - 1)) {
     j = m.yres - 2;
     yloc = 1.0;
   } else
-    yloc = div_rn(X[1] - m.ymin - j * m.dy, m.dy, m.rdy);
+    yloc = div_rn(X[1] - m.ymin - double_of_nonneg(j) * m.dy, m.dy, m.rdy);
   const long nx = m.xres, ny = m.yres;
   const double4_32a* A = w.f0;
   const double4_32a* B = w.f1;
   if (DIMS == 3) {
     double zloc;
-    int k = (int)floor(div_rn(X[2] - m.zmin, m.dz, m.rdz));
+    int k = floor_nonneg_bits(f[2]);
     if (k == (m.zres - 1)) {
       k = m.zres - 2;
       zloc = 1.0;
     } else
-      zloc = div_rn(X[2] - m.zmin - k * m.dz, m.dz, m.rdz);
+      zloc = div_rn(X[2] - m.zmin - double_of_nonneg(k) * m.dz, m.dz, m.rdz);
     double V1 = (tloc) * (xloc) * (yloc) * (zloc);
     double V2 = (tloc) * (xloc) * (yloc) * (1 - zloc);
     double V3 = (tloc) * (xloc) * (1 - yloc) * (zloc);
@@ -311,7 +329,10 @@ __device__ __forceinline__ void load_slot_nodes(const DevWindow& w, int tslot, i
 // coordinates put the point outside by more than their error bound, with one
 // coordinate below all others by more than that bound, the FP64 test fails
 // and selects that face too, so the hop is taken without the FP64 solve.
-// Returns the face slot, or -1 when the FP64 test must decide.
+// Returns the face slot; -2 when every FP32 coordinate exceeds twice the
+// bound, so that every FP64 coordinate is positive and the FP64 test passes
+// (callers that need only the element, not its coordinates, stop there);
+// or -1 when the FP64 test must decide.
 //
 // The FP32 offsets are Xf - x0f, with Xf the position truncated to FP32
 // (f32_trunc, no FP64 instruction) once per walk and x0f the node rounded to
@@ -364,6 +385,7 @@ __device__ __forceinline__ int quick_hop(const DevMesh& m, int e, const PosF& P)
 #pragma unroll
     for (int j = 0; j < 4; j++)
       if (j != k) second = fminf(second, c[j]);
+    if (d > 2.0f * tol) return -2;
     if (!(d < -(1e-10f + 2.0f * tol)) || !(second - d > 1e-10f + 4.0f * tol)) return -1;
     return k;
   } else {
@@ -388,6 +410,7 @@ __device__ __forceinline__ int quick_hop(const DevMesh& m, int e, const PosF& P)
 #pragma unroll
     for (int j = 0; j < 3; j++)
       if (j != k) second = fminf(second, c[j]);
+    if (d > 2.0f * tol) return -2;
     if (!(d < -(1e-10f + 2.0f * tol)) || !(second - d > 1e-10f + 4.0f * tol)) return -1;
     return k;  // 2D slots: 0 r, 1 s, 2 (1 - r - s)
   }
@@ -415,9 +438,14 @@ __device__ __forceinline__ int neighbour(const DevMesh& m, int e, int slot) { re
 // first stage walks from its own hint, which lags the located element
 // whenever the previous step crossed a face: without this those walks
 // repeated the locate's solve, lane by lane.
+//
+// coords = false (a locate that wants only the element): an element the
+// FP32 pre-check puts inside beyond its error bound ends the walk without
+// the FP64 solve (the solve would pass); r, s, t, wv and nd are then unset.
 template <int DIMS>
 __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& eid, bool vel_rule, double& r,
-                                    double& s, double& t, double& wv, int4& nd, const NatCache* nc = nullptr) {
+                                    double& s, double& t, double& wv, int4& nd, const NatCache* nc = nullptr,
+                                    bool coords = true) {
   const PosF P = pos_f32(X);
   int4 nb = neighbours(m, eid);
   for (int hop = 0; hop < m.max_hops;) {
@@ -429,6 +457,7 @@ __device__ __forceinline__ int walk(const DevMesh& m, const double X[3], int& ei
       nb = neighbours(m, eid);
     }
     if (hop >= m.max_hops) break;
+    if (qs == -2 && !coords) return 0;
     if (nc && eid == nc->e) {
       r = nc->r;
       s = nc->s;
@@ -532,7 +561,8 @@ __device__ __forceinline__ int locate_walk(const DevMesh& m, const double X[3], 
   }
   double r, s, t, wv;
   int4 nd;
-  if (walk<DIMS>(m, X, guess, false, r, s, t, wv, nd)) return guess == EID_FAULT ? EID_FAULT : -1;
+  if (walk<DIMS>(m, X, guess, false, r, s, t, wv, nd, nullptr, nc != nullptr))
+    return guess == EID_FAULT ? EID_FAULT : -1;
   if (nc) {
     nc->e = guess;
     nc->nd = nd;
@@ -565,7 +595,8 @@ __device__ __forceinline__ bool contains(const DevMesh& m, int e, const double X
 // Get_Element_Global_Search (ompVC/mesh.c:304-398): lowest element id whose
 // containment test d > -TINY passes, from the point's bucket.  Candidates the
 // walk's FP32 pre-check puts outside beyond its error bound are skipped
-// without the FP64 test (they would fail it).
+// without the FP64 test (they would fail it), and one it puts inside beyond
+// that bound is taken without it (it would pass).
 template <int DIMS>
 __device__ __forceinline__ int global_find(const DevMesh& m, const BucketGrid& g, const double X[3]) {
   int c[3];
@@ -580,8 +611,9 @@ __device__ __forceinline__ int global_find(const DevMesh& m, const BucketGrid& g
   const PosF P = pos_f32(X);
   for (int i = b; i < e; i++) {
     int el = __ldg(g.ids + i);
-    if (quick_hop<DIMS>(m, el, P) >= 0) continue;
-    if (contains<DIMS>(m, el, X)) return el;
+    const int qs = quick_hop<DIMS>(m, el, P);
+    if (qs >= 0) continue;
+    if (qs == -2 || contains<DIMS>(m, el, X)) return el;
   }
   return -1;
 }
@@ -739,13 +771,19 @@ __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, cons
   double kk[4][3];
   NatCache nc;
   nc.e = -1;
+  // a planar flow's stages all give w = +0.0 (2D triangles; a 2D grid whose
+  // frames carry w = 0): the z increment h (0 + 2*0 + 2*0 + 0) / 6 is then a
+  // zero with h's sign, added without the arithmetic
+  const bool planar = DIMS == 2 && (MESH == 1 || w.wz);
   double tc = tstart, h = dsign(in.h, tend - tstart);
   int k = 0;
   while ((tc - tend) * (tend - tstart) < 0.0) {
     if ((tc + h - tend) * (tc + h - tstart) > 0.0) h = dsign(tend - tc, tend - tstart);
     if ((err |= rk4_stages<DIMS, MESH>(m, w, p, tc, h, k, e, l, kk, &nc))) return tend;
 #pragma unroll
-    for (int q = 0; q < 3; q++) p.X[q] = p.X[q] + div_rn(h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]), 6.0, kRcp6);
+    for (int q = 0; q < 3; q++)
+      p.X[q] = (q == 2 && planar) ? p.X[2] + zero_of(h)
+                                  : p.X[q] + div_rn(h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]), 6.0, kRcp6);
     tc = tc + h;
     k++;
     if (MESH == 1) p.eid = locate_walk<DIMS>(m, p.X, p.eid, err, &nc);
@@ -756,7 +794,9 @@ __device__ __forceinline__ double rk4(const DevMesh& m, const DevWindow& w, cons
       p.left = 1;
       p.ldt = tc - h;
 #pragma unroll
-      for (int q = 0; q < 3; q++) p.X[q] = p.X[q] - div_rn(h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]), 6.0, kRcp6);
+      for (int q = 0; q < 3; q++)
+        p.X[q] = (q == 2 && planar) ? p.X[2] - zero_of(h)
+                                    : p.X[q] - div_rn(h * (kk[0][q] + 2 * kk[1][q] + 2 * kk[2][q] + kk[3][q]), 6.0, kRcp6);
       return p.ldt;
     }
     steps++;

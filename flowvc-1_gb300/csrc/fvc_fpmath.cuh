@@ -87,4 +87,53 @@ __device__ __forceinline__ bool above_neg_tiny(double x, bool ge) {
   return ge ? a <= tiny : a < tiny;
 }
 
+// a < b decided on the bit patterns with integer instructions, with the
+// FP64 comparison's outcome for every input: +0 == -0, NaN compares false.
+// Each pattern maps to a signed key in the doubles' order (a negative
+// double's key is minus its magnitude bits, so both zeros map to 0).
+__device__ __forceinline__ bool bits_of(double x, long long& key) {
+  unsigned long long u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+  const unsigned long long a = u & 0x7fffffffffffffffull;
+  key = (u >> 63) ? -(long long)a : (long long)a;
+  return a <= 0x7ff0000000000000ull;  // not NaN
+}
+__device__ __forceinline__ bool lt_bits(double a, double b) {
+  long long ka, kb;
+  const bool na = bits_of(a, ka), nb = bits_of(b, kb);
+  return na && nb && ka < kb;
+}
+
+// (int)floor(x) for 0 <= x < 2^31 (and NaN: 0, as the conversion gives it)
+// with integer instructions; ompVC's cell index of a point inside the grid.
+__device__ __forceinline__ int floor_nonneg_bits(double x) {
+  unsigned long long u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+  const int e = (int)((u >> 52) & 0x7ff) - 1023;
+  if (e < 0 || e > 30) return 0;
+  const unsigned long long m = (u & 0xfffffffffffffull) | 0x10000000000000ull;
+  return (int)(m >> (52 - e));
+}
+
+// A zero with x's sign (x * +0.0 for finite nonzero x), on the bit pattern.
+__device__ __forceinline__ double zero_of(double x) {
+  unsigned long long u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+  u &= 0x8000000000000000ull;
+  double z;
+  asm("mov.b64 %0, %1;" : "=d"(z) : "l"(u));
+  return z;
+}
+
+// (double)i for 0 <= i < 2^31, exactly, with integer instructions.
+__device__ __forceinline__ double double_of_nonneg(int i) {
+  if (i <= 0) return 0.0;
+  const int e = 31 - __clz(i);
+  const unsigned long long u = ((unsigned long long)(1023 + e) << 52) |
+                               (((unsigned long long)i << (52 - e)) & 0xfffffffffffffull);
+  double x;
+  asm("mov.b64 %0, %1;" : "=d"(x) : "l"(u));
+  return x;
+}
+
 }  // namespace fvc

@@ -316,8 +316,9 @@ __global__ void k_global_unique(DevMesh m, BucketGrid g, int n, const double* X,
       const PosF P = pos_f32(x);
       for (int k = b; k < e && hits < 2; k++) {
         const int el = __ldg(g.ids + k);
-        if (quick_hop<DIMS>(m, el, P) >= 0) continue;
-        if (contains<DIMS>(m, el, x)) {
+        const int qs = quick_hop<DIMS>(m, el, P);
+        if (qs >= 0) continue;
+        if (qs == -2 || contains<DIMS>(m, el, x)) {
           if (!hits) first = el;
           hits++;
         }
@@ -592,8 +593,9 @@ __device__ __forceinline__ int holders(const DevMesh& m, const BucketGrid& g, co
   int hits = 0;
   for (int q = b0; q < e0 && hits < 2; q++) {
     const int el = __ldg(g.ids + q);
-    if (quick_hop<DIMS>(m, el, P) >= 0) continue;
-    if (contains<DIMS>(m, el, x)) {
+    const int qs = quick_hop<DIMS>(m, el, P);
+    if (qs >= 0) continue;
+    if (qs == -2 || contains<DIMS>(m, el, x)) {
       if (!hits) first = el;
       hits++;
     }

@@ -1,8 +1,10 @@
 // Checks the helpers of fvc_fpmath.cuh on the GPU: div_rn(a, b,
 // rcp_for_div(b)) must equal CUDA's IEEE a / b bit for bit, and f32_trunc(x)
 // must equal __double2float_rz(x), on many seeded operands from several
-// distributions, and above_neg_tiny(x) must agree with the FP64 comparisons
-// against -1e-10 it stands for (one line of counts on stdout).  With a file argument it
+// distributions, above_neg_tiny(x) must agree with the FP64 comparisons
+// against -1e-10 it stands for, and the integer comparison and conversion
+// helpers with the FP64 operations they replace (one line of counts on
+// stdout).  With a file argument it
 // also writes seeded (x, rn_root4(x)) pairs there for the host to check.
 #include <cstdio>
 #include <cstdint>
@@ -86,6 +88,33 @@ __global__ void k_tiny(uint64_t seed, long n, unsigned long long* bad) {
   if (ge != (x >= -TINY) || ge != ((x + TINY) >= 0) || gt != (x > -TINY)) atomicAdd(bad, 1ull);
 }
 
+// lt_bits against a < b, floor_nonneg_bits against (int)floor(x) on
+// [0, 2^31), double_of_nonneg against (double)i, zero_of against x * +0.0,
+// on random values, neighbours of each other and the special values
+__global__ void k_bits(uint64_t seed, long n, unsigned long long* bad) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t h1 = mix(seed ^ (uint64_t)i), h2 = mix(h1);
+  const double sp[8] = {0.0, -0.0, INFINITY, -INFINITY, NAN, -NAN, 1.0, -1.0};
+  double a, b;
+  const int kind = (int)(i % 6);
+  if (kind == 0) { a = rnd(h1, -60, 60); b = rnd(h2, -60, 60); }
+  else if (kind == 1) { a = rnd(h1, -1022, 1023); b = __longlong_as_double(__double_as_longlong(a) + (long long)(h2 % 5) - 2); }
+  else if (kind == 2) { a = __longlong_as_double((long long)h1); b = __longlong_as_double((long long)h2); }
+  else if (kind == 3) { a = sp[h1 % 8]; b = sp[h2 % 8]; }
+  else if (kind == 4) { a = sp[h1 % 8]; b = rnd(h2, -10, 10); }
+  else { a = rnd(h1, -10, 10); b = -a; }
+  if (lt_bits(a, b) != (a < b) || lt_bits(b, a) != (b < a)) atomicAdd(bad, 1ull);
+  // cell indices: grid coordinates in [0, 2^31), integers and their neighbours
+  const double x = (i & 1) ? fabs(rnd(h1, -30, 30)) * 0.5
+                           : __longlong_as_double(__double_as_longlong((double)(h1 % 100000)) + (long long)(h2 % 3) - 1);
+  if (x >= 0.0 && x < 2147483648.0 && floor_nonneg_bits(x) != (int)floor(x)) atomicAdd(bad + 1, 1ull);
+  const int k = (int)(h2 & 0x7fffffff) >> (int)(h1 % 31);
+  if (__double_as_longlong(double_of_nonneg(k)) != __double_as_longlong((double)k)) atomicAdd(bad + 2, 1ull);
+  const double y = rnd(h2, -60, 60);
+  if (__double_as_longlong(zero_of(y)) != __double_as_longlong(y * 0.0)) atomicAdd(bad + 3, 1ull);
+}
+
 __global__ void k_root4(uint64_t seed, long n, double* out) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -112,9 +141,17 @@ int main(int argc, char** argv) {
   k_tiny<<<(unsigned)((n + 255) / 256), 256>>>(0x5151ull, n, dt);
   if (cudaMemcpy(&bad_tiny, dt, sizeof(bad_tiny), cudaMemcpyDeviceToHost) != cudaSuccess) return 3;
   cudaFree(dt);
+  unsigned long long* db = nullptr, bad_bits[4] = {0, 0, 0, 0};
+  if (cudaMalloc(&db, sizeof(bad_bits)) != cudaSuccess) return 2;
+  cudaMemset(db, 0, sizeof(bad_bits));
+  k_bits<<<(unsigned)((n + 255) / 256), 256>>>(0x7e57ull, n, db);
+  if (cudaMemcpy(bad_bits, db, sizeof(bad_bits), cudaMemcpyDeviceToHost) != cudaSuccess) return 3;
+  cudaFree(db);
   printf("{\"n_div\": %llu, \"bad_div\": %llu, \"n_cvt\": %llu, \"bad_cvt\": %llu, \"n_tiny\": %ld, "
-         "\"bad_tiny\": %llu, \"first_bad\": [%.17g, %.17g, %d]}\n",
-         h.n_div, h.bad_div, h.n_cvt, h.bad_cvt, n, bad_tiny, h.a, h.b, h.kind);
+         "\"bad_tiny\": %llu, \"n_bits\": %ld, \"bad_lt\": %llu, \"bad_floor\": %llu, \"bad_i2d\": %llu, "
+         "\"bad_zero\": %llu, \"first_bad\": [%.17g, %.17g, %d]}\n",
+         h.n_div, h.bad_div, h.n_cvt, h.bad_cvt, n, bad_tiny, n, bad_bits[0], bad_bits[1], bad_bits[2],
+         bad_bits[3], h.a, h.b, h.kind);
   cudaFree(d);
   if (argc > 3) {
     const long nr = 1L << 18;

@@ -3,7 +3,8 @@ Markstein division must return exactly CUDA's IEEE quotient and the integer
 FP32 truncation exactly __double2float_rz, on 2^28 seeded operands each
 (wide exponents, element-volume scales, exact quotients, near-midpoint
 quotients, division by 6 and the fallback edges); rn_root4 must be the
-correctly rounded fourth root on seeded inputs."""
+correctly rounded fourth root on seeded inputs; the comparisons and
+conversions done on bit patterns must match the FP64 operations."""
 import json
 import os
 import subprocess
@@ -30,6 +31,8 @@ def test_div_rn_and_f32_trunc_match_ieee(tmp_path):
     assert out["bad_div"] == 0, out
     assert out["bad_cvt"] == 0, out
     assert out["n_tiny"] == 1 << 26 and out["bad_tiny"] == 0, out
+    assert out["n_bits"] == 1 << 26, out
+    assert out["bad_lt"] == out["bad_floor"] == out["bad_i2d"] == out["bad_zero"] == 0, out
     # rn_root4: correctly rounded, checked exactly on the host with rationals
     # ((c -/+ half an ulp)^4 must bracket x).  The host libm's pow(x, 0.25),
     # which the reference's RKF calls, is not always correctly rounded: how
