@@ -18,10 +18,14 @@ namespace fvc {
 // exact only without underflow, so numerators outside 2^-400 .. 2^400 in
 // magnitude (zero included: IEEE keeps its sign) and divisors without a
 // usable reciprocal (y passed as 0) take the IEEE division.  Cost: one DMUL
-// and four DFMA, against a reciprocal iteration for the IEEE division.
+// and four DFMA, against a reciprocal iteration for the IEEE division.  A
+// divisor that is a power of two (a grid spacing of 2^-7, say) has y = 1/b
+// exactly, so a y is the quotient itself and its rounding is RN(a/b): one
+// DMUL (the test is on b's fraction bits).
 __device__ __forceinline__ double div_rn(double a, double b, double y) {
   const int ea = (__double2hiint(a) >> 20) & 0x7ff;
   if ((unsigned)(ea - (1023 - 400)) > 800u || __double2hiint(y) == 0) return a / b;
+  if (((__double2hiint(b) & 0xfffff) | __double2loint(b)) == 0) return a * y;
   double q = a * y;
   double r = fma(-b, q, a);
   q = fma(r, y, q);

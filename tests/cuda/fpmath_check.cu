@@ -38,7 +38,7 @@ __global__ void k_div(uint64_t seed, long n, Out* o) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint64_t h1 = mix(seed ^ (uint64_t)i), h2 = mix(h1), h3 = mix(h2);
-  int kind = (int)(h3 % 6);
+  int kind = (int)(h3 % 7);
   double a, b;
   switch (kind) {
     case 0: a = rnd(h1, -300, 300); b = rnd(h2, -99, 99); break;      // wide exponents
@@ -51,6 +51,7 @@ __global__ void k_div(uint64_t seed, long n, Out* o) {
       break;
     }
     case 4: a = rnd(h1, -60, 60); b = 6.0; break;                      // the RK4 update
+    case 5: a = rnd(h1, -60, 60); b = ldexp((h2 & 1) ? -1.0 : 1.0, (int)(h2 % 61) - 30); break;  // powers of two
     default: a = rnd(h1, -400, 400); b = rnd(h2, -400, 400); break;   // the fallback edges
   }
   double want = a / b, got = div_rn(a, b, rcp_for_div(b));
