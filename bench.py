@@ -615,7 +615,7 @@ def bench_served(args, tube, frames, cube_inputs):
                                   if out["fp64"]["steps_per_s"] else None)
     if args.served_sweep:
         sweep = {}
-        for prec, rates in (("bf16", (25, 50, 100, 150, 200, 300)), ("fp64", (1, 2, 5, 10, 20))):
+        for prec, rates in (("bf16", (25, 50, 100, 125, 150, 175, 200)), ("fp64", (1, 2, 5, 10, 20))):
             rows = []
             for rate in rates:
                 r = run(prec, rate, args.sweep_seconds, args.sweep_seconds + 20.0, seed=11)
