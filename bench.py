@@ -13,14 +13,15 @@ here with fixed seeds (no dataset is involved).
 value      accepted RK4 steps / s with mesh and frames resident in HBM; each
            step seeds and locates the grid, advects every interval
            (including the early-FTLE advections of points that leave) and
-           reduces the FTLE field.  Early-FTLE advections that repeat the
+           reduces the FTLE field, which stays in HBM (the end-to-end
+           figure reads it back).  Early-FTLE advections that repeat the
            main pass exactly are read from its per-step record; their steps
            are counted (ompVC performs them) and also reported on their own
            (steps_early_recorded).  ftle_points_per_s counts no steps.
 e2e        the same through the C ABI from pinned host buffers: mesh and all
            frames copied host->device inside each step (the mesh validated and
-           its records and bucket grid rebuilt), FTLE fields copied back; one
-           context for all steps.
+           its records and bucket grid rebuilt), both FTLE fields copied back
+           into page-locked arrays; one context for all steps.
 roofline   the main advection kernel (k_ftle_pass1) against the bound that
            applies to it, the FP64 pipe: FP64-pipe instructions per step (the
            committed instruction-mix profile) x steps / CUDA-event time,
@@ -405,7 +406,7 @@ def bench_double_gyre(args, stream_of, barrier, fp64, rank):
     steps, stats = 0, []
     e0.record(stream)
     for _ in range(args.steps):
-        wT, wN, st, js = flow.run_ftle(ctx, ax, DG_GRID, DG_T)
+        wT, wN, st, js = flow.run_ftle(ctx, ax, DG_GRID, DG_T, fetch=False)
         steps += st
         stats.append(js)
     e1.record(stream)
@@ -700,7 +701,7 @@ def precision_forms(ctx, ax, grid, stream, barrier, args, fp64_value, ref, input
         steps, stats, st_last, T_last = 0, [], {}, None
         e0.record(stream)
         for k in range(args.steps):
-            wT, wN, st, js = flow.run_ftle(ctx, ax, grid, T_WINDOW)
+            wT, wN, st, js = flow.run_ftle(ctx, ax, grid, T_WINDOW, fetch=False)
             steps += st
             stats.append(js)
         e1.record(stream)
@@ -793,7 +794,8 @@ def run_engine(args, rank, world, local_rank):
     with ClockSampler(local_rank) as clk:
         e0.record(stream)
         for _ in range(args.steps):
-            wT, wN, st, js = flow.run_ftle(ctx, ax, grid, T_WINDOW)
+            # the fields stay in HBM here; the end-to-end loop reads them back
+            wT, wN, st, js = flow.run_ftle(ctx, ax, grid, T_WINDOW, fetch=False)
             steps_total += st
             stats.append(js)
         e1.record(stream)
@@ -850,13 +852,15 @@ def run_engine(args, rank, world, local_rank):
         # the context stays (as an application keeps it); every step sends
         # the mesh (validated, its records and bucket grid rebuilt on the
         # device) and all frames up again and reads both FTLE fields back
+        # the fields come back into page-locked arrays the application keeps
+        pin = (fvc.PinnedArray((args.grid ** 3,)), fvc.PinnedArray((args.grid ** 3,)))
         barrier()
         t0 = time.perf_counter()
         e2e_steps = 0
         for _ in range(args.steps):
             ctx.set_unstruct_mesh(pxyz, pconn, padj)
             flow.upload_frames(ctx, ax, pframes, asynchronous=True)
-            wT, wN, st, _ = flow.run_ftle(ctx, ax, grid, T_WINDOW)
+            wT, wN, st, _ = flow.run_ftle(ctx, ax, grid, T_WINDOW, out=(pin[0].a, pin[1].a))
             e2e_steps += st
         barrier()
         ctx.close()

@@ -66,12 +66,14 @@ def upload_frames(ctx: fvc.Context, ax: TimeAxis, frames, asynchronous=False):
             ctx.upload_frame(i, f)
 
 
-def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, lsc=1, state=None):
+def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, lsc=1, state=None, out=None,
+             fetch=True):
     """One FTLE slide over its whole integration window, frames resident.
 
     grid = (xmin, xmax, ymin, ymax, zmin, zmax, xres, yres, zres).  Returns
     (ftle_wT, ftle_woT, steps, job stats); a dict passed as state receives
-    the slide's final point state (fvc_ftle_get_state)."""
+    the slide's final point state (fvc_ftle_get_state).  out: host arrays
+    for the two fields; fetch=False leaves them on the device (None)."""
     if ax.periodic:
         stop = t_start + direction * T
     else:
@@ -80,7 +82,7 @@ def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, 
     job = fvc.FtleJob(ctx, spec)
     first, last = ftle_frame_range(ax, t_start, T, direction)
     steps, status = 0, 0
-    out = None
+    res = None
     df = first
     while df != last:
         lo, tmin, tmax = ax.window(df, direction)
@@ -92,7 +94,7 @@ def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, 
             status = 1
             job.interval(launch, t1, t2, wait=False)
             if ((stop - tmax) if direction > 0 else (tmin - stop)) < TINY:
-                out = job.reduce(T)
+                res = job.reduce(T, out=out, fetch=fetch)
                 if state is not None:
                     state.update(job.get_state())
                 break
@@ -100,9 +102,9 @@ def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, 
     st = job.stats()
     steps = st["steps_main"] + st["steps_early"]
     job.close()
-    if out is None:
+    if res is None:
         raise RuntimeError("FTLE window did not complete")
-    return out[0], out[1], steps, st
+    return res[0], res[1], steps, st
 
 
 class OutputWriter:

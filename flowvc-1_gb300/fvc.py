@@ -371,9 +371,15 @@ class FtleJob:
         self.ctx._chk(self.lib.fvc_ftle_interval(self.h, int(launch), t1, t2, C.byref(steps)))
         return steps.value
 
-    def reduce(self, int_t):
-        wT = np.empty(self.n)
-        wN = np.empty(self.n)
+    def reduce(self, int_t, out=None, fetch=True):
+        """The FTLE fields (fvc_ftle_reduce).  out: (wT, wN) float64 arrays of
+        n values to fill (page-locked ones copy fastest); fetch=False leaves
+        the fields on the device and returns (None, None)."""
+        if not fetch:
+            self.ctx._chk(self.lib.fvc_ftle_reduce(self.h, int_t, None, None))
+            return None, None
+        wT, wN = out if out is not None else (np.empty(self.n), np.empty(self.n))
+        assert wT.size == wN.size == self.n and wT.dtype == wN.dtype == np.float64
         self.ctx._chk(self.lib.fvc_ftle_reduce(self.h, int_t, _d(wT), _d(wN)))
         return wT, wN
 
