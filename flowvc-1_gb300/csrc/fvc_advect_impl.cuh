@@ -73,7 +73,7 @@ __device__ __forceinline__ void load_pt(Pt& p, long i, const double* X, const do
   p.ldt = ldt[i];
 }
 
-template <int D, int M>
+template <int D, int M, int I>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_advect(DevMesh m, DevWindow w, DevInteg in, int n, double* X, double* V, int* eid,
                          int* left, double* ldt, double t0, double t1, DevCounters* ctr) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_advect(DevMesh m, DevWin
     Pt p;
     load_pt(p, i, X, V, eid, left, ldt);
     if (!(p.left && !in.extrapolate)) {
-      err = advect<D, M>(m, w, in, p, t0, t1, steps);
+      err = advect<D, M, false, I>(m, w, in, p, t0, t1, steps);
       X[3 * i] = p.X[0];
       X[3 * i + 1] = p.X[1];
       X[3 * i + 2] = p.X[2];
@@ -143,7 +143,7 @@ __global__ void k_ftle_launch(DevMesh m, DevWindow w, FtleDev f, double t, DevCo
 
 // Pass 1: every live point from its frame-start state (ompVC/ftle.c:109-130),
 // one thread per entry of the interval's compacted live list.
-template <int D, int M>
+template <int D, int M, int I>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_pass1(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
                                                     double t1, double t2, DevCounters* ctr) {
   clear_early_counters(ctr);
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_pass1(DevMesh m, De
     load_pt(t, p, f.X, in.extrapolate ? f.V : nullptr, f.eid, f.left, f.ldt);
     const unsigned before = steps;
     const RecOut r{f.rec + 3 * p, 3L * f.n, f.rec_steps, f.rec_e1 ? f.rec_e1 + p : nullptr, t.eid};
-    err |= advect<D, M>(m, w, in, t, t1, t2, steps, nullptr, f.rec ? &r : nullptr);
+    err |= advect<D, M, false, I>(m, w, in, t, t1, t2, steps, nullptr, f.rec ? &r : nullptr);
     if (f.rec) f.kacc[p] = (unsigned char)(steps - before);
     f.flag[p] = 1 | ((t.left && !in.extrapolate) ? 2 : 0) | (t.left ? 4 : 0);
     f.Xn[3 * p] = t.X[0];
@@ -174,22 +174,6 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_ftle_pass1(DevMesh m, De
     f.te[p] = t.ldt;
   }
   flush_counters(&ctr->steps, &ctr->status, steps, err);
-}
-
-template <int D, int M>
-__device__ __forceinline__ int adv_from_start(const DevMesh& m, const DevWindow& w, const DevInteg& in,
-                                              const FtleDev& f, long p, int eid, double t1, double t2,
-                                              Pt& out, unsigned& steps) {
-  out.X[0] = f.X[3 * p];
-  out.X[1] = f.X[3 * p + 1];
-  out.X[2] = f.X[3 * p + 2];
-  out.V[0] = f.V[3 * p];
-  out.V[1] = f.V[3 * p + 1];
-  out.V[2] = f.V[3 * p + 2];
-  out.left = f.left[p];
-  out.eid = eid;
-  out.ldt = 0.0;
-  return advect<D, M>(m, w, in, out, t1, t2, steps);
 }
 
 // Pass 2b: GetFTLEForPointEarly (ompVC/ftle.c:788-1048) for every served point
@@ -423,7 +407,7 @@ __global__ void k_ftle_queue_self(FtleDev f, DevWindow w, int mixed, DevCounters
 
 // The advections of A (phase 0: to te, recording exit times) and C (phase 1:
 // to MinExitTime).
-template <int D, int M>
+template <int D, int M, int I>
 __global__ void __launch_bounds__(128, FVC_TASK_MINBLOCKS) k_ftle_tasks(DevMesh m, DevWindow w, DevInteg in, FtleDev f,
                                                                    double t1, int phase, DevCounters* ctr) {
   const long ntask = *(volatile int*)&ctr->tq[phase].ntask;
@@ -462,7 +446,7 @@ __global__ void __launch_bounds__(128, FVC_TASK_MINBLOCKS) k_ftle_tasks(DevMesh 
       chk.e1 = f.rec_e1[p];
     }
     unsigned st = 0;
-    err |= advect<D, M>(m, w, in, t, t1, tend, st, nullptr, nullptr, check ? &chk : nullptr);
+    err |= advect<D, M, false, I>(m, w, in, t, t1, tend, st, nullptr, nullptr, check ? &chk : nullptr);
     if (chk.hit) {
       // step 1 was computed (st = 1); the record has the rest
       double lt;
@@ -588,7 +572,7 @@ __global__ void k_tracer_launch(DevMesh m, DevWindow w, TracerDev t, double tq, 
 }
 
 
-template <int D, int M>
+template <int D, int M, int I>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_tracer_advance(DevMesh m, DevWindow w, DevInteg in, TracerDev t,
                                                         double t1, double t2, DevCounters* ctr) {
   const long nlive = *(volatile int*)&ctr->nlive;
@@ -600,7 +584,7 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_tracer_advance(DevMesh m
     long i = t.live[idx];
     Pt p;
     load_pt(p, i, t.X, t.V, t.eid, t.left, t.ldt);
-    err |= advect<D, M>(m, w, in, p, t1, t2, steps);
+    err |= advect<D, M, false, I>(m, w, in, p, t1, t2, steps);
     t.X[3 * i] = p.X[0];
     t.X[3 * i + 1] = p.X[1];
     t.X[3 * i + 2] = p.X[2];
@@ -616,12 +600,16 @@ __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_tracer_advance(DevMesh m
 
 
 
+// The advection kernels come in two builds each: RK4 alone (I = 1, the
+// common case, without the other integrators' registers and spills) and any
+// integrator chosen at run time (I = -1).
 template <int D, int M>
 struct Variant {
   static void advect(const DevMesh& m, const DevWindow& w, const DevInteg& in, int n, double* X,
                      double* V, int* eid, int* left, double* ldt, double t0, double t1,
                      DevCounters* ctr, cudaStream_t s) {
-    k_advect<D, M><<<vblk(n, 128), 128, 0, s>>>(m, w, in, n, X, V, eid, left, ldt, t0, t1, ctr);
+    if (in.type == 1) k_advect<D, M, 1><<<vblk(n, 128), 128, 0, s>>>(m, w, in, n, X, V, eid, left, ldt, t0, t1, ctr);
+    else k_advect<D, M, -1><<<vblk(n, 128), 128, 0, s>>>(m, w, in, n, X, V, eid, left, ldt, t0, t1, ctr);
   }
   static void velocity(const DevMesh& m, const DevWindow& w, int n, const double* X, int* eid,
                        int* left, double tq, double* out, DevCounters* ctr, cudaStream_t s) {
@@ -633,14 +621,17 @@ struct Variant {
   }
   static void ftle_pass1(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
                          double t1, double t2, DevCounters* ctr, cudaStream_t s) {
-    static const unsigned res = resident_blocks(k_ftle_pass1<D, M>, 128);
-    k_ftle_pass1<D, M><<<capped(f.n, 128, res), 128, 0, s>>>(m, w, in, f, t1, t2, ctr);
+    static const unsigned res1 = resident_blocks(k_ftle_pass1<D, M, 1>, 128);
+    static const unsigned res = resident_blocks(k_ftle_pass1<D, M, -1>, 128);
+    if (in.type == 1) k_ftle_pass1<D, M, 1><<<capped(f.n, 128, res1), 128, 0, s>>>(m, w, in, f, t1, t2, ctr);
+    else k_ftle_pass1<D, M, -1><<<capped(f.n, 128, res), 128, 0, s>>>(m, w, in, f, t1, t2, ctr);
   }
   static void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
                          double t1, DevCounters* ctr, bool jacobi, cudaStream_t s) {
     static const unsigned res_nb = resident_blocks(k_ftle_queue_nb<D>, 256);
     static const unsigned res_self = resident_blocks(k_ftle_queue_self<D>, 256);
-    static const unsigned res_tasks = resident_blocks(k_ftle_tasks<D, M>, 128);
+    static const unsigned res_tasks1 = resident_blocks(k_ftle_tasks<D, M, 1>, 128);
+    static const unsigned res_tasks = resident_blocks(k_ftle_tasks<D, M, -1>, 128);
     static const unsigned res_final = resident_blocks(k_ftle_early_final<D>, 128);
     static const unsigned res_jacobi = resident_blocks(k_ftle_early_jacobi<D>, 64);
     static const unsigned res_sort = resident_blocks(k_task_sort<D>, 256);
@@ -648,10 +639,12 @@ struct Variant {
     // the task counters were cleared with the served count (ftle_triggers)
     k_ftle_queue_nb<D><<<capped(6L * f.n, 256, res_nb), 256, 0, s>>>(f, w, 0, ctr, t1, inv_h);
     k_task_sort<D><<<capped(6L * f.n, 256, res_sort), 256, 0, s>>>(f, &ctr->tq[0]);
-    k_ftle_tasks<D, M><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 0, ctr);
+    if (in.type == 1) k_ftle_tasks<D, M, 1><<<capped(6L * f.n, 128, res_tasks1), 128, 0, s>>>(m, w, in, f, t1, 0, ctr);
+    else k_ftle_tasks<D, M, -1><<<capped(6L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 0, ctr);
     k_ftle_queue_self<D><<<capped(7L * f.n, 256, res_self), 256, 0, s>>>(f, w, 0, ctr, t1, inv_h);
     k_task_sort<D><<<capped(7L * f.n, 256, res_sort), 256, 0, s>>>(f, &ctr->tq[1]);
-    k_ftle_tasks<D, M><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
+    if (in.type == 1) k_ftle_tasks<D, M, 1><<<capped(7L * f.n, 128, res_tasks1), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
+    else k_ftle_tasks<D, M, -1><<<capped(7L * f.n, 128, res_tasks), 128, 0, s>>>(m, w, in, f, t1, 1, ctr);
     k_ftle_early_final<D><<<capped(f.n, 128, res_final), 128, 0, s>>>(f, ctr);
     if (jacobi) k_ftle_early_jacobi<D><<<capped(f.n, 64, res_jacobi), 64, 0, s>>>(f, ctr);
   }
@@ -661,8 +654,10 @@ struct Variant {
   }
   static void tracer_advance(const DevMesh& m, const DevWindow& w, const DevInteg& in,
                              const TracerDev& t, double t1, double t2, DevCounters* ctr, cudaStream_t s) {
-    static const unsigned res = resident_blocks(k_tracer_advance<D, M>, 128);
-    k_tracer_advance<D, M><<<capped(t.n, 128, res), 128, 0, s>>>(m, w, in, t, t1, t2, ctr);
+    static const unsigned res1 = resident_blocks(k_tracer_advance<D, M, 1>, 128);
+    static const unsigned res = resident_blocks(k_tracer_advance<D, M, -1>, 128);
+    if (in.type == 1) k_tracer_advance<D, M, 1><<<capped(t.n, 128, res1), 128, 0, s>>>(m, w, in, t, t1, t2, ctr);
+    else k_tracer_advance<D, M, -1><<<capped(t.n, 128, res), 128, 0, s>>>(m, w, in, t, t1, t2, ctr);
   }
 };
 

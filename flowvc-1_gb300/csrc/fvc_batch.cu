@@ -166,8 +166,9 @@ __global__ void __launch_bounds__(256, (FVC_MX_MINBLOCKS + 1) / 2) k_batch_advan
 }
 
 // The same in the FP64 form (ompVC's arithmetic): each stage interpolates the
-// job's two frames itself (the window carries no stage-time table).
-template <int D>
+// job's two frames itself (the window carries no stage-time table).  I = 1:
+// built for RK4 alone; -1: the integrator chosen at run time.
+template <int D, int I>
 __global__ void __launch_bounds__(256, FVC_MINBLOCKS / 2) k_batch_advance(DevMesh m, DevInteg in,
                                                                       const BJob* __restrict__ jobs,
                                                                       const int2* __restrict__ queue,
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(256, FVC_MINBLOCKS / 2) k_batch_advance(DevMes
       load_pt(t, p, J.X, nullptr, J.eid, J.left, J.ldt);
       for (int k = 0; k < J.nwin; k++) {
         const BWin& W = J.wins[k];
-        err |= advect<D, 1>(m, *W.w, in, t, W.t1, W.t2, steps);
+        err |= advect<D, 1, false, I>(m, *W.w, in, t, W.t1, W.t2, steps);
         if (t.left || err) break;
       }
       if (J.kind == 0) {
@@ -218,7 +219,7 @@ struct BatchLaunch {
 static unsigned batch_resident(int dims, int prec, int threads) {
   if (prec) return dims == 3 ? resident_blocks(k_batch_advance_mx<3>, threads)
                              : resident_blocks(k_batch_advance_mx<2>, threads);
-  return dims == 3 ? resident_blocks(k_batch_advance<3>, threads) : resident_blocks(k_batch_advance<2>, threads);
+  return dims == 3 ? resident_blocks(k_batch_advance<3, 1>, threads) : resident_blocks(k_batch_advance<2, 1>, threads);
 }
 
 static void batch_advance(const DevMesh& m, const DevInteg& in, const BJob* jobs, const int2* queue, BatchCtr* bc,
@@ -227,8 +228,13 @@ static void batch_advance(const DevMesh& m, const DevInteg& in, const BJob* jobs
     if (m.dims == 3) k_batch_advance_mx<3><<<L.blocks, L.threads, 0, s>>>(m, in.type, jobs, queue, bc);
     else k_batch_advance_mx<2><<<L.blocks, L.threads, 0, s>>>(m, in.type, jobs, queue, bc);
   } else {
-    if (m.dims == 3) k_batch_advance<3><<<L.blocks, L.threads, 0, s>>>(m, in, jobs, queue, bc);
-    else k_batch_advance<2><<<L.blocks, L.threads, 0, s>>>(m, in, jobs, queue, bc);
+    if (in.type == 1) {
+      if (m.dims == 3) k_batch_advance<3, 1><<<L.blocks, L.threads, 0, s>>>(m, in, jobs, queue, bc);
+      else k_batch_advance<2, 1><<<L.blocks, L.threads, 0, s>>>(m, in, jobs, queue, bc);
+    } else {
+      if (m.dims == 3) k_batch_advance<3, -1><<<L.blocks, L.threads, 0, s>>>(m, in, jobs, queue, bc);
+      else k_batch_advance<2, -1><<<L.blocks, L.threads, 0, s>>>(m, in, jobs, queue, bc);
+    }
   }
 }
 
@@ -1763,6 +1769,16 @@ extern "C" fvc_status fvc_batch_job_stats(fvc_batch* b, int id, fvc_job_stats* o
   if (J->state == JQ_FINISHING) retire(b, true);
   memset(out, 0, sizeof(*out));
   if (J->job) *out = J->job->stats;
+  if (J->state == JQ_ACTIVE && J->slot >= 0) {
+    // a running job: its step counters as the ticks completed so far left them
+    DevCounters h;
+    if (cudaMemcpyAsync(&h, b->d_ctrs + J->slot, sizeof(h), cudaMemcpyDeviceToHost, b->res_stream) == cudaSuccess &&
+        cudaStreamSynchronize(b->res_stream) == cudaSuccess) {
+      out->steps_main += (long long)h.steps;
+      out->steps_early += (long long)h.steps_early;
+      out->intervals += J->ticks;
+    }
+  }
   return FVC_OK;
 }
 

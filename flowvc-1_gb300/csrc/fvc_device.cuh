@@ -1000,7 +1000,10 @@ __device__ __noinline__ double rkf(const DevMesh& m, const DevWindow& w, const D
   return tend;
 }
 
-template <int DIMS, int MESH, bool CET = false>
+// I: the integrator when the kernel is compiled for one (1 = RK4: the other
+// integrators' code, and the registers it needs, drop out), or -1 for
+// in.type at run time.
+template <int DIMS, int MESH, bool CET = false, int I = -1>
 __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, const DevInteg& in,
                                       Pt& p, double tstart, double tend, unsigned& steps,
                                       const CetDev* cet = nullptr, const RecOut* rec = nullptr,
@@ -1014,9 +1017,9 @@ __device__ __forceinline__ int advect(const DevMesh& m, const DevWindow& w, cons
   if (p.left) return PT_ERR_STATE;  // "integrate point that already left domain"
   if (MESH == 1 && p.eid < 0) return PT_ERR_STATE;
   double stop;
-  if (in.type == 1) stop = rk4<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet, rec, chk);
-  else if (in.type == 2) stop = rkf<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet);
-  else if (in.type == 3 && !CET) stop = ab2<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
+  if (I == 1 || (I < 0 && in.type == 1)) stop = rk4<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet, rec, chk);
+  else if (I < 0 && in.type == 2) stop = rkf<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet);
+  else if (I < 0 && in.type == 3 && !CET) stop = ab2<DIMS, MESH>(m, w, in, p, tstart, tend, steps, err);
   else stop = euler<DIMS, MESH, CET>(m, w, in, p, tstart, tend, steps, err, cet, rec);
   if (MESH == 1) err |= walk_fault(p.eid);
   if (!err && (fabs(stop - tend) > FVC_TINY) && in.extrapolate) {

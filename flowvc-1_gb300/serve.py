@@ -421,7 +421,9 @@ def sustained(summary, reqs, duration, p99_limit_ms=1000.0):
     """Whether a served run kept up with its arrivals: every request finished
     within 5 s after the last arrival, p99 stayed under p99_limit_ms, and the
     requests arriving in the last third of the window waited (p99) no more
-    than twice those of the first third (a queue that grows fails these)."""
+    than twice those of the first third, or under half the limit (a queue
+    that grows fails these; at light load the thirds' p99s are a few dozen
+    requests each and their ratio is noise)."""
     if summary.get("requests_unfinished"):
         return False
     if summary["wall_s"] > duration + 5.0 or summary["p99_ms"] > p99_limit_ms:
@@ -430,4 +432,5 @@ def sustained(summary, reqs, duration, p99_limit_ms=1000.0):
     late = [r.t_done - r.t_arrive for r in reqs if r.t_done is not None and r.t_arrive > 2 * duration / 3]
     if not early or not late:
         return True
-    return float(np.percentile(late, 99)) <= 2.0 * float(np.percentile(early, 99))
+    late99 = 1e3 * float(np.percentile(late, 99))
+    return late99 <= max(2.0 * 1e3 * float(np.percentile(early, 99)), 0.5 * p99_limit_ms)

@@ -426,6 +426,8 @@ fvc_status fvc_batch_poll(fvc_batch *batch, int id, int *state);
 fvc_status fvc_batch_tracer_result(fvc_batch *batch, int id, double *X, int *eid, int *left, double *ldt);
 fvc_status fvc_batch_residence_result(fvc_batch *batch, int id, double *rt);
 fvc_status fvc_batch_ftle_result(fvc_batch *batch, int id, double *ftle_wT, double *ftle_woT);
+/* A job's statistics; for a job still running, the steps of the ticks that
+ * have completed so far. */
 fvc_status fvc_batch_job_stats(fvc_batch *batch, int id, fvc_job_stats *out);
 
 /* Asynchronous results, for a request loop that must go on ticking while
