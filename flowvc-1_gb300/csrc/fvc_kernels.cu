@@ -549,8 +549,8 @@ __global__ void k_chain_eval(DevMesh m, ChainDev c, DevCounters* ctr) {
 // has that element as its answer whatever its guess, and whether a seed is
 // found at all does not depend on its guess (the global search settles it).
 // Each plane's seeds are cut into chunks of CHAIN_CHUNK in loop order; the
-// seeds that end a chunk and the seeds of each plane's last row are tested
-// (k_chain_marks).  A chunk after a uniquely held seed starts from that
+// seeds that end a chunk, those of each plane's last row and each row's
+// first are tested (k_chain_marks).  A chunk after a uniquely held seed starts from that
 // seed's element; one after any other seed is taken on by the thread of the
 // chunk before it, which goes on past its end.  The guess a plane leaves is
 // the answer of one seed (the first found in its last row, or the plane's
@@ -603,14 +603,17 @@ __device__ __forceinline__ int holders(const DevMesh& m, const BucketGrid& g, co
   return hits;
 }
 
-// R0 and U for the seeds that end a chunk of their plane and for the seeds
-// of each plane's last row; every other seed gets U = 0 and R0 = -1.
+// R0 and U for the seeds that end a chunk of their plane, the seeds of each
+// plane's last row and the first seed of every row; every other seed gets
+// U = 0 and R0 = -1.  A row's first seed is walked to from the previous
+// row's last, across the whole grid; held by one element, it needs no walk.
 template <int DIMS>
 __global__ void k_chain_marks(DevMesh m, BucketGrid g, ChainDev c) {
   const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= c.n) return;
   const int q = (int)(p % c.plane);
-  const bool mark = (q + 1) % CHAIN_CHUNK == 0 || q + 1 == c.plane || q >= (c.res[1] - 1) * c.res[2];
+  const bool mark = (q + 1) % CHAIN_CHUNK == 0 || q + 1 == c.plane || q >= (c.res[1] - 1) * c.res[2] ||
+                    q % c.res[2] == 0;
   int first = -1, hits = 0;
   if (mark && !c.left0[p]) {
     const double x[3] = {c.X[3 * p], c.X[3 * p + 1], c.X[3 * p + 2]};
