@@ -1090,7 +1090,6 @@ extern "C" fvc_status fvc_ftle_create(fvc_ctx* c, const fvc_ftle_spec* sp, fvc_j
               {(void**)&f.flag, n}, {(void**)&f.served, 4 * n}, {(void**)&f.trig, 4 * n}, {(void**)&f.out, 16 * n},
               {(void**)&f.epos, 168 * n}, {(void**)&f.elt, 48 * n}, {(void**)&f.emt, 8 * n},
               {(void**)&f.tasks, 56 * n}, {(void**)&f.tsorted, 56 * n}, {(void**)&f.live, 4 * n},
-              {(void**)&j->live_alt, 4 * n},
               {(void**)&f.block_cnt, sizeof(int) * (2 * (n / 1024 + 1) + 16) + sizeof(long long) * (n / 1048576 + 8)},
               {(void**)&left0, 4 * n}},
              &j->mem_bytes);
@@ -1256,10 +1255,7 @@ extern "C" fvc_status fvc_ftle_interval(fvc_job* j, int launch, double t1, doubl
     ftle_early(c->mesh, c->window, c->integ, j->f, t1, ctr, false, s);
   }
   cudaEventRecord(ev[2], s);
-  // over this interval's live list into the other one, which the next
-  // interval's main pass takes
-  ftle_update(c->mesh, c->integ, j->f, ctr, s, j->live_alt);
-  std::swap(j->f.live, j->live_alt);
+  ftle_update(c->mesh, c->integ, j->f, ctr, s);
   j->live_ready = true;
   if ((st = check_launch(c, "ftle interval"))) return st;
   j->stats.intervals++;

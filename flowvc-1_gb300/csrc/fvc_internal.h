@@ -118,7 +118,6 @@ struct fvc_job {
   int prec = 0;         // arithmetic form the job was created with
   bool packed = false;  // positions held as (X, c) float pairs
   bool live_ready = false;  // FTLE: f.live holds the next interval's live points
-  int* live_alt = nullptr;  // FTLE: the other live list (an interval's update writes the next one there)
   fvc_job_stats stats{};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   void* rec_mem = nullptr;  // FTLE: the main pass's per-step record

@@ -959,15 +959,8 @@ __device__ __forceinline__ long brick_point(const FtleDev& f, const Bricks& b, l
 // With nfall, the first threads first solve the early-FTLE points the
 // closed-form eigenvalue left (k_ftle_early_jacobi's work, a few hundred
 // points; the other blocks' updates run meanwhile).
-//
-// cur (with its count at ncur): the update runs over this interval's live
-// list instead of the grid -- only its points were advected and flagged, and
-// no other point can be live next -- and appends the survivors to out in
-// list order, a block at a time (so a warp's 32 entries stay a compact piece
-// of the grid); without cur it runs over the grid in bricks into f.live.
 __global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, Bricks br, int update, int extrapolate,
-                                                     int unstructured, int* nlive, const int* nfall, int dims,
-                                                     const int* cur, const int* ncur, int* out) {
+                                                     int unstructured, int* nlive, const int* nfall, int dims) {
   __shared__ int warp_off[8];
   __shared__ int block_base;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -979,14 +972,7 @@ __global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, Bricks br, int u
       else early_final_one<2>(f, fall[i], true);
     }
   }
-  long p;
-  if (cur) {
-    const long nc = *(volatile const int*)ncur;
-    if ((long)blockIdx.x * blockDim.x >= nc) return;  // the whole block is past the list
-    p = t < nc ? cur[t] : -1;
-  } else {
-    p = nlive ? (t < br.count ? brick_point(f, br, t) : -1) : t;
-  }
+  const long p = nlive ? (t < br.count ? brick_point(f, br, t) : -1) : t;
   bool live = false;
   if (p >= 0 && p < f.n) {
     const unsigned char fl = update ? f.flag[p] : 1;
@@ -1027,33 +1013,22 @@ __global__ void __launch_bounds__(256) k_ftle_update(FtleDev f, Bricks br, int u
     block_base = c ? atomicAdd(nlive, c) : 0;
   }
   __syncthreads();
-  if (live) (out ? out : f.live)[block_base + warp_off[wid] + __popc(b & ((1u << lane) - 1u))] = (int)p;
+  if (live) f.live[block_base + warp_off[wid] + __popc(b & ((1u << lane) - 1u))] = (int)p;
 }
 
-void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s,
-                 int* next) {
+void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
   const Bricks br = bricks_of(f);
-  if (ctr && next) {
-    // over this interval's list (its count kept), into the next one
-    cudaMemcpyAsync(&ctr->nprev, &ctr->nlive, sizeof(int), cudaMemcpyDeviceToDevice, s);
-    cudaMemsetAsync(&ctr->nlive, 0, sizeof(int) + sizeof(ctr->cur), s);
-    k_ftle_update<<<nblk(f.n, 256), 256, 0, s>>>(f, br, 1, in.extrapolate, m.mesh_type == 1, &ctr->nlive,
-                                                 &ctr->nfall, m.dims, f.live, &ctr->nprev, next);
-    return;
-  }
   // the live count and the next interval's work cursors (adjacent)
   if (ctr) cudaMemsetAsync(&ctr->nlive, 0, sizeof(int) + sizeof(ctr->cur), s);
   k_ftle_update<<<nblk(ctr ? br.count : f.n, 256), 256, 0, s>>>(f, br, 1, in.extrapolate, m.mesh_type == 1,
                                                                  ctr ? &ctr->nlive : nullptr,
-                                                                 ctr ? &ctr->nfall : nullptr, m.dims, nullptr,
-                                                                 nullptr, nullptr);
+                                                                 ctr ? &ctr->nfall : nullptr, m.dims);
 }
 
 void ftle_live(const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s) {
   const Bricks br = bricks_of(f);
   cudaMemsetAsync(&ctr->nlive, 0, sizeof(int) + sizeof(ctr->cur), s);
-  k_ftle_update<<<nblk(br.count, 256), 256, 0, s>>>(f, br, 0, in.extrapolate, 0, &ctr->nlive, nullptr, 0, nullptr,
-                                                   nullptr, nullptr);
+  k_ftle_update<<<nblk(br.count, 256), 256, 0, s>>>(f, br, 0, in.extrapolate, 0, &ctr->nlive, nullptr, 0);
 }
 
 // GetFTLEForPoint (ompVC/ftle.c:1050-1203) for points without a value, and

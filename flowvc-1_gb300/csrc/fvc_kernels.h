@@ -30,7 +30,6 @@ struct DevCounters {
   TaskCounters tq[2];  // the task lists: 0 neighbours to the exit time, 1 to MinExitTime
   int nfall;   // served points whose eigenvalue falls back to the Jacobi solver
   unsigned long long steps_rec;  // early-FTLE steps read from the main pass's record
-  int nprev;   // the update's copy of the list it runs over
 };
 #define FVC_EARLY_COUNTERS_BYTES (offsetof(DevCounters, nfall) + sizeof(int) - offsetof(DevCounters, count))
 static_assert(offsetof(DevCounters, cur) == offsetof(DevCounters, nlive) + sizeof(int),
@@ -139,13 +138,10 @@ void ftle_triggers(const FtleDev& f, DevCounters* ctr, bool cleared, cudaStream_
 // the update kernel that follows (ftle_update with ctr)
 void ftle_early(const DevMesh& m, const DevWindow& w, const DevInteg& in, const FtleDev& f,
                 double t1, DevCounters* ctr, bool jacobi, cudaStream_t s);
-// ctr: also build the next interval's live list (ctr->nlive), clear the work
-// cursors for it and solve the early-FTLE points the closed-form eigenvalue
-// left (ctr->nfall; the list is in f.tasks).  next (with ctr): run over this
-// interval's list f.live (count ctr->nlive) and write the next list to next;
-// else run over the grid and write f.live.
-void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s,
-                 int* next = nullptr);
+// ctr: also build the next interval's live list (f.live, ctr->nlive), clear
+// the work cursors for it and solve the early-FTLE points the closed-form
+// eigenvalue left (ctr->nfall; the list is in f.tasks)
+void ftle_update(const DevMesh& m, const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s);
 // the live list of the current state (every flag and the work cursors
 // cleared)
 void ftle_live(const DevInteg& in, const FtleDev& f, DevCounters* ctr, cudaStream_t s);
