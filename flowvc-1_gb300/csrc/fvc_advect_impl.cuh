@@ -56,6 +56,36 @@ __device__ __forceinline__ long warp_grab(int* cursor) {
   return __shfl_sync(0xffffffffu, base, 0);
 }
 
+// A tracer advance's lists: the one it takes (count, cursor) and, when the
+// advance builds the next call's list itself, the pair it appends to; the
+// pair after that is cleared for the call after next.
+struct TracerLists {
+  int* cnt;
+  int* cur;
+  int* next;
+};
+__device__ __forceinline__ TracerLists tracer_lists(const TracerDev& t, DevCounters* ctr) {
+  if (!t.live_next) return TracerLists{&ctr->nlive, &ctr->cur[0], nullptr};
+  const int a = t.gen % 3;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctr->lcnt[(a + 2) % 3] = 0;
+    ctr->lcur[(a + 2) % 3] = 0;
+  }
+  return TracerLists{&ctr->lcnt[a], &ctr->lcur[a], &ctr->lcnt[(a + 1) % 3]};
+}
+
+// Appends the warp's tracers that stay live to the next list (warp ballot,
+// one atomic per warp), as compact_live would select them.
+__device__ __forceinline__ void append_live(const TracerDev& t, const TracerLists& L, bool keep, long i) {
+  const unsigned b = __ballot_sync(0xffffffffu, keep);
+  if (!b) return;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(L.next, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (keep) t.live_next[base + __popc(b & ((1u << lane) - 1u))] = (int)i;
+}
+
 __device__ __forceinline__ void load_pt(Pt& p, long i, const double* X, const double* V,
                                         const int* eid, const int* left, const double* ldt) {
   p.X[0] = X[3 * i];
@@ -575,25 +605,31 @@ __global__ void k_tracer_launch(DevMesh m, DevWindow w, TracerDev t, double tq, 
 template <int D, int M, int I>
 __global__ void __launch_bounds__(128, FVC_MINBLOCKS) k_tracer_advance(DevMesh m, DevWindow w, DevInteg in, TracerDev t,
                                                         double t1, double t2, DevCounters* ctr) {
-  const long nlive = *(volatile int*)&ctr->nlive;
+  const TracerLists L = tracer_lists(t, ctr);
+  const long nlive = *(volatile int*)L.cnt;
   unsigned steps = 0;
   int err = 0;
-  for (long base = warp_grab(&ctr->cur[0]); base < nlive; base = warp_grab(&ctr->cur[0])) {
+  for (long base = warp_grab(L.cur); base < nlive; base = warp_grab(L.cur)) {
     const long idx = base + (threadIdx.x & 31);
-    if (idx >= nlive) continue;
-    long i = t.live[idx];
-    Pt p;
-    load_pt(p, i, t.X, t.V, t.eid, t.left, t.ldt);
-    err |= advect<D, M, false, I>(m, w, in, p, t1, t2, steps);
-    t.X[3 * i] = p.X[0];
-    t.X[3 * i + 1] = p.X[1];
-    t.X[3 * i + 2] = p.X[2];
-    t.V[3 * i] = p.V[0];
-    t.V[3 * i + 1] = p.V[1];
-    t.V[3 * i + 2] = p.V[2];
-    t.eid[i] = p.eid;
-    t.left[i] = p.left;
-    t.ldt[i] = p.ldt;
+    long i = -1;
+    bool keep = false;
+    if (idx < nlive) {
+      i = t.live[idx];
+      Pt p;
+      load_pt(p, i, t.X, t.V, t.eid, t.left, t.ldt);
+      err |= advect<D, M, false, I>(m, w, in, p, t1, t2, steps);
+      t.X[3 * i] = p.X[0];
+      t.X[3 * i + 1] = p.X[1];
+      t.X[3 * i + 2] = p.X[2];
+      t.V[3 * i] = p.V[0];
+      t.V[3 * i + 1] = p.V[1];
+      t.V[3 * i + 2] = p.V[2];
+      t.eid[i] = p.eid;
+      t.left[i] = p.left;
+      t.ldt[i] = p.ldt;
+      keep = p.ldt > -FVC_TINY && (!p.left || in.extrapolate);
+    }
+    if (L.next) append_live(t, L, keep, i);
   }
   flush_counters(&ctr->steps, &ctr->status, steps, err);
 }

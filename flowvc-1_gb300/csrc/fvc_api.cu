@@ -977,7 +977,10 @@ static fvc_status job_sync(fvc_job* j, const char* what) {
   DevCounters h{};
   FVC_CUDA(c, cudaMemcpyAsync(&h, j->d_ctr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   FVC_CUDA(c, cudaStreamSynchronize(c->stream));
-  FVC_CUDA(c, cudaMemsetAsync(j->d_ctr, 0, sizeof(DevCounters), c->stream));
+  // only the accumulated counts and the fault bits are taken: the live
+  // lists' counts and cursors stay for the job's next call
+  FVC_CUDA(c, cudaMemsetAsync(j->d_ctr, 0, offsetof(DevCounters, changed) + sizeof(int), c->stream));
+  FVC_CUDA(c, cudaMemsetAsync(&j->d_ctr->steps_rec, 0, sizeof(j->d_ctr->steps_rec), c->stream));
   j->stats.steps_main += (long long)h.steps;
   j->stats.steps_early += (long long)h.steps_early;
   j->stats.steps_early_recorded += (long long)h.steps_rec;
@@ -1406,7 +1409,7 @@ extern "C" fvc_status fvc_tracer_create(fvc_ctx* c, const fvc_tracer_spec* sp, i
              {{(void**)&t.X, 24 * nn}, {(void**)&t.V, 24 * nn}, {(void**)&t.ldt, 8 * nn}, {(void**)&t.eid, 4 * nn},
               {(void**)&t.left, 4 * nn}, {(void**)&t.outX, 24 * nn},
               {(void**)&t.block_cnt, sizeof(int) * (2 * nb + 16) + sizeof(long long) * (nb / 1024 + 8)},
-              {(void**)&t.live, 4 * nn},
+              {(void**)&t.live, 4 * nn}, {(void**)&j->live_alt, 4 * nn},
               {(void**)&left0, 4 * nn}},
              &j->mem_bytes);
   if (st) {
@@ -1460,6 +1463,7 @@ extern "C" fvc_status fvc_tracer_launch(fvc_job* j, double t_start) {
   tracer_launch_vel(c->mesh, c->window, j->t, t_start, c->d_ctr, c->stream);
   if ((st = check_launch(c, "tracer launch"))) return st;
   j->stats.launches += 1;
+  j->tlive_ready = false;  // the launch can mark tracers outside
   return finish(c, "tracer launch", nullptr);
 }
 
@@ -1501,16 +1505,42 @@ extern "C" fvc_status fvc_tracer_advance(fvc_job* j, double t1, double t2, long 
   if ((st = job_counters(j))) return st;
   cudaEvent_t ev[3];
   if ((st = job_event_triple(j, ev))) return st;
-  compact_live(j->t.n, j->t.ldt, j->t.left, c->integ.extrapolate, j->t.live, nullptr, j->t.block_cnt, j->d_ctr,
-               c->stream);
+  // the live list: built by the previous advance, or compacted here (the
+  // first advance, after a launch, or with exposure time, whose kernel does
+  // not build it)
+  const bool fused = !c->cet_sub && j->t.n > 0;
+  const int a = j->tgen % 3;
+  bool compacted = false;
+  if (!fused || !j->tlive_ready || j->tlive_extrap != c->integ.extrapolate) {
+    compact_live(j->t.n, j->t.ldt, j->t.left, c->integ.extrapolate, j->t.live, nullptr, j->t.block_cnt, j->d_ctr,
+                 c->stream);
+    compacted = true;
+    if (fused) {
+      FVC_CUDA(c, cudaMemcpyAsync(&j->d_ctr->lcnt[a], &j->d_ctr->nlive, sizeof(int), cudaMemcpyDeviceToDevice,
+                                  c->stream));
+      FVC_CUDA(c, cudaMemsetAsync(&j->d_ctr->lcur[a], 0, sizeof(int), c->stream));
+      FVC_CUDA(c, cudaMemsetAsync(&j->d_ctr->lcnt[(a + 1) % 3], 0, sizeof(int), c->stream));
+    }
+  }
+  TracerDev t = j->t;
+  t.live_next = fused ? j->live_alt : nullptr;
+  t.gen = j->tgen;
   cudaEventRecord(ev[0], c->stream);
-  if (c->cet_sub) tracer_advance_cet(c->mesh, c->window, c->integ, j->t, t1, t2, cet_dev(c), j->d_ctr, c->stream);
-  else tracer_advance(c->mesh, c->window, c->integ, j->t, t1, t2, j->d_ctr, c->stream);
+  if (c->cet_sub) tracer_advance_cet(c->mesh, c->window, c->integ, t, t1, t2, cet_dev(c), j->d_ctr, c->stream);
+  else tracer_advance(c->mesh, c->window, c->integ, t, t1, t2, j->d_ctr, c->stream);
   cudaEventRecord(ev[1], c->stream);
+  if (fused) {
+    std::swap(j->t.live, j->live_alt);
+    j->tgen++;
+    j->tlive_ready = true;
+    j->tlive_extrap = c->integ.extrapolate;
+  } else {
+    j->tlive_ready = false;
+  }
   cudaEventRecord(ev[2], c->stream);
   if ((st = check_launch(c, "tracer advance"))) return st;
   j->stats.intervals++;
-  j->stats.launches += 5 + c->aux_launches;
+  j->stats.launches += 1 + (compacted ? 4 : 0) + c->aux_launches;
   c->aux_launches = 0;
   if (!steps) return FVC_OK;  // asynchronous: accounted by the next call that waits
   const long long before = j->stats.steps_main;

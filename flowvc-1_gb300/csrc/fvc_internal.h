@@ -118,6 +118,12 @@ struct fvc_job {
   int prec = 0;         // arithmetic form the job was created with
   bool packed = false;  // positions held as (X, c) float pairs
   bool live_ready = false;  // FTLE: f.live holds the next interval's live points
+  // tracers: the other live list, which each advance fills for the next
+  // one, and its state (valid until the tracers' state changes otherwise)
+  int* live_alt = nullptr;
+  int tgen = 0;
+  bool tlive_ready = false;
+  int tlive_extrap = 0;
   fvc_job_stats stats{};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   void* rec_mem = nullptr;  // FTLE: the main pass's per-step record

@@ -17,7 +17,8 @@ struct TaskCounters {
   int scat[8];  // fill cursors of the buckets in the sorted list
 };
 
-// Scratch counters shared by the launches of one call.
+// Scratch counters shared by the launches of one call.  steps .. changed
+// (and steps_rec) are the accumulated figures a job's wait takes and clears.
 struct DevCounters {
   unsigned long long steps;
   unsigned long long steps_early;  // accepted steps of the early-FTLE advections
@@ -30,6 +31,11 @@ struct DevCounters {
   TaskCounters tq[2];  // the task lists: 0 neighbours to the exit time, 1 to MinExitTime
   int nfall;   // served points whose eigenvalue falls back to the Jacobi solver
   unsigned long long steps_rec;  // early-FTLE steps read from the main pass's record
+  // a tracer job's live lists built by its advances: three (count, cursor)
+  // pairs in rotation (the call with generation g reads pair g % 3, appends
+  // to (g + 1) % 3 and clears (g + 2) % 3, which the call before read)
+  int lcnt[3];
+  int lcur[3];
 };
 #define FVC_EARLY_COUNTERS_BYTES (offsetof(DevCounters, nfall) + sizeof(int) - offsetof(DevCounters, count))
 static_assert(offsetof(DevCounters, cur) == offsetof(DevCounters, nlive) + sizeof(int),
@@ -157,7 +163,9 @@ struct TracerDev {
   int* left;
   double* outX;
   int* block_cnt;
-  int* live;             // tracers advected by the current call, in seed order
+  int* live;             // tracers advected by the current call
+  int* live_next;        // non-null: the advance appends the tracers still live to it (the next call's list)
+  int gen;               // the advance's generation (the rotation of DevCounters::lcnt / lcur)
 };
 
 // Compacts the indices of live points (LeftDomainTime > -TINY and, unless

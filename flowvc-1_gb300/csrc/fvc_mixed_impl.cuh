@@ -160,23 +160,29 @@ __global__ void k_tracer_launch_mx(DevMesh m, DevWindow w, TracerDev t, float tl
 template <int D>
 __global__ void __launch_bounds__(128, FVC_MX_MINBLOCKS) k_tracer_advance_mx(DevMesh m, DevWindow w, int type, TracerDev t,
                                                            DevCounters* ctr) {
-  const long nlive = *(volatile int*)&ctr->nlive;
+  const TracerLists L = tracer_lists(t, ctr);
+  const long nlive = *(volatile int*)L.cnt;
   unsigned steps = 0;
   int err = 0;
-  for (long base = warp_grab(&ctr->cur[0]); base < nlive; base = warp_grab(&ctr->cur[0])) {
+  for (long base = warp_grab(L.cur); base < nlive; base = warp_grab(L.cur)) {
     const long idx = base + (threadIdx.x & 31);
-    if (idx >= nlive) continue;
-    const long i = t.live[idx];
-    PtM p;
-    load_pos_pair(t.X, i, p.X, p.c);
-    p.eid = t.eid[i];
-    p.left = t.left[i];
-    p.ldt = t.ldt[i];
-    advect_mx<D>(m, w, type, p, w.nsteps, steps, err);
-    store_pos_pair(t.X, i, p.X, p.c);
-    t.eid[i] = p.eid;
-    t.left[i] = p.left;
-    t.ldt[i] = p.ldt;
+    long i = -1;
+    bool keep = false;
+    if (idx < nlive) {
+      i = t.live[idx];
+      PtM p;
+      load_pos_pair(t.X, i, p.X, p.c);
+      p.eid = t.eid[i];
+      p.left = t.left[i];
+      p.ldt = t.ldt[i];
+      advect_mx<D>(m, w, type, p, w.nsteps, steps, err);
+      store_pos_pair(t.X, i, p.X, p.c);
+      t.eid[i] = p.eid;
+      t.left[i] = p.left;
+      t.ldt[i] = p.ldt;
+      keep = p.ldt > -FVC_TINY && !p.left;  // the mixed form does not extrapolate
+    }
+    if (L.next) append_live(t, L, keep, i);
   }
   flush_counters(&ctr->steps, &ctr->status, steps, err);
 }

@@ -67,13 +67,14 @@ def upload_frames(ctx: fvc.Context, ax: TimeAxis, frames, asynchronous=False):
 
 
 def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, lsc=1, state=None, out=None,
-             fetch=True):
+             fetch=True, wait=False):
     """One FTLE slide over its whole integration window, frames resident.
 
     grid = (xmin, xmax, ymin, ymax, zmin, zmax, xres, yres, zres).  Returns
     (ftle_wT, ftle_woT, steps, job stats); a dict passed as state receives
     the slide's final point state (fvc_ftle_get_state).  out: host arrays
-    for the two fields; fetch=False leaves them on the device (None)."""
+    for the two fields; fetch=False leaves them on the device (None).
+    wait=True waits for every interval (the default queues them)."""
     if ax.periodic:
         stop = t_start + direction * T
     else:
@@ -92,7 +93,7 @@ def run_ftle(ctx: fvc.Context, ax: TimeAxis, grid, T, direction=1, t_start=0.0, 
             t1 = t_start if launch else (tmin if direction > 0 else tmax)
             t2 = min(tmax, stop) if direction > 0 else max(tmin, stop)
             status = 1
-            job.interval(launch, t1, t2, wait=False)
+            job.interval(launch, t1, t2, wait=wait)
             if ((stop - tmax) if direction > 0 else (tmin - stop)) < TINY:
                 res = job.reduce(T, out=out, fetch=fetch)
                 if state is not None:

@@ -91,3 +91,30 @@ def test_queued_advance_fault_reported_by_the_output(engine):
     assert e.value.status == fvc.FVC_ERR_WALK
     job.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "bf16"])
+def test_waiting_calls_match_queued_ones(engine, prec):
+    """A job's wait (an FTLE interval or a tracer advance that returns its
+    steps) takes the accumulated counts without losing the live list the
+    next call runs on: windows run with every call waiting give the bytes
+    of the queued ones."""
+    ctx, ax = cube(prec)
+    grid = (0, 1, 0, 1, 0, 1, 12, 11, 10)
+    sa, sb = {}, {}
+    a = flow.run_ftle(ctx, ax, grid, 0.2, state=sa)
+    b = flow.run_ftle(ctx, ax, grid, 0.2, state=sb, wait=True)
+    assert a[2] == b[2] > 0
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    for key in sa:
+        assert np.array_equal(sa[key], sb[key]), key
+    seeds = synth.uniform_seeds(5000, 3, seed=6, lo=-0.05, hi=1.05)
+    ta, tb = {}, {}
+    oa, stp_a, _ = flow.run_tracers(ctx, ax, seeds, 0.0, 0.03, 9, state=ta, asynchronous=True)
+    ob, stp_b, _ = flow.run_tracers(ctx, ax, seeds, 0.0, 0.03, 9, state=tb, asynchronous=False)
+    assert stp_a == stp_b > 0
+    for x, y in zip(oa, ob):
+        assert np.array_equal(x, y)
+    for key in ("X", "eid", "left", "ldt"):
+        assert np.array_equal(ta[key], tb[key]), key
+    ctx.close()
