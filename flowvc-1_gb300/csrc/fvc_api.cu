@@ -89,6 +89,9 @@ static inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 static void drop_quantised(fvc_ctx* c) {
   for (auto& kv : c->qframes) cudaFree(kv.second.q);
   c->qframes.clear();
+  for (auto& kv : c->qpairs) cudaFree(kv.second.q);
+  c->qpairs.clear();
+  c->qpair_bytes = 0;
   cudaFree(c->d_qpair);
   c->d_qpair = nullptr;
   c->window_set = false;
@@ -142,6 +145,7 @@ extern "C" void fvc_destroy(fvc_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto& kv : c->frames) cudaFree(kv.second);
   for (auto& kv : c->qframes) cudaFree(kv.second.q);
+  for (auto& kv : c->qpairs) cudaFree(kv.second.q);
   cudaFree(c->d_qscratch);
   cudaFree(c->d_qpair);
   cudaFree(c->d_steps);
@@ -604,22 +608,52 @@ fvc_status quantised(fvc_ctx* c, int id, fvc_ctx::QFrame** out) {
       return fail(c, FVC_ERR_CUDA, "frame quantisation failed");
     c->aux_launches += 2;
     q.fmt = c->prec;
+    q.ver++;
   }
   *out = &q;
   return FVC_OK;
 }
+
+// pair records kept per window, up to this many bytes; beyond, the window's
+// scratch pair is made afresh each time
+static constexpr size_t QPAIR_CACHE_BYTES = (size_t)1 << 30;
 
 static fvc_status quantised_window(fvc_ctx* c) {
   fvc_ctx::QFrame *a = nullptr, *b = nullptr;
   fvc_status st;
   if ((st = quantised(c, c->window_lo, &a)) || (st = quantised(c, c->window_hi, &b))) return st;
   DevWindow& w = c->window;
-  if (!c->d_qpair && cudaMalloc(&c->d_qpair, sizeof(uint4) * (size_t)c->frame_nodes) != cudaSuccess)
-    return fail(c, FVC_ERR_OOM, "quantised window allocation failed");
-  pair_frames(a->q, b->q, c->frame_nodes, c->d_qpair, c->stream);
-  c->aux_launches++;
-  if ((st = check_launch(c, "pair frames"))) return st;
-  w.qp = c->d_qpair;
+  const size_t bytes = sizeof(uint4) * (size_t)c->frame_nodes;
+  auto key = std::make_pair(c->window_lo, c->window_hi);
+  auto it = c->qpairs.find(key);
+  if (it == c->qpairs.end() && c->qpair_bytes + bytes <= QPAIR_CACHE_BYTES) {
+    fvc_ctx::QPair P;
+    if (cudaMalloc(&P.q, bytes) == cudaSuccess) {
+      c->qpair_bytes += bytes;
+      it = c->qpairs.emplace(key, P).first;
+    }
+  }
+  uint4* qp;
+  if (it != c->qpairs.end()) {
+    fvc_ctx::QPair& P = it->second;
+    if (P.fmt != c->prec || P.va != a->ver || P.vb != b->ver) {
+      pair_frames(a->q, b->q, c->frame_nodes, P.q, c->stream);
+      c->aux_launches++;
+      if ((st = check_launch(c, "pair frames"))) return st;
+      P.fmt = c->prec;
+      P.va = a->ver;
+      P.vb = b->ver;
+    }
+    qp = P.q;
+  } else {
+    if (!c->d_qpair && cudaMalloc(&c->d_qpair, bytes) != cudaSuccess)
+      return fail(c, FVC_ERR_OOM, "quantised window allocation failed");
+    pair_frames(a->q, b->q, c->frame_nodes, c->d_qpair, c->stream);
+    c->aux_launches++;
+    if ((st = check_launch(c, "pair frames"))) return st;
+    qp = c->d_qpair;
+  }
+  w.qp = qp;
   for (int k = 0; k < 3; k++) {
     w.qs0[k] = a->s[k];
     w.qs1[k] = b->s[k];
@@ -1642,10 +1676,9 @@ extern "C" fvc_status fvc_tracer_output_begin(fvc_job* j, int always, long long*
   FVC_CUDA(c, cudaStreamWaitEvent(s, o.copied, 0));
   TracerDev t = j->t;
   t.outX = o.d;
-  tracer_compact(t, always, j->d_ctr, s);
-  if (j->packed) unpack_pairs_counted(o.d, (long)n, &j->d_ctr->count, s);
+  const int nl = tracer_compact(t, always, j->d_ctr, s, j->packed);
   if ((st = check_launch(c, "tracer output"))) return st;
-  j->stats.launches += 5 + (j->packed ? 1 : 0);
+  j->stats.launches += nl;
   FVC_CUDA(c, cudaMemcpyAsync(o.hc, &j->d_ctr->count, sizeof(int), cudaMemcpyDeviceToHost, s));
   FVC_CUDA(c, cudaMemcpyAsync(o.hc + 1, &j->d_ctr->status, sizeof(int), cudaMemcpyDeviceToHost, s));
   // the copy runs on the side stream after the compaction; its length is a
@@ -1723,9 +1756,8 @@ extern "C" fvc_status fvc_tracer_snapshot(fvc_job* j, int always, double* X_out,
   fvc_status st;
   if ((st = use_device(c))) return st;
   if ((st = job_sync(j, "tracer advance"))) return st;  // faults of queued advances
-  tracer_compact(j->t, always, c->d_ctr, c->stream);
+  j->stats.launches += tracer_compact(j->t, always, c->d_ctr, c->stream);
   if ((st = check_launch(c, "tracer snapshot"))) return st;
-  j->stats.launches += 5;
   int cnt = 0;
   FVC_CUDA(c, cudaMemcpyAsync(&cnt, &c->d_ctr->count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   FVC_CUDA(c, cudaStreamSynchronize(c->stream));

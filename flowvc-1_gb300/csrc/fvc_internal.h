@@ -53,10 +53,20 @@ struct fvc_ctx {
     ushort4* q = nullptr;
     float s[3] = {1.f, 1.f, 1.f};
     int fmt = 0;
+    unsigned ver = 0;  // counts the quantisations (a pair made from an older one is stale)
   };
   std::unordered_map<int, QFrame> qframes;
   unsigned* d_qscratch = nullptr;
   uint4* d_qpair = nullptr;  // the window's two quantised frames, interleaved
+  // interleaved pairs kept per (frame_lo, frame_hi), so a window set again
+  // (every interval of a slide or release) reuses its records
+  struct QPair {
+    uint4* q = nullptr;
+    unsigned va = 0, vb = 0;
+    int fmt = 0;
+  };
+  std::map<std::pair<int, int>, QPair> qpairs;
+  size_t qpair_bytes = 0;
   std::vector<StepM> h_steps;
   StepM* d_steps = nullptr;
   size_t steps_cap = 0;

@@ -1160,6 +1160,51 @@ __global__ void k_compact_scatter(TracerDev t, int always, const int* block_off)
 
 __global__ void k_copy_count(const int* src, int* dst) { *dst = *src; }
 
+// The scatter with each block's offset summed from the block counts before
+// it (no scan launches; for up to COMPACT_DIRECT_BLOCKS blocks, a few
+// thousand L2 reads a block); the last block writes the total.  unpack: the
+// mixed form's (X, c) pairs are written as FP64 positions X - c (the same
+// arithmetic as k_unpack_pairs).
+constexpr int COMPACT_DIRECT_BLOCKS = 4096;
+__global__ void __launch_bounds__(1024) k_compact_scatter_direct(TracerDev t, int always, int unpack, int* count) {
+  __shared__ int warp_off[32];
+  __shared__ long long red[32];
+  __shared__ long long block_off;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long part = 0;
+  for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) part += t.block_cnt[b];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if (lane == 0) red[wid] = part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long a = 0;
+    for (int k = 0; k < nw; k++) a += red[k];
+    block_off = a;
+  }
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool sel = tracer_selected(t, i, always);
+  unsigned b = __ballot_sync(0xffffffffu, sel);
+  if (lane == 0) warp_off[wid] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int c = 0;
+    for (int k = 0; k < nw; k++) {
+      int v = warp_off[k];
+      warp_off[k] = c;
+      c += v;
+    }
+    if (blockIdx.x == gridDim.x - 1) *count = (int)(block_off + c);
+  }
+  __syncthreads();
+  if (sel) {
+    long o = (long)block_off + warp_off[wid] + __popc(b & ((1u << lane) - 1u));
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+      t.outX[3 * o + a] = unpack ? join_pos(reinterpret_cast<const float2*>(t.X)[3 * i + a]) : t.X[3 * i + a];
+  }
+}
+
 // Live-point compaction: warp ballots give each lane its rank among the
 // selected lanes; block counts are scanned into offsets so the list keeps the
 // points' order (neighbouring points stay in the same warp).
@@ -1223,19 +1268,25 @@ void compact_live(int n, const double* ldt, const int* left, int extrapolate, in
   k_live_scatter<<<nb, 1024, 0, s>>>(n, ldt, left, extrapolate, off, live, flag, ctr);
 }
 
-void tracer_compact(const TracerDev& t, int always, DevCounters* ctr, cudaStream_t s) {
+int tracer_compact(const TracerDev& t, int always, DevCounters* ctr, cudaStream_t s, bool unpack) {
   if (t.n <= 0) {
     cudaMemsetAsync(&ctr->count, 0, sizeof(int), s);
-    return;
+    return 0;
   }
   unsigned nb = nblk(t.n, 1024);
   k_compact_count<<<nb, 1024, 0, s>>>(t, always);
+  if (nb <= (unsigned)COMPACT_DIRECT_BLOCKS) {
+    k_compact_scatter_direct<<<nb, 1024, 0, s>>>(t, always, unpack ? 1 : 0, &ctr->count);
+    return 2;
+  }
   // block_cnt has room for nb + 1 offsets followed by the scan's block totals
   int* off = t.block_cnt + nb + 1;
   long long* tmp = reinterpret_cast<long long*>(t.block_cnt + ((2 * nb + 4) & ~1u));
   exclusive_scan(t.block_cnt, off, (int)nb, tmp, s);
   k_compact_scatter<<<nb, 1024, 0, s>>>(t, always, off);
   k_copy_count<<<1, 1, 0, s>>>(off + nb, &ctr->count);
+  if (unpack) unpack_pairs_counted(t.outX, t.n, &ctr->count, s);
+  return 5 + (unpack ? 1 : 0);
 }
 
 

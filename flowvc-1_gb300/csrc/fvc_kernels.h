@@ -179,8 +179,9 @@ void tracer_advance(const DevMesh& m, const DevWindow& w, const DevInteg& in, co
                     double t1, double t2, DevCounters* ctr, cudaStream_t s);
 void tracer_init_ldt(const TracerDev& t, cudaStream_t s);
 // Compacts the selected tracers' positions (in seed order) into t.outX;
-// the count lands in ctr->count.
-void tracer_compact(const TracerDev& t, int always, DevCounters* ctr, cudaStream_t s);
+// the count lands in ctr->count.  unpack: the mixed form's (X, c) pairs are
+// written as FP64 positions.  Returns the kernels launched.
+int tracer_compact(const TracerDev& t, int always, DevCounters* ctr, cudaStream_t s, bool unpack = false);
 
 // ---- tracer side analyses (fvc_cet.cu), unstructured meshes, FP64 form
 // tracer_advance with the exposure-time accumulation after every step
