@@ -75,6 +75,11 @@ struct BJob {
   const DevWindow* w;   // FP64 form: the job's window (two frames, no stage table)
   int nwin;             // frame intervals of this tick (tracer jobs may run several)
   const BWin* wins;     // their windows, in order (wins[0] is the one above)
+  // FTLE pass 1: the per-step record the early-FTLE tasks read (null: none)
+  double* rec;
+  unsigned char* kacc;
+  int4* rec_e1;
+  int rec_steps;
 };
 
 struct BatchCtr {
@@ -143,12 +148,17 @@ __global__ void __launch_bounds__(256, (FVC_MX_MINBLOCKS + 1) / 2) k_batch_advan
       t.left = J.left[p];
       t.ldt = J.ldt[p];
       // the job's intervals of this tick in order; a tracer that leaves is
-      // not advanced further (the live test of every later interval)
+      // not advanced further (the live test of every later interval).  An
+      // FTLE job's pass 1 (one interval) writes its per-step record.
+      const unsigned before = steps;
+      const RecOut r{J.rec + 3 * p, 3L * J.n, J.rec_steps, nullptr, 0};
+      const RecOut* rp = (J.kind == 1 && J.rec) ? &r : nullptr;
       for (int k = 0; k < J.nwin; k++) {
         const WinQ w = J.wins[k].q;
-        advect_mx<D>(m, w, type, t, w.nsteps, steps, err);
+        advect_mx<D>(m, w, type, t, w.nsteps, steps, err, rp);
         if (t.left || err) break;
       }
+      if (rp) J.kacc[p] = (unsigned char)(steps - before);
       if (J.kind == 0) {
         store_pos_pair(J.X, p, t.X, t.c);
         J.eid[p] = t.eid;
@@ -185,11 +195,15 @@ __global__ void __launch_bounds__(256, FVC_MINBLOCKS / 2) k_batch_advance(DevMes
       const long p = e.y;
       Pt t;
       load_pt(t, p, J.X, nullptr, J.eid, J.left, J.ldt);
+      const unsigned before = steps;
+      const RecOut r{J.rec + 3 * p, 3L * J.n, J.rec_steps, J.rec_e1 ? J.rec_e1 + p : nullptr, t.eid};
+      const RecOut* rp = (J.kind == 1 && J.rec) ? &r : nullptr;
       for (int k = 0; k < J.nwin; k++) {
         const BWin& W = J.wins[k];
-        err |= advect<D, 1, false, I>(m, *W.w, in, t, W.t1, W.t2, steps);
+        err |= advect<D, 1, false, I>(m, *W.w, in, t, W.t1, W.t2, steps, nullptr, rp);
         if (t.left || err) break;
       }
+      if (rp) J.kacc[p] = (unsigned char)(steps - before);
       if (J.kind == 0) {
         J.X[3 * p] = t.X[0];
         J.X[3 * p + 1] = t.X[1];
@@ -414,6 +428,18 @@ struct PairQ {
 size_t job_bytes(int kind, long n) {
   if (kind == FVC_JOB_FTLE) return (size_t)n * 560 + (1u << 20);
   return (size_t)n * 134 + (1u << 20);
+}
+
+// An FTLE job's per-step record (the steps of one interval, at most 32, as
+// the single-job interval keeps it): positions, accepted steps, step-1
+// element states.
+int rec_steps_of(double tdelta, double h) {
+  const double k = ceil(tdelta / fabs(h)) + 1.0;
+  return k < 32.0 ? (int)k : 32;
+}
+size_t rec_bytes_of(long n, int want) {
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  return al(24 * (size_t)n * (size_t)want) + al((size_t)n) + 16 * (size_t)n;
 }
 
 }  // namespace
@@ -734,6 +760,29 @@ static fvc_status admit_one(fvc_batch* b, HostJob& J) {
       sp.stop_time = J.stop;
       sp.generate = 1;
       st = fvc_ftle_create(c, &sp, &J.job);
+      if (!st) {
+        // the main pass's per-step record, from which early-FTLE advections
+        // that repeat it are read (without room, they are computed)
+        fvc_job* j = J.job;
+        const int want = rec_steps_of(b->o.tdelta, c->integ.h);
+        const size_t n = (size_t)j->f.n;
+        j->rec_bytes = rec_bytes_of((long)n, want);
+        j->rec_mem = pool_get(c, j->rec_bytes);
+        if (j->rec_mem) {
+          j->rec_cap = want;
+          const size_t pos = (24 * n * (size_t)want + 255) & ~(size_t)255;
+          j->f.rec = nullptr;  // per interval, from the tick's plan
+          j->f.kacc = (unsigned char*)j->rec_mem + pos;
+          j->f.rec_e1 = (!j->prec && c->integ.type == 1) ? (int4*)((char*)j->rec_mem + pos + ((n + 255) & ~(size_t)255))
+                                                          : nullptr;
+        } else {
+          j->rec_bytes = 0;
+          j->f.rec = nullptr;
+          j->f.kacc = nullptr;
+          j->f.rec_e1 = nullptr;
+        }
+        j->f.rec_steps = 0;
+      }
     } else {
       fvc_tracer_spec sp{};
       sp.local_search_checking = J.spec.local_search_checking;
@@ -801,6 +850,7 @@ struct TickPlan {
   std::vector<int> ids;           // job ids in BJob order
   std::vector<Interval> iv;       // per job: its first interval of the tick
   std::vector<int> nint;          // per job: intervals in the tick
+  std::vector<int> rec_steps;     // per FTLE job: the record's steps this interval (0: none)
   std::vector<char> last;         // per job: the tick ends the job's window
   std::vector<DevWindow> win;     // per job (launch velocity, early FTLE)
   long long ngroups = 0;
@@ -817,6 +867,7 @@ static fvc_status plan_tick(fvc_batch* b, const std::vector<int>& ids, char* dev
   const size_t nj = ids.size();
   P.iv.resize(nj);
   P.nint.resize(nj);
+  P.rec_steps.assign(nj, 0);
   P.last.resize(nj);
   P.win.resize(nj);
   // every job's intervals of this tick: one for FTLE jobs, up to per_tick
@@ -895,7 +946,28 @@ static fvc_status plan_tick(fvc_batch* b, const std::vector<int>& ids, char* dev
     B.ctr = b->d_ctrs + H.slot;
     B.group0 = groups;
     if (H.kind == FVC_JOB_FTLE) {
+      // the record's steps this interval (as the single-job interval keeps
+      // them: the interval's steps, at most the record's room), for the
+      // pass (here) and the job's early-FTLE kernels (enqueue_tick)
       const FtleDev& f = H.job->f;
+      int rs = 0;
+      if (H.job->rec_mem) {
+        int ns;
+        if (c->prec) {
+          ns = (int)tabs[wi - 1].size() - 1;
+        } else {
+          std::vector<StepM> T;
+          const Interval& I = ivs[k][0];
+          ns = build_steps_for(c->integ.h, I.tmin, I.tmax, I.t1, I.t2, T) ? (int)T.size() - 1 : 0;
+        }
+        const int want = ns < 32 ? ns : 32;
+        rs = (want > 0 && H.job->rec_cap >= want) ? want : 0;
+      }
+      P.rec_steps[k] = rs;
+      B.rec = rs > 0 ? (double*)H.job->rec_mem : nullptr;
+      B.kacc = f.kacc;
+      B.rec_e1 = f.rec_e1;
+      B.rec_steps = rs;
       B.kind = 1;
       B.n = f.n;
       B.X = f.X;
@@ -1017,7 +1089,9 @@ static fvc_status enqueue_tick(fvc_batch* b, const TickPlan& P, const BJob* d_jo
     if (H.kind != FVC_JOB_FTLE) continue;
     cudaStream_t s = nside ? b->side[fj++ % nside] : c->stream;
     DevCounters* ctr = b->d_ctrs + H.slot;
-    const FtleDev& f = H.job->f;
+    FtleDev f = H.job->f;  // with this interval's record, which the pass wrote
+    f.rec = P.rec_steps[k] > 0 ? (double*)H.job->rec_mem : nullptr;
+    f.rec_steps = P.rec_steps[k];
     // the task lists' work cursors start at 0 every interval
     FVC_CUDA(c, cudaMemsetAsync(ctr->cur, 0, sizeof(ctr->cur), s));
     ftle_triggers(f, ctr, false, s);
@@ -1408,6 +1482,7 @@ extern "C" fvc_status fvc_batch_submit(fvc_batch* b, const fvc_batch_job_spec* s
   }
   J->spec.seeds = nullptr;
   J->bytes = job_bytes(sp->kind, n);
+  if (sp->kind == FVC_JOB_FTLE) J->bytes += rec_bytes_of(n, rec_steps_of(b->o.tdelta, c->integ.h));
   if (sp->kind != FVC_JOB_FTLE && b->o.tick_intervals > 0) {
     // the frame intervals the window touches, at most; a long release runs
     // several of them per tick
