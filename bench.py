@@ -152,10 +152,15 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+        # the timed region starts once the sampler is writing (its start-up
+        # would otherwise take most of a short region)
+        t0 = time.time()
+        while self.proc and time.time() - t0 < 3.0 and os.path.getsize(self.path) == 0:
+            time.sleep(0.01)
         return self
 
     def __exit__(self, *a):
