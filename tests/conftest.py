@@ -70,6 +70,28 @@ def run_golden(exe, case, run, tmp_path, extra_args=()):
     return out, r.stdout
 
 
+def check_ic(case, run, tmp_path, who):
+    """The located seed grid a run wrote (its FTLE_ICFile in the case's copied
+    inputs: left flags, and element ids of the seeds inside -- ompVC leaves
+    the others unset) against ompVC's for the same run
+    (tests/golden/<case>/ic.json, made by tests/golden/make_ic_digests.py).
+    Returns False when the run has no recorded grid."""
+    import scale_cases as sc
+    pj = os.path.join(GOLDEN, case, "ic.json")
+    if not os.path.exists(pj):
+        return False
+    with open(pj) as f:
+        exp = json.load(f).get(run)
+    if exp is None:
+        return False
+    got = sc.ic_digests(os.path.join(str(tmp_path), case + "_in", "ftle_ic.bin"))
+    assert got["n"] == exp["n"], f"{who} {case} {run}: {got['n']} seeds in the IC file, ompVC wrote {exp['n']}"
+    assert got["left_sha256"] == exp["left_sha256"], f"{who} {case} {run}: seed left flags differ from ompVC's"
+    assert got["eid_inside_sha256"] == exp["eid_inside_sha256"], \
+        f"{who} {case} {run}: element ids of seeds inside differ from ompVC's"
+    return True
+
+
 # FTLE fields: the engine computes the Cauchy-Green eigenvalue with its own
 # solvers (the trigonometric closed form on C - I, Jacobi where that is
 # ill-conditioned; the reference uses Householder + QL on C), so FTLE values

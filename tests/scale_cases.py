@@ -149,8 +149,13 @@ def ic_arrays(path):
 
 
 def ic_digests(path):
+    """Digests of the IC file's element ids and left flags; eid_inside_sha256
+    covers the ids of the points inside only (ompVC leaves the id of a point
+    it marks outside unset: whatever its heap held)."""
     eid, left = ic_arrays(path)
+    inside = np.where(left != 0, -1, eid).astype(np.int32)
     return {"n": int(len(eid)), "eid_sha256": hashlib.sha256(eid.tobytes()).hexdigest(),
+            "eid_inside_sha256": hashlib.sha256(inside.tobytes()).hexdigest(),
             "left_sha256": hashlib.sha256(left.tobytes()).hexdigest()}
 
 

@@ -1,14 +1,14 @@
 """The GPU engine (fvcflow over libfvc) against ompVC's outputs and the oracle.
 
 Tracer files and FTLE grid states (positions, element ids, exit flags) must
-be bit-identical to the oracle; tracer files byte-identical to ompVC's; FTLE
-fields within the tolerance in conftest."""
+be bit-identical to the oracle; tracer files and the located seed grids
+byte-identical to ompVC's; FTLE fields within the tolerance in conftest."""
 import os
 
 import numpy as np
 import pytest
 
-from conftest import (CET_RTOL, GOLDEN, compare_outputs, compare_state_dumps, golden_cases, run_golden,
+from conftest import (CET_RTOL, GOLDEN, check_ic, compare_outputs, compare_state_dumps, golden_cases, run_golden,
                       undefined_files)
 
 pytestmark = pytest.mark.gpu
@@ -46,6 +46,7 @@ def test_engine_matches_reference(engine, oracle_bin, tmp_path, case, run):
     dump_g.mkdir()
     dump_o.mkdir()
     got, _ = run_golden(engine.FVCFLOW, case, run, tmp_path, extra_args=("--dump-state", str(dump_g)))
+    check_ic(case, run, tmp_path, "engine")  # the located seed grid, byte for byte
     if "rkf" in run:
         if run.startswith("tracer"):
             worst = compare_rkf(os.path.join(GOLDEN, case, "expected", run), got)
